@@ -1,0 +1,239 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Lloyd hot path.
+
+A step is one Lloyd iteration (assignment + center update + SSE) over the resident data set of
+the 4,000,000 x 128, K=1024 workload (1024 anisotropic Gaussians, per-component diagonal std
+log-uniform in [0.3, 3], means uniform in [-20, 20]^128, initial centers a seeded sample of
+points; synthetic, generated on the device). Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--tier fp32|bf16] [--impl reference]
+
+`value` is Lloyd iterations/s with the data resident in HBM (CUDA events on the library's
+stream); `e2e` is the same metric through the public C-ABI one-shot call (kmgb_lloyd_f32) from
+pageable host memory, host<->device copies included; `roofline` covers the assignment kernel
+(2*N*K*D FLOP per launch, per-launch time from CUDA events bracketing it inside the timed
+region); `cpu_baseline` is the CPU restatement (oracle FP32 port, all host threads) on a sample.
+The reference arm (--impl reference) times that CPU path: the reference has no CPU
+implementation of its own and its GPU code cannot be built for this host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, D, K = 4_000_000, 128, 1024
+METRIC = "Lloyd iter/s (N=4M, D=128, K=1024), labels = FP64 arg-min"
+CPU_SAMPLE_ROWS = 65_536
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        j = json.load(open(p))
+        return j.get("bf16_tflops", 1900.0), j.get("hbm_gbs", 6800.0), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampler for the timed region."""
+
+    def __init__(self, index: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait(timeout=10)
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) >= 9 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) >= 9 and r[2].strip().replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            for nme, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nme)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def cpu_baseline(steps: int = 1):
+    """Oracle FP32 port (CPU restatement, OpenMP, all host threads) on a bounded sample: one
+    Lloyd iteration over CPU_SAMPLE_ROWS rows of the workload, scaled to the full N."""
+    import oracle
+    from kmeans_gb300.synthetic import mixture_numpy, sample_init
+    X, _, _ = mixture_numpy(CPU_SAMPLE_ROWS, D, K, seed=5, mean_lo=-20, mean_hi=20, std=(0.3, 3.0))
+    init = X[sample_init(CPU_SAMPLE_ROWS, K, seed=6)]
+    oracle.port_lloyd(X[:4096], init, 1)  # warm the thread pool
+    times = []
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        oracle.port_lloyd(X, init, 1)
+        times.append(time.perf_counter() - t0)
+    t = float(np.median(times))
+    return {"value": (CPU_SAMPLE_ROWS / N) / t, "unit": "iter/s", "cores": oracle.num_threads(),
+            "kind": "port",
+            "sample": f"1 Lloyd iteration over {CPU_SAMPLE_ROWS} of the {N} rows (D={D}, K={K}), "
+                      f"FP32 port of the reference loop, time scaled linearly to N; median of "
+                      f"{len(times)}", "seconds_per_sample_iter": t}
+
+
+def reference_arm(args, rank: int):
+    if rank != 0:
+        return
+    for _ in range(max(0, min(args.warmup, 1))):
+        cpu_baseline(1)
+    cb = cpu_baseline(max(1, min(args.steps, 3)))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "iter/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "lloyd_4Mx128_K1024", "n": N, "d": D, "k": K},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": cb["value"], "unit": "iter/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--tier", default=None, help="fp32 or bf16 (default: bf16 when available)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return reference_arm(args, rank)
+
+    import torch
+    import kmeans_gb300 as km
+    from kmeans_gb300.synthetic import mixture_torch, sample_init
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    km.build()
+    lib = km.lib()
+    tier = args.tier or "fp32"
+    tier_id = km.ASSIGN_BF16 if tier == "bf16" else km.ASSIGN_FP32
+
+    X, _, _ = mixture_torch(N, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+    idx = torch.from_numpy(sample_init(N, K, seed=99)).cuda()
+    init = X[idx].cpu().numpy()
+    h = km.Handle(N, D, K, assign_tier=tier_id, max_iters=args.steps + args.warmup)
+    h.set_data(X, True)
+    h.set_centers(init, False)
+    h.run(args.warmup)
+    h.synchronize()
+
+    stream = torch.cuda.ExternalStream(h.stream)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    h.set_profiling(True)
+    launches0 = km.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    ev0.record(stream)
+    h.run(args.steps)
+    ev1.record(stream)
+    h.synchronize()
+    torch.cuda.synchronize()
+    cl = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = km.launch_count() - launches0
+    phase, piters = h.phase_ms()
+    st = h.stats()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * args.steps / (ms / 1000.0)
+
+    flop = 2.0 * N * K * D
+    assign_ms = phase[1] / max(piters, 1)
+    achieved = flop / (assign_ms / 1000.0) / 1e12
+    bf16_peak, hbm_peak, src = peaks()
+    roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
+                "frac": achieved / bf16_peak, "traffic": None,
+                "kernel": "assign_bf16_tc" if tier == "bf16" else "assign_fp32_kernel",
+                "peak_source": f"{src} bf16 dense (MEASURED_PEAKS.json)",
+                "flop_per_launch": flop, "ms_per_launch": assign_ms}
+
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        Xh = X.cpu().numpy()
+        del X
+        torch.cuda.empty_cache()
+        t0 = time.perf_counter()
+        res = km.lloyd(Xh, K, init=init, max_iters=args.steps, assign_tier=tier_id)
+        t1 = time.perf_counter()
+        e2e = {"value": args.steps / (t1 - t0), "unit": "iter/s",
+               "h2d_bytes_per_step": (Xh.nbytes + init.nbytes) // args.steps,
+               "d2h_bytes_per_step": (res.centers.nbytes + res.labels.nbytes + res.sse.nbytes)
+               // args.steps,
+               "call": "kmgb_lloyd_f32 (host pageable X, init, centers/labels/SSE out)",
+               "seconds": t1 - t0}
+    cb = None
+    if not args.no_cpu and rank == 0:
+        cb = cpu_baseline(1)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16" if tier == "bf16" else "f32", "data": "synthetic",
+                "config": {"workload": "lloyd_4Mx128_K1024", "n": N, "d": D, "k": K,
+                           "tier": tier, "certified_labels": True,
+                           "l2": "inputs larger than L2 (X: 2.05 GB FP32 per pass)",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "assign_tflops": achieved,
+                "phase_ms_per_iter": {n: p / max(piters, 1) for n, p in
+                                      zip(["prep", "assign", "rerank", "update"], phase)},
+                "reranked_points_total": st.reranked, "reranked_fp64_total": st.reranked_fp64,
+                "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+                "gpu_launches": launches, "clocks": cl}
+        print(json.dumps(line), flush=True)
+    h.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

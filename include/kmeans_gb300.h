@@ -1,0 +1,244 @@
+/*
+ * kmeans_gb300 -- C-ABI of the GB300 (sm_103a) K-means Lloyd hot path.
+ *
+ * Drop-in boundary for PaulMullowney/kmeans. Three groups of entry points, all `extern "C"`
+ * with plain pointers and sizes:
+ *
+ *  1. The reference's public driver API (main/cpp/kmeans.hpp:44-132): computeKmeansF,
+ *     computeKmeansD, kmeansGetErrorString, with the same signatures, enum values and the same
+ *     D x K ("K fastest") layout of `result`.
+ *  2. The reference's per-kernel API (main/cuda/KmeansCudaKernels.h:174-474): device-pointer
+ *     entry points with the same names, argument meaning and kmeansCudaErrorStatus codes.
+ *  3. An extension (kmgb_*) that the reference cannot express: explicit initial centers,
+ *     labels and per-iteration SSE out, precision tier selection, a resident handle for
+ *     repeated runs, and statistics.
+ *
+ * Everything runs on the calling thread's current CUDA device.
+ */
+#ifndef KMEANS_GB300_H_
+#define KMEANS_GB300_H_
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define KMGB_EXPORT __attribute__((visibility("default")))
+#else
+#define KMGB_EXPORT
+#endif
+
+#if defined(__cplusplus)
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------------
+ * 1. Reference driver API
+ * ------------------------------------------------------------------------------------- */
+
+/* Same names and values as the reference (main/cpp/kmeans.hpp:44-59). */
+typedef enum kmeansErrorStatus {
+  KMEANS_SUCCESS = 0,
+  KMEANS_ERROR_BUILDDATA = 1,
+  KMEANS_ERROR_INITIALIZE = 2,
+  KMEANS_ERROR_CLOSEST_CENTERS = 3,
+  KMEANS_ERROR_CLUSTER_CENTERS = 4,
+  KMEANS_ERROR_COMPACTNESS = 5,
+  KMEANS_ERROR_TRANSPOSE = 6,
+  KMEANS_ERROR_RESET = 7,
+  KMEANS_ERROR_COMPUTE = 8,
+  KMEANS_ERROR_GET_CENTERS = 9,
+  KMEANS_ERROR_TILING = 10,
+  KMEANS_ERROR_COPY_TILE = 11,
+  KMEANS_ERROR_CONSTRUCT_MINIBATCH = 12,
+  KMEANS_NONCONVERGENCE = 13
+} kmeansErrorStatus;
+
+/* Replaces kmeansGetErrorString (main/cpp/kmeans.hpp:66-82); same strings. */
+KMGB_EXPORT const char* kmeansGetErrorString(kmeansErrorStatus err);
+
+/* Replaces computeKmeansF (main/cpp/kmeans.hpp:102-107, main/cpp/kmeans.cpp:1316-1361).
+ * data: host, m x n row-major. result: host, n x k with result[j*k + i] = dim j of center i;
+ * it receives the initial centers, then the final centers. The data are shuffled with
+ * std::shuffle(default_random_engine(0)) and the initial centers picked with srand(42)/rand()
+ * exactly as the reference does. numRetries and initAlgorithm are accepted and ignored (the
+ * reference ignores them too); doFullSGEMM (0/1/2) and matrixFormat (0/1) are accepted and
+ * all map to the same fused assignment. miniBatchFraction < 1 selects the reference's
+ * sliding mini-batch windows. Returns KMEANS_NONCONVERGENCE (13) when the relative SSE change
+ * is still above `criterion` after maxIters iterations (criterion < 0 always runs maxIters). */
+KMGB_EXPORT kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, const int k,
+                                 const float criterion, const int maxIters,
+                                 const int numRetries, const int initAlgorithm,
+                                 const int doFullSGEMM, const int matrixFormat, float* result,
+                                 const float miniBatchFraction);
+
+/* Replaces computeKmeansD (main/cpp/kmeans.hpp:127-132, main/cpp/kmeans.cpp:1364-1409). */
+KMGB_EXPORT kmeansErrorStatus computeKmeansD(const double* data, const int m, const int n, const int k,
+                                 const double criterion, const int maxIters,
+                                 const int numRetries, const int initAlgorithm,
+                                 const int doFullSGEMM, const int matrixFormat, double* result,
+                                 const double miniBatchFraction);
+
+/* ---------------------------------------------------------------------------------------
+ * 2. Reference per-kernel API (device pointers, asynchronous on the default stream)
+ * ------------------------------------------------------------------------------------- */
+
+/* Same names and values as main/cuda/KmeansCudaKernels.h:174-183. */
+typedef enum kmeansCudaErrorStatus {
+  NO_ERROR = 0,
+  ERROR_MATMATMULT = 1,
+  ERROR_ROWTRANSFORMMINIMUM = 2,
+  ERROR_CLOSESTCENTERS = 3,
+  ERROR_CLUSTERCENTERS = 4,
+  ERROR_COMPACTNESS = 5,
+  ERROR_ROWNORMALIZE = 6,
+  ERROR_COLNORMALIZE = 7
+} kmeansCudaErrorStatus;
+
+/* Replaces ClosestCentersF (KmeansCudaKernels.h:238-244, ClosestCenters.cu:392-403).
+ * A: nRowsA x nColsA row-major; B: nColsA x nColsB (centers are columns, K fastest);
+ * CindicesFinal[m0 + i] = arg-min_j normColsOfB_squared[j] - 2 A_i.B_j, lowest j on ties,
+ * equal to the FP64 evaluation of that expression. Bpadded, normRowsOfA_squared, nColsC, C and
+ * Cindices are the reference's scratch arguments: accepted, not required (may be NULL). */
+KMGB_EXPORT kmeansCudaErrorStatus ClosestCentersF(const int m0, const int nRowsA, const int nColsA,
+                                      const float* A, const int nColsB, const float* B,
+                                      float* Bpadded, const float* normRowsOfA_squared,
+                                      const float* normColsOfB_squared, const int nColsC,
+                                      float* C, int* Cindices, int* CindicesFinal);
+/* Replaces ClosestCentersD (KmeansCudaKernels.h:267-273): FP64 data, exact FP64 arg-min. */
+KMGB_EXPORT kmeansCudaErrorStatus ClosestCentersD(const int m0, const int nRowsA, const int nColsA,
+                                      const double* A, const int nColsB, const double* B,
+                                      double* Bpadded, const double* normRowsOfA_squared,
+                                      const double* normColsOfB_squared, const int nColsC,
+                                      double* C, int* Cindices, int* CindicesFinal);
+
+/* Replace rowTransformMinimumF/D (KmeansCudaKernels.h:290-313, RowTransformMinimum.cu:3-99):
+ * output[m0+i] = arg-min_j normA[i] + normB[j] - 2 input[i*n+j], evaluated with the reference's
+ * expression and rounding, lowest j on ties. normA is indexed from the start of the tile as in
+ * the reference (RowTransformMinimum.cu:21). */
+KMGB_EXPORT kmeansCudaErrorStatus rowTransformMinimumF(const int m0, const int m, const int n,
+                                           const float* normRowsOfA_squared,
+                                           const float* normColsOfB_squared, const float* input,
+                                           int* output);
+KMGB_EXPORT kmeansCudaErrorStatus rowTransformMinimumD(const int m0, const int m, const int n,
+                                           const double* normRowsOfA_squared,
+                                           const double* normColsOfB_squared,
+                                           const double* input, int* output);
+
+/* Replace ClusterCentersF/D (KmeansCudaKernels.h:337-369, ClusterCenters.cu:101-188):
+ * data: m x n rows of the tile, indices[m0 + i] their labels. Sums accumulate across calls
+ * in counts_large/centers_large (K ints / K x n FP64 values viewed through the caller's
+ * buffers, which must hold at least K x n doubles and K ints); on lastTile the means are written
+ * to centers (K x n row-major, NaN for an empty cluster) and the member counts to counts. */
+KMGB_EXPORT kmeansCudaErrorStatus ClusterCentersF(const int m0, const int m, const int n, const int k,
+                                      const bool lastTile, const float* data, const int* indices,
+                                      float* centers_large, int* counts_large, float* centers,
+                                      int* counts);
+KMGB_EXPORT kmeansCudaErrorStatus ClusterCentersD(const int m0, const int m, const int n, const int k,
+                                      const bool lastTile, const double* data, const int* indices,
+                                      double* centers_large, int* counts_large, double* centers,
+                                      int* counts);
+
+/* Replace CompactnessF/D (KmeansCudaKernels.h:389-414, Compactness.cu:258-327): the squared
+ * distance of every row to centers[indices[m0+i]] (K x n row-major) is added to a running FP64
+ * total kept inside the caller's buffer (compactness[2..3] viewed as one double for F,
+ * compactness[1] for D; the caller zeroes the buffer before the first tile, as the reference's
+ * reset does); on lastTile compactness[0] receives the total. */
+KMGB_EXPORT kmeansCudaErrorStatus CompactnessF(const int m0, const int m, const bool lastTile, const int n,
+                                   const int k, const float* data, const int* indices,
+                                   const float* centers, float* compactness);
+KMGB_EXPORT kmeansCudaErrorStatus CompactnessD(const int m0, const int m, const bool lastTile, const int n,
+                                   const int k, const double* data, const int* indices,
+                                   const double* centers, double* compactness);
+
+/* Replace rowNormalizeF/D and colNormalizeF/D (KmeansCudaKernels.h:428-474,
+ * Normalize.cu:3-47): squared L2 norm of each row (output[m0+i]) / of each column of an m x n
+ * matrix, accumulated in FP64 and rounded once. */
+KMGB_EXPORT kmeansCudaErrorStatus rowNormalizeF(const int m0, const int m, const int n, const float* input,
+                                    float* output);
+KMGB_EXPORT kmeansCudaErrorStatus rowNormalizeD(const int m0, const int m, const int n, const double* input,
+                                    double* output);
+KMGB_EXPORT kmeansCudaErrorStatus colNormalizeF(const int m, const int n, const float* input, float* output);
+KMGB_EXPORT kmeansCudaErrorStatus colNormalizeD(const int m, const int n, const double* input,
+                                    double* output);
+
+/* ---------------------------------------------------------------------------------------
+ * 3. Extension (no counterpart in the reference ABI, which returns neither labels nor SSE)
+ * ------------------------------------------------------------------------------------- */
+
+enum kmgb_assign_tier {
+  KMGB_ASSIGN_FP32 = 0, /* plain FP32 fused kernel (TMA + FFMA) */
+  KMGB_ASSIGN_BF16 = 1  /* tcgen05 BF16 tensor cores, FP32 accumulate in TMEM */
+};
+
+enum kmgb_empty_policy {
+  KMGB_EMPTY_NAN = 0, /* reference behaviour: 0/0 = NaN center (ClusterCenters.cu:81) */
+  KMGB_EMPTY_KEEP = 1 /* keep the previous center */
+};
+
+typedef struct kmgb_options {
+  int assign_tier;           /* kmgb_assign_tier */
+  int certify;               /* 1: labels equal the FP64 arg-min (margin test + re-rank) */
+  int empty_policy;          /* kmgb_empty_policy */
+  int max_iters;             /* iterations (upper bound when criterion >= 0) */
+  double criterion;          /* stop when |dSSE|/SSE <= criterion; < 0: run max_iters */
+  float mini_batch_fraction; /* < 1: reference mini-batch windows of (int)(f*m) rows */
+  int reserved[8];
+} kmgb_options;
+
+typedef struct kmgb_stats {
+  int iterations;
+  int status;                      /* kmeansErrorStatus of the run */
+  unsigned long long reranked;     /* points sent to the exact re-rank (all iterations) */
+  unsigned long long reranked_fp64;/* of those, points that needed the FP64 evaluation */
+  long long empty_clusters;        /* empty clusters seen after the last update */
+  double ms_total;                 /* wall time of the iterations (CUDA events) */
+  long long reserved[8];
+} kmgb_stats;
+
+/* Defaults: FP32 tier, certify on, NaN policy, 20 iterations, criterion -1, full batch. */
+KMGB_EXPORT void kmgb_default_options(kmgb_options* opt);
+
+/* One-shot Lloyd run. X: n x d row-major FP32 (host or device pointer). init: k x d row-major
+ * initial centers (host or device), or NULL for the reference initialisation. Outputs (host or
+ * device, each may be NULL): centers k x d row-major, labels[n] of the last assignment
+ * (source-row order; -1 outside the last mini-batch window), sse[max_iters] per iteration
+ * (FP64, against the updated centers, as the reference's compactness). */
+KMGB_EXPORT int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
+                   const kmgb_options* opt, float* centers, int* labels, double* sse,
+                   kmgb_stats* stats);
+
+/* Resident handle: data uploaded once, iterations run on the handle's own stream. */
+typedef struct kmgb_handle kmgb_handle;
+KMGB_EXPORT int kmgb_create(kmgb_handle** h, long long n, int d, int k, const kmgb_options* opt);
+KMGB_EXPORT int kmgb_set_data(kmgb_handle* h, const float* X, int x_on_device);
+KMGB_EXPORT int kmgb_set_centers(kmgb_handle* h, const float* C, int c_on_device); /* NULL: reference init */
+/* Runs up to `iters` iterations from the current centers (asynchronous when criterion < 0). */
+KMGB_EXPORT int kmgb_run(kmgb_handle* h, int iters, double criterion);
+KMGB_EXPORT int kmgb_synchronize(kmgb_handle* h);
+KMGB_EXPORT int kmgb_get_centers(kmgb_handle* h, float* C, int c_on_device);
+KMGB_EXPORT int kmgb_get_labels(kmgb_handle* h, int* labels, int on_device);
+KMGB_EXPORT int kmgb_get_sse(kmgb_handle* h, double* sse, int max_count); /* returns the count written */
+KMGB_EXPORT int kmgb_get_stats(kmgb_handle* h, kmgb_stats* stats);
+KMGB_EXPORT void* kmgb_stream(kmgb_handle* h); /* cudaStream_t of the handle */
+KMGB_EXPORT int kmgb_destroy(kmgb_handle* h);
+
+/* Phase timing: with profiling on, CUDA events on the handle's stream bracket every phase of
+ * every iteration. kmgb_get_phase_ms waits for the stream and returns, summed over the
+ * iterations run since the previous call, ms[0] center preparation, ms[1] assignment kernel,
+ * ms[2] exact re-rank, ms[3] update (sort, sums, SSE); *iters = iterations covered. */
+KMGB_EXPORT int kmgb_set_profiling(kmgb_handle* h, int on);
+KMGB_EXPORT int kmgb_get_phase_ms(kmgb_handle* h, double* ms, int* iters);
+/* Kernels launched by this library since the process started. */
+KMGB_EXPORT long long kmgb_launch_count(void);
+
+/* Last error message of the calling thread (empty string if none). */
+KMGB_EXPORT const char* kmgb_last_error(void);
+/* Library constants: piece size of the canonical FP64 center sums, version. */
+KMGB_EXPORT int kmgb_sum_piece(void);
+KMGB_EXPORT const char* kmgb_version(void);
+
+#if defined(__cplusplus)
+}
+#endif
+
+#endif /* KMEANS_GB300_H_ */

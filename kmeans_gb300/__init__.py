@@ -1,0 +1,372 @@
+"""kmeans_gb300: GB300-native (sm_103a) K-means Lloyd hot path.
+
+Python mirror of the reference's interfaces (PaulMullowney/kmeans):
+
+* ``computeKmeansF`` / ``computeKmeansD`` -- the reference driver entry points
+  (main/cpp/kmeans.hpp:102-132) with the same arguments, return codes and D x K result layout;
+* ``ClosestCentersF``, ``rowTransformMinimumF/D``, ``ClusterCentersF/D``, ``CompactnessF/D``,
+  ``rowNormalizeF/D``, ``colNormalizeF/D`` -- the per-kernel entry points
+  (main/cuda/KmeansCudaKernels.h:198-474) on device pointers;
+* ``lloyd`` / ``Handle`` -- the extension: explicit initial centers, labels, per-iteration SSE,
+  precision tier, resident data.
+
+Everything calls the in-tree C-ABI library ``libkmeans_gb300.so`` through ctypes. There is no
+CPU fallback: if the library is missing or no GPU is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libkmeans_gb300.so")
+HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "kmeans_gb300.h")
+
+KMEANS_SUCCESS = 0
+KMEANS_NONCONVERGENCE = 13
+ASSIGN_FP32 = 0
+ASSIGN_BF16 = 1
+EMPTY_NAN = 0
+EMPTY_KEEP = 1
+
+ERROR_STRINGS = {
+    1: "error in building the data",
+    2: "error in the initialization",
+    3: "error in computing the closest centers",
+    4: "error in computing the cluster centers",
+    5: "error in computing the compactness",
+    6: "error in transpose",
+    7: "error in reset",
+    8: "error in compute",
+    9: "error in copying the data back to the host",
+    10: "error in the tiling",
+    11: "error in copy tile",
+    12: "error in constructing the minibatch",
+    13: "algorithm did not converge",
+}
+
+
+class KmeansError(RuntimeError):
+    def __init__(self, code: int, msg: str = ""):
+        super().__init__(f"kmeans_gb300 error {code}: {ERROR_STRINGS.get(code, 'no error')}"
+                         + (f" ({msg})" if msg else ""))
+        self.code = code
+
+
+class kmgb_options(C.Structure):
+    _fields_ = [("assign_tier", C.c_int), ("certify", C.c_int), ("empty_policy", C.c_int),
+                ("max_iters", C.c_int), ("criterion", C.c_double),
+                ("mini_batch_fraction", C.c_float), ("reserved", C.c_int * 8)]
+
+
+class kmgb_stats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("reranked", C.c_ulonglong),
+                ("reranked_fp64", C.c_ulonglong), ("empty_clusters", C.c_longlong),
+                ("ms_total", C.c_double), ("reserved", C.c_longlong * 8)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the CUDA library for sm_103a (nvcc) if needed."""
+    return _build.build(force=force)
+
+
+def lib():
+    """Load libkmeans_gb300.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: run kmeans_gb300.build() (nvcc, sm_103a)")
+        L = C.CDLL(LIB_PATH)
+        P, i32, i64, f32, f64 = C.c_void_p, C.c_int, C.c_longlong, C.c_float, C.c_double
+        b = C.c_bool
+        sig = {
+            "kmeansGetErrorString": (C.c_char_p, [i32]),
+            "computeKmeansF": (i32, [P, i32, i32, i32, f32, i32, i32, i32, i32, i32, P, f32]),
+            "computeKmeansD": (i32, [P, i32, i32, i32, f64, i32, i32, i32, i32, i32, P, f64]),
+            "ClosestCentersF": (i32, [i32, i32, i32, P, i32, P, P, P, P, i32, P, P, P]),
+            "ClosestCentersD": (i32, [i32, i32, i32, P, i32, P, P, P, P, i32, P, P, P]),
+            "rowTransformMinimumF": (i32, [i32, i32, i32, P, P, P, P]),
+            "rowTransformMinimumD": (i32, [i32, i32, i32, P, P, P, P]),
+            "ClusterCentersF": (i32, [i32, i32, i32, i32, b, P, P, P, P, P, P]),
+            "ClusterCentersD": (i32, [i32, i32, i32, i32, b, P, P, P, P, P, P]),
+            "CompactnessF": (i32, [i32, i32, b, i32, i32, P, P, P, P]),
+            "CompactnessD": (i32, [i32, i32, b, i32, i32, P, P, P, P]),
+            "rowNormalizeF": (i32, [i32, i32, i32, P, P]),
+            "rowNormalizeD": (i32, [i32, i32, i32, P, P]),
+            "colNormalizeF": (i32, [i32, i32, P, P]),
+            "colNormalizeD": (i32, [i32, i32, P, P]),
+            "kmgb_default_options": (None, [P]),
+            "kmgb_lloyd_f32": (i32, [P, i64, i32, i32, P, P, P, P, P, P]),
+            "kmgb_create": (i32, [P, i64, i32, i32, P]),
+            "kmgb_set_data": (i32, [P, P, i32]),
+            "kmgb_set_centers": (i32, [P, P, i32]),
+            "kmgb_run": (i32, [P, i32, f64]),
+            "kmgb_synchronize": (i32, [P]),
+            "kmgb_get_centers": (i32, [P, P, i32]),
+            "kmgb_get_labels": (i32, [P, P, i32]),
+            "kmgb_get_sse": (i32, [P, P, i32]),
+            "kmgb_get_stats": (i32, [P, P]),
+            "kmgb_stream": (P, [P]),
+            "kmgb_destroy": (i32, [P]),
+            "kmgb_last_error": (C.c_char_p, []),
+            "kmgb_set_profiling": (i32, [P, i32]),
+            "kmgb_get_phase_ms": (i32, [P, P, P]),
+            "kmgb_launch_count": (i64, []),
+            "kmgb_sum_piece": (i32, []),
+            "kmgb_version": (C.c_char_p, []),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def launch_count() -> int:
+    return int(lib().kmgb_launch_count())
+
+
+def last_error() -> str:
+    return lib().kmgb_last_error().decode()
+
+
+def default_options(**kw) -> kmgb_options:
+    o = kmgb_options()
+    lib().kmgb_default_options(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def _ptr(a) -> Optional[int]:
+    """Address of a numpy array (host) or a torch tensor (device or host)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())
+
+
+# ----------------------------------------------------------------------------------------
+# reference driver API
+# ----------------------------------------------------------------------------------------
+
+def computeKmeansF(data: np.ndarray, m: int, n: int, k: int, criterion: float, maxIters: int,
+                   numRetries: int, initAlgorithm: int, doFullSGEMM: int, matrixFormat: int,
+                   result: np.ndarray, miniBatchFraction: float = 1.0) -> int:
+    """Same arguments and return code as the reference (kmeans.hpp:102-107); `result` (n*k
+    float32, K fastest) receives the final centers."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    assert result.dtype == np.float32 and result.flags.c_contiguous and result.size >= n * k
+    return int(lib().computeKmeansF(_ptr(data), m, n, k, criterion, maxIters, numRetries,
+                                    initAlgorithm, doFullSGEMM, matrixFormat, _ptr(result),
+                                    miniBatchFraction))
+
+
+def computeKmeansD(data: np.ndarray, m: int, n: int, k: int, criterion: float, maxIters: int,
+                   numRetries: int, initAlgorithm: int, doFullSGEMM: int, matrixFormat: int,
+                   result: np.ndarray, miniBatchFraction: float = 1.0) -> int:
+    data = np.ascontiguousarray(data, dtype=np.float64)
+    assert result.dtype == np.float64 and result.flags.c_contiguous and result.size >= n * k
+    return int(lib().computeKmeansD(_ptr(data), m, n, k, criterion, maxIters, numRetries,
+                                    initAlgorithm, doFullSGEMM, matrixFormat, _ptr(result),
+                                    miniBatchFraction))
+
+
+def kmeansGetErrorString(err: int) -> str:
+    return lib().kmeansGetErrorString(err).decode()
+
+
+# ----------------------------------------------------------------------------------------
+# per-kernel API (device tensors; torch is used only as device memory)
+# ----------------------------------------------------------------------------------------
+
+def ClosestCentersF(m0, nRowsA, nColsA, A, nColsB, B, Bpadded, normRowsOfA_squared,
+                    normColsOfB_squared, nColsC, Cpart, Cindices, CindicesFinal) -> int:
+    return int(lib().ClosestCentersF(m0, nRowsA, nColsA, _ptr(A), nColsB, _ptr(B), _ptr(Bpadded),
+                                     _ptr(normRowsOfA_squared), _ptr(normColsOfB_squared),
+                                     nColsC, _ptr(Cpart), _ptr(Cindices), _ptr(CindicesFinal)))
+
+
+def ClosestCentersD(m0, nRowsA, nColsA, A, nColsB, B, Bpadded, normRowsOfA_squared,
+                    normColsOfB_squared, nColsC, Cpart, Cindices, CindicesFinal) -> int:
+    return int(lib().ClosestCentersD(m0, nRowsA, nColsA, _ptr(A), nColsB, _ptr(B), _ptr(Bpadded),
+                                     _ptr(normRowsOfA_squared), _ptr(normColsOfB_squared),
+                                     nColsC, _ptr(Cpart), _ptr(Cindices), _ptr(CindicesFinal)))
+
+
+def rowTransformMinimumF(m0, m, n, normA, normB, inp, out) -> int:
+    return int(lib().rowTransformMinimumF(m0, m, n, _ptr(normA), _ptr(normB), _ptr(inp), _ptr(out)))
+
+
+def rowTransformMinimumD(m0, m, n, normA, normB, inp, out) -> int:
+    return int(lib().rowTransformMinimumD(m0, m, n, _ptr(normA), _ptr(normB), _ptr(inp), _ptr(out)))
+
+
+def ClusterCentersF(m0, m, n, k, lastTile, data, indices, centers_large, counts_large, centers,
+                    counts) -> int:
+    return int(lib().ClusterCentersF(m0, m, n, k, bool(lastTile), _ptr(data), _ptr(indices),
+                                     _ptr(centers_large), _ptr(counts_large), _ptr(centers),
+                                     _ptr(counts)))
+
+
+def ClusterCentersD(m0, m, n, k, lastTile, data, indices, centers_large, counts_large, centers,
+                    counts) -> int:
+    return int(lib().ClusterCentersD(m0, m, n, k, bool(lastTile), _ptr(data), _ptr(indices),
+                                     _ptr(centers_large), _ptr(counts_large), _ptr(centers),
+                                     _ptr(counts)))
+
+
+def CompactnessF(m0, m, lastTile, n, k, data, indices, centers, compactness) -> int:
+    return int(lib().CompactnessF(m0, m, bool(lastTile), n, k, _ptr(data), _ptr(indices),
+                                  _ptr(centers), _ptr(compactness)))
+
+
+def CompactnessD(m0, m, lastTile, n, k, data, indices, centers, compactness) -> int:
+    return int(lib().CompactnessD(m0, m, bool(lastTile), n, k, _ptr(data), _ptr(indices),
+                                  _ptr(centers), _ptr(compactness)))
+
+
+def rowNormalizeF(m0, m, n, inp, out) -> int:
+    return int(lib().rowNormalizeF(m0, m, n, _ptr(inp), _ptr(out)))
+
+
+def rowNormalizeD(m0, m, n, inp, out) -> int:
+    return int(lib().rowNormalizeD(m0, m, n, _ptr(inp), _ptr(out)))
+
+
+def colNormalizeF(m, n, inp, out) -> int:
+    return int(lib().colNormalizeF(m, n, _ptr(inp), _ptr(out)))
+
+
+def colNormalizeD(m, n, inp, out) -> int:
+    return int(lib().colNormalizeD(m, n, _ptr(inp), _ptr(out)))
+
+
+# ----------------------------------------------------------------------------------------
+# extension
+# ----------------------------------------------------------------------------------------
+
+@dataclass
+class LloydResult:
+    status: int
+    centers: np.ndarray
+    labels: np.ndarray
+    sse: np.ndarray
+    iterations: int
+    reranked: int
+    reranked_fp64: int
+    empty_clusters: int
+    ms_total: float
+
+
+def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
+          assign_tier: int = ASSIGN_FP32, certify: bool = True, empty_policy: int = EMPTY_NAN,
+          mini_batch_fraction: float = 1.0) -> LloydResult:
+    """One-shot Lloyd run through kmgb_lloyd_f32. X: numpy (host) or torch (device) n x d
+    float32; init: k x d float32 or None (reference initialisation)."""
+    if isinstance(X, np.ndarray):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+    n, d = X.shape
+    if init is not None and isinstance(init, np.ndarray):
+        init = np.ascontiguousarray(init, dtype=np.float32)
+    opt = default_options(assign_tier=assign_tier, certify=int(certify),
+                          empty_policy=empty_policy, max_iters=max_iters, criterion=criterion,
+                          mini_batch_fraction=mini_batch_fraction)
+    cen = np.empty((k, d), dtype=np.float32)
+    lab = np.empty(n, dtype=np.int32)
+    sse = np.zeros(max(max_iters, 1), dtype=np.float64)
+    st = kmgb_stats()
+    rc = lib().kmgb_lloyd_f32(_ptr(X), n, d, k, _ptr(init), C.byref(opt), _ptr(cen), _ptr(lab),
+                              _ptr(sse), C.byref(st))
+    if rc not in (KMEANS_SUCCESS, KMEANS_NONCONVERGENCE):
+        raise KmeansError(rc, last_error())
+    return LloydResult(rc, cen, lab, sse[:st.iterations], st.iterations, st.reranked,
+                       st.reranked_fp64, st.empty_clusters, st.ms_total)
+
+
+class Handle:
+    """Resident data set + centers; iterations run on the handle's own CUDA stream."""
+
+    def __init__(self, n: int, d: int, k: int, **opts):
+        self._h = C.c_void_p()
+        o = default_options(**opts)
+        rc = lib().kmgb_create(C.byref(self._h), n, d, k, C.byref(o))
+        if rc:
+            raise KmeansError(rc, last_error())
+        self.n, self.d, self.k = n, d, k
+
+    def _chk(self, rc):
+        if rc not in (KMEANS_SUCCESS,):
+            raise KmeansError(rc, last_error())
+
+    def set_data(self, X, on_device: bool):
+        self._chk(lib().kmgb_set_data(self._h, _ptr(X), int(on_device)))
+
+    def set_centers(self, Cn=None, on_device: bool = False):
+        self._chk(lib().kmgb_set_centers(self._h, _ptr(Cn), int(on_device)))
+
+    def run(self, iters: int, criterion: float = -1.0):
+        self._chk(lib().kmgb_run(self._h, iters, criterion))
+
+    def synchronize(self):
+        self._chk(lib().kmgb_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(lib().kmgb_stream(self._h) or 0)
+
+    def centers(self) -> np.ndarray:
+        out = np.empty((self.k, self.d), dtype=np.float32)
+        self._chk(lib().kmgb_get_centers(self._h, _ptr(out), 0))
+        return out
+
+    def labels(self) -> np.ndarray:
+        out = np.empty(self.n, dtype=np.int32)
+        self._chk(lib().kmgb_get_labels(self._h, _ptr(out), 0))
+        return out
+
+    def sse(self, count: int) -> np.ndarray:
+        out = np.zeros(max(count, 1), dtype=np.float64)
+        c = lib().kmgb_get_sse(self._h, _ptr(out), count)
+        return out[:c]
+
+    def stats(self) -> kmgb_stats:
+        st = kmgb_stats()
+        self._chk(lib().kmgb_get_stats(self._h, C.byref(st)))
+        return st
+
+    def set_profiling(self, on: bool = True):
+        self._chk(lib().kmgb_set_profiling(self._h, int(on)))
+
+    def phase_ms(self):
+        """(ms[prep, assign, rerank, update] summed, iterations covered)."""
+        ms = (C.c_double * 4)()
+        it = C.c_int(0)
+        self._chk(lib().kmgb_get_phase_ms(self._h, ms, C.byref(it)))
+        return list(ms), it.value
+
+    def close(self):
+        if self._h:
+            lib().kmgb_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

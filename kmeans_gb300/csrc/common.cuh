@@ -1,0 +1,138 @@
+// Shared device/host helpers for the GB300 (sm_103a) Lloyd kernels.
+//
+// Every wait on an mbarrier is bounded: a wait gives up after KMGB_WAIT_NS nanoseconds of
+// %globaltimer, records an error code in the launch's error word and returns false; an abort
+// flag in shared memory then makes every later wait of the CTA return at once so the CTA
+// drains and exits (no unbounded spin, no __trap).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#ifndef KMGB_WAIT_NS
+#define KMGB_WAIT_NS 2000000000ull  // 2 s per wait
+#endif
+
+// Error codes written to the device error word (first writer wins).
+enum kmgb_dev_error {
+  KMGB_DEV_OK = 0,
+  KMGB_DEV_TIMEOUT_FULL = 1,     // consumer waited too long for a TMA stage
+  KMGB_DEV_TIMEOUT_EMPTY = 2,    // producer waited too long for a free stage
+  KMGB_DEV_TIMEOUT_ACC = 3,      // MMA / epilogue accumulator hand-off timed out
+  KMGB_DEV_BAD_LABEL = 4,        // a label outside [0, K) reached the update
+  KMGB_DEV_BAD_SHAPE = 5,
+};
+
+namespace kmgb {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void set_error(int* err, int code) {
+  if (err) atomicCAS(err, 0, code);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait. `abort_flag` is a CTA-shared word: once set, waits return false at once.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                          int* err, int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  while (true) {
+    if (*abort_flag) return false;
+    if (mbar_try_wait(bar, parity)) return true;
+    if (globaltimer() - t0 > KMGB_WAIT_NS) {
+      *abort_flag = 1;
+      set_error(err, code);
+      return false;
+    }
+  }
+}
+
+// 2-D TMA tile load into shared memory, completion signalled on `bar` (complete_tx bytes).
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar,
+                                            int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tmap(const CUtensorMap* map) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
+}
+
+// Byte offset of the 16-byte chunk `chunk` of row `row` inside a tile written by TMA with
+// CU_TENSOR_MAP_SWIZZLE_128B (rows of 128 bytes, tile base 1024-byte aligned): the chunk index
+// is XOR-ed with the row index modulo 8.
+__device__ __forceinline__ uint32_t swz128(uint32_t row, uint32_t chunk) {
+  return row * 128u + ((chunk ^ (row & 7u)) << 4);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+}  // namespace kmgb
+
+// Host-side: 2-D row-major tensor map (inner dim = columns) with 128-byte swizzle.
+// dtype: CU_TENSOR_MAP_DATA_TYPE_FLOAT32 or _BFLOAT16. Returns cudaSuccess or an error.
+cudaError_t kmgb_make_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype,
+                              int elem_bytes, uint64_t cols, uint64_t rows, uint64_t row_stride_bytes,
+                              uint32_t box_cols, uint32_t box_rows);
+
+// Number of kernels this library has launched (process-wide), for launch accounting.
+namespace kmgb {
+void count_launches(long long n);
+long long launch_count();
+}  // namespace kmgb
+
+#define KMGB_CUDA_TRY(expr)                        \
+  do {                                             \
+    cudaError_t _e = (expr);                       \
+    if (_e != cudaSuccess) return _e;              \
+  } while (0)

@@ -1,0 +1,752 @@
+// Host engine of the GB300 Lloyd hot path: the resident handle, the iteration pipeline, the
+// reference initialisation and the reference-compatible driver entry points.
+//
+// Replaces the reference's kmeans<TYPE> driver (main/cpp/kmeans.hpp:174-658,
+// main/cpp/kmeans.cpp:3-1409). Differences by design:
+//   * one stream per handle, no per-step host synchronisation (the reference brackets every
+//     step with cudaEventSynchronize, kmeans.hpp:158-171); the host only reads the SSE back when
+//     a convergence criterion >= 0 has to be evaluated;
+//   * 64-bit sizes and offsets throughout (the reference overflows int once m*n > 2^31,
+//     kmeans.cpp:561,710,761);
+//   * centers kept K x D row-major on the device (no cublasSgeam transpose, kmeans.cpp:1108-1139);
+//     the D x K layout exists only at the computeKmeansF boundary;
+//   * the update needs O(K*D) FP64 partials per piece instead of G*K*D privatised sums
+//     (kmeans.cpp:597-599), so the full data set stays resident for every configuration that
+//     fits in HBM.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/kmeans_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace kmgb;
+
+namespace kmgb {
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace kmgb
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_err(const char* where, cudaError_t e) {
+  g_last_error = std::string(where) + ": " + cudaGetErrorString(e);
+}
+void set_err(const std::string& msg) { g_last_error = msg; }
+
+#define KM_TRY(expr, code)                      \
+  do {                                          \
+    cudaError_t _e = (expr);                    \
+    if (_e != cudaSuccess) {                    \
+      set_err(#expr, _e);                       \
+      return (code);                            \
+    }                                           \
+  } while (0)
+
+long long round_up(long long v, long long m) { return (v + m - 1) / m * m; }
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
+}
+
+bool is_device_ptr(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+}  // namespace
+
+// Reference shuffle permutation (kmeans.cpp:554-557): perm[i] = source row of shuffled row i.
+static void reference_perm(int m, std::vector<int>& perm) {
+  perm.resize(m);
+  for (int i = 0; i < m; ++i) perm[i] = i;
+  unsigned seed = 0;
+  std::shuffle(perm.begin(), perm.end(), std::default_random_engine(seed));
+}
+
+// Reference initial picks (kmeans.cpp:876-883): srand(42), rand() % m, redrawn while
+// binary_search over the unsorted pick list finds the index. glibc random_r with a private
+// TYPE_3 state seeded with 42 yields the srand(42)/rand() stream without touching the
+// process-wide generator.
+static bool reference_picks(int m, int k, std::vector<int>& picks) {
+  if (m <= 0 || k <= 0 || k > m) return false;
+  struct random_data rd;
+  std::memset(&rd, 0, sizeof(rd));
+  std::vector<char> state(128, 0);
+  if (initstate_r(42u, state.data(), state.size(), &rd) != 0) return false;
+  picks.clear();
+  picks.reserve(k);
+  for (int i = 0; i < k; ++i) {
+    int32_t r = 0;
+    random_r(&rd, &r);
+    int index = r % m;
+    while (std::binary_search(picks.begin(), picks.end(), index)) {
+      random_r(&rd, &r);
+      index = r % m;
+    }
+    picks.push_back(index);
+  }
+  return true;
+}
+
+struct kmgb_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  long long n = 0;  // rows of the data set
+  int d = 0, k = 0;
+  long long ldx = 0;  // FP32 row stride (multiple of 4)
+  long long ldb = 0;  // BF16 row stride (multiple of 8)
+  kmgb_options opt;
+  bool mini = false;
+  long long m_mb = 0;  // rows per mini-batch window
+  long long n_act = 0; // rows processed per iteration
+  int iter_base = 0;   // iterations already run (mini-batch window index)
+
+  // data set
+  float* X = nullptr;
+  void* Xb = nullptr;
+  double* qn = nullptr;
+  float* xn = nullptr;
+  bool have_data = false;
+  // mini-batch windows
+  int* perm = nullptr;
+  float* Xw = nullptr;
+  void* Xbw = nullptr;
+  double* qnw = nullptr;
+  float* xnw = nullptr;
+  // centers
+  float* C = nullptr;
+  float* Cop = nullptr;
+  void* Cb = nullptr;
+  float* cn = nullptr;
+  float* cmax = nullptr;
+  bool have_centers = false;
+  // assignment
+  int* labels = nullptr;
+  int* rr_list = nullptr;
+  int* rr_count = nullptr;
+  unsigned long long* rr_stats = nullptr;
+  int* err = nullptr;
+  // update
+  UpdateWork uw{};
+  double* sse_dev = nullptr;
+  int sse_cap = 0;
+  std::vector<double> sse_host;
+  double* sse_pinned = nullptr;
+  int iterations = 0;
+  int status = 0;
+  double ms_total = 0.0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // phase profiling: 5 events per iteration
+  bool prof = false;
+  std::vector<cudaEvent_t> pev;
+  int pused = 0;
+
+  cudaError_t pmark(int slot) {
+    if (!prof) return cudaSuccess;
+    const size_t idx = (size_t)pused * 5 + slot;
+    while (pev.size() <= idx) {
+      cudaEvent_t e;
+      cudaError_t r = cudaEventCreate(&e);
+      if (r != cudaSuccess) return r;
+      pev.push_back(e);
+    }
+    return cudaEventRecord(pev[idx], stream);
+  }
+
+  ~kmgb_handle() {
+    for (cudaEvent_t e : pev) cudaEventDestroy(e);
+    void* ptrs[] = {X, Xb, qn, xn, perm, Xw, Xbw, qnw, xnw, C, Cop, Cb, cn, cmax, labels,
+                    rr_list, rr_count, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
+                    uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev};
+    for (void* p : ptrs)
+      if (p) cudaFree(p);
+    if (sse_pinned) cudaFreeHost(sse_pinned);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_options* opt) {
+  *out = nullptr;
+  if (n <= 0 || d <= 0 || k <= 0) {
+    set_err("kmgb_create: n, d and k must be positive");
+    return KMEANS_ERROR_BUILDDATA;
+  }
+  if (n >= 0x7fffffffLL) {
+    set_err("kmgb_create: n must be below 2^31-1 rows per resident data set");
+    return KMEANS_ERROR_BUILDDATA;
+  }
+  kmgb_handle* h = new kmgb_handle();
+  if (opt) h->opt = *opt;
+  else kmgb_default_options(&h->opt);
+  if (h->opt.assign_tier == KMGB_ASSIGN_BF16 && !bf16_tc_supported(d)) {
+    delete h;
+    set_err("kmgb_create: the BF16 tensor-core tier does not support this dimension");
+    return KMEANS_ERROR_BUILDDATA;
+  }
+  cudaGetDevice(&h->device);
+  h->n = n;
+  h->d = d;
+  h->k = k;
+  h->ldx = round_up(d, 4);
+  h->ldb = round_up(d, 8);
+  h->mini = h->opt.mini_batch_fraction < 1.0f;
+  if (h->mini) {
+    // (int)(fraction * m) in float arithmetic as kmeans.cpp:79
+    h->m_mb = (long long)(int)(h->opt.mini_batch_fraction * (float)n);
+    if (h->m_mb <= 0) {
+      delete h;
+      set_err("kmgb_create: mini-batch window is empty");
+      return KMEANS_ERROR_TILING;
+    }
+  }
+  h->n_act = h->mini ? h->m_mb : n;
+  const bool bf16 = h->opt.assign_tier == KMGB_ASSIGN_BF16;
+  const int code = KMEANS_ERROR_BUILDDATA;
+  KM_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), (delete h, code));
+  KM_TRY(cudaEventCreate(&h->ev0), (delete h, code));
+  KM_TRY(cudaEventCreate(&h->ev1), (delete h, code));
+  KM_TRY(dalloc(&h->X, (size_t)n * h->ldx), (delete h, code));
+  KM_TRY(dalloc(&h->qn, n), (delete h, code));
+  KM_TRY(dalloc(&h->xn, n), (delete h, code));
+  if (bf16) KM_TRY(cudaMalloc(&h->Xb, (size_t)n * h->ldb * 2), (delete h, code));
+  if (h->mini) {
+    KM_TRY(dalloc(&h->perm, n), (delete h, code));
+    KM_TRY(dalloc(&h->Xw, (size_t)h->m_mb * h->ldx), (delete h, code));
+    KM_TRY(dalloc(&h->qnw, h->m_mb), (delete h, code));
+    KM_TRY(dalloc(&h->xnw, h->m_mb), (delete h, code));
+    if (bf16) KM_TRY(cudaMalloc(&h->Xbw, (size_t)h->m_mb * h->ldb * 2), (delete h, code));
+  }
+  KM_TRY(dalloc(&h->C, (size_t)k * h->ldx), (delete h, code));
+  KM_TRY(dalloc(&h->Cop, (size_t)k * h->ldx), (delete h, code));
+  if (bf16) KM_TRY(cudaMalloc(&h->Cb, (size_t)k * h->ldb * 2), (delete h, code));
+  KM_TRY(dalloc(&h->cn, k), (delete h, code));
+  KM_TRY(dalloc(&h->cmax, 1), (delete h, code));
+  const long long na = h->n_act;
+  KM_TRY(dalloc(&h->labels, na), (delete h, code));
+  KM_TRY(dalloc(&h->rr_list, na), (delete h, code));
+  KM_TRY(dalloc(&h->rr_count, 1), (delete h, code));
+  KM_TRY(dalloc(&h->rr_stats, 2), (delete h, code));
+  KM_TRY(dalloc(&h->err, 1), (delete h, code));
+  KM_TRY(cudaMemset(h->labels, 0, sizeof(int) * na), (delete h, code));
+  KM_TRY(cudaMemset(h->rr_stats, 0, sizeof(unsigned long long) * 2), (delete h, code));
+  KM_TRY(cudaMemset(h->err, 0, sizeof(int)), (delete h, code));
+  // update work space
+  UpdateWork& w = h->uw;
+  w.n = na;
+  w.k = k;
+  w.d = d;
+  w.ldx = h->ldx;
+  plan_update_tiles(na, k, &w.tile_pts, &w.ntiles);
+  w.max_pieces = na / kSumPiece + k + 1;
+  const long long hist_elems = (long long)k * w.ntiles;
+  KM_TRY(dalloc(&w.hist, hist_elems), (delete h, code));
+  KM_TRY(dalloc(&w.scan_tmp, update_scan_tmp_elems(std::max<long long>(hist_elems, k + 1))),
+         (delete h, code));
+  KM_TRY(dalloc(&w.label_off, k + 1), (delete h, code));
+  KM_TRY(dalloc(&w.piece_cnt, k + 1), (delete h, code));
+  KM_TRY(dalloc(&w.sorted, na), (delete h, code));
+  KM_TRY(dalloc(&w.part, (size_t)w.max_pieces * d), (delete h, code));
+  KM_TRY(dalloc(&w.partq, w.max_pieces), (delete h, code));
+  KM_TRY(dalloc(&w.sse_k, k), (delete h, code));
+  KM_TRY(dalloc(&w.counts, k), (delete h, code));
+  w.err = h->err;
+  h->sse_cap = std::max(1, h->opt.max_iters);
+  KM_TRY(dalloc(&h->sse_dev, h->sse_cap), (delete h, code));
+  KM_TRY(cudaMallocHost(&h->sse_pinned, sizeof(double)), (delete h, code));
+  *out = h;
+  return 0;
+}
+
+// Upload (or copy) the data set and compute its per-point norms and BF16 copy.
+int set_data(kmgb_handle* h, const float* X, bool on_device) {
+  const int code = KMEANS_ERROR_BUILDDATA;
+  const size_t row_bytes = sizeof(float) * h->d;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (h->ldx == h->d) {
+    KM_TRY(cudaMemcpyAsync(h->X, X, row_bytes * h->n, kind, h->stream), code);
+  } else {
+    KM_TRY(cudaMemsetAsync(h->X, 0, sizeof(float) * h->ldx * h->n, h->stream), code);
+    KM_TRY(cudaMemcpy2DAsync(h->X, sizeof(float) * h->ldx, X, row_bytes, row_bytes, h->n, kind,
+                             h->stream),
+           code);
+  }
+  KM_TRY(launch_point_norms(h->X, h->ldx, h->n, h->d, h->qn, h->xn, h->stream), code);
+  if (h->Xb) KM_TRY(launch_to_bf16(h->X, h->ldx, h->n, h->d, h->Xb, h->ldb, h->stream), code);
+  if (h->mini) {
+    std::vector<int> perm;
+    reference_perm((int)h->n, perm);
+    KM_TRY(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * h->n, cudaMemcpyHostToDevice,
+                           h->stream),
+           code);
+    KM_TRY(cudaStreamSynchronize(h->stream), code);  // perm is a stack buffer
+  }
+  h->have_data = true;
+  h->iter_base = 0;
+  return 0;
+}
+
+// Window start of mini-batch iteration `it` (kmeans.cpp:426-447: += m_mb, wrap past m).
+long long window_start(long long m, long long m_mb, int it) {
+  long long s = 0;
+  for (int t = 0; t < it; ++t) {
+    s += m_mb;
+    if (s > m) s %= m;
+    else if (s == m) s = 0;
+  }
+  return s;
+}
+
+// One Lloyd iteration on the handle's stream; SSE lands in sse_dev[slot].
+int step(kmgb_handle* h, int slot) {
+  cudaStream_t s = h->stream;
+  const float* Xa = h->X;
+  const void* Xba = h->Xb;
+  const double* qna = h->qn;
+  const float* xna = h->xn;
+  if (h->mini) {
+    const long long st = window_start(h->n, h->m_mb, h->iter_base);
+    KM_TRY(launch_gather_rows(h->X, h->ldx, h->perm, h->n, st, h->m_mb, h->d, h->Xw, h->ldx, s),
+           KMEANS_ERROR_CONSTRUCT_MINIBATCH);
+    KM_TRY(launch_gather_vec(h->qn, h->xn, h->perm, h->n, st, h->m_mb, h->qnw, h->xnw, s),
+           KMEANS_ERROR_CONSTRUCT_MINIBATCH);
+    if (h->Xbw)
+      KM_TRY(launch_to_bf16(h->Xw, h->ldx, h->m_mb, h->d, h->Xbw, h->ldb, s),
+             KMEANS_ERROR_CONSTRUCT_MINIBATCH);
+    Xa = h->Xw;
+    Xba = h->Xbw;
+    qna = h->qnw;
+    xna = h->xnw;
+  }
+  const long long na = h->n_act;
+  KM_TRY(h->pmark(0), KMEANS_ERROR_RESET);
+  // reset (kmeans.cpp:1142-1170): norms of the current centers, cleared counters
+  KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
+  KM_TRY(cudaMemsetAsync(h->rr_count, 0, sizeof(int), s), KMEANS_ERROR_RESET);
+  KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s),
+         KMEANS_ERROR_RESET);
+  KM_TRY(h->pmark(1), KMEANS_ERROR_RESET);
+  // closest centers (kmeans.cpp:910-1014)
+  AssignArgs a{};
+  a.cn = h->cn;
+  a.xnorm = xna;
+  a.cmax = h->cmax;
+  a.labels = h->labels;
+  a.rerank_list = h->rr_list;
+  a.rerank_count = h->rr_count;
+  a.err = h->err;
+  a.n = na;
+  a.k = h->k;
+  a.d = h->d;
+  a.certify = h->opt.certify;
+  if (h->opt.assign_tier == KMGB_ASSIGN_BF16) {
+    a.gamma = assign_bf16_gamma(h->d);
+    KM_TRY(launch_assign_bf16(Xba, h->ldb, h->Cb, h->ldb, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
+  } else {
+    a.gamma = assign_fp32_gamma(h->d);
+    KM_TRY(launch_assign_fp32(Xa, h->ldx, h->Cop, h->ldx, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
+  }
+  KM_TRY(h->pmark(2), KMEANS_ERROR_CLOSEST_CENTERS);
+  if (h->opt.certify) {
+    RerankArgs r{};
+    r.X = Xa;
+    r.ldx = h->ldx;
+    r.C = h->Cop;
+    r.ldc = h->ldx;
+    r.cn = h->cn;
+    r.list = h->rr_list;
+    r.count = h->rr_count;
+    r.labels = h->labels;
+    r.stats = h->rr_stats;
+    r.n = na;
+    r.k = h->k;
+    r.d = h->d;
+    r.mode = 0;
+    r.max_list = na;
+    KM_TRY(launch_rerank(r, s), KMEANS_ERROR_CLOSEST_CENTERS);
+  }
+  KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
+  // cluster centers + compactness (kmeans.cpp:1018-1104)
+  KM_TRY(launch_update(Xa, qna, h->labels, h->C, h->ldx, h->opt.empty_policy, h->uw,
+                       h->sse_dev + slot, s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  KM_TRY(h->pmark(4), KMEANS_ERROR_CLUSTER_CENTERS);
+  if (h->prof) ++h->pused;
+  return 0;
+}
+
+int run(kmgb_handle* h, int iters, double criterion) {
+  if (!h->have_data || !h->have_centers) {
+    set_err("kmgb_run: data and centers must be set first");
+    return KMEANS_ERROR_COMPUTE;
+  }
+  if (iters > h->sse_cap) {
+    double* nd = nullptr;
+    KM_TRY(dalloc(&nd, iters), KMEANS_ERROR_COMPUTE);
+    cudaFree(h->sse_dev);
+    h->sse_dev = nd;
+    h->sse_cap = iters;
+  }
+  h->sse_host.assign(std::max(iters, 0), 0.0);
+  KM_TRY(cudaEventRecord(h->ev0, h->stream), KMEANS_ERROR_COMPUTE);
+  double sse_old = 0.0, rel = 1.0;
+  int it = 0;
+  while (it < iters && rel > criterion) {
+    int rc = step(h, it);
+    if (rc) return rc;
+    ++h->iter_base;
+    if (criterion >= 0.0) {
+      KM_TRY(cudaMemcpyAsync(h->sse_pinned, h->sse_dev + it, sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream),
+             KMEANS_ERROR_COMPACTNESS);
+      KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);
+      const double sse = *h->sse_pinned;
+      rel = std::fabs(sse - sse_old) / std::fabs(sse);
+      sse_old = sse;
+    }
+    ++it;
+  }
+  KM_TRY(cudaEventRecord(h->ev1, h->stream), KMEANS_ERROR_COMPUTE);
+  h->iterations = it;
+  // kmeans.hpp:198-200: success only when relErr <= criterion, which never holds for
+  // criterion < 0 (fixed-iteration runs return KMEANS_NONCONVERGENCE).
+  h->status = (criterion >= 0.0 && rel <= criterion) ? KMEANS_SUCCESS : KMEANS_NONCONVERGENCE;
+  return 0;
+}
+
+int finish(kmgb_handle* h) {
+  KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);
+  int e = 0;
+  KM_TRY(cudaMemcpy(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPUTE);
+  if (e) {
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), "device error word %d (see kmgb_dev_error)", e);
+    set_err(buf);
+    return e == KMGB_DEV_BAD_LABEL ? KMEANS_ERROR_CLUSTER_CENTERS : KMEANS_ERROR_CLOSEST_CENTERS;
+  }
+  float ms = 0.f;
+  if (h->iterations > 0 && cudaEventElapsedTime(&ms, h->ev0, h->ev1) == cudaSuccess)
+    h->ms_total = ms;
+  if (h->iterations > 0) {
+    KM_TRY(cudaMemcpy(h->sse_host.data(), h->sse_dev, sizeof(double) * h->iterations,
+                      cudaMemcpyDeviceToHost),
+           KMEANS_ERROR_COMPACTNESS);
+  }
+  return 0;
+}
+
+int reference_init_host(kmgb_handle* h, const float* data_host, std::vector<float>& init_kxd) {
+  std::vector<int> perm, picks;
+  if (!reference_picks((int)h->n, h->k, picks)) {
+    set_err("reference initialisation needs 0 < k <= m");
+    return KMEANS_ERROR_INITIALIZE;
+  }
+  reference_perm((int)h->n, perm);
+  init_kxd.resize((size_t)h->k * h->d);
+  for (int i = 0; i < h->k; ++i)
+    std::memcpy(&init_kxd[(size_t)i * h->d], data_host + (size_t)perm[picks[i]] * h->d,
+                sizeof(float) * h->d);
+  return 0;
+}
+
+int set_centers(kmgb_handle* h, const float* C, bool on_device) {
+  const size_t row_bytes = sizeof(float) * h->d;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  KM_TRY(cudaMemsetAsync(h->C, 0, sizeof(float) * h->ldx * h->k, h->stream),
+         KMEANS_ERROR_INITIALIZE);
+  KM_TRY(cudaMemcpy2DAsync(h->C, sizeof(float) * h->ldx, C, row_bytes, row_bytes, h->k, kind,
+                           h->stream),
+         KMEANS_ERROR_INITIALIZE);
+  if (!on_device) KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_INITIALIZE);
+  h->have_centers = true;
+  return 0;
+}
+
+int get_centers(kmgb_handle* h, float* out, bool on_device) {
+  const size_t row_bytes = sizeof(float) * h->d;
+  KM_TRY(cudaMemcpy2DAsync(out, row_bytes, h->C, sizeof(float) * h->ldx, row_bytes, h->k,
+                           on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                           h->stream),
+         KMEANS_ERROR_GET_CENTERS);
+  KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_GET_CENTERS);
+  return 0;
+}
+
+// Labels of the last assignment in source-row order.
+int get_labels(kmgb_handle* h, int* out, bool on_device) {
+  KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_GET_CENTERS);
+  if (!h->mini) {
+    KM_TRY(cudaMemcpy(out, h->labels, sizeof(int) * h->n,
+                      on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost),
+           KMEANS_ERROR_GET_CENTERS);
+    return 0;
+  }
+  // mini-batch: scatter the last window's labels to their source rows, -1 elsewhere
+  std::vector<int> win(h->m_mb), perm;
+  KM_TRY(cudaMemcpy(win.data(), h->labels, sizeof(int) * h->m_mb, cudaMemcpyDeviceToHost),
+         KMEANS_ERROR_GET_CENTERS);
+  reference_perm((int)h->n, perm);
+  std::vector<int> full(h->n, -1);
+  const long long st = window_start(h->n, h->m_mb, std::max(0, h->iter_base - 1));
+  for (long long r = 0; r < h->m_mb; ++r) {
+    long long pos = st + r;
+    if (pos >= h->n) pos -= h->n;
+    full[perm[pos]] = win[r];
+  }
+  KM_TRY(cudaMemcpy(out, full.data(), sizeof(int) * h->n,
+                    on_device ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost),
+         KMEANS_ERROR_GET_CENTERS);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void kmgb_default_options(kmgb_options* opt) {
+  std::memset(opt, 0, sizeof(*opt));
+  opt->assign_tier = KMGB_ASSIGN_FP32;
+  opt->certify = 1;
+  opt->empty_policy = KMGB_EMPTY_NAN;
+  opt->max_iters = 20;
+  opt->criterion = -1.0;
+  opt->mini_batch_fraction = 1.0f;
+}
+
+const char* kmgb_last_error(void) { return g_last_error.c_str(); }
+int kmgb_sum_piece(void) { return kSumPiece; }
+const char* kmgb_version(void) { return "kmeans_gb300 0.1 (sm_103a)"; }
+
+int kmgb_create(kmgb_handle** h, long long n, int d, int k, const kmgb_options* opt) {
+  return create_handle(h, n, d, k, opt);
+}
+
+int kmgb_set_data(kmgb_handle* h, const float* X, int x_on_device) {
+  if (!h || !X) return KMEANS_ERROR_BUILDDATA;
+  return set_data(h, X, x_on_device != 0);
+}
+
+int kmgb_set_centers(kmgb_handle* h, const float* C, int c_on_device) {
+  if (!h) return KMEANS_ERROR_INITIALIZE;
+  if (C) return set_centers(h, C, c_on_device != 0);
+  // reference initialisation from the resident data (needs a host copy of the picked rows)
+  std::vector<int> perm, picks;
+  if (!reference_picks((int)h->n, h->k, picks)) {
+    set_err("reference initialisation needs 0 < k <= m");
+    return KMEANS_ERROR_INITIALIZE;
+  }
+  reference_perm((int)h->n, perm);
+  std::vector<float> init((size_t)h->k * h->d);
+  KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_INITIALIZE);
+  for (int i = 0; i < h->k; ++i)
+    KM_TRY(cudaMemcpy(&init[(size_t)i * h->d], h->X + (size_t)perm[picks[i]] * h->ldx,
+                      sizeof(float) * h->d, cudaMemcpyDeviceToHost),
+           KMEANS_ERROR_INITIALIZE);
+  return set_centers(h, init.data(), false);
+}
+
+int kmgb_run(kmgb_handle* h, int iters, double criterion) {
+  if (!h) return KMEANS_ERROR_COMPUTE;
+  return run(h, iters, criterion);
+}
+
+int kmgb_synchronize(kmgb_handle* h) {
+  if (!h) return KMEANS_ERROR_COMPUTE;
+  return finish(h);
+}
+
+int kmgb_get_centers(kmgb_handle* h, float* C, int c_on_device) {
+  if (!h || !C) return KMEANS_ERROR_GET_CENTERS;
+  return get_centers(h, C, c_on_device != 0);
+}
+
+int kmgb_get_labels(kmgb_handle* h, int* labels, int on_device) {
+  if (!h || !labels) return KMEANS_ERROR_GET_CENTERS;
+  return get_labels(h, labels, on_device != 0);
+}
+
+int kmgb_get_sse(kmgb_handle* h, double* sse, int max_count) {
+  if (!h || !sse) return 0;
+  const int c = std::min<int>(max_count, (int)h->sse_host.size());
+  const int cnt = std::min(c, h->iterations);
+  for (int i = 0; i < cnt; ++i) sse[i] = h->sse_host[i];
+  return cnt;
+}
+
+int kmgb_get_stats(kmgb_handle* h, kmgb_stats* st) {
+  if (!h || !st) return KMEANS_ERROR_COMPUTE;
+  std::memset(st, 0, sizeof(*st));
+  st->iterations = h->iterations;
+  st->status = h->status;
+  st->ms_total = h->ms_total;
+  unsigned long long rs[2] = {0, 0};
+  KM_TRY(cudaMemcpy(rs, h->rr_stats, sizeof(rs), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPUTE);
+  st->reranked = rs[0];
+  st->reranked_fp64 = rs[1];
+  std::vector<long long> cnt(h->k);
+  KM_TRY(cudaMemcpy(cnt.data(), h->uw.counts, sizeof(long long) * h->k, cudaMemcpyDeviceToHost),
+         KMEANS_ERROR_COMPUTE);
+  long long e = 0;
+  for (long long c : cnt) e += (c == 0);
+  st->empty_clusters = e;
+  return 0;
+}
+
+void* kmgb_stream(kmgb_handle* h) { return h ? (void*)h->stream : nullptr; }
+
+int kmgb_set_profiling(kmgb_handle* h, int on) {
+  if (!h) return KMEANS_ERROR_COMPUTE;
+  h->prof = on != 0;
+  h->pused = 0;
+  return 0;
+}
+
+int kmgb_get_phase_ms(kmgb_handle* h, double* ms, int* iters) {
+  if (!h || !ms) return KMEANS_ERROR_COMPUTE;
+  KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);
+  for (int p = 0; p < 4; ++p) ms[p] = 0.0;
+  for (int i = 0; i < h->pused; ++i)
+    for (int p = 0; p < 4; ++p) {
+      float t = 0.f;
+      KM_TRY(cudaEventElapsedTime(&t, h->pev[(size_t)i * 5 + p], h->pev[(size_t)i * 5 + p + 1]),
+             KMEANS_ERROR_COMPUTE);
+      ms[p] += t;
+    }
+  if (iters) *iters = h->pused;
+  h->pused = 0;
+  return 0;
+}
+
+long long kmgb_launch_count(void) { return launch_count(); }
+
+int kmgb_destroy(kmgb_handle* h) {
+  delete h;
+  return 0;
+}
+
+int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
+                   const kmgb_options* opt, float* centers, int* labels, double* sse,
+                   kmgb_stats* stats) {
+  kmgb_options o;
+  if (opt) o = *opt;
+  else kmgb_default_options(&o);
+  if (!X) return KMEANS_ERROR_BUILDDATA;
+  kmgb_handle* h = nullptr;
+  int rc = create_handle(&h, n, d, k, &o);
+  if (rc) return rc;
+  const bool x_dev = is_device_ptr(X);
+  rc = set_data(h, X, x_dev);
+  if (!rc) {
+    if (init) {
+      rc = set_centers(h, init, is_device_ptr(init));
+    } else if (!x_dev) {
+      std::vector<float> ini;
+      rc = reference_init_host(h, X, ini);
+      if (!rc) rc = set_centers(h, ini.data(), false);
+    } else {
+      rc = kmgb_set_centers(h, nullptr, 0);
+    }
+  }
+  if (!rc) rc = run(h, o.max_iters, o.criterion);
+  if (!rc) rc = finish(h);
+  if (!rc && centers) rc = get_centers(h, centers, is_device_ptr(centers));
+  if (!rc && labels) rc = get_labels(h, labels, is_device_ptr(labels));
+  if (!rc && sse) kmgb_get_sse(h, sse, o.max_iters);
+  if (stats) {
+    if (kmgb_get_stats(h, stats) != 0) std::memset(stats, 0, sizeof(*stats));
+    if (rc) stats->status = rc;
+  }
+  const int status = h->status;
+  delete h;
+  if (rc) return rc;
+  return status;
+}
+
+const char* kmeansGetErrorString(kmeansErrorStatus err) {
+  switch (err) {
+    case KMEANS_ERROR_BUILDDATA: return "error in building the data";
+    case KMEANS_ERROR_INITIALIZE: return "error in the initialization";
+    case KMEANS_ERROR_CLOSEST_CENTERS: return "error in computing the closest centers";
+    case KMEANS_ERROR_CLUSTER_CENTERS: return "error in computing the cluster centers";
+    case KMEANS_ERROR_COMPACTNESS: return "error in computing the compactness";
+    case KMEANS_ERROR_TRANSPOSE: return "error in transpose";
+    case KMEANS_ERROR_RESET: return "error in reset";
+    case KMEANS_ERROR_COMPUTE: return "error in compute";
+    case KMEANS_ERROR_GET_CENTERS: return "error in copying the data back to the host";
+    case KMEANS_ERROR_TILING: return "error in the tiling";
+    case KMEANS_ERROR_COPY_TILE: return "error in copy tile";
+    case KMEANS_ERROR_CONSTRUCT_MINIBATCH: return "error in constructing the minibatch";
+    case KMEANS_NONCONVERGENCE: return "algorithm did not converge";
+    default: return "no error";
+  }
+}
+
+kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, const int k,
+                                 const float criterion, const int maxIters,
+                                 const int numRetries, const int initAlgorithm,
+                                 const int doFullSGEMM, const int matrixFormat, float* result,
+                                 const float miniBatchFraction) {
+  (void)numRetries;
+  (void)initAlgorithm;
+  if (!data || !result || m <= 0 || n <= 0 || k <= 0) return KMEANS_ERROR_BUILDDATA;
+  if (doFullSGEMM < 0 || doFullSGEMM > 2 || matrixFormat < 0 || matrixFormat > 1)
+    return KMEANS_ERROR_BUILDDATA;
+  if (k > m) return KMEANS_ERROR_INITIALIZE;
+  kmgb_options o;
+  kmgb_default_options(&o);
+  const char* tier = std::getenv("KMGB_ASSIGN");
+  if (tier && std::strcmp(tier, "bf16") == 0 && bf16_tc_supported(n)) o.assign_tier = KMGB_ASSIGN_BF16;
+  o.max_iters = maxIters < 0 ? 0 : maxIters;
+  o.criterion = criterion;
+  o.mini_batch_fraction = miniBatchFraction;
+  kmgb_handle* h = nullptr;
+  int rc = create_handle(&h, m, n, k, &o);
+  if (rc) return (kmeansErrorStatus)rc;
+  rc = set_data(h, data, false);
+  std::vector<float> init;
+  if (!rc) rc = reference_init_host(h, data, init);
+  if (!rc) {
+    // the reference writes the initial centers into result (kmeans.cpp:886-888)
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < n; ++j) result[(size_t)j * k + i] = init[(size_t)i * n + j];
+    rc = set_centers(h, init.data(), false);
+  }
+  if (!rc) rc = run(h, o.max_iters, (double)criterion);
+  if (!rc) rc = finish(h);
+  std::vector<float> fin;
+  if (!rc) {
+    fin.resize((size_t)k * n);
+    rc = get_centers(h, fin.data(), false);
+  }
+  if (!rc) {
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < n; ++j) result[(size_t)j * k + i] = fin[(size_t)i * n + j];
+  }
+  const int status = h->status;
+  delete h;
+  if (rc) return (kmeansErrorStatus)rc;
+  return (kmeansErrorStatus)status;
+}
+
+}  // extern "C"

@@ -1,0 +1,264 @@
+// computeKmeansD: the reference's double-precision driver entry (main/cpp/kmeans.cpp:1364-1409).
+//
+// The reference's FP64 custom assignment is broken (its partial reduction for double2 is an
+// empty function, main/cuda/reduction.hcu:7-11, so every label becomes 0); only its cuBLAS path
+// (cublasDgemm + rowTransformMinimumD, kmeans.cpp:958-993) defines FP64 behaviour. This path
+// computes what that one intends, exactly: label = FP64 arg-min of sum_d (x_d - c_d)^2 (lowest
+// index on ties), centers = canonical FP64 sums / counts, SSE in FP64 against the new centers.
+// FP64 throughput on GB300 is low (about 1.25 TFLOP/s), so this is the correctness path, not a
+// fast one; every kernel is plain SIMT.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "../../include/kmeans_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace kmgb;
+
+namespace {
+
+// CT[t][j] = C[j][t]
+__global__ void transpose_d_kernel(const double* __restrict__ C, int k, int d, double* __restrict__ CT) {
+  const long long total = (long long)k * d;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e / d), t = (int)(e % d);
+    CT[(size_t)t * k + j] = C[e];
+  }
+}
+
+// One warp per point, lanes over centers (coalesced reads of CT); exact FP64 direct distance.
+__global__ void assign_d_kernel(const double* __restrict__ X, long long n, int d,
+                                const double* __restrict__ CT, int k, int* __restrict__ labels) {
+  extern __shared__ double xs_all[];
+  const int warps = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* xs = xs_all + (size_t)w * d;
+  for (long long i = (long long)blockIdx.x * warps + w; i < n; i += (long long)gridDim.x * warps) {
+    for (int t = lane; t < d; t += 32) xs[t] = X[(size_t)i * d + t];
+    __syncwarp();
+    double best = INFINITY;
+    int bi = -1;
+    for (int j = lane; j < k; j += 32) {
+      double s = 0.0;
+      for (int t = 0; t < d; ++t) {
+        const double u = xs[t] - CT[(size_t)t * k + j];
+        s = fma(u, u, s);
+      }
+      if (s < best) {
+        best = s;
+        bi = j;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      const bool take = (ob < best) || (ob == best && (unsigned)oi < (unsigned)bi);
+      best = take ? ob : best;
+      bi = take ? oi : bi;
+    }
+    if (lane == 0) labels[i] = bi < 0 ? 0 : bi;
+    __syncwarp();
+  }
+}
+
+__global__ void sse_d_partial_kernel(const double* __restrict__ X, long long n, int d,
+                                     const int* __restrict__ lab, const double* __restrict__ C,
+                                     double* __restrict__ partial) {
+  __shared__ double red[8];
+  const int warps = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double acc = 0.0;
+  for (long long i = (long long)blockIdx.x * warps + w; i < n; i += (long long)gridDim.x * warps) {
+    const int l = lab[i];
+    double s = 0.0;
+    for (int t = lane; t < d; t += 32) {
+      const double u = X[(size_t)i * d + t] - C[(size_t)l * d + t];
+      s = fma(u, u, s);
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    acc += s;
+  }
+  if (lane == 0) red[w] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < warps; ++i) t += red[i];
+    partial[blockIdx.x] = t;
+  }
+}
+
+__global__ void sse_d_final_kernel(const double* __restrict__ partial, int nb, double* out) {
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int i = 0; i < nb; ++i) t += partial[i];
+    *out = t;
+  }
+}
+
+__global__ void gather_d_kernel(const double* __restrict__ X, int d, const int* __restrict__ perm,
+                                long long m, long long start, long long m_mb, double* __restrict__ Xw) {
+  const long long total = m_mb * d;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long r = e / d;
+    long long pos = start + r;
+    if (pos >= m) pos -= m;
+    Xw[e] = X[(size_t)perm[pos] * d + (e % d)];
+  }
+}
+
+struct DevBufs {
+  std::vector<void*> ptrs;
+  ~DevBufs() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  cudaError_t alloc(T** p, size_t count) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess) ptrs.push_back(*p);
+    return e;
+  }
+};
+
+#define KD_TRY(expr, code)                \
+  do {                                    \
+    if ((expr) != cudaSuccess) return (code); \
+  } while (0)
+
+kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterion, int maxIters,
+                        double* result, double fraction) {
+  const bool mini = fraction < 1.0;
+  const long long m_mb = mini ? (long long)(int)((float)fraction * (float)m) : m;
+  if (m_mb <= 0) return KMEANS_ERROR_TILING;
+  // reference initialisation on the host (kmeans.cpp:554-564, 876-888)
+  std::vector<int> perm(m);
+  for (int i = 0; i < m; ++i) perm[i] = i;
+  {
+    unsigned seed = 0;
+    std::shuffle(perm.begin(), perm.end(), std::default_random_engine(seed));
+  }
+  std::vector<int> picks;
+  {
+    struct random_data rd;
+    std::memset(&rd, 0, sizeof(rd));
+    std::vector<char> state(128, 0);
+    if (initstate_r(42u, state.data(), state.size(), &rd) != 0) return KMEANS_ERROR_INITIALIZE;
+    for (int i = 0; i < k; ++i) {
+      int32_t r = 0;
+      random_r(&rd, &r);
+      int index = r % m;
+      while (std::binary_search(picks.begin(), picks.end(), index)) {
+        random_r(&rd, &r);
+        index = r % m;
+      }
+      picks.push_back(index);
+    }
+  }
+  std::vector<double> C((size_t)k * n);
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < n; ++j) {
+      C[(size_t)i * n + j] = data[(size_t)perm[picks[i]] * n + j];
+      result[(size_t)j * k + i] = C[(size_t)i * n + j];
+    }
+
+  DevBufs B;
+  double *X = nullptr, *Xw = nullptr, *Cd = nullptr, *CT = nullptr, *acc = nullptr, *part = nullptr,
+         *sse = nullptr;
+  int *lab = nullptr, *cnt = nullptr, *permd = nullptr;
+  const cudaStream_t s = 0;
+  const kmeansErrorStatus E = KMEANS_ERROR_BUILDDATA;
+  KD_TRY(B.alloc(&X, (size_t)m * n), E);
+  KD_TRY(cudaMemcpy(X, data, sizeof(double) * (size_t)m * n, cudaMemcpyHostToDevice), E);
+  if (mini) {
+    KD_TRY(B.alloc(&Xw, (size_t)m_mb * n), E);
+    KD_TRY(B.alloc(&permd, m), E);
+    KD_TRY(cudaMemcpy(permd, perm.data(), sizeof(int) * m, cudaMemcpyHostToDevice), E);
+  }
+  KD_TRY(B.alloc(&Cd, (size_t)k * n), E);
+  KD_TRY(B.alloc(&CT, (size_t)k * n), E);
+  KD_TRY(B.alloc(&acc, (size_t)k * n), E);
+  KD_TRY(B.alloc(&cnt, k), E);
+  KD_TRY(B.alloc(&lab, m_mb), E);
+  const int sse_blocks = 152 * 4;
+  KD_TRY(B.alloc(&part, sse_blocks), E);
+  KD_TRY(B.alloc(&sse, 1), E);
+  KD_TRY(cudaMemcpy(Cd, C.data(), sizeof(double) * C.size(), cudaMemcpyHostToDevice), E);
+  UpdateWork w{};
+  w.n = m_mb;
+  w.k = k;
+  w.d = n;
+  w.ldx = n;
+  plan_update_tiles(m_mb, k, &w.tile_pts, &w.ntiles);
+  w.max_pieces = m_mb / kSumPiece + k + 1;
+  const long long hist_elems = (long long)k * w.ntiles;
+  KD_TRY(B.alloc(&w.hist, hist_elems), E);
+  KD_TRY(B.alloc(&w.scan_tmp, update_scan_tmp_elems(std::max<long long>(hist_elems, k + 1))), E);
+  KD_TRY(B.alloc(&w.label_off, k + 1), E);
+  KD_TRY(B.alloc(&w.piece_cnt, k + 1), E);
+  KD_TRY(B.alloc(&w.sorted, m_mb), E);
+  KD_TRY(B.alloc(&w.part, (size_t)w.max_pieces * n), E);
+
+  const int threads = 256;
+  const size_t smem = sizeof(double) * n * (threads / 32);
+  if (smem > 200 * 1024) return KMEANS_ERROR_CLOSEST_CENTERS;
+  if (smem > 48 * 1024)
+    KD_TRY(cudaFuncSetAttribute(assign_d_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem),
+           KMEANS_ERROR_CLOSEST_CENTERS);
+  double sse_old = 0.0, rel = 1.0;
+  int it = 0;
+  long long start = 0;
+  while (it < maxIters && rel > criterion) {
+    const double* Xa = X;
+    if (mini) {
+      gather_d_kernel<<<152 * 8, 256, 0, s>>>(X, n, permd, m, start, m_mb, Xw); kmgb::count_launches(1);
+      Xa = Xw;
+    }
+    transpose_d_kernel<<<152 * 4, 256, 0, s>>>(Cd, k, n, CT); kmgb::count_launches(1);
+    assign_d_kernel<<<152 * 8, threads, smem, s>>>(Xa, m_mb, n, CT, k, lab); kmgb::count_launches(1);
+    KD_TRY(cudaGetLastError(), KMEANS_ERROR_CLOSEST_CENTERS);
+    KD_TRY(cudaMemsetAsync(acc, 0, sizeof(double) * (size_t)k * n, s), KMEANS_ERROR_RESET);
+    KD_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * k, s), KMEANS_ERROR_RESET);
+    KD_TRY(launch_tile_accumulate<double>(Xa, n, lab, w, acc, cnt, s), KMEANS_ERROR_CLUSTER_CENTERS);
+    KD_TRY(launch_finalize_acc<double>(acc, cnt, k, n, Cd, nullptr, s), KMEANS_ERROR_CLUSTER_CENTERS);
+    sse_d_partial_kernel<<<sse_blocks, 256, 0, s>>>(Xa, m_mb, n, lab, Cd, part); kmgb::count_launches(1);
+    sse_d_final_kernel<<<1, 32, 0, s>>>(part, sse_blocks, sse); kmgb::count_launches(1);
+    KD_TRY(cudaGetLastError(), KMEANS_ERROR_COMPACTNESS);
+    double h = 0.0;
+    KD_TRY(cudaMemcpy(&h, sse, sizeof(double), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPACTNESS);
+    rel = std::fabs(h - sse_old) / std::fabs(h);
+    sse_old = h;
+    ++it;
+    if (mini) {
+      start += m_mb;
+      if (start > m) start %= m;
+      else if (start == m) start = 0;
+    }
+  }
+  KD_TRY(cudaMemcpy(C.data(), Cd, sizeof(double) * C.size(), cudaMemcpyDeviceToHost),
+         KMEANS_ERROR_GET_CENTERS);
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < n; ++j) result[(size_t)j * k + i] = C[(size_t)i * n + j];
+  return (rel <= criterion) ? KMEANS_SUCCESS : KMEANS_NONCONVERGENCE;
+}
+
+}  // namespace
+
+extern "C" kmeansErrorStatus computeKmeansD(const double* data, const int m, const int n,
+                                            const int k, const double criterion,
+                                            const int maxIters, const int numRetries,
+                                            const int initAlgorithm, const int doFullSGEMM,
+                                            const int matrixFormat, double* result,
+                                            const double miniBatchFraction) {
+  (void)numRetries;
+  (void)initAlgorithm;
+  if (!data || !result || m <= 0 || n <= 0 || k <= 0) return KMEANS_ERROR_BUILDDATA;
+  if (doFullSGEMM < 0 || doFullSGEMM > 2 || matrixFormat < 0 || matrixFormat > 1)
+    return KMEANS_ERROR_BUILDDATA;
+  if (k > m) return KMEANS_ERROR_INITIALIZE;
+  return run_d(data, m, n, k, criterion, maxIters < 0 ? 0 : maxIters, result, miniBatchFraction);
+}

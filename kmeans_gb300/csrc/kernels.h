@@ -1,0 +1,112 @@
+// Internal launch interface of the GB300 Lloyd kernels (not part of the public C-ABI).
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace kmgb {
+
+// Certified assignment: labels plus a list of points whose top-2 margin does not prove the
+// FP64 arg-min. `gamma` is the relative error of the approximate dot product
+// (|fl(x.c) - x.c| <= gamma * ||x|| * ||c||).
+struct AssignArgs {
+  const float* cn;        // [k] ||c_j||^2 rounded to FP32, +inf for unusable (NaN) centers
+  const float* xnorm;     // [n] upper bound of ||x_i||
+  const float* cmax;      // device scalar: upper bound of max ||c_j|| over usable centers
+  int* labels;            // [n]
+  int* rerank_list;       // [n]
+  int* rerank_count;      // device scalar
+  int* err;               // device error word
+  long long n;
+  int k;
+  int d;
+  int certify;            // 0: write arg-min labels only
+  float gamma;
+};
+
+// FP32 SIMT assignment. X: [n][ldx] FP32, Cop: [k][ldc] FP32 (ld multiples of 4 floats).
+cudaError_t launch_assign_fp32(const float* X, long long ldx, const float* Cop, long long ldc,
+                               const AssignArgs& a, cudaStream_t s);
+float assign_fp32_gamma(int d);
+
+// tcgen05 BF16 assignment. Xb: [n][ldb] BF16, Cb: [k][ldb] BF16, ldb a multiple of 8.
+cudaError_t launch_assign_bf16(const void* Xb, long long ldxb, const void* Cb, long long ldcb,
+                               const AssignArgs& a, cudaStream_t s);
+float assign_bf16_gamma(int d);
+bool bf16_tc_supported(int d);
+
+// Exact re-rank of flagged points. mode 0 (Lloyd): FP64 arg-min of sum_d (x_d - c_d)^2.
+// mode 1 (expansion, caller norms): FP64 arg-min of nb_j - 2 x.c_j with the given nb.
+struct RerankArgs {
+  const float* X; long long ldx;
+  const float* C; long long ldc;   // usable-center operand copy (zero rows for NaN centers)
+  const float* cn;                 // [k] +inf marks an unusable center (mode 0)
+  const float* nb;                 // [k] caller norms (mode 1)
+  const float* xnorm;              // [n] (mode 1 bound)
+  const float* cmax;               // (mode 1 bound)
+  const int* list; const int* count;
+  int* labels;
+  unsigned long long* stats;       // [2]: points re-ranked, points that needed FP64
+  long long n; int k; int d;
+  int mode;
+  long long max_list;
+};
+cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s);
+
+// Center preparation: from the official centers C[k][ldc] write the operand copy Cop (NaN
+// rows -> 0), optional BF16 copy Cb[k][ldcb], cn (+inf for NaN rows) and atomically raise
+// *cmax (must be zeroed before).
+cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop,
+                                void* Cb, long long ldcb, float* cn, float* cmax, cudaStream_t s);
+
+// Per-point norms, computed once per data set: qn = ||x||^2 (FP64), xn = upper bound ||x||.
+cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,
+                               float* xn, cudaStream_t s);
+// BF16 copy of the data set (zero padded to ldb columns).
+cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
+                           long long ldb, cudaStream_t s);
+
+// Deterministic update: stable counting sort by label, FP64 piece sums, finalize.
+struct UpdateWork {
+  // sizes
+  long long n; int k; int d; long long ldx; int tile_pts; int ntiles;
+  long long max_pieces;
+  // buffers (device)
+  int* hist;            // [k * ntiles]
+  int* scan_tmp;        // [scan_blocks]
+  int* label_off;       // [k + 1]
+  int* piece_cnt;       // [k + 1] -> exclusive scan = piece start
+  int* sorted;          // [n]
+  double* part;         // [max_pieces * d]
+  double* partq;        // [max_pieces]
+  double* sse_k;        // [k]
+  long long* counts;    // [k]
+  int* err;
+};
+size_t update_scan_tmp_elems(long long elems);
+cudaError_t launch_update(const float* X, const double* qn, const int* labels, float* C,
+                          long long ldc, int empty_policy, const UpdateWork& w, double* sse_out,
+                          cudaStream_t s);
+
+// Per-kernel ABI accumulation across tiles: adds the tile's canonical FP64 per-center sums to
+// acc[k][d] and its member counts to acc_counts[k]; finalize writes acc/count (NaN if empty).
+template <typename T>
+cudaError_t launch_tile_accumulate(const T* X, long long ldx, const int* labels, const UpdateWork& w,
+                                   double* acc, int* acc_counts, cudaStream_t s);
+template <typename T>
+cudaError_t launch_finalize_acc(const double* acc, const int* acc_counts, int k, int d, T* centers,
+                                int* counts, cudaStream_t s);
+void plan_update_tiles(long long n, int k, int* tile_pts, int* ntiles);
+
+// Mini-batch gather: rows perm[(start + r) mod m] of Xsrc into Xdst (m_mb rows).
+cudaError_t launch_gather_rows(const float* Xsrc, long long ldx, const int* perm, long long m,
+                               long long start, long long m_mb, int d, float* Xdst,
+                               long long ldd, cudaStream_t s);
+cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* perm,
+                              long long m, long long start, long long m_mb, double* qdst,
+                              float* xdst, cudaStream_t s);
+
+constexpr int kSumPiece = 128;
+
+}  // namespace kmgb

@@ -1,0 +1,154 @@
+// Per-iteration center preparation and once-per-data-set point preparation.
+//
+// Replaces the reference's colNormalize (main/cuda/Normalize.cu:33-47, run every iteration from
+// kmeans.cpp:1161-1163) and rowNormalize (Normalize.cu:3-31, kmeans.cpp:838-840). Norms are
+// accumulated in FP64 and rounded once; an empty-cluster (NaN) center becomes an unusable
+// center: zero operand row, +inf norm, so it can never win an arg-min (the reference's
+// rowTransformMinimum skips NaN the same way, RowTransformMinimum.cu:31).
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace kmgb {
+namespace {
+
+// One warp per center.
+__global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, int k, int d,
+                                    float* __restrict__ Cop, __nv_bfloat16* __restrict__ Cb,
+                                    long long ldcb, float* __restrict__ cn, float* cmax) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= k) return;
+  const float* c = C + (size_t)warp * ldc;
+  double s = 0.0;
+  bool bad = false;
+  for (int t = lane; t < d; t += 32) {
+    const float v = c[t];
+    bad |= !isfinite(v);
+    s = fma((double)v, (double)v, s);
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  bad = __any_sync(0xffffffffu, bad);
+  float* op = Cop + (size_t)warp * ldc;
+  for (int t = lane; t < (int)ldc; t += 32) op[t] = (bad || t >= d) ? 0.0f : c[t];
+  if (Cb) {
+    __nv_bfloat16* ob = Cb + (size_t)warp * ldcb;
+    for (int t = lane; t < (int)ldcb; t += 32)
+      ob[t] = __float2bfloat16_rn((bad || t >= d) ? 0.0f : c[t]);
+  }
+  if (lane == 0) {
+    if (bad) {
+      cn[warp] = INFINITY;
+    } else {
+      cn[warp] = __double2float_rn(s);
+      // upper bound of ||c||: round the FP64 sqrt up and add a relative margin
+      const float nrm = __double2float_ru(sqrt(s) * (1.0 + 1e-12));
+      atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(nrm));
+    }
+  }
+}
+
+// One warp per point: qn = ||x||^2 in FP64, xn = FP32 upper bound of ||x||.
+__global__ void point_norms_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
+                                   double* __restrict__ qn, float* __restrict__ xn) {
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const float* x = X + (size_t)warp * ldx;
+  double s = 0.0;
+  for (int t = lane; t < d; t += 32) s = fma((double)x[t], (double)x[t], s);
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    if (qn) qn[warp] = s;
+    if (xn) xn[warp] = __double2float_ru(sqrt(s) * (1.0 + 1e-12));
+  }
+}
+
+__global__ void to_bf16_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
+                               __nv_bfloat16* __restrict__ Xb, long long ldb) {
+  const long long total = n * ldb;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long r = e / ldb;
+    const int c = (int)(e - r * ldb);
+    Xb[e] = __float2bfloat16_rn(c < d ? X[(size_t)r * ldx + c] : 0.0f);
+  }
+}
+
+__global__ void gather_rows_kernel(const float* __restrict__ Xs, long long ldx,
+                                   const int* __restrict__ perm, long long m, long long start,
+                                   long long m_mb, int d, float* __restrict__ Xd, long long ldd) {
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= m_mb) return;
+  long long pos = start + warp;
+  if (pos >= m) pos -= m;
+  const float* src = Xs + (size_t)perm[pos] * ldx;
+  float* dst = Xd + (size_t)warp * ldd;
+  for (int t = lane; t < (int)ldd; t += 32) dst[t] = t < d ? src[t] : 0.0f;
+}
+
+__global__ void gather_vec_kernel(const double* __restrict__ qs, const float* __restrict__ xs,
+                                  const int* __restrict__ perm, long long m, long long start,
+                                  long long m_mb, double* __restrict__ qd, float* __restrict__ xd) {
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < m_mb;
+       r += (long long)gridDim.x * blockDim.x) {
+    long long pos = start + r;
+    if (pos >= m) pos -= m;
+    const int src = perm[pos];
+    qd[r] = qs[src];
+    xd[r] = xs[src];
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop, void* Cb,
+                                long long ldcb, float* cn, float* cmax, cudaStream_t s) {
+  if (k <= 0) return cudaSuccess;
+  const int threads = 256;
+  const int blocks = (int)(((long long)k * 32 + threads - 1) / threads);
+  prep_centers_kernel<<<blocks, threads, 0, s>>>(C, ldc, k, d, Cop,
+                                                 reinterpret_cast<__nv_bfloat16*>(Cb), ldcb, cn,
+                                                 cmax); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,
+                               float* xn, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int threads = 256;
+  const long long blocks = (n * 32 + threads - 1) / threads;
+  point_norms_kernel<<<(unsigned)blocks, threads, 0, s>>>(X, ldx, n, d, qn, xn); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
+                           long long ldb, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  to_bf16_kernel<<<152 * 16, 256, 0, s>>>(X, ldx, n, d, reinterpret_cast<__nv_bfloat16*>(Xb),
+                                          ldb); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_rows(const float* Xsrc, long long ldx, const int* perm, long long m,
+                               long long start, long long m_mb, int d, float* Xdst, long long ldd,
+                               cudaStream_t s) {
+  if (m_mb <= 0) return cudaSuccess;
+  const int threads = 256;
+  const long long blocks = (m_mb * 32 + threads - 1) / threads;
+  gather_rows_kernel<<<(unsigned)blocks, threads, 0, s>>>(Xsrc, ldx, perm, m, start, m_mb, d,
+                                                          Xdst, ldd); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* perm, long long m,
+                              long long start, long long m_mb, double* qdst, float* xdst,
+                              cudaStream_t s) {
+  if (m_mb <= 0) return cudaSuccess;
+  gather_vec_kernel<<<152 * 4, 256, 0, s>>>(qsrc, xsrc, perm, m, start, m_mb, qdst, xdst); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace kmgb

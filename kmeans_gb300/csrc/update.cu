@@ -1,0 +1,426 @@
+// Deterministic center update and SSE for sm_103a.
+//
+// Replaces the reference's privatised accumulation (main/cuda/ClusterCenters.cu:3-23, one
+// G x K x D partial buffer), its per-center reduce and divide (ClusterCenters.cu:47-87), and the
+// compactness reduction (main/cuda/Compactness.cu:3-59). Instead of G*K*D partials:
+//   1. hist     per-tile label histogram (tile = `tile_pts` consecutive points), K x T int32,
+//               warp-aggregated integer atomics;
+//   2. scan     exclusive scan of the K-major histogram = start of every (label, tile) run;
+//   3. scatter  one warp per tile walks its points in order and writes each point id to
+//               start + rank, so the sort by label is stable (ascending point id per label);
+//   4. pieces   every label's run is cut into pieces of kSumPiece points; one warp per piece
+//               sums its rows in FP64 in point order (and the rows' FP64 ||x||^2);
+//   5. finalize one warp per center adds its pieces in order, divides by the count in FP64,
+//               rounds once to FP32 (empty cluster: NaN as in ClusterCenters.cu:81, or keep the
+//               previous center), and evaluates the cluster's SSE against the new center with
+//               Q - 2 mu.S + n ||mu||^2 in FP64;
+//   6. sse      one block adds the K cluster SSEs in a fixed order.
+// No floating-point atomics: the result is bit-identical run to run and equals the oracle's
+// canonical FP64 order.
+#include <cfloat>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace kmgb {
+namespace {
+
+constexpr int SCAN_T = 1024;
+constexpr int SCAN_V = 8;
+constexpr long long SCAN_SEG = SCAN_T * SCAN_V;
+
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one int per thread (blockDim.x == SCAN_T).
+__device__ int block_excl_scan(int v) {
+  __shared__ int warp_tot[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int inc = warp_incl_scan(v, lane);
+  if (lane == 31) warp_tot[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    const int t = warp_tot[lane];
+    const int ti = warp_incl_scan(t, lane);
+    warp_tot[lane] = ti - t;
+  }
+  __syncthreads();
+  const int res = warp_tot[w] + inc - v;
+  __syncthreads();
+  return res;
+}
+
+__global__ void scan_reduce_kernel(const int* __restrict__ in, long long n, int* __restrict__ sums) {
+  const long long base = (long long)blockIdx.x * SCAN_SEG + (long long)threadIdx.x * SCAN_V;
+  int s = 0;
+#pragma unroll
+  for (int v = 0; v < SCAN_V; ++v)
+    if (base + v < n) s += in[base + v];
+  __shared__ int red[32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int t = red[threadIdx.x];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (threadIdx.x == 0) sums[blockIdx.x] = t;
+  }
+}
+
+// In-place exclusive scan of segment blockIdx.x, plus offset (*offsets)[blockIdx.x] if given.
+__global__ void scan_seg_kernel(int* __restrict__ data, long long n, const int* __restrict__ offsets) {
+  const long long base = (long long)blockIdx.x * SCAN_SEG + (long long)threadIdx.x * SCAN_V;
+  int vals[SCAN_V];
+  int s = 0;
+#pragma unroll
+  for (int v = 0; v < SCAN_V; ++v) {
+    vals[v] = (base + v < n) ? data[base + v] : 0;
+    s += vals[v];
+  }
+  int pre = block_excl_scan(s);
+  if (offsets) pre += offsets[blockIdx.x];
+#pragma unroll
+  for (int v = 0; v < SCAN_V; ++v) {
+    if (base + v < n) data[base + v] = pre;
+    pre += vals[v];
+  }
+}
+
+__global__ void hist_kernel(const int* __restrict__ labels, long long n, int k, int tile_pts,
+                            int ntiles, int* __restrict__ hist, int* err) {
+  const int tile = blockIdx.x;
+  const long long i0 = (long long)tile * tile_pts;
+  const long long i1 = min(n, i0 + tile_pts);
+  const int lane = threadIdx.x & 31;
+  for (long long b = i0; b < i1; b += blockDim.x) {
+    const long long i = b + threadIdx.x;
+    int l = -1;
+    if (i < i1) {
+      l = labels[i];
+      if (l < 0 || l >= k) {
+        set_error(err, KMGB_DEV_BAD_LABEL);
+        l = -1;
+      }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    const int leader = __ffs(peers) - 1;
+    if (l >= 0 && lane == leader) atomicAdd(&hist[(size_t)l * ntiles + tile], __popc(peers));
+  }
+}
+
+// label_off[j] = start of label j in the sorted order, label_off[k] = n; piece_cnt[j] = pieces
+// of label j (piece_cnt[k] = 0, the scan turns it into the total); counts[j] = members.
+__global__ void label_offsets_kernel(const int* __restrict__ hist, long long n, int k, int ntiles,
+                                     int* __restrict__ label_off, int* __restrict__ piece_cnt,
+                                     long long* __restrict__ counts) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > k) return;
+  if (j == k) {
+    label_off[k] = (int)n;
+    piece_cnt[k] = 0;
+    return;
+  }
+  const int a = hist[(size_t)j * ntiles];
+  const int b = (j + 1 < k) ? hist[(size_t)(j + 1) * ntiles] : (int)n;
+  label_off[j] = a;
+  piece_cnt[j] = (b - a + kSumPiece - 1) / kSumPiece;
+  if (counts) counts[j] = b - a;
+}
+
+template <bool SMEM>
+__global__ void scatter_kernel(const int* __restrict__ labels, long long n, int k, int tile_pts,
+                               int ntiles, int* pos, int* __restrict__ sorted) {
+  extern __shared__ int cnt_s[];
+  const int tile = blockIdx.x;
+  const int lane = threadIdx.x;
+  if (tile >= ntiles) return;
+  if (SMEM) {
+    for (int j = lane; j < k; j += 32) cnt_s[j] = pos[(size_t)j * ntiles + tile];
+    __syncwarp();
+  }
+  volatile int* vpos = pos;
+  const long long i0 = (long long)tile * tile_pts;
+  const long long i1 = min(n, i0 + tile_pts);
+  for (long long b = i0; b < i1; b += 32) {
+    const long long i = b + lane;
+    int l = -1;
+    if (i < i1) {
+      l = labels[i];
+      if (l < 0 || l >= k) l = -1;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    const int leader = __ffs(peers) - 1;
+    const int rank = __popc(peers & lanemask_lt());
+    int base = 0;
+    if (l >= 0 && lane == leader)
+      base = SMEM ? cnt_s[l] : vpos[(size_t)l * ntiles + tile];
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (l >= 0) sorted[base + rank] = (int)i;
+    if (l >= 0 && lane == leader) {
+      const int nv = base + __popc(peers);
+      if (SMEM) cnt_s[l] = nv;
+      else vpos[(size_t)l * ntiles + tile] = nv;
+    }
+    __syncwarp();
+  }
+}
+
+__device__ __forceinline__ int find_label(const int* __restrict__ pstart, int k, int p) {
+  int lo = 0, hi = k - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(pstart + mid) <= p) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// One warp per piece; dims lane + 32 r in chunks of 256.
+template <typename T>
+__global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
+                                  const double* __restrict__ qn, const int* __restrict__ sorted,
+                                  const int* __restrict__ label_off, const int* __restrict__ pstart,
+                                  int k, int d, double* __restrict__ part,
+                                  double* __restrict__ partq) {
+  const int ptot = pstart[k];
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long p = gw; p < ptot; p += nw) {
+    const int j = find_label(pstart, k, (int)p);
+    const int q = (int)p - pstart[j];
+    const int b = label_off[j] + q * kSumPiece;
+    const int e = min(b + kSumPiece, label_off[j + 1]);
+    for (int d0 = 0; d0 < d; d0 += 256) {
+      double acc[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) acc[r] = 0.0;
+      double qs = 0.0;
+#pragma unroll 4
+      for (int t = b; t < e; ++t) {
+        const int i = __ldg(sorted + t);
+        const T* x = X + (size_t)i * ldx + d0;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+          const int c = lane + 32 * r;
+          if (d0 + c < d) acc[r] += (double)__ldg(x + c);
+        }
+        if (qn && d0 == 0) qs += __ldg(qn + i);
+      }
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int c = d0 + lane + 32 * r;
+        if (c < d) part[(size_t)p * d + c] = acc[r];
+      }
+      if (d0 == 0 && lane == 0 && partq) partq[p] = qs;
+    }
+  }
+}
+
+// One warp per center.
+__global__ void finalize_kernel(const double* __restrict__ part, const double* __restrict__ partq,
+                                const int* __restrict__ label_off, const int* __restrict__ pstart,
+                                int k, int d, float* __restrict__ C, long long ldc,
+                                int empty_policy, double* __restrict__ sse_k) {
+  const int j = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (j >= k) return;
+  const long long n = (long long)label_off[j + 1] - label_off[j];
+  const int p0 = pstart[j], p1 = pstart[j + 1];
+  double sse = 0.0;
+  for (int c = lane; c < d; c += 32) {
+    double s = 0.0;
+    for (int p = p0; p < p1; ++p) s += part[(size_t)p * d + c];
+    float mu;
+    if (n > 0) {
+      mu = __double2float_rn(__ddiv_rn(s, (double)n));
+      const double m = (double)mu;
+      sse += fma((double)n * m, m, -2.0 * m * s);
+    } else if (empty_policy == 1) {
+      mu = C[(size_t)j * ldc + c];
+    } else {
+      mu = __int_as_float(0x7fc00000);
+    }
+    C[(size_t)j * ldc + c] = mu;
+  }
+  for (int o = 16; o > 0; o >>= 1) sse += __shfl_xor_sync(0xffffffffu, sse, o);
+  if (lane == 0 && sse_k) {
+    double q = 0.0;
+    if (partq && n > 0)
+      for (int p = p0; p < p1; ++p) q += partq[p];
+    sse_k[j] = (n > 0) ? sse + q : 0.0;
+  }
+}
+
+__global__ void sse_reduce_kernel(const double* __restrict__ sse_k, int k, double* __restrict__ out) {
+  __shared__ double red[1024];
+  const int per = (k + blockDim.x - 1) / blockDim.x;
+  double s = 0.0;
+  for (int j = threadIdx.x * per; j < min(k, (int)(threadIdx.x + 1) * per); ++j) s += sse_k[j];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x >> 1; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
+}
+
+cudaError_t excl_scan(int* data, long long n, int* tmp, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const long long nb = (n + SCAN_SEG - 1) / SCAN_SEG;
+  if (nb > SCAN_SEG) return cudaErrorInvalidValue;
+  if (nb == 1) {
+    scan_seg_kernel<<<1, SCAN_T, 0, s>>>(data, n, nullptr); kmgb::count_launches(1);
+    return cudaGetLastError();
+  }
+  scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp); kmgb::count_launches(1);
+  scan_seg_kernel<<<1, SCAN_T, 0, s>>>(tmp, nb, nullptr); kmgb::count_launches(1);
+  scan_seg_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Tile size of the label histogram: keeps K x T below ~16M entries (one scan of <= 64 MB).
+void plan_update_tiles(long long n, int k, int* tile_pts, int* ntiles) {
+  const long long per = (n * (long long)k + (16LL << 20) - 1) / (16LL << 20);
+  long long tp = per < 1024 ? 1024 : (per + 31) / 32 * 32;
+  if (tp > (1LL << 30)) tp = 1LL << 30;
+  *tile_pts = (int)tp;
+  *ntiles = (int)((n + tp - 1) / tp);
+}
+
+size_t update_scan_tmp_elems(long long elems) {
+  return (size_t)((elems + SCAN_SEG - 1) / SCAN_SEG) + 1;
+}
+
+// Stable sort of the point ids by label + per-label offsets and piece starts.
+static cudaError_t sort_by_label(const int* labels, const UpdateWork& w, cudaStream_t s) {
+  const long long n = w.n;
+  const int k = w.k;
+  const long long hist_elems = (long long)k * w.ntiles;
+  KMGB_CUDA_TRY(cudaMemsetAsync(w.hist, 0, sizeof(int) * hist_elems, s));
+  hist_kernel<<<w.ntiles, 256, 0, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist, w.err); kmgb::count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  KMGB_CUDA_TRY(excl_scan(w.hist, hist_elems, w.scan_tmp, s));
+  label_offsets_kernel<<<(k + 1 + 255) / 256, 256, 0, s>>>(w.hist, n, k, w.ntiles, w.label_off,
+                                                          w.piece_cnt, w.counts); kmgb::count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  KMGB_CUDA_TRY(excl_scan(w.piece_cnt, k + 1, w.scan_tmp, s));
+  const size_t smem = sizeof(int) * (size_t)k;
+  if (smem <= 96 * 1024) {
+    static int attr_k = -1;
+    if (smem > 48 * 1024 && attr_k < k) {
+      KMGB_CUDA_TRY(cudaFuncSetAttribute(scatter_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+      attr_k = k;
+    }
+    scatter_kernel<true><<<w.ntiles, 32, smem, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist,
+                                                    w.sorted); kmgb::count_launches(1);
+  } else {
+    scatter_kernel<false><<<w.ntiles, 32, 0, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist,
+                                                  w.sorted); kmgb::count_launches(1);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update(const float* X, const double* qn, const int* labels, float* C,
+                          long long ldc, int empty_policy, const UpdateWork& w, double* sse_out,
+                          cudaStream_t s) {
+  const int k = w.k;
+  if (w.n <= 0 || k <= 0) return cudaSuccess;
+  KMGB_CUDA_TRY(sort_by_label(labels, w, s));
+  const long long max_pieces = w.max_pieces;
+  long long warps = max_pieces < 152LL * 64 ? max_pieces : 152LL * 64;
+  piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+      X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq); kmgb::count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  finalize_kernel<<<(unsigned)(((long long)k * 32 + 255) / 256), 256, 0, s>>>(
+      w.part, qn ? w.partq : nullptr, w.label_off, w.piece_cnt, k, w.d, C, ldc, empty_policy,
+      w.sse_k); kmgb::count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  if (sse_out) {
+    sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, k, sse_out); kmgb::count_launches(1);
+    KMGB_CUDA_TRY(cudaGetLastError());
+  }
+  return cudaSuccess;
+}
+
+namespace {
+
+// Per-kernel ABI: add this tile's canonical per-center sums to FP64 accumulators.
+__global__ void accumulate_kernel(const double* __restrict__ part, const int* __restrict__ label_off,
+                                  const int* __restrict__ pstart, int k, int d,
+                                  double* __restrict__ acc, int* __restrict__ acc_counts) {
+  const int j = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (j >= k) return;
+  const int p0 = pstart[j], p1 = pstart[j + 1];
+  for (int c = lane; c < d; c += 32) {
+    double s = 0.0;
+    for (int p = p0; p < p1; ++p) s += part[(size_t)p * d + c];
+    acc[(size_t)j * d + c] += s;
+  }
+  if (lane == 0) acc_counts[j] += label_off[j + 1] - label_off[j];
+}
+
+template <typename T>
+__global__ void finalize_acc_kernel(const double* __restrict__ acc, const int* __restrict__ acc_counts,
+                                    int k, int d, T* __restrict__ centers, int* __restrict__ counts) {
+  const long long total = (long long)k * d;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int j = (int)(e / d);
+    const int n = acc_counts[j];
+    T v;
+    if (n > 0) {
+      const double q = __ddiv_rn(acc[e], (double)n);
+      v = (T)q;
+    } else {
+      v = (T)__longlong_as_double(0x7ff8000000000000LL);
+    }
+    centers[e] = v;
+    if (counts && e % d == 0) counts[j] = n;
+  }
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_tile_accumulate(const T* X, long long ldx, const int* labels, const UpdateWork& w,
+                                   double* acc, int* acc_counts, cudaStream_t s) {
+  if (w.n <= 0 || w.k <= 0) return cudaSuccess;
+  KMGB_CUDA_TRY(sort_by_label(labels, w, s));
+  long long warps = w.max_pieces < 152LL * 64 ? w.max_pieces : 152LL * 64;
+  piece_sums_kernel<T><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+      X, ldx, nullptr, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, nullptr); kmgb::count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  accumulate_kernel<<<(unsigned)(((long long)w.k * 32 + 255) / 256), 256, 0, s>>>(
+      w.part, w.label_off, w.piece_cnt, w.k, w.d, acc, acc_counts); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_finalize_acc(const double* acc, const int* acc_counts, int k, int d, T* centers,
+                                int* counts, cudaStream_t s) {
+  finalize_acc_kernel<T><<<152 * 4, 256, 0, s>>>(acc, acc_counts, k, d, centers, counts); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_tile_accumulate<float>(const float*, long long, const int*,
+                                                   const UpdateWork&, double*, int*, cudaStream_t);
+template cudaError_t launch_tile_accumulate<double>(const double*, long long, const int*,
+                                                    const UpdateWork&, double*, int*, cudaStream_t);
+template cudaError_t launch_finalize_acc<float>(const double*, const int*, int, int, float*, int*,
+                                                cudaStream_t);
+template cudaError_t launch_finalize_acc<double>(const double*, const int*, int, int, double*, int*,
+                                                 cudaStream_t);
+
+}  // namespace kmgb

@@ -1,0 +1,218 @@
+"""CPU oracle for the Lloyd hot path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference-arm leg may
+import this package, and only as the checker (or as the timed CPU stand-in for the
+reference, which has no CPU path of its own). The product library never imports it.
+
+`build()` compiles oracle.cpp with g++ (OpenMP, -ffp-contract=off so FP64 results are the
+same on x86-64 and aarch64) into oracle/liboracle.so; `lib()` loads it with ctypes
+signatures; the numpy helpers below wrap the calls.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_SRC = os.path.join(_HERE, "oracle.cpp")
+_SO = os.path.join(_HERE, "liboracle.so")
+_lock = threading.Lock()
+_lib = None
+
+# Canonical FP64 center-sum piece size; must equal the product's (checked by a test).
+PIECE = 128
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library if it is missing or older than its source."""
+    if (not force and os.path.exists(_SO)
+            and os.path.getmtime(_SO) >= os.path.getmtime(_SRC)):
+        return _SO
+    cmd = ["g++", "-O3", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           _SRC, "-o", _SO + ".tmp"]
+    subprocess.check_call(cmd)
+    os.replace(_SO + ".tmp", _SO)
+    return _SO
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        build()
+        L = C.CDLL(_SO)
+        P = C.c_void_p
+        i32, i64, f32, f64 = C.c_int, C.c_longlong, C.c_float, C.c_double
+        L.orc_shuffle_perm.argtypes = [i32, P]
+        L.orc_init_picks.argtypes = [i32, i32, P]
+        L.orc_init_picks.restype = i32
+        L.orc_reference_init.argtypes = [P, i32, i32, i32, P]
+        L.orc_reference_init.restype = i32
+        L.orc_assign.argtypes = [P, i64, i32, P, i32, P, P]
+        L.orc_update.argtypes = [P, i64, i32, P, i32, i32, P, i32, P, P, P]
+        L.orc_sse.argtypes = [P, i64, i32, P, P]
+        L.orc_sse.restype = f64
+        L.orc_lloyd.argtypes = [P, i64, i32, i32, P, i32, f64, f32, i32, i32, P, P, P, P]
+        L.orc_lloyd.restype = i32
+        L.orc_assign_d.argtypes = [P, i64, i32, P, i32, P, P]
+        L.orc_update_d.argtypes = [P, i64, i32, P, i32, i32, P, i32, P, P, P]
+        L.orc_sse_d.argtypes = [P, i64, i32, P, P]
+        L.orc_sse_d.restype = f64
+        L.orc_lloyd_d.argtypes = [P, i64, i32, i32, P, i32, f64, f32, i32, i32, P, P, P, P]
+        L.orc_lloyd_d.restype = i32
+        L.orc_closest_expansion.argtypes = [P, i32, i32, P, i32, P, P]
+        L.orc_closest_expansion_d.argtypes = [P, i32, i32, P, i32, P, P]
+        L.orc_row_transform_min_f.argtypes = [i32, i32, i32, P, P, P, P]
+        L.orc_row_transform_min_d.argtypes = [i32, i32, i32, P, P, P, P]
+        L.orc_port_lloyd.argtypes = [P, i64, i32, i32, P, i32, i32, P, P, P]
+        L.orc_port_lloyd.restype = i32
+        L.orc_num_threads.restype = i32
+        _lib = L
+        return L
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def shuffle_perm(m: int) -> np.ndarray:
+    out = np.empty(m, dtype=np.int32)
+    lib().orc_shuffle_perm(m, _p(out))
+    return out
+
+
+def init_picks(m: int, k: int) -> np.ndarray:
+    out = np.empty(k, dtype=np.int32)
+    rc = lib().orc_init_picks(m, k, _p(out))
+    if rc:
+        raise ValueError(f"init picks failed ({rc})")
+    return out
+
+
+def reference_init(X: np.ndarray, k: int) -> np.ndarray:
+    X = _f32(X)
+    m, d = X.shape
+    out = np.empty((k, d), dtype=np.float32)
+    rc = lib().orc_reference_init(_p(X), m, d, k, _p(out))
+    if rc:
+        raise ValueError(f"reference init failed ({rc})")
+    return out
+
+
+def assign(X: np.ndarray, Cn: np.ndarray, with_dist: bool = False):
+    X, Cn = _f32(X), _f32(Cn)
+    m, d = X.shape
+    k = Cn.shape[0]
+    lab = np.empty(m, dtype=np.int32)
+    dist = np.empty(m, dtype=np.float64) if with_dist else None
+    lib().orc_assign(_p(X), m, d, _p(Cn), k, _p(lab), _p(dist) if with_dist else None)
+    return (lab, dist) if with_dist else lab
+
+
+def update(X, labels, k, old_centers=None, empty_policy=0, piece=PIECE):
+    X = _f32(X)
+    m, d = X.shape
+    labels = np.ascontiguousarray(labels, dtype=np.int32)
+    oc = _f32(old_centers) if old_centers is not None else None
+    newc = np.empty((k, d), dtype=np.float32)
+    cnt = np.empty(k, dtype=np.int64)
+    sums = np.empty((k, d), dtype=np.float64)
+    lib().orc_update(_p(X), m, d, _p(labels), k, piece, _p(oc) if oc is not None else None,
+                     empty_policy, _p(newc), _p(cnt), _p(sums))
+    return newc, cnt, sums
+
+
+def sse(X, labels, centers) -> float:
+    X, centers = _f32(X), _f32(centers)
+    m, d = X.shape
+    labels = np.ascontiguousarray(labels, dtype=np.int32)
+    return float(lib().orc_sse(_p(X), m, d, _p(labels), _p(centers)))
+
+
+def lloyd(X, init, max_iters, criterion=-1.0, mb_fraction=1.0, empty_policy=0, piece=PIECE):
+    """Returns (status, centers KxD, labels, sse[iters], iters)."""
+    X, init = _f32(X), _f32(init)
+    m, d = X.shape
+    k = init.shape[0]
+    cen = np.empty((k, d), dtype=np.float32)
+    lab = np.empty(m, dtype=np.int32)
+    sse_ = np.zeros(max(max_iters, 1), dtype=np.float64)
+    its = C.c_int(0)
+    st = lib().orc_lloyd(_p(X), m, d, k, _p(init), max_iters, float(criterion),
+                         float(mb_fraction), empty_policy, piece, _p(cen), _p(lab), _p(sse_),
+                         C.byref(its))
+    return st, cen, lab, sse_[:its.value], its.value
+
+
+def lloyd_d(X, init, max_iters, criterion=-1.0, mb_fraction=1.0, empty_policy=0, piece=PIECE):
+    """FP64-data Lloyd loop. Returns (status, centers KxD float64, labels, sse, iters)."""
+    X = np.ascontiguousarray(X, dtype=np.float64)
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    m, d = X.shape
+    k = init.shape[0]
+    cen = np.empty((k, d), dtype=np.float64)
+    lab = np.empty(m, dtype=np.int32)
+    sse_ = np.zeros(max(max_iters, 1), dtype=np.float64)
+    its = C.c_int(0)
+    st = lib().orc_lloyd_d(_p(X), m, d, k, _p(init), max_iters, float(criterion),
+                           float(mb_fraction), empty_policy, piece, _p(cen), _p(lab), _p(sse_),
+                           C.byref(its))
+    return st, cen, lab, sse_[:its.value], its.value
+
+
+def closest_expansion(A, B, nb):
+    """FP64 arg-min_j nb_j - 2 A_i.B_j (B is d x k), the per-kernel ClosestCenters semantics."""
+    f64 = A.dtype == np.float64
+    dt = np.float64 if f64 else np.float32
+    A = np.ascontiguousarray(A, dtype=dt)
+    B = np.ascontiguousarray(B, dtype=dt)
+    nb = np.ascontiguousarray(nb, dtype=dt)
+    m, d = A.shape
+    k = B.shape[1]
+    out = np.empty(m, dtype=np.int32)
+    fn = lib().orc_closest_expansion_d if f64 else lib().orc_closest_expansion
+    fn(_p(A), m, d, _p(B), k, _p(nb), _p(out))
+    return out
+
+
+def row_transform_min_f(m0, normA, normB, G, out_len):
+    normA, normB, G = _f32(normA), _f32(normB), _f32(G)
+    m, n = G.shape
+    out = np.zeros(out_len, dtype=np.int32)
+    lib().orc_row_transform_min_f(m0, m, n, _p(normA), _p(normB), _p(G), _p(out))
+    return out
+
+
+def row_transform_min_d(m0, normA, normB, G, out_len):
+    normA = np.ascontiguousarray(normA, dtype=np.float64)
+    normB = np.ascontiguousarray(normB, dtype=np.float64)
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    m, n = G.shape
+    out = np.zeros(out_len, dtype=np.int32)
+    lib().orc_row_transform_min_d(m0, m, n, _p(normA), _p(normB), _p(G), _p(out))
+    return out
+
+
+def port_lloyd(X, init, iters, piece=PIECE):
+    """FP32 port of the loop (CPU baseline). Returns (centers, labels, sse[iters])."""
+    X, init = _f32(X), _f32(init)
+    m, d = X.shape
+    k = init.shape[0]
+    cen = np.empty((k, d), dtype=np.float32)
+    lab = np.empty(m, dtype=np.int32)
+    s = np.zeros(max(iters, 1), dtype=np.float64)
+    lib().orc_port_lloyd(_p(X), m, d, k, _p(init), iters, piece, _p(cen), _p(lab), _p(s))
+    return cen, lab, s[:iters]
+
+
+def num_threads() -> int:
+    return int(lib().orc_num_threads())

@@ -1,0 +1,63 @@
+"""CPU checks of the C-ABI library: it builds for sm_103a, loads, and exports every entry point
+that include/kmeans_gb300.h declares; host-only calls behave as the reference's."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+
+def declared_symbols(km):
+    src = open(km.HEADER_PATH).read()
+    return sorted(set(re.findall(r"KMGB_EXPORT\s+[\w\s\*]+?\b(\w+)\(", src)))
+
+
+def test_library_exports_every_declared_symbol(km):
+    km.lib()
+    out = subprocess.run(["nm", "-D", "--defined-only", km.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if " T " in l}
+    decl = declared_symbols(km)
+    assert len(decl) >= 30
+    missing = [s for s in decl if s not in exported]
+    assert not missing, missing
+    lib = km.lib()
+    for s in decl:
+        assert getattr(lib, s) is not None
+
+
+def test_reference_entry_points_present(km):
+    names = ["computeKmeansF", "computeKmeansD", "kmeansGetErrorString", "ClosestCentersF",
+             "ClosestCentersD", "rowTransformMinimumF", "rowTransformMinimumD",
+             "ClusterCentersF", "ClusterCentersD", "CompactnessF", "CompactnessD",
+             "rowNormalizeF", "rowNormalizeD", "colNormalizeF", "colNormalizeD"]
+    decl = declared_symbols(km)
+    for n in names:
+        assert n in decl
+
+
+def test_error_strings_match_reference(km):
+    for code, s in km.ERROR_STRINGS.items():
+        assert km.kmeansGetErrorString(code) == s
+    assert km.kmeansGetErrorString(0) == "no error"
+
+
+def test_piece_size_matches_oracle(km, orc):
+    assert km.lib().kmgb_sum_piece() == orc.PIECE
+
+
+def test_default_options(km):
+    o = km.default_options()
+    assert (o.assign_tier, o.certify, o.empty_policy, o.max_iters) == (0, 1, 0, 20)
+    assert o.criterion < 0 and o.mini_batch_fraction == 1.0
+
+
+def test_invalid_arguments_rejected_without_gpu(km):
+    import numpy as np
+    res = np.zeros(16, np.float32)
+    data = np.zeros((2, 2), np.float32)
+    # argument validation happens before any device call
+    assert km.computeKmeansF(data, 2, 2, 0, -1.0, 1, 1, 0, 0, 0, res, 1.0) == 1
+    assert km.computeKmeansF(data, 2, 2, 3, -1.0, 1, 1, 0, 0, 0, res, 1.0) == 2
+    assert km.computeKmeansF(data, 2, 2, 1, -1.0, 1, 1, 0, 3, 0, res, 1.0) == 1

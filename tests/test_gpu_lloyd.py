@@ -1,0 +1,177 @@
+"""GPU parity of the Lloyd loop (assignment + update + SSE + stop rule + mini-batch) against the
+FP64 oracle: labels bit-exact, centers bit-exact (canonical FP64 sums rounded once), SSE within
+1e-10 relative (the GPU evaluates each cluster's SSE as Q - 2 mu.S + n|mu|^2 in FP64, the
+oracle sums the direct form), iteration count and status equal."""
+import numpy as np
+import pytest
+
+from kmeans_gb300.synthetic import mixture_numpy, sample_init
+
+pytestmark = pytest.mark.gpu
+SSE_RTOL = 1e-10
+
+
+def check_same(res, ref, sse_rtol=SSE_RTOL):
+    st, c, lab, sse, it = ref
+    assert res.iterations == it
+    assert res.status == st
+    assert np.array_equal(res.labels, lab)
+    assert np.array_equal(res.centers, c, equal_nan=True)
+    np.testing.assert_allclose(res.sse, sse, rtol=sse_rtol)
+
+
+def test_c1_config_fp32(km, orc, torch_cuda):
+    X, _, _ = mixture_numpy(100_000, 32, 64, seed=101, mean_lo=-10, mean_hi=10)
+    init = X[sample_init(len(X), 64, seed=102)]
+    res = km.lloyd(X, 64, init=init, max_iters=20)
+    check_same(res, orc.lloyd(X, init, 20))
+    assert res.status == 13
+
+
+@pytest.mark.parametrize("n,d,k", [(1, 1, 1), (130, 3, 7), (1000, 129, 200), (4097, 64, 129),
+                                   (20000, 128, 256), (3001, 17, 1)])
+def test_odd_shapes(km, orc, torch_cuda, n, d, k):
+    X, _, _ = mixture_numpy(n, d, max(k, 1), seed=n + d + k)
+    init = X[sample_init(n, k, seed=3)]
+    res = km.lloyd(X, k, init=init, max_iters=6)
+    check_same(res, orc.lloyd(X, init, 6))
+
+
+def test_near_ties_are_resolved_exactly(km, orc, torch_cuda):
+    # points placed on (or within a few ulps of) the bisector of two centers
+    rng = np.random.default_rng(17)
+    d, k = 48, 20
+    Cn = rng.uniform(-5, 5, size=(k, d)).astype(np.float32)
+    a, b = rng.integers(0, k, 4000), rng.integers(0, k, 4000)
+    t = 0.5 + rng.integers(-3, 4, 4000) * 1e-7
+    X = (Cn[a] * t[:, None] + Cn[b] * (1 - t[:, None])).astype(np.float32)
+    X = np.concatenate([X, Cn, Cn[:5]])  # exact duplicates of centers too
+    res = km.lloyd(X, k, init=Cn, max_iters=1)
+    check_same(res, orc.lloyd(X, Cn, 1))
+    assert res.reranked > 0
+
+
+def test_reference_init_compute_kmeans_f(km, orc, torch_cuda):
+    X, _, _ = mixture_numpy(50_000, 24, 40, seed=7)
+    m, n, k = X.shape[0], X.shape[1], 40
+    result = np.zeros(n * k, np.float32)
+    rc = km.computeKmeansF(X, m, n, k, -1.0, 12, 1, 0, 0, 0, result, 1.0)
+    assert rc == 13
+    st, c, lab, sse, it = orc.lloyd(X, orc.reference_init(X, k), 12)
+    assert np.array_equal(result.reshape(n, k), c.T)  # D x K, K fastest
+    # doFullSGEMM / matrixFormat map to the same implementation
+    r2 = np.zeros_like(result)
+    assert km.computeKmeansF(X, m, n, k, -1.0, 12, 3, 1, 1, 1, r2, 1.0) == 13
+    assert np.array_equal(r2, result)
+
+
+def test_convergence_criterion(km, orc, torch_cuda):
+    X, _, _ = mixture_numpy(30_000, 8, 12, seed=8)
+    m, n, k = X.shape[0], X.shape[1], 12
+    ref = orc.lloyd(X, orc.reference_init(X, k), 200, criterion=1e-6)
+    assert ref[0] == 0 and ref[4] < 200
+    result = np.zeros(n * k, np.float32)
+    rc = km.computeKmeansF(X, m, n, k, 1e-6, 200, 1, 0, 0, 0, result, 1.0)
+    assert rc == 0
+    assert np.array_equal(result.reshape(n, k), ref[1].T)
+    res = km.lloyd(X, k, init=None, max_iters=200, criterion=1e-6)
+    check_same(res, ref)
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+def test_empty_cluster_policy(km, orc, torch_cuda, policy):
+    X, _, _ = mixture_numpy(8000, 10, 6, seed=9)
+    init = np.concatenate([X[:6], np.full((2, 10), 1e4, np.float32)])  # two far centers
+    res = km.lloyd(X, 8, init=init, max_iters=5, empty_policy=policy)
+    ref = orc.lloyd(X, init, 5, empty_policy=policy)
+    check_same(res, ref)
+    assert res.empty_clusters == 2
+    if policy == 0:
+        assert np.isnan(res.centers[6:]).all()
+    else:
+        assert np.array_equal(res.centers[6:], init[6:])
+
+
+@pytest.mark.parametrize("frac", [0.25, 0.3333, 0.9])
+def test_minibatch_windows(km, orc, torch_cuda, frac):
+    X, _, _ = mixture_numpy(20_000, 16, 10, seed=10)
+    init = X[sample_init(len(X), 10, seed=4)]
+    res = km.lloyd(X, 10, init=init, max_iters=9, mini_batch_fraction=frac)
+    check_same(res, orc.lloyd(X, init, 9, mb_fraction=frac))
+
+
+def test_minibatch_compute_kmeans_f(km, orc, torch_cuda):
+    X, _, _ = mixture_numpy(20_000, 16, 10, seed=12)
+    m, n, k = X.shape[0], X.shape[1], 10
+    result = np.zeros(n * k, np.float32)
+    assert km.computeKmeansF(X, m, n, k, -1.0, 7, 1, 0, 0, 0, result, 0.2) == 13
+    ref = orc.lloyd(X, orc.reference_init(X, k), 7, mb_fraction=0.2)
+    assert np.array_equal(result.reshape(n, k), ref[1].T)
+
+
+def test_device_input_and_handle_resume(km, orc, torch_cuda):
+    torch = torch_cuda
+    X, _, _ = mixture_numpy(60_000, 40, 50, seed=13)
+    init = X[sample_init(len(X), 50, seed=5)]
+    Xd = torch.from_numpy(X).cuda()
+    res = km.lloyd(Xd, 50, init=init, max_iters=5)
+    check_same(res, orc.lloyd(X, init, 5))
+    h = km.Handle(len(X), 40, 50, max_iters=8)
+    h.set_data(Xd, True)
+    h.set_centers(init, False)
+    h.run(3)
+    h.run(2)  # resumes from the current centers
+    h.synchronize()
+    ref = orc.lloyd(X, init, 5)
+    assert np.array_equal(h.centers(), ref[1])
+    assert np.array_equal(h.labels(), ref[2])
+    h.close()
+
+
+def test_compute_kmeans_d(km, orc, torch_cuda):
+    X, _, _ = mixture_numpy(12_000, 9, 15, seed=14)
+    X = X.astype(np.float64) * 1.0000001
+    m, n, k = X.shape[0], X.shape[1], 15
+    result = np.zeros(n * k, np.float64)
+    assert km.computeKmeansD(X, m, n, k, -1.0, 6, 1, 0, 1, 0, result, 1.0) == 13
+    perm = orc.shuffle_perm(m)
+    init = X[perm[orc.init_picks(m, k)]]
+    st, c, lab, sse, it = orc.lloyd_d(X, init, 6)
+    assert np.array_equal(result.reshape(n, k), c.T)
+
+
+def test_c2_scale_properties(km, orc, torch_cuda):
+    """Full c2 size (4M x 128, K=1024): sampled labels equal the oracle's FP64 arg-min with the
+    centers that produced them, centers equal FP64 means of their members, SSE equals an
+    independent FP64 evaluation."""
+    torch = torch_cuda
+    from kmeans_gb300.synthetic import mixture_torch
+    n, d, k = 4_000_000, 128, 1024
+    X, _, _ = mixture_torch(n, d, k, seed=20, mean_lo=-20, mean_hi=20, std=(0.3, 3.0))
+    idx = torch.from_numpy(sample_init(n, k, seed=21)).cuda()
+    init = X[idx].cpu().numpy()
+    h = km.Handle(n, d, k, max_iters=4)
+    h.set_data(X, True)
+    h.set_centers(init, False)
+    h.run(2)
+    h.synchronize()
+    c_prev = h.centers()
+    h.run(1)
+    h.synchronize()
+    lab = h.labels()
+    c_new = h.centers()
+    sse = h.sse(1)[0]
+    rng = np.random.default_rng(0)
+    s = rng.choice(n, 3000, replace=False)
+    Xs = X[torch.from_numpy(s).cuda()].cpu().numpy()
+    assert np.array_equal(lab[s], orc.assign(Xs, c_prev))
+    Xg = X.double()
+    lt = torch.from_numpy(lab).cuda().long()
+    sums = torch.zeros((k, d), dtype=torch.float64, device="cuda").index_add_(0, lt, Xg)
+    cnt = torch.bincount(lt, minlength=k).double()
+    means = (sums / cnt[:, None]).float().cpu().numpy()
+    ok = cnt.cpu().numpy() > 0
+    np.testing.assert_allclose(c_new[ok], means[ok], rtol=2e-7, atol=1e-6)
+    ref_sse = ((Xg - torch.from_numpy(c_new).cuda().double()[lt]) ** 2).sum().item()
+    assert abs(sse - ref_sse) <= 1e-9 * ref_sse
+    h.close()
