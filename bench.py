@@ -129,6 +129,8 @@ def main():
     ap.add_argument("--tier", default=None, help="fp32 or bf16 (default: bf16 when available)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=N, help="rows (default: the 4M workload); smaller "
+                    "values are for profiling captures only")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -151,10 +153,11 @@ def main():
     tier = args.tier or "fp32"
     tier_id = km.ASSIGN_BF16 if tier == "bf16" else km.ASSIGN_FP32
 
-    X, _, _ = mixture_torch(N, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
-    idx = torch.from_numpy(sample_init(N, K, seed=99)).cuda()
+    n = args.n
+    X, _, _ = mixture_torch(n, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+    idx = torch.from_numpy(sample_init(n, K, seed=99)).cuda()
     init = X[idx].cpu().numpy()
-    h = km.Handle(N, D, K, assign_tier=tier_id, max_iters=args.steps + args.warmup)
+    h = km.Handle(n, D, K, assign_tier=tier_id, max_iters=args.steps + args.warmup)
     h.set_data(X, True)
     h.set_centers(init, False)
     h.run(args.warmup)
@@ -185,7 +188,7 @@ def main():
         ms = float(t.item())
     value = world * args.steps / (ms / 1000.0)
 
-    flop = 2.0 * N * K * D
+    flop = 2.0 * n * K * D
     assign_ms = phase[1] / max(piters, 1)
     achieved = flop / (assign_ms / 1000.0) / 1e12
     bf16_peak, hbm_peak, src = peaks()
@@ -219,7 +222,8 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "bf16" if tier == "bf16" else "f32", "data": "synthetic",
-                "config": {"workload": "lloyd_4Mx128_K1024", "n": N, "d": D, "k": K,
+                "config": {"workload": "lloyd_4Mx128_K1024" if n == N else f"lloyd_{n}x128_K1024",
+                           "n": n, "d": D, "k": K,
                            "tier": tier, "certified_labels": True,
                            "l2": "inputs larger than L2 (X: 2.05 GB FP32 per pass)",
                            "parallelism": "replicas" if world > 1 else "single"},

@@ -45,6 +45,7 @@ __device__ __forceinline__ float bound_e(float xn, float cm, float gamma, int d)
 __global__ void __launch_bounds__(NTHREADS, 1)
 assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmC,
                    AssignArgs p) {
+  if (stopped(p.stop)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));

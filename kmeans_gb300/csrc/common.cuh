@@ -111,6 +111,12 @@ __device__ __forceinline__ uint32_t swz128(uint32_t row, uint32_t chunk) {
   return row * 128u + ((chunk ^ (row & 7u)) << 4);
 }
 
+// Device-side stop rule of the Lloyd loop: once the flag is set every later kernel of the run
+// returns at once, so the host never has to synchronise to evaluate the criterion.
+__device__ __forceinline__ bool stopped(const int* stop) {
+  return stop != nullptr && *reinterpret_cast<volatile const int*>(stop) != 0;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

@@ -144,14 +144,22 @@ struct kmgb_handle {
   int* rr_count = nullptr;
   unsigned long long* rr_stats = nullptr;
   int* err = nullptr;
+  // device-side loop state: stop flag, previous SSE, last relErr, iterations done
+  int* stop = nullptr;
+  double* loopf = nullptr;  // [0] SSE_old, [1] relErr
+  int* iters_done = nullptr;
+  int run_base = 0;         // iter_base when the current run started
   // update
   UpdateWork uw{};
   double* sse_dev = nullptr;
   int sse_cap = 0;
   std::vector<double> sse_host;
   double* sse_pinned = nullptr;
+  double* loop_init = nullptr;  // pinned [2]
   int iterations = 0;
   int status = 0;
+  double criterion = -1.0;
+  bool pending = false;
   double ms_total = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // phase profiling: 5 events per iteration
@@ -175,10 +183,12 @@ struct kmgb_handle {
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
     void* ptrs[] = {X, Xb, qn, xn, perm, Xw, Xbw, qnw, xnw, C, Cop, Cb, cn, cmax, labels,
                     rr_list, rr_count, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
-                    uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev};
+                    uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
+                    stop, loopf, iters_done};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     if (sse_pinned) cudaFreeHost(sse_pinned);
+    if (loop_init) cudaFreeHost(loop_init);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -249,6 +259,9 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(dalloc(&h->rr_count, 1), (delete h, code));
   KM_TRY(dalloc(&h->rr_stats, 2), (delete h, code));
   KM_TRY(dalloc(&h->err, 1), (delete h, code));
+  KM_TRY(dalloc(&h->stop, 1), (delete h, code));
+  KM_TRY(dalloc(&h->loopf, 2), (delete h, code));
+  KM_TRY(dalloc(&h->iters_done, 1), (delete h, code));
   KM_TRY(cudaMemset(h->labels, 0, sizeof(int) * na), (delete h, code));
   KM_TRY(cudaMemset(h->rr_stats, 0, sizeof(unsigned long long) * 2), (delete h, code));
   KM_TRY(cudaMemset(h->err, 0, sizeof(int)), (delete h, code));
@@ -272,9 +285,14 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(dalloc(&w.sse_k, k), (delete h, code));
   KM_TRY(dalloc(&w.counts, k), (delete h, code));
   w.err = h->err;
+  w.stop = h->stop;
+  w.sse_prev = h->loopf;
+  w.rel_out = h->loopf + 1;
+  w.iters_done = h->iters_done;
   h->sse_cap = std::max(1, h->opt.max_iters);
   KM_TRY(dalloc(&h->sse_dev, h->sse_cap), (delete h, code));
   KM_TRY(cudaMallocHost(&h->sse_pinned, sizeof(double)), (delete h, code));
+  KM_TRY(cudaMallocHost(&h->loop_init, 2 * sizeof(double)), (delete h, code));
   *out = h;
   return 0;
 }
@@ -326,13 +344,15 @@ int step(kmgb_handle* h, int slot) {
   const double* qna = h->qn;
   const float* xna = h->xn;
   if (h->mini) {
-    const long long st = window_start(h->n, h->m_mb, h->iter_base);
-    KM_TRY(launch_gather_rows(h->X, h->ldx, h->perm, h->n, st, h->m_mb, h->d, h->Xw, h->ldx, s),
+    const long long st = window_start(h->n, h->m_mb, h->run_base + slot);
+    KM_TRY(launch_gather_rows(h->X, h->ldx, h->perm, h->n, st, h->m_mb, h->d, h->Xw, h->ldx, s,
+                              h->stop),
            KMEANS_ERROR_CONSTRUCT_MINIBATCH);
-    KM_TRY(launch_gather_vec(h->qn, h->xn, h->perm, h->n, st, h->m_mb, h->qnw, h->xnw, s),
+    KM_TRY(launch_gather_vec(h->qn, h->xn, h->perm, h->n, st, h->m_mb, h->qnw, h->xnw, s,
+                             h->stop),
            KMEANS_ERROR_CONSTRUCT_MINIBATCH);
     if (h->Xbw)
-      KM_TRY(launch_to_bf16(h->Xw, h->ldx, h->m_mb, h->d, h->Xbw, h->ldb, s),
+      KM_TRY(launch_to_bf16(h->Xw, h->ldx, h->m_mb, h->d, h->Xbw, h->ldb, s, h->stop),
              KMEANS_ERROR_CONSTRUCT_MINIBATCH);
     Xa = h->Xw;
     Xba = h->Xbw;
@@ -344,7 +364,8 @@ int step(kmgb_handle* h, int slot) {
   // reset (kmeans.cpp:1142-1170): norms of the current centers, cleared counters
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
   KM_TRY(cudaMemsetAsync(h->rr_count, 0, sizeof(int), s), KMEANS_ERROR_RESET);
-  KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s),
+  KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
+                             h->stop),
          KMEANS_ERROR_RESET);
   KM_TRY(h->pmark(1), KMEANS_ERROR_RESET);
   // closest centers (kmeans.cpp:910-1014)
@@ -360,6 +381,7 @@ int step(kmgb_handle* h, int slot) {
   a.k = h->k;
   a.d = h->d;
   a.certify = h->opt.certify;
+  a.stop = h->stop;
   if (h->opt.assign_tier == KMGB_ASSIGN_BF16) {
     a.gamma = assign_bf16_gamma(h->d);
     KM_TRY(launch_assign_bf16(Xba, h->ldb, h->Cb, h->ldb, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
@@ -384,6 +406,7 @@ int step(kmgb_handle* h, int slot) {
     r.d = h->d;
     r.mode = 0;
     r.max_list = na;
+    r.stop = h->stop;
     KM_TRY(launch_rerank(r, s), KMEANS_ERROR_CLOSEST_CENTERS);
   }
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
@@ -401,6 +424,7 @@ int run(kmgb_handle* h, int iters, double criterion) {
     set_err("kmgb_run: data and centers must be set first");
     return KMEANS_ERROR_COMPUTE;
   }
+  iters = std::max(iters, 0);
   if (iters > h->sse_cap) {
     double* nd = nullptr;
     KM_TRY(dalloc(&nd, iters), KMEANS_ERROR_COMPUTE);
@@ -408,35 +432,46 @@ int run(kmgb_handle* h, int iters, double criterion) {
     h->sse_dev = nd;
     h->sse_cap = iters;
   }
-  h->sse_host.assign(std::max(iters, 0), 0.0);
+  h->sse_host.assign(iters, 0.0);
+  h->run_base = h->iter_base;
+  h->uw.criterion = criterion;
+  h->criterion = criterion;
+  // loop state (kmeans.cpp:40-41): SSE_old = 0, relErr = 1, not stopped
+  KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);  // pinned init buffer reuse
+  h->loop_init[0] = 0.0;
+  h->loop_init[1] = 1.0;
+  KM_TRY(cudaMemsetAsync(h->stop, 0, sizeof(int), h->stream), KMEANS_ERROR_COMPUTE);
+  KM_TRY(cudaMemsetAsync(h->iters_done, 0, sizeof(int), h->stream), KMEANS_ERROR_COMPUTE);
+  KM_TRY(cudaMemcpyAsync(h->loopf, h->loop_init, 2 * sizeof(double), cudaMemcpyHostToDevice,
+                         h->stream),
+         KMEANS_ERROR_COMPUTE);
   KM_TRY(cudaEventRecord(h->ev0, h->stream), KMEANS_ERROR_COMPUTE);
-  double sse_old = 0.0, rel = 1.0;
-  int it = 0;
-  while (it < iters && rel > criterion) {
+  // Every iteration is enqueued; the SSE reduction evaluates the stop rule on the device and
+  // the kernels of later iterations return at once after it fires.
+  for (int it = 0; it < iters; ++it) {
     int rc = step(h, it);
     if (rc) return rc;
-    ++h->iter_base;
-    if (criterion >= 0.0) {
-      KM_TRY(cudaMemcpyAsync(h->sse_pinned, h->sse_dev + it, sizeof(double),
-                             cudaMemcpyDeviceToHost, h->stream),
-             KMEANS_ERROR_COMPACTNESS);
-      KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);
-      const double sse = *h->sse_pinned;
-      rel = std::fabs(sse - sse_old) / std::fabs(sse);
-      sse_old = sse;
-    }
-    ++it;
   }
   KM_TRY(cudaEventRecord(h->ev1, h->stream), KMEANS_ERROR_COMPUTE);
-  h->iterations = it;
-  // kmeans.hpp:198-200: success only when relErr <= criterion, which never holds for
-  // criterion < 0 (fixed-iteration runs return KMEANS_NONCONVERGENCE).
-  h->status = (criterion >= 0.0 && rel <= criterion) ? KMEANS_SUCCESS : KMEANS_NONCONVERGENCE;
+  h->pending = true;
   return 0;
 }
 
 int finish(kmgb_handle* h) {
   KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);
+  if (h->pending) {
+    int done = 0;
+    double loop[2] = {0.0, 1.0};
+    KM_TRY(cudaMemcpy(&done, h->iters_done, sizeof(int), cudaMemcpyDeviceToHost),
+           KMEANS_ERROR_COMPUTE);
+    KM_TRY(cudaMemcpy(loop, h->loopf, sizeof(loop), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPUTE);
+    h->iterations = done;
+    h->iter_base = h->run_base + done;
+    // kmeans.hpp:198-200: success only when relErr <= criterion (never for criterion < 0, NaN
+    // relErr included)
+    h->status = (loop[1] <= h->criterion) ? KMEANS_SUCCESS : KMEANS_NONCONVERGENCE;
+    h->pending = false;
+  }
   int e = 0;
   KM_TRY(cudaMemcpy(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPUTE);
   if (e) {

@@ -23,6 +23,7 @@ struct AssignArgs {
   int d;
   int certify;            // 0: write arg-min labels only
   float gamma;
+  const int* stop;        // device stop flag of the run (nullable)
 };
 
 // FP32 SIMT assignment. X: [n][ldx] FP32, Cop: [k][ldc] FP32 (ld multiples of 4 floats).
@@ -51,6 +52,7 @@ struct RerankArgs {
   long long n; int k; int d;
   int mode;
   long long max_list;
+  const int* stop;
 };
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s);
 
@@ -58,14 +60,15 @@ cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s);
 // rows -> 0), optional BF16 copy Cb[k][ldcb], cn (+inf for NaN rows) and atomically raise
 // *cmax (must be zeroed before).
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop,
-                                void* Cb, long long ldcb, float* cn, float* cmax, cudaStream_t s);
+                                void* Cb, long long ldcb, float* cn, float* cmax, cudaStream_t s,
+                                const int* stop = nullptr);
 
 // Per-point norms, computed once per data set: qn = ||x||^2 (FP64), xn = upper bound ||x||.
 cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,
                                float* xn, cudaStream_t s);
 // BF16 copy of the data set (zero padded to ldb columns).
 cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
-                           long long ldb, cudaStream_t s);
+                           long long ldb, cudaStream_t s, const int* stop = nullptr);
 
 // Deterministic update: stable counting sort by label, FP64 piece sums, finalize.
 struct UpdateWork {
@@ -83,6 +86,12 @@ struct UpdateWork {
   double* sse_k;        // [k]
   long long* counts;    // [k]
   int* err;
+  // stop rule (kmeans.cpp:1194-1237), evaluated on the device by the SSE reduction
+  int* stop;            // nullable
+  double criterion;
+  double* sse_prev;     // previous SSE (0 before the first iteration)
+  double* rel_out;      // last relErr
+  int* iters_done;      // iterations completed
 };
 size_t update_scan_tmp_elems(long long elems);
 cudaError_t launch_update(const float* X, const double* qn, const int* labels, float* C,
@@ -102,10 +111,10 @@ void plan_update_tiles(long long n, int k, int* tile_pts, int* ntiles);
 // Mini-batch gather: rows perm[(start + r) mod m] of Xsrc into Xdst (m_mb rows).
 cudaError_t launch_gather_rows(const float* Xsrc, long long ldx, const int* perm, long long m,
                                long long start, long long m_mb, int d, float* Xdst,
-                               long long ldd, cudaStream_t s);
+                               long long ldd, cudaStream_t s, const int* stop = nullptr);
 cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* perm,
                               long long m, long long start, long long m_mb, double* qdst,
-                              float* xdst, cudaStream_t s);
+                              float* xdst, cudaStream_t s, const int* stop = nullptr);
 
 constexpr int kSumPiece = 128;
 

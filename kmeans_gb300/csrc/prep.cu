@@ -16,7 +16,9 @@ namespace {
 // One warp per center.
 __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, int k, int d,
                                     float* __restrict__ Cop, __nv_bfloat16* __restrict__ Cb,
-                                    long long ldcb, float* __restrict__ cn, float* cmax) {
+                                    long long ldcb, float* __restrict__ cn, float* cmax,
+                                    const int* stop) {
+  if (stopped(stop)) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= k) return;
@@ -66,7 +68,8 @@ __global__ void point_norms_kernel(const float* __restrict__ X, long long ldx, l
 }
 
 __global__ void to_bf16_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
-                               __nv_bfloat16* __restrict__ Xb, long long ldb) {
+                               __nv_bfloat16* __restrict__ Xb, long long ldb, const int* stop) {
+  if (stopped(stop)) return;
   const long long total = n * ldb;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
@@ -78,7 +81,9 @@ __global__ void to_bf16_kernel(const float* __restrict__ X, long long ldx, long 
 
 __global__ void gather_rows_kernel(const float* __restrict__ Xs, long long ldx,
                                    const int* __restrict__ perm, long long m, long long start,
-                                   long long m_mb, int d, float* __restrict__ Xd, long long ldd) {
+                                   long long m_mb, int d, float* __restrict__ Xd, long long ldd,
+                                   const int* stop) {
+  if (stopped(stop)) return;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= m_mb) return;
@@ -91,7 +96,9 @@ __global__ void gather_rows_kernel(const float* __restrict__ Xs, long long ldx,
 
 __global__ void gather_vec_kernel(const double* __restrict__ qs, const float* __restrict__ xs,
                                   const int* __restrict__ perm, long long m, long long start,
-                                  long long m_mb, double* __restrict__ qd, float* __restrict__ xd) {
+                                  long long m_mb, double* __restrict__ qd, float* __restrict__ xd,
+                                  const int* stop) {
+  if (stopped(stop)) return;
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < m_mb;
        r += (long long)gridDim.x * blockDim.x) {
     long long pos = start + r;
@@ -105,13 +112,14 @@ __global__ void gather_vec_kernel(const double* __restrict__ qs, const float* __
 }  // namespace
 
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop, void* Cb,
-                                long long ldcb, float* cn, float* cmax, cudaStream_t s) {
+                                long long ldcb, float* cn, float* cmax, cudaStream_t s,
+                                const int* stop) {
   if (k <= 0) return cudaSuccess;
   const int threads = 256;
   const int blocks = (int)(((long long)k * 32 + threads - 1) / threads);
   prep_centers_kernel<<<blocks, threads, 0, s>>>(C, ldc, k, d, Cop,
                                                  reinterpret_cast<__nv_bfloat16*>(Cb), ldcb, cn,
-                                                 cmax); kmgb::count_launches(1);
+                                                 cmax, stop); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 
@@ -125,29 +133,29 @@ cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d
 }
 
 cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
-                           long long ldb, cudaStream_t s) {
+                           long long ldb, cudaStream_t s, const int* stop) {
   if (n <= 0) return cudaSuccess;
   to_bf16_kernel<<<152 * 16, 256, 0, s>>>(X, ldx, n, d, reinterpret_cast<__nv_bfloat16*>(Xb),
-                                          ldb); kmgb::count_launches(1);
+                                          ldb, stop); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gather_rows(const float* Xsrc, long long ldx, const int* perm, long long m,
                                long long start, long long m_mb, int d, float* Xdst, long long ldd,
-                               cudaStream_t s) {
+                               cudaStream_t s, const int* stop) {
   if (m_mb <= 0) return cudaSuccess;
   const int threads = 256;
   const long long blocks = (m_mb * 32 + threads - 1) / threads;
   gather_rows_kernel<<<(unsigned)blocks, threads, 0, s>>>(Xsrc, ldx, perm, m, start, m_mb, d,
-                                                          Xdst, ldd); kmgb::count_launches(1);
+                                                          Xdst, ldd, stop); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* perm, long long m,
                               long long start, long long m_mb, double* qdst, float* xdst,
-                              cudaStream_t s) {
+                              cudaStream_t s, const int* stop) {
   if (m_mb <= 0) return cudaSuccess;
-  gather_vec_kernel<<<152 * 4, 256, 0, s>>>(qsrc, xsrc, perm, m, start, m_mb, qdst, xdst); kmgb::count_launches(1);
+  gather_vec_kernel<<<152 * 4, 256, 0, s>>>(qsrc, xsrc, perm, m, start, m_mb, qdst, xdst, stop); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

@@ -48,6 +48,7 @@ __device__ __forceinline__ double exact_value(int mode, const float* __restrict_
 }
 
 __global__ void rerank_kernel(RerankArgs a) {
+  if (stopped(a.stop)) return;
   extern __shared__ float xs_all[];
   const int warps = blockDim.x >> 5;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;

@@ -56,7 +56,9 @@ __device__ int block_excl_scan(int v) {
   return res;
 }
 
-__global__ void scan_reduce_kernel(const int* __restrict__ in, long long n, int* __restrict__ sums) {
+__global__ void scan_reduce_kernel(const int* __restrict__ in, long long n, int* __restrict__ sums,
+                                   const int* stop) {
+  if (stopped(stop)) return;
   const long long base = (long long)blockIdx.x * SCAN_SEG + (long long)threadIdx.x * SCAN_V;
   int s = 0;
 #pragma unroll
@@ -74,7 +76,9 @@ __global__ void scan_reduce_kernel(const int* __restrict__ in, long long n, int*
 }
 
 // In-place exclusive scan of segment blockIdx.x, plus offset (*offsets)[blockIdx.x] if given.
-__global__ void scan_seg_kernel(int* __restrict__ data, long long n, const int* __restrict__ offsets) {
+__global__ void scan_seg_kernel(int* __restrict__ data, long long n, const int* __restrict__ offsets,
+                                const int* stop) {
+  if (stopped(stop)) return;
   const long long base = (long long)blockIdx.x * SCAN_SEG + (long long)threadIdx.x * SCAN_V;
   int vals[SCAN_V];
   int s = 0;
@@ -93,7 +97,8 @@ __global__ void scan_seg_kernel(int* __restrict__ data, long long n, const int* 
 }
 
 __global__ void hist_kernel(const int* __restrict__ labels, long long n, int k, int tile_pts,
-                            int ntiles, int* __restrict__ hist, int* err) {
+                            int ntiles, int* __restrict__ hist, int* err, const int* stop) {
+  if (stopped(stop)) return;
   const int tile = blockIdx.x;
   const long long i0 = (long long)tile * tile_pts;
   const long long i1 = min(n, i0 + tile_pts);
@@ -118,7 +123,8 @@ __global__ void hist_kernel(const int* __restrict__ labels, long long n, int k, 
 // of label j (piece_cnt[k] = 0, the scan turns it into the total); counts[j] = members.
 __global__ void label_offsets_kernel(const int* __restrict__ hist, long long n, int k, int ntiles,
                                      int* __restrict__ label_off, int* __restrict__ piece_cnt,
-                                     long long* __restrict__ counts) {
+                                     long long* __restrict__ counts, const int* stop) {
+  if (stopped(stop)) return;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j > k) return;
   if (j == k) {
@@ -135,7 +141,8 @@ __global__ void label_offsets_kernel(const int* __restrict__ hist, long long n, 
 
 template <bool SMEM>
 __global__ void scatter_kernel(const int* __restrict__ labels, long long n, int k, int tile_pts,
-                               int ntiles, int* pos, int* __restrict__ sorted) {
+                               int ntiles, int* pos, int* __restrict__ sorted, const int* stop) {
+  if (stopped(stop)) return;
   extern __shared__ int cnt_s[];
   const int tile = blockIdx.x;
   const int lane = threadIdx.x;
@@ -187,7 +194,8 @@ __global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
                                   const double* __restrict__ qn, const int* __restrict__ sorted,
                                   const int* __restrict__ label_off, const int* __restrict__ pstart,
                                   int k, int d, double* __restrict__ part,
-                                  double* __restrict__ partq) {
+                                  double* __restrict__ partq, const int* stop) {
+  if (stopped(stop)) return;
   const int ptot = pstart[k];
   const int lane = threadIdx.x & 31;
   const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -227,7 +235,8 @@ __global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
 __global__ void finalize_kernel(const double* __restrict__ part, const double* __restrict__ partq,
                                 const int* __restrict__ label_off, const int* __restrict__ pstart,
                                 int k, int d, float* __restrict__ C, long long ldc,
-                                int empty_policy, double* __restrict__ sse_k) {
+                                int empty_policy, double* __restrict__ sse_k, const int* stop) {
+  if (stopped(stop)) return;
   const int j = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (j >= k) return;
@@ -258,7 +267,12 @@ __global__ void finalize_kernel(const double* __restrict__ part, const double* _
   }
 }
 
-__global__ void sse_reduce_kernel(const double* __restrict__ sse_k, int k, double* __restrict__ out) {
+// Second level of the SSE reduction plus the loop's stop rule (kmeans.cpp:1234-1237,1194):
+// relErr = |SSE - SSE_old| / |SSE|; the run stops once !(relErr > criterion), NaN included.
+__global__ void sse_reduce_kernel(const double* __restrict__ sse_k, int k, double* __restrict__ out,
+                                  int* stop, double criterion, double* sse_prev, double* rel_out,
+                                  int* iters_done) {
+  if (stopped(stop)) return;
   __shared__ double red[1024];
   const int per = (k + blockDim.x - 1) / blockDim.x;
   double s = 0.0;
@@ -269,20 +283,30 @@ __global__ void sse_reduce_kernel(const double* __restrict__ sse_k, int k, doubl
     if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = red[0];
+  if (threadIdx.x == 0) {
+    const double sse = red[0];
+    *out = sse;
+    if (sse_prev) {
+      const double rel = fabs(sse - *sse_prev) / fabs(sse);
+      *sse_prev = sse;
+      *rel_out = rel;
+      *iters_done += 1;
+      if (stop && !(rel > criterion)) *stop = 1;
+    }
+  }
 }
 
-cudaError_t excl_scan(int* data, long long n, int* tmp, cudaStream_t s) {
+cudaError_t excl_scan(int* data, long long n, int* tmp, cudaStream_t s, const int* stop) {
   if (n <= 0) return cudaSuccess;
   const long long nb = (n + SCAN_SEG - 1) / SCAN_SEG;
   if (nb > SCAN_SEG) return cudaErrorInvalidValue;
   if (nb == 1) {
-    scan_seg_kernel<<<1, SCAN_T, 0, s>>>(data, n, nullptr); kmgb::count_launches(1);
+    scan_seg_kernel<<<1, SCAN_T, 0, s>>>(data, n, nullptr, stop); kmgb::count_launches(1);
     return cudaGetLastError();
   }
-  scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp); kmgb::count_launches(1);
-  scan_seg_kernel<<<1, SCAN_T, 0, s>>>(tmp, nb, nullptr); kmgb::count_launches(1);
-  scan_seg_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp); kmgb::count_launches(1);
+  scan_reduce_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp, stop); kmgb::count_launches(1);
+  scan_seg_kernel<<<1, SCAN_T, 0, s>>>(tmp, nb, nullptr, stop); kmgb::count_launches(1);
+  scan_seg_kernel<<<(unsigned)nb, SCAN_T, 0, s>>>(data, n, tmp, stop); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 
@@ -307,13 +331,13 @@ static cudaError_t sort_by_label(const int* labels, const UpdateWork& w, cudaStr
   const int k = w.k;
   const long long hist_elems = (long long)k * w.ntiles;
   KMGB_CUDA_TRY(cudaMemsetAsync(w.hist, 0, sizeof(int) * hist_elems, s));
-  hist_kernel<<<w.ntiles, 256, 0, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist, w.err); kmgb::count_launches(1);
+  hist_kernel<<<w.ntiles, 256, 0, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist, w.err, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
-  KMGB_CUDA_TRY(excl_scan(w.hist, hist_elems, w.scan_tmp, s));
+  KMGB_CUDA_TRY(excl_scan(w.hist, hist_elems, w.scan_tmp, s, w.stop));
   label_offsets_kernel<<<(k + 1 + 255) / 256, 256, 0, s>>>(w.hist, n, k, w.ntiles, w.label_off,
-                                                          w.piece_cnt, w.counts); kmgb::count_launches(1);
+                                                          w.piece_cnt, w.counts, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
-  KMGB_CUDA_TRY(excl_scan(w.piece_cnt, k + 1, w.scan_tmp, s));
+  KMGB_CUDA_TRY(excl_scan(w.piece_cnt, k + 1, w.scan_tmp, s, w.stop));
   const size_t smem = sizeof(int) * (size_t)k;
   if (smem <= 96 * 1024) {
     static int attr_k = -1;
@@ -323,10 +347,10 @@ static cudaError_t sort_by_label(const int* labels, const UpdateWork& w, cudaStr
       attr_k = k;
     }
     scatter_kernel<true><<<w.ntiles, 32, smem, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist,
-                                                    w.sorted); kmgb::count_launches(1);
+                                                    w.sorted, w.stop); kmgb::count_launches(1);
   } else {
     scatter_kernel<false><<<w.ntiles, 32, 0, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist,
-                                                  w.sorted); kmgb::count_launches(1);
+                                                  w.sorted, w.stop); kmgb::count_launches(1);
   }
   return cudaGetLastError();
 }
@@ -340,14 +364,15 @@ cudaError_t launch_update(const float* X, const double* qn, const int* labels, f
   const long long max_pieces = w.max_pieces;
   long long warps = max_pieces < 152LL * 64 ? max_pieces : 152LL * 64;
   piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-      X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq); kmgb::count_launches(1);
+      X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   finalize_kernel<<<(unsigned)(((long long)k * 32 + 255) / 256), 256, 0, s>>>(
       w.part, qn ? w.partq : nullptr, w.label_off, w.piece_cnt, k, w.d, C, ldc, empty_policy,
-      w.sse_k); kmgb::count_launches(1);
+      w.sse_k, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   if (sse_out) {
-    sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, k, sse_out); kmgb::count_launches(1);
+    sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, k, sse_out, w.stop, w.criterion, w.sse_prev,
+                                         w.rel_out, w.iters_done); kmgb::count_launches(1);
     KMGB_CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;
@@ -400,7 +425,7 @@ cudaError_t launch_tile_accumulate(const T* X, long long ldx, const int* labels,
   KMGB_CUDA_TRY(sort_by_label(labels, w, s));
   long long warps = w.max_pieces < 152LL * 64 ? w.max_pieces : 152LL * 64;
   piece_sums_kernel<T><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-      X, ldx, nullptr, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, nullptr); kmgb::count_launches(1);
+      X, ldx, nullptr, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, nullptr, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   accumulate_kernel<<<(unsigned)(((long long)w.k * 32 + 255) / 256), 256, 0, s>>>(
       w.part, w.label_off, w.piece_cnt, w.k, w.d, acc, acc_counts); kmgb::count_launches(1);

@@ -9,6 +9,7 @@ from kmeans_gb300.synthetic import mixture_numpy, sample_init
 
 pytestmark = pytest.mark.gpu
 SSE_RTOL = 1e-10
+TIERS = [0, 1]  # plain FP32 fused kernel, tcgen05 BF16 tensor-core kernel
 
 
 def check_same(res, ref, sse_rtol=SSE_RTOL):
@@ -20,24 +21,27 @@ def check_same(res, ref, sse_rtol=SSE_RTOL):
     np.testing.assert_allclose(res.sse, sse, rtol=sse_rtol)
 
 
-def test_c1_config_fp32(km, orc, torch_cuda):
+@pytest.mark.parametrize("tier", TIERS)
+def test_c1_config(km, orc, torch_cuda, tier):
     X, _, _ = mixture_numpy(100_000, 32, 64, seed=101, mean_lo=-10, mean_hi=10)
     init = X[sample_init(len(X), 64, seed=102)]
-    res = km.lloyd(X, 64, init=init, max_iters=20)
+    res = km.lloyd(X, 64, init=init, max_iters=20, assign_tier=tier)
     check_same(res, orc.lloyd(X, init, 20))
     assert res.status == 13
 
 
 @pytest.mark.parametrize("n,d,k", [(1, 1, 1), (130, 3, 7), (1000, 129, 200), (4097, 64, 129),
                                    (20000, 128, 256), (3001, 17, 1)])
-def test_odd_shapes(km, orc, torch_cuda, n, d, k):
+@pytest.mark.parametrize("tier", TIERS)
+def test_odd_shapes(km, orc, torch_cuda, n, d, k, tier):
     X, _, _ = mixture_numpy(n, d, max(k, 1), seed=n + d + k)
     init = X[sample_init(n, k, seed=3)]
-    res = km.lloyd(X, k, init=init, max_iters=6)
+    res = km.lloyd(X, k, init=init, max_iters=6, assign_tier=tier)
     check_same(res, orc.lloyd(X, init, 6))
 
 
-def test_near_ties_are_resolved_exactly(km, orc, torch_cuda):
+@pytest.mark.parametrize("tier", TIERS)
+def test_near_ties_are_resolved_exactly(km, orc, torch_cuda, tier):
     # points placed on (or within a few ulps of) the bisector of two centers
     rng = np.random.default_rng(17)
     d, k = 48, 20
@@ -46,7 +50,7 @@ def test_near_ties_are_resolved_exactly(km, orc, torch_cuda):
     t = 0.5 + rng.integers(-3, 4, 4000) * 1e-7
     X = (Cn[a] * t[:, None] + Cn[b] * (1 - t[:, None])).astype(np.float32)
     X = np.concatenate([X, Cn, Cn[:5]])  # exact duplicates of centers too
-    res = km.lloyd(X, k, init=Cn, max_iters=1)
+    res = km.lloyd(X, k, init=Cn, max_iters=1, assign_tier=tier)
     check_same(res, orc.lloyd(X, Cn, 1))
     assert res.reranked > 0
 
@@ -78,11 +82,12 @@ def test_convergence_criterion(km, orc, torch_cuda):
     check_same(res, ref)
 
 
+@pytest.mark.parametrize("tier", TIERS)
 @pytest.mark.parametrize("policy", [0, 1])
-def test_empty_cluster_policy(km, orc, torch_cuda, policy):
+def test_empty_cluster_policy(km, orc, torch_cuda, policy, tier):
     X, _, _ = mixture_numpy(8000, 10, 6, seed=9)
     init = np.concatenate([X[:6], np.full((2, 10), 1e4, np.float32)])  # two far centers
-    res = km.lloyd(X, 8, init=init, max_iters=5, empty_policy=policy)
+    res = km.lloyd(X, 8, init=init, max_iters=5, empty_policy=policy, assign_tier=tier)
     ref = orc.lloyd(X, init, 5, empty_policy=policy)
     check_same(res, ref)
     assert res.empty_clusters == 2
@@ -92,11 +97,12 @@ def test_empty_cluster_policy(km, orc, torch_cuda, policy):
         assert np.array_equal(res.centers[6:], init[6:])
 
 
+@pytest.mark.parametrize("tier", TIERS)
 @pytest.mark.parametrize("frac", [0.25, 0.3333, 0.9])
-def test_minibatch_windows(km, orc, torch_cuda, frac):
+def test_minibatch_windows(km, orc, torch_cuda, frac, tier):
     X, _, _ = mixture_numpy(20_000, 16, 10, seed=10)
     init = X[sample_init(len(X), 10, seed=4)]
-    res = km.lloyd(X, 10, init=init, max_iters=9, mini_batch_fraction=frac)
+    res = km.lloyd(X, 10, init=init, max_iters=9, mini_batch_fraction=frac, assign_tier=tier)
     check_same(res, orc.lloyd(X, init, 9, mb_fraction=frac))
 
 
@@ -140,7 +146,8 @@ def test_compute_kmeans_d(km, orc, torch_cuda):
     assert np.array_equal(result.reshape(n, k), c.T)
 
 
-def test_c2_scale_properties(km, orc, torch_cuda):
+@pytest.mark.parametrize("tier", TIERS)
+def test_c2_scale_properties(km, orc, torch_cuda, tier):
     """Full c2 size (4M x 128, K=1024): sampled labels equal the oracle's FP64 arg-min with the
     centers that produced them, centers equal FP64 means of their members, SSE equals an
     independent FP64 evaluation."""
@@ -150,7 +157,7 @@ def test_c2_scale_properties(km, orc, torch_cuda):
     X, _, _ = mixture_torch(n, d, k, seed=20, mean_lo=-20, mean_hi=20, std=(0.3, 3.0))
     idx = torch.from_numpy(sample_init(n, k, seed=21)).cuda()
     init = X[idx].cpu().numpy()
-    h = km.Handle(n, d, k, max_iters=4)
+    h = km.Handle(n, d, k, max_iters=4, assign_tier=tier)
     h.set_data(X, True)
     h.set_centers(init, False)
     h.run(2)
@@ -175,3 +182,19 @@ def test_c2_scale_properties(km, orc, torch_cuda):
     ref_sse = ((Xg - torch.from_numpy(c_new).cuda().double()[lt]) ** 2).sum().item()
     assert abs(sse - ref_sse) <= 1e-9 * ref_sse
     h.close()
+
+
+def test_zero_sse_stops_like_the_reference(km, orc, torch_cuda):
+    """relErr = |0 - 0| / |0| is NaN: the reference loop ends (NaN > criterion is false) even for
+    criterion < 0 (kmeans.cpp:1194, 1237)."""
+    X = np.array([[1.5, -2.0]], np.float32)
+    res = km.lloyd(X, 1, init=X.copy(), max_iters=6)
+    assert res.iterations == 1 and res.status == 13 and res.sse[0] == 0.0
+
+
+def test_bf16_tier_certifies_well_separated_points(km, orc, torch_cuda):
+    """On well separated clusters almost every point is certified by the tensor-core pass."""
+    X, comp, means = mixture_numpy(200_000, 64, 100, seed=31, mean_lo=-50, mean_hi=50)
+    res = km.lloyd(X, 100, init=means, max_iters=2, assign_tier=1)
+    check_same(res, orc.lloyd(X, means, 2))
+    assert res.reranked < 0.01 * 2 * len(X)
