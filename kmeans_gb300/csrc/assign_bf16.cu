@@ -38,7 +38,7 @@ constexpr uint32_t KB_BYTES = BM * BK * 2;  // 16 KB: one tile k-block == one C 
 constexpr int MAX_STAGES = 8;
 constexpr int MAX_D = 256;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr size_t SMEM_LIMIT = 227 * 1024;
+constexpr size_t SMEM_CAP = 227 * 1024;  // upper bound; the device's opt-in limit is queried
 
 // UMMA instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, N>>3, M>>4.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -369,6 +369,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
 }
 
 int g_num_sms = 0;
+size_t g_smem_budget = 0;  // dynamic shared memory a CTA of this kernel may use
 
 }  // namespace
 
@@ -384,27 +385,33 @@ cudaError_t launch_assign_bf16(const void* Xb, long long ldxb, const void* Cb, l
   if (!bf16_tc_supported(a.d) || (ldxb % 8) || (ldcb % 8) ||
       (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15))
     return cudaErrorInvalidValue;
+  if (g_num_sms == 0) {
+    int dev = 0, optin = 0;
+    KMGB_CUDA_TRY(cudaGetDevice(&dev));
+    KMGB_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+    KMGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel));
+    size_t budget = (size_t)optin - fa.sharedSizeBytes;
+    if (budget > SMEM_CAP) budget = SMEM_CAP;
+    KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
+    g_smem_budget = budget;
+  }
   const int nkb = (a.d + BK - 1) / BK;
   const size_t xbytes = (size_t)TILES * nkb * KB_BYTES;
   // double-buffer the unit's points when that still leaves a 4-stage ring for C
-  const int xbufs = (2 * xbytes + 4 * KB_BYTES + 1024 <= SMEM_LIMIT) ? 2 : 1;
-  int stages = (int)((SMEM_LIMIT - 1024 - xbufs * xbytes) / KB_BYTES);
+  const size_t lim = g_smem_budget;
+  const int xbufs = (2 * xbytes + 4 * KB_BYTES + 1024 <= lim) ? 2 : 1;
+  if (lim < xbufs * xbytes + 1024 + 2 * KB_BYTES) return cudaErrorInvalidValue;
+  int stages = (int)((lim - 1024 - xbufs * xbytes) / KB_BYTES);
   if (stages > MAX_STAGES) stages = MAX_STAGES;
-  if (stages < 2) return cudaErrorInvalidValue;
   const size_t smem = xbufs * xbytes + (size_t)stages * KB_BYTES + 1024;
   CUtensorMap tmX, tmC;
   KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmX, Xb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.d,
                                   (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
   KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmC, Cb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.d,
                                   (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BN));
-  if (g_num_sms == 0) {
-    int dev = 0;
-    KMGB_CUDA_TRY(cudaGetDevice(&dev));
-    KMGB_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
-    KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)SMEM_LIMIT));
-  }
   const long long n_units = (a.n + UNIT - 1) / UNIT;
   const int grid = (int)(n_units < g_num_sms ? n_units : g_num_sms);
   assign_bf16_kernel<<<grid, NTHREADS, smem, s>>>(tmX, tmC, a, stages, xbufs);

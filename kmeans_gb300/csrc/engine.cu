@@ -141,7 +141,8 @@ struct kmgb_handle {
   // assignment
   int* labels = nullptr;
   int* rr_list = nullptr;
-  int* rr_count = nullptr;
+  int* rr_count = nullptr;     // [0] flagged by the assignment, [1] left for the FP64 stage
+  int* rr_list2 = nullptr;
   unsigned long long* rr_stats = nullptr;
   int* err = nullptr;
   // device-side loop state: stop flag, previous SSE, last relErr, iterations done
@@ -182,7 +183,7 @@ struct kmgb_handle {
   ~kmgb_handle() {
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
     void* ptrs[] = {X, Xb, qn, xn, perm, Xw, Xbw, qnw, xnw, C, Cop, Cb, cn, cmax, labels,
-                    rr_list, rr_count, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
+                    rr_list, rr_count, rr_list2, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
                     uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
                     stop, loopf, iters_done};
     for (void* p : ptrs)
@@ -256,7 +257,8 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   const long long na = h->n_act;
   KM_TRY(dalloc(&h->labels, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_list, na), (delete h, code));
-  KM_TRY(dalloc(&h->rr_count, 1), (delete h, code));
+  KM_TRY(dalloc(&h->rr_count, 2), (delete h, code));
+  KM_TRY(dalloc(&h->rr_list2, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_stats, 2), (delete h, code));
   KM_TRY(dalloc(&h->err, 1), (delete h, code));
   KM_TRY(dalloc(&h->stop, 1), (delete h, code));
@@ -363,7 +365,7 @@ int step(kmgb_handle* h, int slot) {
   KM_TRY(h->pmark(0), KMEANS_ERROR_RESET);
   // reset (kmeans.cpp:1142-1170): norms of the current centers, cleared counters
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
-  KM_TRY(cudaMemsetAsync(h->rr_count, 0, sizeof(int), s), KMEANS_ERROR_RESET);
+  KM_TRY(cudaMemsetAsync(h->rr_count, 0, 2 * sizeof(int), s), KMEANS_ERROR_RESET);
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
                              h->stop),
          KMEANS_ERROR_RESET);
@@ -407,7 +409,13 @@ int step(kmgb_handle* h, int slot) {
     r.mode = 0;
     r.max_list = na;
     r.stop = h->stop;
+    // FP32 stage over the flagged points, exact FP64 stage over what FP32 cannot separate
+    KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 1, s), KMEANS_ERROR_CLOSEST_CENTERS);
+    r.list = h->rr_list2;
+    r.count = h->rr_count + 1;
+    r.stats = nullptr;
     KM_TRY(launch_rerank(r, s), KMEANS_ERROR_CLOSEST_CENTERS);
+    KM_TRY(launch_count_stats(h->rr_count, h->rr_stats, h->stop, s), KMEANS_ERROR_CLOSEST_CENTERS);
   }
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
   // cluster centers + compactness (kmeans.cpp:1018-1104)

@@ -55,6 +55,11 @@ struct RerankArgs {
   const int* stop;
 };
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s);
+// FP32 stage of the Lloyd re-rank (mode 0): certifies what FP32 can, passes the rest to list2.
+cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, cudaStream_t s);
+// stats[0] += counts[0] (points re-ranked), stats[1] += counts[1] (points that needed FP64).
+cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, const int* stop,
+                               cudaStream_t s);
 
 // Center preparation: from the official centers C[k][ldc] write the operand copy Cop (NaN
 // rows -> 0), optional BF16 copy Cb[k][ldcb], cn (+inf for NaN rows) and atomically raise

@@ -128,7 +128,182 @@ __global__ void rerank_kernel(RerankArgs a) {
   }
 }
 
+// Tiled FP32 stage of the Lloyd re-rank (mode 0): 32 flagged points per CTA iteration against
+// 64-center blocks staged in shared memory; each thread accumulates 4 points x 2 centers of
+// sum_d (x_d - c_d)^2 with float4 loads. Per point (best, index, second) is merged over the 32
+// threads that share it (lowest index on ties) and certified with the relative bound of the
+// direct form; uncertified points go to list2 for the exact FP64 stage.
+constexpr int TP = 32;   // points per CTA iteration
+constexpr int TC = 64;   // centers per block
+
+__global__ void __launch_bounds__(256)
+rerank_tiled_kernel(RerankArgs a, int* __restrict__ list2, int* __restrict__ count2) {
+  if (stopped(a.stop)) return;
+  extern __shared__ float4 sm4[];
+  const int dq = (a.d + 3) >> 2;          // float4 per row
+  const int rs = dq + 1;                  // row stride in float4 (padded: conflict-free)
+  float4* xs = sm4;                       // [TP][rs]
+  float4* cs = xs + TP * rs;              // [TC][rs]
+  float* cflag = reinterpret_cast<float*>(cs + TC * rs);  // [TC] 0 usable, +inf unusable
+  __shared__ float mb1[8][TP], mb2[8][TP];
+  __shared__ int mi1[8][TP];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int pq = tid & 7;                 // points pq*4 .. pq*4+3
+  const int cq = tid >> 3;                // centers cq*2, cq*2+1 of the block
+  const long long cnt = min((long long)*(volatile const int*)a.count, a.max_list);
+  const float u = 5.9604645e-8f;
+  const float gam = (float)(a.d + 4) * 2.0f * u * 1.01f;
+
+  for (long long g0 = (long long)blockIdx.x * TP; g0 < cnt; g0 += (long long)gridDim.x * TP) {
+    __syncthreads();
+    // stage the points (zero rows past the list end)
+    for (int e = tid; e < TP * dq; e += blockDim.x) {
+      const int r = e / dq, q = e % dq;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (g0 + r < cnt) {
+        const float* x = a.X + (size_t)a.list[g0 + r] * a.ldx;
+        const int c0 = q * 4;
+        v.x = c0 < a.d ? x[c0] : 0.f;
+        v.y = c0 + 1 < a.d ? x[c0 + 1] : 0.f;
+        v.z = c0 + 2 < a.d ? x[c0 + 2] : 0.f;
+        v.w = c0 + 3 < a.d ? x[c0 + 3] : 0.f;
+      }
+      xs[r * rs + q] = v;
+    }
+    float b1[4], b2[4];
+    int i1[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      b1[i] = INFINITY;
+      b2[i] = INFINITY;
+      i1[i] = -1;
+    }
+    for (int j0 = 0; j0 < a.k; j0 += TC) {
+      __syncthreads();
+      for (int e = tid; e < TC * dq; e += blockDim.x) {
+        const int r = e / dq, q = e % dq;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (j0 + r < a.k) {
+          const float* c = a.C + (size_t)(j0 + r) * a.ldc;
+          const int c0 = q * 4;  // ldc is a multiple of 4 and rows are zero padded
+          v = *reinterpret_cast<const float4*>(c + c0);
+        }
+        cs[r * rs + q] = v;
+      }
+      if (tid < TC) {
+        const int j = j0 + tid;
+        cflag[tid] = (j < a.k && a.cn[j] < INFINITY) ? 0.0f : INFINITY;
+      }
+      __syncthreads();
+      float acc[4][2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = 0.0f;
+      for (int q = 0; q < dq; ++q) {
+        const float4 c0 = cs[(cq * 2) * rs + q];
+        const float4 c1 = cs[(cq * 2 + 1) * rs + q];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float4 x = xs[(pq * 4 + i) * rs + q];
+          float t;
+          t = x.x - c0.x; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.y - c0.y; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.z - c0.z; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.w - c0.w; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.x - c1.x; acc[i][1] = fmaf(t, t, acc[i][1]);
+          t = x.y - c1.y; acc[i][1] = fmaf(t, t, acc[i][1]);
+          t = x.z - c1.z; acc[i][1] = fmaf(t, t, acc[i][1]);
+          t = x.w - c1.w; acc[i][1] = fmaf(t, t, acc[i][1]);
+        }
+      }
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {
+        const int j = j0 + cq * 2 + jj;
+        const float f = cflag[cq * 2 + jj];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float v = acc[i][jj] + f;  // +inf for unusable / padding centers
+          const float nb2 = fminf(b2[i], fmaxf(b1[i], v));
+          const bool lt = v < b1[i];
+          b1[i] = lt ? v : b1[i];
+          i1[i] = lt ? j : i1[i];
+          b2[i] = nb2;
+        }
+      }
+    }
+    // merge the 32 threads of each point: lanes pq, pq+8, pq+16, pq+24 of every warp
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+      for (int off = 8; off < 32; off <<= 1) {
+        const float ob1 = __shfl_xor_sync(0xffffffffu, b1[i], off);
+        const float ob2 = __shfl_xor_sync(0xffffffffu, b2[i], off);
+        const int oi1 = __shfl_xor_sync(0xffffffffu, i1[i], off);
+        const float nb2 = fminf(fminf(b2[i], ob2), fmaxf(b1[i], ob1));
+        const bool take = (ob1 < b1[i]) || (ob1 == b1[i] && (unsigned)oi1 < (unsigned)i1[i]);
+        b1[i] = take ? ob1 : b1[i];
+        i1[i] = take ? oi1 : i1[i];
+        b2[i] = nb2;
+      }
+      if (lane < 8) {
+        mb1[w][pq * 4 + i] = b1[i];
+        mb2[w][pq * 4 + i] = b2[i];
+        mi1[w][pq * 4 + i] = i1[i];
+      }
+    }
+    __syncthreads();
+    if (tid < TP && g0 + tid < cnt) {
+      float f1 = mb1[0][tid], f2 = mb2[0][tid];
+      int fi = mi1[0][tid];
+      for (int ww = 1; ww < 8; ++ww) {
+        const float ob1 = mb1[ww][tid], ob2 = mb2[ww][tid];
+        const int oi1 = mi1[ww][tid];
+        const float nb2 = fminf(fminf(f2, ob2), fmaxf(f1, ob1));
+        const bool take = (ob1 < f1) || (ob1 == f1 && (unsigned)oi1 < (unsigned)fi);
+        f1 = take ? ob1 : f1;
+        fi = take ? oi1 : fi;
+        f2 = nb2;
+      }
+      const int pt = a.list[g0 + tid];
+      // certified when every other center's lower end exceeds the best's upper end
+      if (fi >= 0 && f2 * (1.0f - gam) - 1e-30f > f1 * (1.0f + gam) + 1e-30f) {
+        a.labels[pt] = fi;
+      } else {
+        const int slot = atomicAdd(count2, 1);
+        list2[slot] = pt;
+      }
+    }
+  }
+}
+
 }  // namespace
+
+namespace {
+__global__ void count_stats_kernel(const int* counts, unsigned long long* stats, const int* stop) {
+  if (stopped(stop)) return;
+  stats[0] += (unsigned long long)counts[0];
+  stats[1] += (unsigned long long)counts[1];
+}
+}  // namespace
+
+cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, const int* stop,
+                               cudaStream_t s) {
+  count_stats_kernel<<<1, 1, 0, s>>>(counts, stats, stop);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, cudaStream_t s) {
+  if (a.n <= 0 || a.k <= 0) return cudaSuccess;
+  const int dq = (a.d + 3) / 4;
+  const size_t smem = sizeof(float4) * (size_t)(TP + TC) * (dq + 1) + sizeof(float) * TC;
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024)
+    KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_tiled_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  rerank_tiled_kernel<<<152 * 2, 256, smem, s>>>(a, list2, count2);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s) {
   if (a.n <= 0 || a.k <= 0) return cudaSuccess;
