@@ -195,6 +195,13 @@ typedef struct kmgb_stats {
   long long reserved[8];
 } kmgb_stats;
 
+/* The reference's initial centers, computed on the host: k x d row-major copies of data rows
+ * perm[picks[i]], perm from std::shuffle(default_random_engine(0)) and picks from srand(42) /
+ * rand() % m with the unsorted binary_search (main/cpp/kmeans.cpp:554-557, 876-888). perm and
+ * picks (each nullable) receive the permutation (m) and the picks (k). Needs no GPU. */
+KMGB_EXPORT int kmgb_reference_init(const float* data, int m, int d, int k, float* centers,
+                                    int* perm, int* picks);
+
 /* Defaults: FP32 tier, certify on, NaN policy, 20 iterations, criterion -1, full batch. */
 KMGB_EXPORT void kmgb_default_options(kmgb_options* opt);
 

@@ -126,6 +126,7 @@ def lib():
             "kmgb_get_phase_ms": (i32, [P, P, P]),
             "kmgb_launch_count": (i64, []),
             "kmgb_sum_piece": (i32, []),
+            "kmgb_reference_init": (i32, [P, i32, i32, i32, P, P, P]),
             "kmgb_version": (C.c_char_p, []),
         }
         for name, (res, args) in sig.items():
@@ -185,6 +186,19 @@ def computeKmeansD(data: np.ndarray, m: int, n: int, k: int, criterion: float, m
     return int(lib().computeKmeansD(_ptr(data), m, n, k, criterion, maxIters, numRetries,
                                     initAlgorithm, doFullSGEMM, matrixFormat, _ptr(result),
                                     miniBatchFraction))
+
+
+def reference_init(data: np.ndarray, k: int):
+    """The reference's initial centers (host only): returns (centers k x d, perm, picks)."""
+    data = np.ascontiguousarray(data, dtype=np.float32)
+    m, d = data.shape
+    cen = np.empty((k, d), np.float32)
+    perm = np.empty(m, np.int32)
+    picks = np.empty(k, np.int32)
+    rc = lib().kmgb_reference_init(_ptr(data), m, d, k, _ptr(cen), _ptr(perm), _ptr(picks))
+    if rc:
+        raise KmeansError(rc, last_error())
+    return cen, perm, picks
 
 
 def kmeansGetErrorString(err: int) -> str:

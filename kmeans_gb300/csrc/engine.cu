@@ -143,6 +143,7 @@ struct kmgb_handle {
   int* rr_list = nullptr;
   int* rr_count = nullptr;     // [0] flagged by the assignment, [1] left for the FP64 stage
   int* rr_list2 = nullptr;
+  float* rr_hi2 = nullptr;
   unsigned long long* rr_stats = nullptr;
   int* err = nullptr;
   // device-side loop state: stop flag, previous SSE, last relErr, iterations done
@@ -183,7 +184,7 @@ struct kmgb_handle {
   ~kmgb_handle() {
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
     void* ptrs[] = {X, Xb, qn, xn, perm, Xw, Xbw, qnw, xnw, C, Cop, Cb, cn, cmax, labels,
-                    rr_list, rr_count, rr_list2, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
+                    rr_list, rr_count, rr_list2, rr_hi2, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
                     uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
                     stop, loopf, iters_done};
     for (void* p : ptrs)
@@ -259,6 +260,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(dalloc(&h->rr_list, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_count, 2), (delete h, code));
   KM_TRY(dalloc(&h->rr_list2, na), (delete h, code));
+  KM_TRY(dalloc(&h->rr_hi2, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_stats, 2), (delete h, code));
   KM_TRY(dalloc(&h->err, 1), (delete h, code));
   KM_TRY(dalloc(&h->stop, 1), (delete h, code));
@@ -410,11 +412,12 @@ int step(kmgb_handle* h, int slot) {
     r.max_list = na;
     r.stop = h->stop;
     // FP32 stage over the flagged points, exact FP64 stage over what FP32 cannot separate
-    KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 1, s), KMEANS_ERROR_CLOSEST_CENTERS);
+    KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 1, h->rr_hi2, s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
     r.list = h->rr_list2;
     r.count = h->rr_count + 1;
     r.stats = nullptr;
-    KM_TRY(launch_rerank(r, s), KMEANS_ERROR_CLOSEST_CENTERS);
+    KM_TRY(launch_rerank_exact(r, h->rr_hi2, s), KMEANS_ERROR_CLOSEST_CENTERS);
     KM_TRY(launch_count_stats(h->rr_count, h->rr_stats, h->stop, s), KMEANS_ERROR_CLOSEST_CENTERS);
   }
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
@@ -580,6 +583,21 @@ void kmgb_default_options(kmgb_options* opt) {
 const char* kmgb_last_error(void) { return g_last_error.c_str(); }
 int kmgb_sum_piece(void) { return kSumPiece; }
 const char* kmgb_version(void) { return "kmeans_gb300 0.1 (sm_103a)"; }
+
+int kmgb_reference_init(const float* data, int m, int d, int k, float* centers, int* perm_out,
+                        int* picks_out) {
+  std::vector<int> perm, picks;
+  if (!data || !centers || d <= 0 || !reference_picks(m, k, picks)) {
+    set_err("kmgb_reference_init: needs data, centers, d > 0 and 0 < k <= m");
+    return KMEANS_ERROR_INITIALIZE;
+  }
+  reference_perm(m, perm);
+  for (int i = 0; i < k; ++i)
+    std::memcpy(centers + (size_t)i * d, data + (size_t)perm[picks[i]] * d, sizeof(float) * d);
+  if (perm_out) std::memcpy(perm_out, perm.data(), sizeof(int) * (size_t)m);
+  if (picks_out) std::memcpy(picks_out, picks.data(), sizeof(int) * (size_t)k);
+  return 0;
+}
 
 int kmgb_create(kmgb_handle** h, long long n, int d, int k, const kmgb_options* opt) {
   return create_handle(h, n, d, k, opt);

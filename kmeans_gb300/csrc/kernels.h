@@ -56,7 +56,11 @@ struct RerankArgs {
 };
 cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s);
 // FP32 stage of the Lloyd re-rank (mode 0): certifies what FP32 can, passes the rest to list2.
-cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, cudaStream_t s);
+// hi2[slot] receives the FP32 upper end of the best center of every point passed on.
+cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, float* hi2,
+                                cudaStream_t s);
+// FP64 stage over list2 (one CTA per point), candidates bounded by hi2.
+cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s);
 // stats[0] += counts[0] (points re-ranked), stats[1] += counts[1] (points that needed FP64).
 cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, const int* stop,
                                cudaStream_t s);

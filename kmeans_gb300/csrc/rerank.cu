@@ -137,7 +137,8 @@ constexpr int TP = 32;   // points per CTA iteration
 constexpr int TC = 64;   // centers per block
 
 __global__ void __launch_bounds__(256)
-rerank_tiled_kernel(RerankArgs a, int* __restrict__ list2, int* __restrict__ count2) {
+rerank_tiled_kernel(RerankArgs a, int* __restrict__ list2, int* __restrict__ count2,
+                    float* __restrict__ hi2) {
   if (stopped(a.stop)) return;
   extern __shared__ float4 sm4[];
   const int dq = (a.d + 3) >> 2;          // float4 per row
@@ -270,7 +271,64 @@ rerank_tiled_kernel(RerankArgs a, int* __restrict__ list2, int* __restrict__ cou
       } else {
         const int slot = atomicAdd(count2, 1);
         list2[slot] = pt;
+        hi2[slot] = f1 * (1.0f + gam) + 1e-30f;  // no usable center: +inf
       }
+    }
+  }
+}
+
+// Exact stage of the Lloyd re-rank (mode 0), one CTA per residual point: every usable center
+// whose FP32 lower end is within the point's best upper end (from the FP32 stage) is evaluated
+// in FP64 exactly as the oracle does; the smallest value wins, lowest index on ties.
+__global__ void __launch_bounds__(256)
+rerank_exact_kernel(RerankArgs a, const float* __restrict__ hi2) {
+  if (stopped(a.stop)) return;
+  extern __shared__ float xsm[];
+  __shared__ double rb[8];
+  __shared__ int ri[8];
+  const long long cnt = min((long long)*(volatile const int*)a.count, a.max_list);
+  const float u = 5.9604645e-8f;
+  const float gam = (float)(a.d + 4) * 2.0f * u * 1.01f;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (long long slot = blockIdx.x; slot < cnt; slot += gridDim.x) {
+    __syncthreads();
+    const int pt = a.list[slot];
+    const float* x = a.X + (size_t)pt * a.ldx;
+    for (int t = threadIdx.x; t < a.d; t += blockDim.x) xsm[t] = x[t];
+    __syncthreads();
+    const float best_hi = hi2[slot];
+    double best = INFINITY;
+    int bidx = -1;
+    for (int j = threadIdx.x; j < a.k; j += blockDim.x) {
+      if (!(a.cn[j] < INFINITY)) continue;
+      const float* c = a.C + (size_t)j * a.ldc;
+      const float v = approx_value(0, xsm, c, a.d, 0.0f);
+      if (!(v * (1.0f - gam) - 1e-30f <= best_hi)) continue;
+      const double ex = exact_value(0, xsm, c, a.d, 0.0f);
+      if (ex < best) {
+        best = ex;
+        bidx = j;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+      const bool take = (ob < best) || (ob == best && (unsigned)oi < (unsigned)bidx);
+      best = take ? ob : best;
+      bidx = take ? oi : bidx;
+    }
+    if (lane == 0) {
+      rb[w] = best;
+      ri[w] = bidx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int ww = 1; ww < (int)(blockDim.x >> 5); ++ww) {
+        const bool take = (rb[ww] < best) || (rb[ww] == best && (unsigned)ri[ww] < (unsigned)bidx);
+        best = take ? rb[ww] : best;
+        bidx = take ? ri[ww] : bidx;
+      }
+      a.labels[pt] = bidx < 0 ? 0 : bidx;
     }
   }
 }
@@ -292,7 +350,20 @@ cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, con
   return cudaGetLastError();
 }
 
-cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, cudaStream_t s) {
+cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s) {
+  if (a.n <= 0 || a.k <= 0) return cudaSuccess;
+  const size_t smem = sizeof(float) * (size_t)a.d;
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024)
+    KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  rerank_exact_kernel<<<152 * 4, 256, smem, s>>>(a, hi2);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, float* hi2,
+                                cudaStream_t s) {
   if (a.n <= 0 || a.k <= 0) return cudaSuccess;
   const int dq = (a.d + 3) / 4;
   const size_t smem = sizeof(float4) * (size_t)(TP + TC) * (dq + 1) + sizeof(float) * TC;
@@ -300,7 +371,7 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, cu
   if (smem > 48 * 1024)
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_tiled_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  rerank_tiled_kernel<<<152 * 2, 256, smem, s>>>(a, list2, count2);
+  rerank_tiled_kernel<<<152 * 2, 256, smem, s>>>(a, list2, count2, hi2);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -61,3 +61,22 @@ def test_invalid_arguments_rejected_without_gpu(km):
     assert km.computeKmeansF(data, 2, 2, 0, -1.0, 1, 1, 0, 0, 0, res, 1.0) == 1
     assert km.computeKmeansF(data, 2, 2, 3, -1.0, 1, 1, 0, 0, 0, res, 1.0) == 2
     assert km.computeKmeansF(data, 2, 2, 1, -1.0, 1, 1, 0, 3, 0, res, 1.0) == 1
+
+
+def test_reference_init_matches_oracle_and_fixtures(km, orc):
+    import json
+    import numpy as np
+    from kmeans_gb300.synthetic import mixture_numpy
+    X, _, _ = mixture_numpy(50_000, 24, 40, seed=7)
+    cen, perm, picks = km.reference_init(X, 40)
+    assert np.array_equal(perm, orc.shuffle_perm(50_000))
+    assert np.array_equal(picks, orc.init_picks(50_000, 40))
+    assert np.array_equal(cen, orc.reference_init(X, 40))
+    gold = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "picks.json")))
+    for key, v in gold.items():
+        m, k = map(int, key.split("_"))
+        Z = np.zeros((m, 1), np.float32) if m <= 100_000 else None
+        if Z is None:
+            continue
+        _, _, p = km.reference_init(Z, k)
+        assert p.tolist() == v, key
