@@ -38,7 +38,8 @@ constexpr uint32_t KB_BYTES = BM * BK * 2;  // 16 KB: one tile k-block == one C 
 constexpr int MAX_STAGES = 8;
 constexpr int MAX_D = 256;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr size_t SMEM_CAP = 227 * 1024;  // upper bound; the device's opt-in limit is queried
+constexpr size_t SMEM_CAP = 227 * 1024;
+constexpr float kUnusable = -3.0e38f;      // accumulator start of padding / unusable centers  // upper bound; the device's opt-in limit is queried
 
 // UMMA instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, N>>3, M>>4.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -281,18 +282,23 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16);
     const float cm = p.certify ? __ldg(p.cmax) : 0.0f;
 
-    // pre-load accumulator buffer (g & 1) with -||c||^2/2 of chunk (g mod nchunks)
+    // pre-load accumulator buffer (g & 1) with the chunk's accumulator start values
+    // (-||c||^2/2, or a huge negative number for padding / unusable centers; prepared once per
+    // iteration in p.cinit, padded to whole chunks)
     auto init_buf = [&](long long g) {
       const int c = (int)(g % nchunks);
       const uint32_t base = lane_addr + (uint32_t)((g & 1) * (TILES * BN) + t * BN);
-#pragma unroll 1
+      const float4* src = reinterpret_cast<const float4*>(p.cinit + (size_t)c * BN);
+#pragma unroll
       for (int cb = 0; cb < BN / 32; ++cb) {
         uint32_t v[32];
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const int col = c * BN + cb * 32 + j;
-          const float cnv = col < p.k ? __ldg(p.cn + col) : INFINITY;
-          v[j] = __float_as_uint(-0.5f * cnv);
+        for (int q = 0; q < 8; ++q) {
+          const float4 f = __ldg(src + cb * 8 + q);
+          v[4 * q + 0] = __float_as_uint(f.x);
+          v[4 * q + 1] = __float_as_uint(f.y);
+          v[4 * q + 2] = __float_as_uint(f.z);
+          v[4 * q + 3] = __float_as_uint(f.w);
         }
         tmem_st32(base + cb * 32, v);
       }
@@ -321,20 +327,26 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         tc_fence_after();
         const float before = b1;
         const uint32_t base = lane_addr + (uint32_t)(b * (TILES * BN) + t * BN);
-#pragma unroll 1
+        // two 32-column register buffers: the load of block cb+1 is in flight while block cb
+        // is folded into (b1, b2)
+        uint32_t ra[32], rb[32];
+        tmem_ld32(base, ra);
+        tmem_ld_wait();
+#pragma unroll
         for (int cb = 0; cb < BN / 32; ++cb) {
-          uint32_t r[32];
-          tmem_ld32(base + cb * 32, r);
-          tmem_ld_wait();
+          uint32_t (&cur)[32] = (cb & 1) ? rb : ra;
+          uint32_t (&nxt)[32] = (cb & 1) ? ra : rb;
+          if (cb + 1 < BN / 32) tmem_ld32(base + (cb + 1) * 32, nxt);
 #pragma unroll
           for (int j = 0; j < 32; j += 2) {
-            const float k0 = __uint_as_float((r[j] & ~0x7Fu) | (uint32_t)(cb * 32 + j));
-            const float k1 = __uint_as_float((r[j + 1] & ~0x7Fu) | (uint32_t)(cb * 32 + j + 1));
+            const float k0 = __uint_as_float((cur[j] & ~0x7Fu) | (uint32_t)(cb * 32 + j));
+            const float k1 = __uint_as_float((cur[j + 1] & ~0x7Fu) | (uint32_t)(cb * 32 + j + 1));
             const float hi = fmaxf(k0, k1);
             const float lo = fminf(k0, k1);
             b2 = fmax3(b2, lo, fminf(b1, hi));
             b1 = fmaxf(b1, hi);
           }
+          if (cb + 1 < BN / 32) tmem_ld_wait();
         }
         if (b1 != before) bc = c;
         if (g + 2 < total_chunks) init_buf(g + 2);
@@ -345,11 +357,12 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       if (!alive) break;
       const long long pt = u * UNIT + t * BM + q * 32 + lane;
       if (pt < p.n) {
-        const int label = bc < 0 ? 0 : bc * BN + (int)(__float_as_uint(b1) & 0x7Fu);
+        const bool none = !(b1 > -1.0e38f);  // no usable center at all
+        const int label = (bc < 0 || none) ? 0 : bc * BN + (int)(__float_as_uint(b1) & 0x7Fu);
         p.labels[pt] = label;
         if (p.certify) {
           const float eb = bound_acc(__ldg(p.xnorm + pt), cm, p.d);
-          if (!(b1 - b2 > 2.0f * eb)) {
+          if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
             p.rerank_list[slot] = (int)pt;
           }

@@ -137,6 +137,7 @@ struct kmgb_handle {
   void* Cb = nullptr;
   float* cn = nullptr;
   float* cmax = nullptr;
+  float* cinit = nullptr;  // BF16 tier accumulator start values, padded to 128
   bool have_centers = false;
   // assignment
   int* labels = nullptr;
@@ -183,7 +184,7 @@ struct kmgb_handle {
 
   ~kmgb_handle() {
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
-    void* ptrs[] = {X, Xb, qn, xn, perm, Xw, Xbw, qnw, xnw, C, Cop, Cb, cn, cmax, labels,
+    void* ptrs[] = {X, Xb, qn, xn, perm, Xw, Xbw, qnw, xnw, C, Cop, Cb, cn, cmax, cinit, labels,
                     rr_list, rr_count, rr_list2, rr_hi2, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
                     uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
                     stop, loopf, iters_done};
@@ -255,6 +256,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   if (bf16) KM_TRY(cudaMalloc(&h->Cb, (size_t)k * h->ldb * 2), (delete h, code));
   KM_TRY(dalloc(&h->cn, k), (delete h, code));
   KM_TRY(dalloc(&h->cmax, 1), (delete h, code));
+  if (bf16) KM_TRY(dalloc(&h->cinit, (size_t)(k + 127) / 128 * 128), (delete h, code));
   const long long na = h->n_act;
   KM_TRY(dalloc(&h->labels, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_list, na), (delete h, code));
@@ -301,9 +303,22 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   return 0;
 }
 
+// Device inputs may have been produced on the legacy default stream (where most callers, torch
+// included, work); the handle's non-blocking stream waits for that work before reading them.
+cudaError_t order_after_default_stream(kmgb_handle* h) {
+  cudaEvent_t e;
+  cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  if (r != cudaSuccess) return r;
+  r = cudaEventRecord(e, cudaStreamLegacy);
+  if (r == cudaSuccess) r = cudaStreamWaitEvent(h->stream, e, 0);
+  cudaEventDestroy(e);
+  return r;
+}
+
 // Upload (or copy) the data set and compute its per-point norms and BF16 copy.
 int set_data(kmgb_handle* h, const float* X, bool on_device) {
   const int code = KMEANS_ERROR_BUILDDATA;
+  if (on_device) KM_TRY(order_after_default_stream(h), code);
   const size_t row_bytes = sizeof(float) * h->d;
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   if (h->ldx == h->d) {
@@ -369,7 +384,7 @@ int step(kmgb_handle* h, int slot) {
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
   KM_TRY(cudaMemsetAsync(h->rr_count, 0, 2 * sizeof(int), s), KMEANS_ERROR_RESET);
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
-                             h->stop),
+                             h->stop, h->cinit),
          KMEANS_ERROR_RESET);
   KM_TRY(h->pmark(1), KMEANS_ERROR_RESET);
   // closest centers (kmeans.cpp:910-1014)
@@ -386,6 +401,7 @@ int step(kmgb_handle* h, int slot) {
   a.d = h->d;
   a.certify = h->opt.certify;
   a.stop = h->stop;
+  a.cinit = h->cinit;
   if (h->opt.assign_tier == KMGB_ASSIGN_BF16) {
     a.gamma = assign_bf16_gamma(h->d);
     KM_TRY(launch_assign_bf16(Xba, h->ldb, h->Cb, h->ldb, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
@@ -518,6 +534,7 @@ int reference_init_host(kmgb_handle* h, const float* data_host, std::vector<floa
 
 int set_centers(kmgb_handle* h, const float* C, bool on_device) {
   const size_t row_bytes = sizeof(float) * h->d;
+  if (on_device) KM_TRY(order_after_default_stream(h), KMEANS_ERROR_INITIALIZE);
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   KM_TRY(cudaMemsetAsync(h->C, 0, sizeof(float) * h->ldx * h->k, h->stream),
          KMEANS_ERROR_INITIALIZE);

@@ -14,6 +14,7 @@ struct AssignArgs {
   const float* cn;        // [k] ||c_j||^2 rounded to FP32, +inf for unusable (NaN) centers
   const float* xnorm;     // [n] upper bound of ||x_i||
   const float* cmax;      // device scalar: upper bound of max ||c_j|| over usable centers
+  const float* cinit;     // [round_up(k,128)] accumulator start -||c_j||^2/2 (BF16 tier)
   int* labels;            // [n]
   int* rerank_list;       // [n]
   int* rerank_count;      // device scalar
@@ -68,9 +69,11 @@ cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, con
 // Center preparation: from the official centers C[k][ldc] write the operand copy Cop (NaN
 // rows -> 0), optional BF16 copy Cb[k][ldcb], cn (+inf for NaN rows) and atomically raise
 // *cmax (must be zeroed before).
+// cinit (nullable, round_up(k,128) floats) receives -cn/2 per usable center and -3e38 for
+// unusable centers and padding.
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop,
                                 void* Cb, long long ldcb, float* cn, float* cmax, cudaStream_t s,
-                                const int* stop = nullptr);
+                                const int* stop = nullptr, float* cinit = nullptr);
 
 // Per-point norms, computed once per data set: qn = ||x||^2 (FP64), xn = upper bound ||x||.
 cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,

@@ -17,11 +17,14 @@ namespace {
 __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, int k, int d,
                                     float* __restrict__ Cop, __nv_bfloat16* __restrict__ Cb,
                                     long long ldcb, float* __restrict__ cn, float* cmax,
-                                    const int* stop) {
+                                    const int* stop, float* __restrict__ cinit, int kpad) {
   if (stopped(stop)) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (warp >= k) return;
+  if (warp >= k) {
+    if (cinit && warp < kpad && lane == 0) cinit[warp] = -3.0e38f;
+    return;
+  }
   const float* c = C + (size_t)warp * ldc;
   double s = 0.0;
   bool bad = false;
@@ -42,8 +45,10 @@ __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, 
   if (lane == 0) {
     if (bad) {
       cn[warp] = INFINITY;
+      if (cinit) cinit[warp] = -3.0e38f;
     } else {
       cn[warp] = __double2float_rn(s);
+      if (cinit) cinit[warp] = -0.5f * __double2float_rn(s);
       // upper bound of ||c||: round the FP64 sqrt up and add a relative margin
       const float nrm = __double2float_ru(sqrt(s) * (1.0 + 1e-12));
       atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(nrm));
@@ -113,13 +118,14 @@ __global__ void gather_vec_kernel(const double* __restrict__ qs, const float* __
 
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop, void* Cb,
                                 long long ldcb, float* cn, float* cmax, cudaStream_t s,
-                                const int* stop) {
+                                const int* stop, float* cinit) {
   if (k <= 0) return cudaSuccess;
   const int threads = 256;
-  const int blocks = (int)(((long long)k * 32 + threads - 1) / threads);
+  const int kpad = (k + 127) / 128 * 128;
+  const int blocks = (int)(((long long)(cinit ? kpad : k) * 32 + threads - 1) / threads);
   prep_centers_kernel<<<blocks, threads, 0, s>>>(C, ldc, k, d, Cop,
                                                  reinterpret_cast<__nv_bfloat16*>(Cb), ldcb, cn,
-                                                 cmax, stop); kmgb::count_launches(1);
+                                                 cmax, stop, cinit, kpad); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

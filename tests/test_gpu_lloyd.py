@@ -62,11 +62,11 @@ def test_reference_init_compute_kmeans_f(km, orc, torch_cuda):
     rc = km.computeKmeansF(X, m, n, k, -1.0, 12, 1, 0, 0, 0, result, 1.0)
     assert rc == 13
     st, c, lab, sse, it = orc.lloyd(X, orc.reference_init(X, k), 12)
-    assert np.array_equal(result.reshape(n, k), c.T)  # D x K, K fastest
+    assert np.array_equal(result.reshape(n, k), c.T, equal_nan=True)  # D x K, K fastest
     # doFullSGEMM / matrixFormat map to the same implementation
     r2 = np.zeros_like(result)
     assert km.computeKmeansF(X, m, n, k, -1.0, 12, 3, 1, 1, 1, r2, 1.0) == 13
-    assert np.array_equal(r2, result)
+    assert np.array_equal(r2, result, equal_nan=True)
 
 
 def test_convergence_criterion(km, orc, torch_cuda):
@@ -77,7 +77,7 @@ def test_convergence_criterion(km, orc, torch_cuda):
     result = np.zeros(n * k, np.float32)
     rc = km.computeKmeansF(X, m, n, k, 1e-6, 200, 1, 0, 0, 0, result, 1.0)
     assert rc == 0
-    assert np.array_equal(result.reshape(n, k), ref[1].T)
+    assert np.array_equal(result.reshape(n, k), ref[1].T, equal_nan=True)
     res = km.lloyd(X, k, init=None, max_iters=200, criterion=1e-6)
     check_same(res, ref)
 
@@ -112,7 +112,7 @@ def test_minibatch_compute_kmeans_f(km, orc, torch_cuda):
     result = np.zeros(n * k, np.float32)
     assert km.computeKmeansF(X, m, n, k, -1.0, 7, 1, 0, 0, 0, result, 0.2) == 13
     ref = orc.lloyd(X, orc.reference_init(X, k), 7, mb_fraction=0.2)
-    assert np.array_equal(result.reshape(n, k), ref[1].T)
+    assert np.array_equal(result.reshape(n, k), ref[1].T, equal_nan=True)
 
 
 def test_device_input_and_handle_resume(km, orc, torch_cuda):
@@ -129,7 +129,7 @@ def test_device_input_and_handle_resume(km, orc, torch_cuda):
     h.run(2)  # resumes from the current centers
     h.synchronize()
     ref = orc.lloyd(X, init, 5)
-    assert np.array_equal(h.centers(), ref[1])
+    assert np.array_equal(h.centers(), ref[1], equal_nan=True)
     assert np.array_equal(h.labels(), ref[2])
     h.close()
 
@@ -143,7 +143,7 @@ def test_compute_kmeans_d(km, orc, torch_cuda):
     perm = orc.shuffle_perm(m)
     init = X[perm[orc.init_picks(m, k)]]
     st, c, lab, sse, it = orc.lloyd_d(X, init, 6)
-    assert np.array_equal(result.reshape(n, k), c.T)
+    assert np.array_equal(result.reshape(n, k), c.T, equal_nan=True)
 
 
 @pytest.mark.parametrize("tier", TIERS)
