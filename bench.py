@@ -151,7 +151,7 @@ def main():
     km.build()
     lib = km.lib()
     tier = args.tier or "fp32"
-    tier_id = km.ASSIGN_BF16 if tier == "bf16" else km.ASSIGN_FP32
+    tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3}[tier]
 
     n = args.n
     X, _, _ = mixture_torch(n, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
@@ -194,7 +194,7 @@ def main():
     bf16_peak, hbm_peak, src = peaks()
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
                 "frac": achieved / bf16_peak, "traffic": None,
-                "kernel": "assign_bf16_tc" if tier == "bf16" else "assign_fp32_kernel",
+                "kernel": "assign_fp32_kernel" if tier == "fp32" else "assign_bf16_kernel",
                 "peak_source": f"{src} bf16 dense (MEASURED_PEAKS.json)",
                 "flop_per_launch": flop, "ms_per_launch": assign_ms}
 
@@ -221,7 +221,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "bf16" if tier == "bf16" else "f32", "data": "synthetic",
+                "dtype": "f32" if tier == "fp32" else "bf16", "data": "synthetic",
                 "config": {"workload": "lloyd_4Mx128_K1024" if n == N else f"lloyd_{n}x128_K1024",
                            "n": n, "d": D, "k": K,
                            "tier": tier, "certified_labels": True,

@@ -166,8 +166,9 @@ KMGB_EXPORT kmeansCudaErrorStatus colNormalizeD(const int m, const int n, const 
  * ------------------------------------------------------------------------------------- */
 
 enum kmgb_assign_tier {
-  KMGB_ASSIGN_FP32 = 0, /* plain FP32 fused kernel (TMA + FFMA) */
-  KMGB_ASSIGN_BF16 = 1  /* tcgen05 BF16 tensor cores, FP32 accumulate in TMEM */
+  KMGB_ASSIGN_FP32 = 0,  /* plain FP32 fused kernel (TMA + FFMA) */
+  KMGB_ASSIGN_BF16 = 1,  /* tcgen05 BF16 tensor cores, FP32 accumulate in TMEM (D <= 256) */
+  KMGB_ASSIGN_BF16X3 = 2 /* tcgen05 split BF16: x.c = xh.ch + xh.cl + xl.ch (D <= 128) */
 };
 
 enum kmgb_empty_policy {
@@ -228,6 +229,13 @@ KMGB_EXPORT int kmgb_get_sse(kmgb_handle* h, double* sse, int max_count); /* ret
 KMGB_EXPORT int kmgb_get_stats(kmgb_handle* h, kmgb_stats* stats);
 KMGB_EXPORT void* kmgb_stream(kmgb_handle* h); /* cudaStream_t of the handle */
 KMGB_EXPORT int kmgb_destroy(kmgb_handle* h);
+
+/* Diagnostic: raw tcgen05 accumulators x.c_j - ||c_j||^2/2 for every point and center, as the
+ * BF16 (split = 0) or split BF16 (split = 1) assignment kernel computes them. X: n x d, C: k x d,
+ * host row-major FP32; out: host n x k. For validating the accumulation-error model on a
+ * device; allocates device memory, small problems only. */
+KMGB_EXPORT int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int k,
+                                     int split, float* out);
 
 /* Phase timing: with profiling on, CUDA events on the handle's stream bracket every phase of
  * every iteration. kmgb_get_phase_ms waits for the stream and returns, summed over the

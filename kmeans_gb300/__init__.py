@@ -33,6 +33,7 @@ KMEANS_SUCCESS = 0
 KMEANS_NONCONVERGENCE = 13
 ASSIGN_FP32 = 0
 ASSIGN_BF16 = 1
+ASSIGN_BF16X3 = 2
 EMPTY_NAN = 0
 EMPTY_KEEP = 1
 
@@ -127,6 +128,7 @@ def lib():
             "kmgb_launch_count": (i64, []),
             "kmgb_sum_piece": (i32, []),
             "kmgb_reference_init": (i32, [P, i32, i32, i32, P, P, P]),
+            "kmgb_tc_accumulators": (i32, [P, i64, i32, P, i32, i32, P]),
             "kmgb_version": (C.c_char_p, []),
         }
         for name, (res, args) in sig.items():
@@ -199,6 +201,19 @@ def reference_init(data: np.ndarray, k: int):
     if rc:
         raise KmeansError(rc, last_error())
     return cen, perm, picks
+
+
+def tc_accumulators(X: np.ndarray, C: np.ndarray, split: bool) -> np.ndarray:
+    """Raw tcgen05 accumulators x.c_j - ||c_j||^2/2 (n x k) of the BF16 / split BF16 kernel."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    C = np.ascontiguousarray(C, dtype=np.float32)
+    n, d = X.shape
+    k = C.shape[0]
+    out = np.empty((n, k), np.float32)
+    rc = lib().kmgb_tc_accumulators(_ptr(X), n, d, _ptr(C), k, int(split), _ptr(out))
+    if rc:
+        raise KmeansError(rc, last_error())
+    return out
 
 
 def kmeansGetErrorString(err: int) -> str:

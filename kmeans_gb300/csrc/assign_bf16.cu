@@ -117,15 +117,19 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
 }
 
 // Rigorous bound (in accumulator units) of |key - (x.c - ||c||^2/2)| for any usable center.
-__device__ __forceinline__ float bound_acc(float xn, float cm, int d) {
+__device__ __forceinline__ float bound_acc(float xn, float cm, int d, int planes) {
   const float u = 5.9604645e-8f;            // 2^-24, FP32 rounding
   const float ub = 1.953125e-3f;            // 2^-9, BF16 rounding
-  const float gacc = (float)(d + 32) * 4.76837158e-7f;  // (D+32) 2^-21, TMEM accumulation
+  // operand error: plain (2ub + ub^2) |x||c|; split x = xh + xl + ex, c = ch + cl + ec with
+  // |xl| <= ub|x|, |ex| <= ub^2|x|: dropping xl.cl and the residues leaves <= 3.03 ub^2 |x||c|
+  const float op = planes > 1 ? 3.03f * ub * ub : 2.0f * ub + ub * ub;
+  const int terms = planes > 1 ? 3 * d : d;
+  const float gacc = (float)(terms + 32) * 4.76837158e-7f;  // (terms+32) 2^-21, accumulation
   const float pack = 1.52587891e-5f;        // 2^-16, index bits in the mantissa
   const float cc = 0.5f * cm * cm;
   const float xc = xn * cm * 1.01f;
   const float s64 = (float)(d + 2) * 1.2e-16f * (xn + cm) * (xn + cm);
-  const float e = 0.5f * u * cm * cm + (2.0f * ub + ub * ub) * xc + (gacc + pack) * (cc + xc) + s64;
+  const float e = 0.5f * u * cm * cm + op * xc + (gacc + pack) * (cc + xc) + s64;
   return e * 1.02f + 1e-30f;
 }
 
@@ -136,8 +140,9 @@ struct Bars {
 };
 
 __global__ void __launch_bounds__(NTHREADS, 1)
-assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmC,
-                   AssignArgs p, int stages, int xbufs) {
+assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmXl,
+                   const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmCl,
+                   AssignArgs p, int stages, int xbufs, int planes) {
   if (stopped(p.stop)) return;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
@@ -154,7 +159,10 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   if ((long long)blockIdx.x < n_units)
     my_units = (n_units - 1 - blockIdx.x) / gridDim.x + 1;
   const long long total_chunks = my_units * nchunks;
-  const size_t xbuf_bytes = (size_t)TILES * nkb * KB_BYTES;
+  // X buffer: [plane][tile][k-block] 16 KB boxes; C stage: [plane] 16 KB boxes of one
+  // (chunk, k-block). plane 0 = BF16 value, plane 1 = BF16 residual (split tier).
+  const size_t xbuf_bytes = (size_t)planes * TILES * nkb * KB_BYTES;
+  const uint32_t stage_bytes = (uint32_t)planes * KB_BYTES;
   uint8_t* xs0 = smem;                       // X buffer b at xs0 + b * xbuf_bytes
   uint8_t* cs = smem + (size_t)xbufs * xbuf_bytes;
 
@@ -176,6 +184,10 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     fence_mbar_init();
     prefetch_tmap(&tmX);
     prefetch_tmap(&tmC);
+    if (planes > 1) {
+      prefetch_tmap(&tmXl);
+      prefetch_tmap(&tmCl);
+    }
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -206,10 +218,11 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         const uint32_t xb = smem_u32(&bars.x_full[xi]);
         uint8_t* xs = xs0 + (size_t)xi * xbuf_bytes;
         mbar_arrive_expect_tx(xb, (uint32_t)xbuf_bytes);
-        for (int t = 0; t < TILES; ++t)
-          for (int kb = 0; kb < nkb; ++kb)
-            tma_load_2d(smem_u32(xs + (size_t)(t * nkb + kb) * KB_BYTES), &tmX, xb, kb * BK,
-                        (int)(u * UNIT + t * BM));
+        for (int pl = 0; pl < planes; ++pl)
+          for (int t = 0; t < TILES; ++t)
+            for (int kb = 0; kb < nkb; ++kb)
+              tma_load_2d(smem_u32(xs + (size_t)((pl * TILES + t) * nkb + kb) * KB_BYTES),
+                          pl ? &tmXl : &tmX, xb, kb * BK, (int)(u * UNIT + t * BM));
         for (int c = 0; c < nchunks && ok; ++c) {
           for (int kb = 0; kb < nkb; ++kb, ++s) {
             const int stage = (int)(s % stages);
@@ -220,8 +233,10 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               break;
             }
             const uint32_t cb = smem_u32(&bars.c_full[stage]);
-            mbar_arrive_expect_tx(cb, KB_BYTES);
-            tma_load_2d(smem_u32(cs + (size_t)stage * KB_BYTES), &tmC, cb, kb * BK, c * BN);
+            mbar_arrive_expect_tx(cb, stage_bytes);
+            for (int pl = 0; pl < planes; ++pl)
+              tma_load_2d(smem_u32(cs + (size_t)stage * stage_bytes + pl * KB_BYTES),
+                          pl ? &tmCl : &tmC, cb, kb * BK, c * BN);
           }
         }
       }
@@ -255,14 +270,20 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               break;
             }
             tc_fence_after();
-            const uint32_t cbase = smem_u32(cs + (size_t)stage * KB_BYTES);
+            const uint32_t cbase = smem_u32(cs + (size_t)stage * stage_bytes);
 #pragma unroll
             for (int t = 0; t < TILES; ++t) {
-              const uint32_t xbase = smem_u32(xs + (size_t)(t * nkb + kb) * KB_BYTES);
+              const uint32_t xhi = smem_u32(xs + (size_t)(t * nkb + kb) * KB_BYTES);
               const uint32_t dcol = tmem_base + (uint32_t)(b * (TILES * BN) + t * BN);
+              // plain: x_hi.c_hi; split: + x_hi.c_lo + x_lo.c_hi (x_lo.c_lo is below the bound)
+              for (int term = 0; term < (planes > 1 ? 3 : 1); ++term) {
+                const uint32_t abase =
+                    term == 2 ? smem_u32(xs + (size_t)((TILES + t) * nkb + kb) * KB_BYTES) : xhi;
+                const uint32_t bbase = term == 1 ? cbase + KB_BYTES : cbase;
 #pragma unroll
-              for (int k16 = 0; k16 < BK / 16; ++k16)
-                umma_bf16(dcol, sdesc_sw128(xbase + k16 * 32), sdesc_sw128(cbase + k16 * 32), 1u);
+                for (int k16 = 0; k16 < BK / 16; ++k16)
+                  umma_bf16(dcol, sdesc_sw128(abase + k16 * 32), sdesc_sw128(bbase + k16 * 32), 1u);
+              }
             }
             umma_commit(smem_u32(&bars.c_empty[stage]));
           }
@@ -337,6 +358,14 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           uint32_t (&cur)[32] = (cb & 1) ? rb : ra;
           uint32_t (&nxt)[32] = (cb & 1) ? ra : rb;
           if (cb + 1 < BN / 32) tmem_ld32(base + (cb + 1) * 32, nxt);
+          if (p.dump) {  // diagnostic: raw accumulators of this point
+            const long long pt = u * UNIT + t * BM + q * 32 + lane;
+            if (pt < p.n) {
+              float* dst = p.dump + (size_t)pt * (size_t)nchunks * BN + (size_t)c * BN + cb * 32;
+#pragma unroll
+              for (int j = 0; j < 32; ++j) dst[j] = __uint_as_float(cur[j]);
+            }
+          }
 #pragma unroll
           for (int j = 0; j < 32; j += 2) {
             const float k0 = __uint_as_float((cur[j] & ~0x7Fu) | (uint32_t)(cb * 32 + j));
@@ -361,7 +390,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         const int label = (bc < 0 || none) ? 0 : bc * BN + (int)(__float_as_uint(b1) & 0x7Fu);
         p.labels[pt] = label;
         if (p.certify) {
-          const float eb = bound_acc(__ldg(p.xnorm + pt), cm, p.d);
+          const float eb = bound_acc(__ldg(p.xnorm + pt), cm, p.d, planes);
           if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
             p.rerank_list[slot] = (int)pt;
@@ -386,17 +415,29 @@ size_t g_smem_budget = 0;  // dynamic shared memory a CTA of this kernel may use
 
 }  // namespace
 
-bool bf16_tc_supported(int d) { return d > 0 && d <= MAX_D; }
+// Shared memory of one X buffer for a dimension: planes x TILES x k-blocks x 16 KB.
+static size_t xbuf_bytes_for(int d, int planes) {
+  return (size_t)planes * TILES * ((d + BK - 1) / BK) * KB_BYTES;
+}
+
+bool bf16_tc_supported(int d, int planes) {
+  if (d <= 0 || d > MAX_D) return false;
+  // one X buffer and two C stages must fit the 227 KB a CTA can use
+  return xbuf_bytes_for(d, planes) + 2 * (size_t)planes * KB_BYTES + 1024 + 1024 <= SMEM_CAP;
+}
 
 float assign_bf16_gamma(int d) {
   return (float)(2.0 * 1.953125e-3 + (d + 32) * 4.76837158e-7);
 }
 
-cudaError_t launch_assign_bf16(const void* Xb, long long ldxb, const void* Cb, long long ldcb,
-                               const AssignArgs& a, cudaStream_t s) {
+cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, const void* Cb,
+                               const void* Cl, long long ldcb, const AssignArgs& a,
+                               cudaStream_t s) {
   if (a.n <= 0 || a.k <= 0 || a.d <= 0) return cudaSuccess;
-  if (!bf16_tc_supported(a.d) || (ldxb % 8) || (ldcb % 8) ||
-      (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15))
+  const int planes = (Xl && Cl) ? 2 : 1;
+  if (!bf16_tc_supported(a.d, planes) || (ldxb % 8) || (ldcb % 8) ||
+      (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15) ||
+      (reinterpret_cast<uintptr_t>(Xl) & 15) || (reinterpret_cast<uintptr_t>(Cl) & 15))
     return cudaErrorInvalidValue;
   if (g_num_sms == 0) {
     int dev = 0, optin = 0;
@@ -411,23 +452,31 @@ cudaError_t launch_assign_bf16(const void* Xb, long long ldxb, const void* Cb, l
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
     g_smem_budget = budget;
   }
-  const int nkb = (a.d + BK - 1) / BK;
-  const size_t xbytes = (size_t)TILES * nkb * KB_BYTES;
-  // double-buffer the unit's points when that still leaves a 4-stage ring for C
+  const size_t xbytes = xbuf_bytes_for(a.d, planes);
+  const size_t stage_bytes = (size_t)planes * KB_BYTES;
   const size_t lim = g_smem_budget;
-  const int xbufs = (2 * xbytes + 4 * KB_BYTES + 1024 <= lim) ? 2 : 1;
-  if (lim < xbufs * xbytes + 1024 + 2 * KB_BYTES) return cudaErrorInvalidValue;
-  int stages = (int)((lim - 1024 - xbufs * xbytes) / KB_BYTES);
+  // double-buffer the unit's points when that still leaves a 4-stage ring for C
+  const int xbufs = (2 * xbytes + 4 * stage_bytes + 1024 <= lim) ? 2 : 1;
+  if (lim < xbufs * xbytes + 1024 + 2 * stage_bytes) return cudaErrorInvalidValue;
+  int stages = (int)((lim - 1024 - xbufs * xbytes) / stage_bytes);
   if (stages > MAX_STAGES) stages = MAX_STAGES;
-  const size_t smem = xbufs * xbytes + (size_t)stages * KB_BYTES + 1024;
-  CUtensorMap tmX, tmC;
+  const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes + 1024;
+  CUtensorMap tmX, tmC, tmXl, tmCl;
   KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmX, Xb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.d,
                                   (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
   KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmC, Cb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.d,
                                   (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BN));
+  tmXl = tmX;
+  tmCl = tmC;
+  if (planes > 1) {
+    KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmXl, Xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                    (uint64_t)a.d, (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
+    KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmCl, Cl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                    (uint64_t)a.d, (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BN));
+  }
   const long long n_units = (a.n + UNIT - 1) / UNIT;
   const int grid = (int)(n_units < g_num_sms ? n_units : g_num_sms);
-  assign_bf16_kernel<<<grid, NTHREADS, smem, s>>>(tmX, tmC, a, stages, xbufs);
+  assign_bf16_kernel<<<grid, NTHREADS, smem, s>>>(tmX, tmXl, tmC, tmCl, a, stages, xbufs, planes);
   count_launches(1);
   return cudaGetLastError();
 }

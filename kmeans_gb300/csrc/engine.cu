@@ -122,6 +122,7 @@ struct kmgb_handle {
   // data set
   float* X = nullptr;
   void* Xb = nullptr;
+  void* Xl = nullptr;   // split tier residual plane
   double* qn = nullptr;
   float* xn = nullptr;
   bool have_data = false;
@@ -129,12 +130,14 @@ struct kmgb_handle {
   int* perm = nullptr;
   float* Xw = nullptr;
   void* Xbw = nullptr;
+  void* Xlw = nullptr;
   double* qnw = nullptr;
   float* xnw = nullptr;
   // centers
   float* C = nullptr;
   float* Cop = nullptr;
   void* Cb = nullptr;
+  void* Cl = nullptr;
   float* cn = nullptr;
   float* cmax = nullptr;
   float* cinit = nullptr;  // BF16 tier accumulator start values, padded to 128
@@ -184,7 +187,7 @@ struct kmgb_handle {
 
   ~kmgb_handle() {
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
-    void* ptrs[] = {X, Xb, qn, xn, perm, Xw, Xbw, qnw, xnw, C, Cop, Cb, cn, cmax, cinit, labels,
+    void* ptrs[] = {X, Xb, Xl, qn, xn, perm, Xw, Xbw, Xlw, qnw, xnw, C, Cop, Cb, Cl, cn, cmax, cinit, labels,
                     rr_list, rr_count, rr_list2, rr_hi2, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
                     uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
                     stop, loopf, iters_done};
@@ -213,7 +216,8 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   kmgb_handle* h = new kmgb_handle();
   if (opt) h->opt = *opt;
   else kmgb_default_options(&h->opt);
-  if (h->opt.assign_tier == KMGB_ASSIGN_BF16 && !bf16_tc_supported(d)) {
+  const int planes = h->opt.assign_tier == KMGB_ASSIGN_BF16X3 ? 2 : 1;
+  if (h->opt.assign_tier != KMGB_ASSIGN_FP32 && !bf16_tc_supported(d, planes)) {
     delete h;
     set_err("kmgb_create: the BF16 tensor-core tier does not support this dimension");
     return KMEANS_ERROR_BUILDDATA;
@@ -235,7 +239,8 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     }
   }
   h->n_act = h->mini ? h->m_mb : n;
-  const bool bf16 = h->opt.assign_tier == KMGB_ASSIGN_BF16;
+  const bool bf16 = h->opt.assign_tier != KMGB_ASSIGN_FP32;
+  const bool split = h->opt.assign_tier == KMGB_ASSIGN_BF16X3;
   const int code = KMEANS_ERROR_BUILDDATA;
   KM_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), (delete h, code));
   KM_TRY(cudaEventCreate(&h->ev0), (delete h, code));
@@ -244,16 +249,19 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(dalloc(&h->qn, n), (delete h, code));
   KM_TRY(dalloc(&h->xn, n), (delete h, code));
   if (bf16) KM_TRY(cudaMalloc(&h->Xb, (size_t)n * h->ldb * 2), (delete h, code));
+  if (split) KM_TRY(cudaMalloc(&h->Xl, (size_t)n * h->ldb * 2), (delete h, code));
   if (h->mini) {
     KM_TRY(dalloc(&h->perm, n), (delete h, code));
     KM_TRY(dalloc(&h->Xw, (size_t)h->m_mb * h->ldx), (delete h, code));
     KM_TRY(dalloc(&h->qnw, h->m_mb), (delete h, code));
     KM_TRY(dalloc(&h->xnw, h->m_mb), (delete h, code));
     if (bf16) KM_TRY(cudaMalloc(&h->Xbw, (size_t)h->m_mb * h->ldb * 2), (delete h, code));
+    if (split) KM_TRY(cudaMalloc(&h->Xlw, (size_t)h->m_mb * h->ldb * 2), (delete h, code));
   }
   KM_TRY(dalloc(&h->C, (size_t)k * h->ldx), (delete h, code));
   KM_TRY(dalloc(&h->Cop, (size_t)k * h->ldx), (delete h, code));
   if (bf16) KM_TRY(cudaMalloc(&h->Cb, (size_t)k * h->ldb * 2), (delete h, code));
+  if (split) KM_TRY(cudaMalloc(&h->Cl, (size_t)k * h->ldb * 2), (delete h, code));
   KM_TRY(dalloc(&h->cn, k), (delete h, code));
   KM_TRY(dalloc(&h->cmax, 1), (delete h, code));
   if (bf16) KM_TRY(dalloc(&h->cinit, (size_t)(k + 127) / 128 * 128), (delete h, code));
@@ -330,7 +338,9 @@ int set_data(kmgb_handle* h, const float* X, bool on_device) {
            code);
   }
   KM_TRY(launch_point_norms(h->X, h->ldx, h->n, h->d, h->qn, h->xn, h->stream), code);
-  if (h->Xb) KM_TRY(launch_to_bf16(h->X, h->ldx, h->n, h->d, h->Xb, h->ldb, h->stream), code);
+  if (h->Xb)
+    KM_TRY(launch_to_bf16(h->X, h->ldx, h->n, h->d, h->Xb, h->ldb, h->stream, nullptr, h->Xl),
+           code);
   if (h->mini) {
     std::vector<int> perm;
     reference_perm((int)h->n, perm);
@@ -360,6 +370,7 @@ int step(kmgb_handle* h, int slot) {
   cudaStream_t s = h->stream;
   const float* Xa = h->X;
   const void* Xba = h->Xb;
+  const void* Xla = h->Xl;
   const double* qna = h->qn;
   const float* xna = h->xn;
   if (h->mini) {
@@ -371,10 +382,11 @@ int step(kmgb_handle* h, int slot) {
                              h->stop),
            KMEANS_ERROR_CONSTRUCT_MINIBATCH);
     if (h->Xbw)
-      KM_TRY(launch_to_bf16(h->Xw, h->ldx, h->m_mb, h->d, h->Xbw, h->ldb, s, h->stop),
+      KM_TRY(launch_to_bf16(h->Xw, h->ldx, h->m_mb, h->d, h->Xbw, h->ldb, s, h->stop, h->Xlw),
              KMEANS_ERROR_CONSTRUCT_MINIBATCH);
     Xa = h->Xw;
     Xba = h->Xbw;
+    Xla = h->Xlw;
     qna = h->qnw;
     xna = h->xnw;
   }
@@ -384,7 +396,7 @@ int step(kmgb_handle* h, int slot) {
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
   KM_TRY(cudaMemsetAsync(h->rr_count, 0, 2 * sizeof(int), s), KMEANS_ERROR_RESET);
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
-                             h->stop, h->cinit),
+                             h->stop, h->cinit, h->Cl),
          KMEANS_ERROR_RESET);
   KM_TRY(h->pmark(1), KMEANS_ERROR_RESET);
   // closest centers (kmeans.cpp:910-1014)
@@ -402,9 +414,10 @@ int step(kmgb_handle* h, int slot) {
   a.certify = h->opt.certify;
   a.stop = h->stop;
   a.cinit = h->cinit;
-  if (h->opt.assign_tier == KMGB_ASSIGN_BF16) {
+  if (h->opt.assign_tier != KMGB_ASSIGN_FP32) {
     a.gamma = assign_bf16_gamma(h->d);
-    KM_TRY(launch_assign_bf16(Xba, h->ldb, h->Cb, h->ldb, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
+    KM_TRY(launch_assign_bf16(Xba, Xla, h->ldb, h->Cb, h->Cl, h->ldb, a, s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
   } else {
     a.gamma = assign_fp32_gamma(h->d);
     KM_TRY(launch_assign_fp32(Xa, h->ldx, h->Cop, h->ldx, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
@@ -717,6 +730,61 @@ int kmgb_get_phase_ms(kmgb_handle* h, double* ms, int* iters) {
 }
 
 long long kmgb_launch_count(void) { return launch_count(); }
+
+int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int k, int split,
+                         float* out) {
+  if (!X || !C || !out || n <= 0 || d <= 0 || k <= 0) return KMEANS_ERROR_BUILDDATA;
+  kmgb_options o;
+  kmgb_default_options(&o);
+  o.assign_tier = split ? KMGB_ASSIGN_BF16X3 : KMGB_ASSIGN_BF16;
+  o.certify = 0;
+  o.max_iters = 1;
+  kmgb_handle* h = nullptr;
+  int rc = create_handle(&h, n, d, k, &o);
+  if (rc) return rc;
+  const int kpad = (k + 127) / 128 * 128;
+  float* dump = nullptr;
+  std::vector<float> host;
+  rc = set_data(h, X, false);
+  if (!rc) rc = set_centers(h, C, false);
+  if (!rc && cudaMalloc(&dump, sizeof(float) * (size_t)n * kpad) != cudaSuccess)
+    rc = KMEANS_ERROR_BUILDDATA;
+  if (!rc) {
+    cudaStream_t s = h->stream;
+    AssignArgs a{};
+    a.cn = h->cn;
+    a.xnorm = h->xn;
+    a.cmax = h->cmax;
+    a.labels = h->labels;
+    a.rerank_list = h->rr_list;
+    a.rerank_count = h->rr_count;
+    a.err = h->err;
+    a.n = n;
+    a.k = k;
+    a.d = d;
+    a.certify = 0;
+    a.cinit = h->cinit;
+    a.dump = dump;
+    if (cudaMemsetAsync(h->cmax, 0, sizeof(float), s) != cudaSuccess ||
+        launch_prep_centers(h->C, h->ldx, k, d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s, nullptr,
+                            h->cinit, h->Cl) != cudaSuccess ||
+        launch_assign_bf16(h->Xb, h->Xl, h->ldb, h->Cb, h->Cl, h->ldb, a, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      rc = KMEANS_ERROR_CLOSEST_CENTERS;
+  }
+  if (!rc) {
+    host.resize((size_t)n * kpad);
+    if (cudaMemcpy(host.data(), dump, sizeof(float) * host.size(), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+      rc = KMEANS_ERROR_GET_CENTERS;
+    else
+      for (long long i = 0; i < n; ++i)
+        std::memcpy(out + (size_t)i * k, host.data() + (size_t)i * kpad, sizeof(float) * k);
+  }
+  if (dump) cudaFree(dump);
+  delete h;
+  return rc;
+}
 
 int kmgb_destroy(kmgb_handle* h) {
   delete h;

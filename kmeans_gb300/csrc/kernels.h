@@ -15,6 +15,7 @@ struct AssignArgs {
   const float* xnorm;     // [n] upper bound of ||x_i||
   const float* cmax;      // device scalar: upper bound of max ||c_j|| over usable centers
   const float* cinit;     // [round_up(k,128)] accumulator start -||c_j||^2/2 (BF16 tier)
+  float* dump;            // diagnostic (nullable): raw accumulators [n][round_up(k,128)]
   int* labels;            // [n]
   int* rerank_list;       // [n]
   int* rerank_count;      // device scalar
@@ -32,11 +33,14 @@ cudaError_t launch_assign_fp32(const float* X, long long ldx, const float* Cop, 
                                const AssignArgs& a, cudaStream_t s);
 float assign_fp32_gamma(int d);
 
-// tcgen05 BF16 assignment. Xb: [n][ldb] BF16, Cb: [k][ldb] BF16, ldb a multiple of 8.
-cudaError_t launch_assign_bf16(const void* Xb, long long ldxb, const void* Cb, long long ldcb,
-                               const AssignArgs& a, cudaStream_t s);
+// tcgen05 BF16 assignment. Xb: [n][ldb] BF16, Cb: [k][ldb] BF16, ldb a multiple of 8. With the
+// residual planes Xl / Cl (x - bf16(x), same layout; both nullable) the split tier computes
+// x_hi.c_hi + x_hi.c_lo + x_lo.c_hi.
+cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, const void* Cb,
+                               const void* Cl, long long ldcb, const AssignArgs& a,
+                               cudaStream_t s);
 float assign_bf16_gamma(int d);
-bool bf16_tc_supported(int d);
+bool bf16_tc_supported(int d, int planes = 1);
 
 // Exact re-rank of flagged points. mode 0 (Lloyd): FP64 arg-min of sum_d (x_d - c_d)^2.
 // mode 1 (expansion, caller norms): FP64 arg-min of nb_j - 2 x.c_j with the given nb.
@@ -73,14 +77,17 @@ cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, con
 // unusable centers and padding.
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop,
                                 void* Cb, long long ldcb, float* cn, float* cmax, cudaStream_t s,
-                                const int* stop = nullptr, float* cinit = nullptr);
+                                const int* stop = nullptr, float* cinit = nullptr,
+                                void* Cl = nullptr);
 
 // Per-point norms, computed once per data set: qn = ||x||^2 (FP64), xn = upper bound ||x||.
 cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,
                                float* xn, cudaStream_t s);
 // BF16 copy of the data set (zero padded to ldb columns).
+// Xl (nullable) receives the residual plane bf16(x - bf16(x)).
 cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
-                           long long ldb, cudaStream_t s, const int* stop = nullptr);
+                           long long ldb, cudaStream_t s, const int* stop = nullptr,
+                           void* Xl = nullptr);
 
 // Deterministic update: stable counting sort by label, FP64 piece sums, finalize.
 struct UpdateWork {

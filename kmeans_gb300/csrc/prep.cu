@@ -17,7 +17,8 @@ namespace {
 __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, int k, int d,
                                     float* __restrict__ Cop, __nv_bfloat16* __restrict__ Cb,
                                     long long ldcb, float* __restrict__ cn, float* cmax,
-                                    const int* stop, float* __restrict__ cinit, int kpad) {
+                                    const int* stop, float* __restrict__ cinit, int kpad,
+                                    __nv_bfloat16* __restrict__ Cl) {
   if (stopped(stop)) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -39,8 +40,13 @@ __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, 
   for (int t = lane; t < (int)ldc; t += 32) op[t] = (bad || t >= d) ? 0.0f : c[t];
   if (Cb) {
     __nv_bfloat16* ob = Cb + (size_t)warp * ldcb;
-    for (int t = lane; t < (int)ldcb; t += 32)
-      ob[t] = __float2bfloat16_rn((bad || t >= d) ? 0.0f : c[t]);
+    __nv_bfloat16* ol = Cl ? Cl + (size_t)warp * ldcb : nullptr;
+    for (int t = lane; t < (int)ldcb; t += 32) {
+      const float v = (bad || t >= d) ? 0.0f : c[t];
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      ob[t] = hi;
+      if (ol) ol[t] = __float2bfloat16_rn(v - __bfloat162float(hi));
+    }
   }
   if (lane == 0) {
     if (bad) {
@@ -73,14 +79,18 @@ __global__ void point_norms_kernel(const float* __restrict__ X, long long ldx, l
 }
 
 __global__ void to_bf16_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
-                               __nv_bfloat16* __restrict__ Xb, long long ldb, const int* stop) {
+                               __nv_bfloat16* __restrict__ Xb, long long ldb, const int* stop,
+                               __nv_bfloat16* __restrict__ Xl) {
   if (stopped(stop)) return;
   const long long total = n * ldb;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (long long)gridDim.x * blockDim.x) {
     const long long r = e / ldb;
     const int c = (int)(e - r * ldb);
-    Xb[e] = __float2bfloat16_rn(c < d ? X[(size_t)r * ldx + c] : 0.0f);
+    const float v = c < d ? X[(size_t)r * ldx + c] : 0.0f;
+    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+    Xb[e] = hi;
+    if (Xl) Xl[e] = __float2bfloat16_rn(v - __bfloat162float(hi));
   }
 }
 
@@ -118,14 +128,15 @@ __global__ void gather_vec_kernel(const double* __restrict__ qs, const float* __
 
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop, void* Cb,
                                 long long ldcb, float* cn, float* cmax, cudaStream_t s,
-                                const int* stop, float* cinit) {
+                                const int* stop, float* cinit, void* Cl) {
   if (k <= 0) return cudaSuccess;
   const int threads = 256;
   const int kpad = (k + 127) / 128 * 128;
   const int blocks = (int)(((long long)(cinit ? kpad : k) * 32 + threads - 1) / threads);
   prep_centers_kernel<<<blocks, threads, 0, s>>>(C, ldc, k, d, Cop,
                                                  reinterpret_cast<__nv_bfloat16*>(Cb), ldcb, cn,
-                                                 cmax, stop, cinit, kpad); kmgb::count_launches(1);
+                                                 cmax, stop, cinit, kpad,
+                                                 reinterpret_cast<__nv_bfloat16*>(Cl)); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 
@@ -139,10 +150,10 @@ cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d
 }
 
 cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
-                           long long ldb, cudaStream_t s, const int* stop) {
+                           long long ldb, cudaStream_t s, const int* stop, void* Xl) {
   if (n <= 0) return cudaSuccess;
   to_bf16_kernel<<<152 * 16, 256, 0, s>>>(X, ldx, n, d, reinterpret_cast<__nv_bfloat16*>(Xb),
-                                          ldb, stop); kmgb::count_launches(1);
+                                          ldb, stop, reinterpret_cast<__nv_bfloat16*>(Xl)); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

@@ -9,7 +9,8 @@
 //   3. scatter  one warp per tile walks its points in order and writes each point id to
 //               start + rank, so the sort by label is stable (ascending point id per label);
 //   4. pieces   every label's run is cut into pieces of kSumPiece points; one warp per piece
-//               sums its rows in FP64 in point order (and the rows' FP64 ||x||^2);
+//               sums its rows in point order (FP32 data: error-free float-float sum turned into
+//               FP64 once per piece; FP64 data: FP64) and the rows' FP64 ||x||^2;
 //   5. finalize one warp per center adds its pieces in order, divides by the count in FP64,
 //               rounds once to FP32 (empty cluster: NaN as in ClusterCenters.cu:81, or keep the
 //               previous center), and evaluates the cluster's SSE against the new center with
@@ -178,6 +179,33 @@ __global__ void scatter_kernel(const int* __restrict__ labels, long long n, int 
   }
 }
 
+// Piece accumulator. FP32 data: an error-free float-float sum (Knuth's TwoSum on the FP32
+// pipe: hi + lo carries ~48 significant bits), turned into one FP64 value per piece; FP64 data:
+// a plain FP64 sum. GB300 issues FP64 (and FP32->FP64 conversions) at a small fraction of the
+// FP32 rate, so converting every element would bound the update.
+template <typename T>
+struct PieceAcc;
+
+template <>
+struct PieceAcc<float> {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(t, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    hi = t;
+    lo = __fadd_rn(lo, err);
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <>
+struct PieceAcc<double> {
+  double s = 0.0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
 __device__ __forceinline__ int find_label(const int* __restrict__ pstart, int k, int p) {
   int lo = 0, hi = k - 1;
   while (lo < hi) {
@@ -206,9 +234,7 @@ __global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
     const int b = label_off[j] + q * kSumPiece;
     const int e = min(b + kSumPiece, label_off[j + 1]);
     for (int d0 = 0; d0 < d; d0 += 256) {
-      double acc[8];
-#pragma unroll
-      for (int r = 0; r < 8; ++r) acc[r] = 0.0;
+      PieceAcc<T> acc[8];
       double qs = 0.0;
 #pragma unroll 4
       for (int t = b; t < e; ++t) {
@@ -217,14 +243,14 @@ __global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
           const int c = lane + 32 * r;
-          if (d0 + c < d) acc[r] += (double)__ldg(x + c);
+          if (d0 + c < d) acc[r].add(__ldg(x + c));
         }
         if (qn && d0 == 0) qs += __ldg(qn + i);
       }
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
         const int c = d0 + lane + 32 * r;
-        if (c < d) part[(size_t)p * d + c] = acc[r];
+        if (c < d) part[(size_t)p * d + c] = acc[r].value();
       }
       if (d0 == 0 && lane == 0 && partq) partq[p] = qs;
     }

@@ -26,9 +26,10 @@
 //                RowTransformMinimum.cu:31 ('val<dataReg' is false for NaN).
 //  * update    : new center = sum of member points / count (ClusterCenters.cu:3-23,47-87);
 //                count 0 gives 0/0 = NaN (ClusterCenters.cu:81) under the reference policy.
-//                Sums are FP64 in a canonical order: members in ascending point order,
-//                grouped in pieces of `piece` points, each piece summed from 0.0, pieces
-//                summed in order from 0.0; the quotient is rounded once to FP32.
+//                Sums in a canonical order: members in ascending point order, grouped in
+//                pieces of `piece` points; each piece is summed from zero (FP32 data: an
+//                error-free float-float TwoSum, ~48 bits, converted to FP64 once; FP64 data:
+//                FP64), pieces are summed in order in FP64; the quotient is rounded once.
 //  * SSE       : sum_i ||x_i - c_new[label_i]||^2 against the NEW centers with the labels of
 //                the OLD centers (Compactness.cu:3-59, kmeans.cpp:1044-1104), FP64.
 //  * loop      : while (iters < maxIters && relErr > criterion), relErr =
@@ -154,6 +155,30 @@ void assign_rows(const T* X, long long nrows, const long long* rows, int d, cons
   }
 }
 
+// Piece accumulator, the same operation sequence as the device: FP32 data are summed with an
+// error-free float-float TwoSum (hi + lo), converted to FP64 once per piece; FP64 data are
+// summed in FP64.
+template <typename T>
+struct PieceAcc;
+template <>
+struct PieceAcc<float> {
+  float hi = 0.0f, lo = 0.0f;
+  void add(float x) {
+    const float t = hi + x;
+    const float bp = t - hi;
+    const float err = (hi - (t - bp)) + (x - bp);
+    hi = t;
+    lo = lo + err;
+  }
+  double value() const { return (double)hi + (double)lo; }
+};
+template <>
+struct PieceAcc<double> {
+  double s = 0.0;
+  void add(double x) { s += x; }
+  double value() const { return s; }
+};
+
 // Canonical FP64 center update over `rows` (nullptr = 0..m-1), labels indexed like rows.
 // new_centers: K x D of T (the FP64 quotient rounded once to T). counts: K (nullable).
 // sums: K x D FP64 (nullable). empty_policy 0: NaN center for an empty cluster (reference);
@@ -172,17 +197,18 @@ void update_rows(const T* X, long long nrows, const long long* rows, int d, cons
 
 #pragma omp parallel for schedule(dynamic, 1)
   for (int j = 0; j < k; ++j) {
-    std::vector<double> total(d, 0.0), part(d);
+    std::vector<double> total(d, 0.0);
+    std::vector<PieceAcc<T>> part(d);
     for (long long p0 = off[j]; p0 < off[j + 1]; p0 += piece) {
       long long p1 = std::min(p0 + (long long)piece, off[j + 1]);
-      std::fill(part.begin(), part.end(), 0.0);
+      std::fill(part.begin(), part.end(), PieceAcc<T>());
       for (long long q = p0; q < p1; ++q) {
         const long long r = sorted[q];
         const long long i = rows ? rows[r] : r;
         const T* x = X + (size_t)i * d;
-        for (int t = 0; t < d; ++t) part[t] += (double)x[t];
+        for (int t = 0; t < d; ++t) part[t].add(x[t]);
       }
-      for (int t = 0; t < d; ++t) total[t] += part[t];
+      for (int t = 0; t < d; ++t) total[t] += part[t].value();
     }
     const long long n = cnt[j];
     for (int t = 0; t < d; ++t) {

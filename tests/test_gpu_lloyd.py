@@ -9,7 +9,7 @@ from kmeans_gb300.synthetic import mixture_numpy, sample_init
 
 pytestmark = pytest.mark.gpu
 SSE_RTOL = 1e-10
-TIERS = [0, 1]  # plain FP32 fused kernel, tcgen05 BF16 tensor-core kernel
+TIERS = [0, 1, 2]  # plain FP32 fused kernel, tcgen05 BF16, tcgen05 split BF16 (x3)
 
 
 def check_same(res, ref, sse_rtol=SSE_RTOL):
@@ -31,9 +31,11 @@ def test_c1_config(km, orc, torch_cuda, tier):
 
 
 @pytest.mark.parametrize("n,d,k", [(1, 1, 1), (130, 3, 7), (1000, 129, 200), (4097, 64, 129),
-                                   (20000, 128, 256), (3001, 17, 1)])
+                                   (20000, 128, 256), (3001, 17, 1), (2000, 256, 300)])
 @pytest.mark.parametrize("tier", TIERS)
 def test_odd_shapes(km, orc, torch_cuda, n, d, k, tier):
+    if tier == 2 and d > 128:
+        pytest.skip("the split BF16 tier covers D <= 128")
     X, _, _ = mixture_numpy(n, d, max(k, 1), seed=n + d + k)
     init = X[sample_init(n, k, seed=3)]
     res = km.lloyd(X, k, init=init, max_iters=6, assign_tier=tier)
@@ -192,9 +194,23 @@ def test_zero_sse_stops_like_the_reference(km, orc, torch_cuda):
     assert res.iterations == 1 and res.status == 13 and res.sse[0] == 0.0
 
 
-def test_bf16_tier_certifies_well_separated_points(km, orc, torch_cuda):
+@pytest.mark.parametrize("tier", [1, 2])
+def test_bf16_tiers_certify_well_separated_points(km, orc, torch_cuda, tier):
     """On well separated clusters almost every point is certified by the tensor-core pass."""
     X, comp, means = mixture_numpy(200_000, 64, 100, seed=31, mean_lo=-50, mean_hi=50)
-    res = km.lloyd(X, 100, init=means, max_iters=2, assign_tier=1)
+    res = km.lloyd(X, 100, init=means, max_iters=2, assign_tier=tier)
     check_same(res, orc.lloyd(X, means, 2))
     assert res.reranked < 0.01 * 2 * len(X)
+
+
+def test_split_tier_certifies_more_than_plain_bf16(km, orc, torch_cuda):
+    """Overlapping clusters: the split operand (x_hi.c_hi + x_hi.c_lo + x_lo.c_hi) leaves far fewer
+    points to the exact re-rank than plain BF16, with identical labels."""
+    X, _, _ = mixture_numpy(100_000, 128, 256, seed=33, mean_lo=-20, mean_hi=20, std=(0.3, 3.0))
+    init = X[sample_init(len(X), 256, seed=34)]
+    ref = orc.lloyd(X, init, 2)
+    r1 = km.lloyd(X, 256, init=init, max_iters=2, assign_tier=1)
+    r2 = km.lloyd(X, 256, init=init, max_iters=2, assign_tier=2)
+    check_same(r1, ref)
+    check_same(r2, ref)
+    assert r2.reranked * 5 < r1.reranked

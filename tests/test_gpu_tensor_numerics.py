@@ -1,0 +1,55 @@
+"""Tensor-core numerics behind the certified BF16 assignment: the raw tcgen05 accumulators
+(x.c - ||c||^2/2 with FP32 accumulation in TMEM) are compared with the exact sums of the same
+BF16 products. The kernel's certificate assumes the accumulation error stays below
+(terms + 32) * 2^-21 * (|start| + sum |products|); this test measures the worst case on the
+device and requires it to be at least 4x below that model."""
+import numpy as np
+import pytest
+
+from test_bounds_cpu import bf16, split
+
+pytestmark = pytest.mark.gpu
+
+
+def cases():
+    rng = np.random.default_rng(3)
+    n, d, k = 384, 128, 256
+    X = (rng.standard_normal((n, d)) * 10.0 ** rng.uniform(-1, 1, (n, 1))).astype(np.float32)
+    C = (rng.standard_normal((k, d)) * 10.0 ** rng.uniform(-1, 1, (k, 1))).astype(np.float32)
+    yield "mixed", X, C
+    # heavy cancellation: points close to centers, large common offset
+    C2 = (rng.uniform(-20, 20, (k, d)) + 50).astype(np.float32)
+    X2 = (C2[rng.integers(0, k, n)] + rng.standard_normal((n, d)).astype(np.float32) * 0.1)
+    yield "offset", X2.astype(np.float32), C2
+    X3 = rng.uniform(-1, 1, (n, 64)).astype(np.float32)
+    C3 = rng.uniform(-1, 1, (k, 64)).astype(np.float32)
+    yield "d64", X3, C3
+
+
+@pytest.mark.parametrize("use_split", [False, True])
+def test_tc_accumulation_error_model(km, torch_cuda, use_split):
+    f = lambda a: a.astype(np.float64)
+    for name, X, C in cases():
+        d = X.shape[1]
+        acc = km.tc_accumulators(X, C, use_split).astype(np.float64)
+        cn = (f(C) ** 2).sum(1).astype(np.float32)  # ||c||^2 rounded once to FP32
+        start = -0.5 * f(cn)
+        if use_split:
+            xh, xl = split(X)
+            ch, cl = split(C)
+            prod = f(xh) @ f(ch).T + f(xh) @ f(cl).T + f(xl) @ f(ch).T
+            mag = np.abs(f(xh)) @ np.abs(f(ch)).T + np.abs(f(xh)) @ np.abs(f(cl)).T \
+                + np.abs(f(xl)) @ np.abs(f(ch)).T
+            terms = 3 * d
+        else:
+            xb, cb = bf16(X), bf16(C)
+            prod = f(xb) @ f(cb).T
+            mag = np.abs(f(xb)) @ np.abs(f(cb)).T
+            terms = d
+        exact = prod + start[None, :]
+        scale = mag + np.abs(start)[None, :]
+        err = np.max(np.abs(acc - exact) / scale)
+        model = (terms + 32) * 2.0 ** -21
+        print(f"{name} split={use_split}: max accumulation error {err:.3e} of scale, "
+              f"model {model:.3e} (ratio {err / model:.4f})")
+        assert err * 4 <= model, (name, err, model)
