@@ -138,6 +138,23 @@ KMGB_EXPORT kmeansCudaErrorStatus ClusterCentersD(const int m0, const int m, con
                                       double* centers_large, int* counts_large, double* centers,
                                       int* counts);
 
+/* No counterpart in the reference. ClusterCentersF for callers that cannot allocate device
+ * memory (programs that reserve all device memory up front and forbid allocation afterwards, or
+ * whose memory pool owns the GPU): same arguments and results as ClusterCentersF, but the
+ * working memory (label histogram, sorted ids, FP64 piece sums) comes from one 8 MiB array in
+ * device global memory that the library holds on every GPU that loads it, instead of the
+ * stream-ordered allocator; nothing is allocated. Sizes that need more than 8 MiB of working
+ * memory (roughly (m/128 + k) * n * 8 + (m + 2k + k*tiles) * 4 bytes) return
+ * ERROR_CLUSTERCENTERS with a message in kmgb_last_error(). The first call on a device looks up
+ * the array's device address: make it before any stream capture. All calls share the array and
+ * it keeps the last call's contents; calls that overlap on the GPU race and must be serialised
+ * by the caller. */
+KMGB_EXPORT kmeansCudaErrorStatus ClusterCentersF_noalloc(const int m0, const int m, const int n,
+                                                          const int k, const bool lastTile,
+                                                          const float* data, const int* indices,
+                                                          float* centers_large, int* counts_large,
+                                                          float* centers, int* counts);
+
 /* Replace CompactnessF/D (KmeansCudaKernels.h:389-414, Compactness.cu:258-327): the squared
  * distance of every row to centers[indices[m0+i]] (K x n row-major) is added to a running FP64
  * total kept inside the caller's buffer (compactness[2..3] viewed as one double for F,

@@ -103,6 +103,7 @@ def lib():
             "rowTransformMinimumD": (i32, [i32, i32, i32, P, P, P, P]),
             "ClusterCentersF": (i32, [i32, i32, i32, i32, b, P, P, P, P, P, P]),
             "ClusterCentersD": (i32, [i32, i32, i32, i32, b, P, P, P, P, P, P]),
+            "ClusterCentersF_noalloc": (i32, [i32, i32, i32, i32, b, P, P, P, P, P, P]),
             "CompactnessF": (i32, [i32, i32, b, i32, i32, P, P, P, P]),
             "CompactnessD": (i32, [i32, i32, b, i32, i32, P, P, P, P]),
             "rowNormalizeF": (i32, [i32, i32, i32, P, P]),
@@ -258,6 +259,15 @@ def ClusterCentersD(m0, m, n, k, lastTile, data, indices, centers_large, counts_
     return int(lib().ClusterCentersD(m0, m, n, k, bool(lastTile), _ptr(data), _ptr(indices),
                                      _ptr(centers_large), _ptr(counts_large), _ptr(centers),
                                      _ptr(counts)))
+
+
+def ClusterCentersF_noalloc(m0, m, n, k, lastTile, data, indices, centers_large, counts_large,
+                            centers, counts) -> int:
+    """ClusterCentersF without any device allocation (working memory in the library's static
+    8 MiB device array); for callers that cannot allocate."""
+    return int(lib().ClusterCentersF_noalloc(m0, m, n, k, bool(lastTile), _ptr(data),
+                                             _ptr(indices), _ptr(centers_large),
+                                             _ptr(counts_large), _ptr(centers), _ptr(counts)))
 
 
 def CompactnessF(m0, m, lastTile, n, k, data, indices, centers, compactness) -> int:

@@ -32,6 +32,7 @@ using namespace kmgb;
 namespace kmgb {
 static std::atomic<long long> g_launches{0};
 void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+void set_last_error(const char* msg);
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 }  // namespace kmgb
 
@@ -72,6 +73,8 @@ bool is_device_ptr(const void* p) {
 }
 
 }  // namespace
+
+void kmgb::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 
 // Reference shuffle permutation (kmeans.cpp:554-557): perm[i] = source row of shuffled row i.
 static void reference_perm(int m, std::vector<int>& perm) {

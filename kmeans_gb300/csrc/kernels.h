@@ -137,4 +137,7 @@ cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* 
 
 constexpr int kSumPiece = 128;
 
+// Message returned by kmgb_last_error() on the calling thread.
+void set_last_error(const char* msg);
+
 }  // namespace kmgb
