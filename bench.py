@@ -6,7 +6,7 @@ the 4,000,000 x 128, K=1024 workload (1024 anisotropic Gaussians, per-component 
 log-uniform in [0.3, 3], means uniform in [-20, 20]^128, initial centers a seeded sample of
 points; synthetic, generated on the device). Prints one JSON line.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--tier fp32|bf16] [--impl reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--tier bf16x3|bf16|fp32] [--impl reference]
 
 `value` is Lloyd iterations/s with the data resident in HBM (CUDA events on the library's
 stream); `e2e` is the same metric through the public C-ABI one-shot call (kmgb_lloyd_f32) from
@@ -126,7 +126,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--tier", default=None, help="fp32 or bf16 (default: bf16 when available)")
+    ap.add_argument("--tier", default="bf16x3",
+                    help="assignment tier: bf16x3 (split BF16 tensor cores, default), bf16, fp32")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N, help="rows (default: the 4M workload); smaller "
@@ -150,7 +151,7 @@ def main():
         dist.init_process_group("nccl")
     km.build()
     lib = km.lib()
-    tier = args.tier or "fp32"
+    tier = args.tier
     tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3}[tier]
 
     n = args.n
