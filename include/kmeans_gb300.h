@@ -206,8 +206,10 @@ typedef struct kmgb_options {
 typedef struct kmgb_stats {
   int iterations;
   int status;                      /* kmeansErrorStatus of the run */
-  unsigned long long reranked;     /* points sent to the exact re-rank (all iterations) */
-  unsigned long long reranked_fp64;/* of those, points that needed the FP64 evaluation */
+  unsigned long long reranked;     /* points whose approximate margin did not certify the label
+                                      (all iterations); each is settled exactly */
+  unsigned long long reranked_fp64;/* of those, points that needed a full rescan of the centers
+                                      (FP32 then FP64) instead of their recorded candidates */
   long long empty_clusters;        /* empty clusters seen after the last update */
   double ms_total;                 /* wall time of the iterations (CUDA events) */
   long long reserved[8];

@@ -157,7 +157,14 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nkb = (p.d + BK - 1) / BK;
   const int nchunks = (p.k + BN - 1) / BN;
-  const long long n_units = (p.n + UNIT - 1) / UNIT;
+  // rows of this launch: [row0, row0 + n_rows); a device count bounds them in candidate mode
+  long long n_rows = p.n;
+  if (p.n_dev) {
+    const long long c = (long long)*p.n_dev - p.row0;
+    n_rows = c < 0 ? 0 : (c < p.n ? c : p.n);
+  }
+  const long long n_units = (n_rows + UNIT - 1) / UNIT;
+  const bool cand_mode = p.thr_in != nullptr;
   long long my_units = 0;
   if ((long long)blockIdx.x < n_units)
     my_units = (n_units - 1 - blockIdx.x) / gridDim.x + 1;
@@ -225,7 +232,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           for (int t = 0; t < TILES; ++t)
             for (int kb = 0; kb < nkb; ++kb)
               tma_load_2d(smem_u32(xs + (size_t)((pl * TILES + t) * nkb + kb) * KB_BYTES),
-                          pl ? &tmXl : &tmX, xb, kb * BK, (int)(u * UNIT + t * BM));
+                          pl ? &tmXl : &tmX, xb, kb * BK, (int)(p.row0 + u * UNIT + t * BM));
         for (int c = 0; c < nchunks && ok; ++c) {
           for (int kb = 0; kb < nkb; ++kb, ++s) {
             const int stage = (int)(s % stages);
@@ -340,6 +347,10 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     for (long long u = blockIdx.x; u < n_units && alive; u += gridDim.x) {
       float b1 = -INFINITY, b2 = -INFINITY;
       int bblk = -1;  // global 32-column block holding the best key
+      const long long prow = u * UNIT + t * BM + q * 32 + lane;  // row within the launch
+      float floor_key = INFINITY;  // candidate mode: record keys >= floor_key
+      int ncand = 0;
+      if (cand_mode && prow < n_rows) floor_key = __ldg(p.thr_in + p.row0 + prow);
       for (int c = 0; c < nchunks; ++c, ++g) {
         const int b = (int)(g & 1);
         bool ok = mbar_wait(smem_u32(&bars.acc_full[b]), (uint32_t)((g >> 1) & 1), &abort_flag,
@@ -362,13 +373,26 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           if (cb + 1 < BN / 32) tmem_ld32(base + (cb + 1) * 32, nxt);
           if (p.dump) {  // diagnostic: raw accumulators of this point
             const long long pt = u * UNIT + t * BM + q * 32 + lane;
-            if (pt < p.n) {
+            if (pt < n_rows) {
               float* dst = p.dump + (size_t)pt * (size_t)nchunks * BN + (size_t)c * BN + cb * 32;
 #pragma unroll
               for (int j = 0; j < 32; ++j) dst[j] = __uint_as_float(cur[j]);
             }
           }
+          if (cand_mode) {
+            // second pass over flagged points: every key at or above the floor is a candidate
 #pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const float key = __uint_as_float((cur[j] & ~0x1Fu) | (uint32_t)j);
+              if (key >= floor_key) {
+                if (ncand < kMaxCand)
+                  p.cand[(size_t)(p.row0 + prow) * kMaxCand + ncand] = c * BN + cb * 32 + j;
+                ++ncand;
+              }
+            }
+            if (cb + 1 < BN / 32) tmem_ld_wait();
+            continue;
+          }
           const float blk_before = b1;
 #pragma unroll
           for (int j = 0; j < 32; j += 2) {
@@ -388,8 +412,12 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         if (lane == 0) mbar_arrive(smem_u32(&bars.acc_empty[b]));
       }
       if (!alive) break;
-      const long long pt = u * UNIT + t * BM + q * 32 + lane;
-      if (pt < p.n) {
+      if (cand_mode) {
+        if (prow < n_rows) p.cand_cnt[p.row0 + prow] = ncand > kMaxCand ? -1 : ncand;
+        continue;
+      }
+      const long long pt = prow;
+      if (pt < n_rows) {
         const bool none = !(b1 > -1.0e38f);  // no usable center at all
         const int label = (bblk < 0 || none) ? 0 : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
         p.labels[pt] = label;
@@ -398,6 +426,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
             p.rerank_list[slot] = (int)pt;
+            // the FP64 arg-min's key is >= b1 - 2E (E bounds every key's error)
+            if (p.thr_out) p.thr_out[pt] = none ? -INFINITY : __fsub_rd(b1, 2.0f * eb);
           }
         }
       }
@@ -480,6 +510,7 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   }
   const long long n_units = (a.n + UNIT - 1) / UNIT;
   const int grid = (int)(n_units < g_num_sms ? n_units : g_num_sms);
+  if (grid <= 0) return cudaSuccess;
   assign_bf16_kernel<<<grid, NTHREADS, smem, s>>>(tmX, tmXl, tmC, tmCl, a, stages, xbufs, planes);
   count_launches(1);
   return cudaGetLastError();

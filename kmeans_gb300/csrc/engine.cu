@@ -148,9 +148,19 @@ struct kmgb_handle {
   // assignment
   int* labels = nullptr;
   int* rr_list = nullptr;
-  int* rr_count = nullptr;     // [0] flagged by the assignment, [1] left for the FP64 stage
+  // re-rank lists: [0] flagged by the assignment (rr_list), [1] BF16 tiers: candidates overflowed
+  // (rr_over), [2] left for the exact FP64 stage after the FP32 rescan (rr_list2, rr_hi2)
+  int* rr_count = nullptr;
+  int* rr_over = nullptr;
   int* rr_list2 = nullptr;
   float* rr_hi2 = nullptr;
+  // BF16 tiers: candidate floors and the compact second pass over the flagged rows
+  float* thr_full = nullptr;
+  float* thr_c = nullptr;
+  void* XbC = nullptr;
+  void* XlC = nullptr;
+  int* cand = nullptr;
+  int* cand_cnt = nullptr;
   unsigned long long* rr_stats = nullptr;
   int* err = nullptr;
   // device-side loop state: stop flag, previous SSE, last relErr, iterations done
@@ -191,7 +201,8 @@ struct kmgb_handle {
   ~kmgb_handle() {
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
     void* ptrs[] = {X, Xb, Xl, qn, xn, perm, Xw, Xbw, Xlw, qnw, xnw, C, Cop, Cb, Cl, cn, cmax, cinit, labels,
-                    rr_list, rr_count, rr_list2, rr_hi2, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
+                    rr_list, rr_count, rr_over, rr_list2, rr_hi2, thr_full, thr_c, XbC, XlC, cand,
+                    cand_cnt, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
                     uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
                     stop, loopf, iters_done};
     for (void* p : ptrs)
@@ -271,9 +282,18 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   const long long na = h->n_act;
   KM_TRY(dalloc(&h->labels, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_list, na), (delete h, code));
-  KM_TRY(dalloc(&h->rr_count, 2), (delete h, code));
+  KM_TRY(dalloc(&h->rr_count, 3), (delete h, code));
   KM_TRY(dalloc(&h->rr_list2, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_hi2, na), (delete h, code));
+  if (bf16) {
+    KM_TRY(dalloc(&h->rr_over, na), (delete h, code));
+    KM_TRY(dalloc(&h->thr_full, na), (delete h, code));
+    KM_TRY(dalloc(&h->thr_c, na), (delete h, code));
+    KM_TRY(cudaMalloc(&h->XbC, (size_t)na * h->ldb * 2), (delete h, code));
+    if (split) KM_TRY(cudaMalloc(&h->XlC, (size_t)na * h->ldb * 2), (delete h, code));
+    KM_TRY(dalloc(&h->cand, (size_t)na * kMaxCand), (delete h, code));
+    KM_TRY(dalloc(&h->cand_cnt, na), (delete h, code));
+  }
   KM_TRY(dalloc(&h->rr_stats, 2), (delete h, code));
   KM_TRY(dalloc(&h->err, 1), (delete h, code));
   KM_TRY(dalloc(&h->stop, 1), (delete h, code));
@@ -397,7 +417,7 @@ int step(kmgb_handle* h, int slot) {
   KM_TRY(h->pmark(0), KMEANS_ERROR_RESET);
   // reset (kmeans.cpp:1142-1170): norms of the current centers, cleared counters
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
-  KM_TRY(cudaMemsetAsync(h->rr_count, 0, 2 * sizeof(int), s), KMEANS_ERROR_RESET);
+  KM_TRY(cudaMemsetAsync(h->rr_count, 0, 3 * sizeof(int), s), KMEANS_ERROR_RESET);
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
                              h->stop, h->cinit, h->Cl),
          KMEANS_ERROR_RESET);
@@ -417,8 +437,10 @@ int step(kmgb_handle* h, int slot) {
   a.certify = h->opt.certify;
   a.stop = h->stop;
   a.cinit = h->cinit;
-  if (h->opt.assign_tier != KMGB_ASSIGN_FP32) {
+  const bool tc = h->opt.assign_tier != KMGB_ASSIGN_FP32;
+  if (tc) {
     a.gamma = assign_bf16_gamma(h->d);
+    a.thr_out = h->opt.certify ? h->thr_full : nullptr;
     KM_TRY(launch_assign_bf16(Xba, Xla, h->ldb, h->Cb, h->Cl, h->ldb, a, s),
            KMEANS_ERROR_CLOSEST_CENTERS);
   } else {
@@ -443,14 +465,41 @@ int step(kmgb_handle* h, int slot) {
     r.mode = 0;
     r.max_list = na;
     r.stop = h->stop;
-    // FP32 stage over the flagged points, exact FP64 stage over what FP32 cannot separate
-    KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 1, h->rr_hi2, s),
+    if (tc) {
+      // BF16 tiers: a second tensor-core pass over the flagged rows records every center whose
+      // key reaches the point's floor (best - 2E); those few candidates are resolved in FP64.
+      // Points with more than kMaxCand candidates take the full rescan below.
+      KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, na, Xba, Xla, h->ldb, h->thr_full,
+                                   h->XbC, Xla ? h->XlC : nullptr, h->thr_c, h->stop, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+      AssignArgs c2 = a;
+      c2.labels = nullptr;
+      c2.certify = 0;
+      c2.thr_out = nullptr;
+      c2.n_dev = h->rr_count;
+      c2.row0 = 0;
+      c2.thr_in = h->thr_c;
+      c2.cand = h->cand;
+      c2.cand_cnt = h->cand_cnt;
+      KM_TRY(launch_assign_bf16(h->XbC, Xla ? h->XlC : nullptr, h->ldb, h->Cb, h->Cl, h->ldb, c2,
+                                s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+      KM_TRY(launch_resolve_candidates(h->rr_list, h->rr_count, na, h->cand, h->cand_cnt, Xa,
+                                       h->ldx, h->Cop, h->ldx, h->cn, h->d, h->labels, h->rr_over,
+                                       h->rr_count + 1, h->stop, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+      r.list = h->rr_over;
+      r.count = h->rr_count + 1;
+    }
+    // FP32 stage over the points still open, exact FP64 stage over what FP32 cannot separate
+    KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 2, h->rr_hi2, s),
            KMEANS_ERROR_CLOSEST_CENTERS);
     r.list = h->rr_list2;
-    r.count = h->rr_count + 1;
+    r.count = h->rr_count + 2;
     r.stats = nullptr;
     KM_TRY(launch_rerank_exact(r, h->rr_hi2, s), KMEANS_ERROR_CLOSEST_CENTERS);
-    KM_TRY(launch_count_stats(h->rr_count, h->rr_stats, h->stop, s), KMEANS_ERROR_CLOSEST_CENTERS);
+    KM_TRY(launch_count_stats(h->rr_count, tc ? 1 : 0, h->rr_stats, h->stop, s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
   }
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
   // cluster centers + compactness (kmeans.cpp:1018-1104)

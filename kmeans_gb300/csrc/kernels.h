@@ -16,6 +16,13 @@ struct AssignArgs {
   const float* cmax;      // device scalar: upper bound of max ||c_j|| over usable centers
   const float* cinit;     // [round_up(k,128)] accumulator start -||c_j||^2/2 (BF16 tier)
   float* dump;            // diagnostic (nullable): raw accumulators [n][round_up(k,128)]
+  // BF16 tiers only:
+  const int* n_dev;       // nullable: rows actually present = min(*n_dev, n) (device count)
+  long long row0;         // first row of this batch (rows row0 .. row0 + present - 1)
+  float* thr_out;         // nullable: for every flagged point, best key - 2E (candidate floor)
+  const float* thr_in;    // candidate mode: per-row floor; keys >= floor are recorded in cand
+  int* cand;              // candidate mode: [n][kMaxCand] center indices
+  int* cand_cnt;          // candidate mode: [n] count, -1 if more than kMaxCand
   int* labels;            // [n]
   int* rerank_list;       // [n]
   int* rerank_count;      // device scalar
@@ -66,9 +73,21 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, fl
                                 cudaStream_t s);
 // FP64 stage over list2 (one CTA per point), candidates bounded by hi2.
 cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s);
-// stats[0] += counts[0] (points re-ranked), stats[1] += counts[1] (points that needed FP64).
-cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, const int* stop,
-                               cudaStream_t s);
+// Candidate re-rank of the BF16 tiers: compact copy of the flagged rows, then FP64 resolution
+// of their recorded candidates (overflowing points are appended to `over`).
+cudaError_t launch_gather_flagged(const int* list, const int* count, long long max_list,
+                                  const void* Xb, const void* Xl, long long ldb, const float* thr,
+                                  void* XbC, void* XlC, float* thrC, const int* stop,
+                                  cudaStream_t s);
+cudaError_t launch_resolve_candidates(const int* list, const int* count, long long max_list,
+                                      const int* cand, const int* cand_cnt, const float* X,
+                                      long long ldx, const float* C, long long ldc, const float* cn,
+                                      int d, int* labels, int* over, int* over_count,
+                                      const int* stop, cudaStream_t s);
+// stats[0] += counts[0] (points flagged by the assignment), stats[1] += counts[full_idx]
+// (points that needed a full rescan of the centers).
+cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long long* stats,
+                               const int* stop, cudaStream_t s);
 
 // Center preparation: from the official centers C[k][ldc] write the operand copy Cop (NaN
 // rows -> 0), optional BF16 copy Cb[k][ldcb], cn (+inf for NaN rows) and atomically raise
@@ -136,6 +155,7 @@ cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* 
                               float* xdst, cudaStream_t s, const int* stop = nullptr);
 
 constexpr int kSumPiece = 128;
+constexpr int kMaxCand = 16;  // candidate centers recorded per flagged point
 
 // Message returned by kmgb_last_error() on the calling thread.
 void set_last_error(const char* msg);

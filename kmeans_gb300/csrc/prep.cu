@@ -62,35 +62,54 @@ __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, 
   }
 }
 
-// One warp per point: qn = ||x||^2 in FP64, xn = FP32 upper bound of ||x||.
+// One warp per point: qn = ||x||^2 in FP64, xn = FP32 upper bound of ||x||. Each lane sums its
+// squares as an error-free float-float value (exact products x*x = p + e by FMA, TwoSum
+// accumulation) on the FP32 pipe; the 32 lane sums are combined in FP64.
 __global__ void point_norms_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
                                    double* __restrict__ qn, float* __restrict__ xn) {
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
   const float* x = X + (size_t)warp * ldx;
-  double s = 0.0;
-  for (int t = lane; t < d; t += 32) s = fma((double)x[t], (double)x[t], s);
+  float hi = 0.0f, lo = 0.0f;
+  for (int t = lane; t < d; t += 32) {
+    const float v = __ldg(x + t);
+    const float p = __fmul_rn(v, v);
+    const float e = __fmaf_rn(v, v, -p);  // v*v - p exactly
+    const float s1 = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(s1, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s1, bp)), __fsub_rn(p, bp));
+    hi = s1;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+  }
+  double s = (double)hi + (double)lo;
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) {
     if (qn) qn[warp] = s;
-    if (xn) xn[warp] = __double2float_ru(sqrt(s) * (1.0 + 1e-12));
+    // the float-float sum is within ~2^-40 of ||x||^2; 1e-9 covers it
+    if (xn) xn[warp] = __double2float_ru(sqrt(s) * (1.0 + 1e-9));
   }
 }
 
+// One warp per row (grid-stride over rows): BF16 value plane and, when requested, the BF16
+// residual plane bf16(x - bf16(x)).
 __global__ void to_bf16_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
                                __nv_bfloat16* __restrict__ Xb, long long ldb, const int* stop,
                                __nv_bfloat16* __restrict__ Xl) {
   if (stopped(stop)) return;
-  const long long total = n * ldb;
-  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long r = e / ldb;
-    const int c = (int)(e - r * ldb);
-    const float v = c < d ? X[(size_t)r * ldx + c] : 0.0f;
-    const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-    Xb[e] = hi;
-    if (Xl) Xl[e] = __float2bfloat16_rn(v - __bfloat162float(hi));
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long r = w0; r < n; r += nw) {
+    const float* x = X + (size_t)r * ldx;
+    __nv_bfloat16* ob = Xb + (size_t)r * ldb;
+    __nv_bfloat16* ol = Xl ? Xl + (size_t)r * ldb : nullptr;
+    for (int c = lane; c < (int)ldb; c += 32) {
+      const float v = c < d ? __ldg(x + c) : 0.0f;
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      ob[c] = hi;
+      if (ol) ol[c] = __float2bfloat16_rn(v - __bfloat162float(hi));
+    }
   }
 }
 

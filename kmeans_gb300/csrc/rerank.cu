@@ -336,16 +336,196 @@ rerank_exact_kernel(RerankArgs a, const float* __restrict__ hi2) {
 }  // namespace
 
 namespace {
-__global__ void count_stats_kernel(const int* counts, unsigned long long* stats, const int* stop) {
+__global__ void count_stats_kernel(const int* counts, int full_idx, unsigned long long* stats,
+                                   const int* stop) {
   if (stopped(stop)) return;
   stats[0] += (unsigned long long)counts[0];
-  stats[1] += (unsigned long long)counts[1];
+  stats[1] += (unsigned long long)counts[full_idx];
+}
+
+// Copies the BF16 rows (and residual rows) of the flagged points into a compact buffer, row
+// `slot` for list[slot], with the point's candidate floor. One warp per row, 16-byte moves.
+__global__ void gather_flagged_kernel(const int* __restrict__ list, const int* __restrict__ count,
+                                      long long max_list, const uint4* __restrict__ Xb,
+                                      const uint4* __restrict__ Xl, long long row_vec,
+                                      const float* __restrict__ thr, uint4* __restrict__ XbC,
+                                      uint4* __restrict__ XlC, float* __restrict__ thrC,
+                                      const int* stop) {
+  if (stopped(stop)) return;
+  const long long cnt = min((long long)*(volatile const int*)count, max_list);
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long slot = w0; slot < cnt; slot += nw) {
+    const long long pt = list[slot];
+    for (long long v = lane; v < row_vec; v += 32) {
+      XbC[slot * row_vec + v] = Xb[pt * row_vec + v];
+      if (Xl) XlC[slot * row_vec + v] = Xl[pt * row_vec + v];
+    }
+    if (lane == 0) thrC[slot] = thr[pt];
+  }
+}
+
+// Error-free float-float helpers (FP32 pipe). two_sum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// ||x - c||^2 as a float-float (hi, lo), summed over the warp (every lane ends with the total).
+// Lane l takes dimensions l, l+32, ... For each: u = x - c is split exactly into uh + ul
+// (two_sum), uh^2 = p + e exactly (FMA), and the remaining 2*uh*ul + ul^2 + e is added with one
+// rounding; hi collects the p's by two_sum, lo the rest.
+__device__ __forceinline__ void ff_dist(const float* __restrict__ x, const float* __restrict__ c,
+                                        int d, int lane, float& hi, float& lo) {
+  hi = 0.0f;
+  lo = 0.0f;
+  for (int t = lane; t < d; t += 32) {
+    float uh, ul;
+    two_sum(__ldg(x + t), -__ldg(c + t), uh, ul);
+    const float p = __fmul_rn(uh, uh);
+    const float e = __fmaf_rn(uh, uh, -p);
+    const float r = __fmaf_rn(ul, ul, __fmaf_rn(__fadd_rn(uh, uh), ul, e));
+    float s, err;
+    two_sum(hi, p, s, err);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, r));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s, err;
+    two_sum(hi, oh, s, err);
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(ol, err));
+  }
+}
+
+// Resolves every flagged point from its recorded candidates. The candidate set holds every center
+// whose FP64 distance can be the minimum; the label is the oracle's: smallest FP64 distance
+// (sequential fma over the dimensions), lowest index on ties.
+//
+// Fast path (FP32 pipe, whole warp per candidate): the float-float distance v of each candidate
+// is within rel*v + abs of the exact distance, and the oracle's FP64 value is within
+// (d+2)*2^-52 relative of it. Per lane (m = ceil(d/32) terms) the lo accumulator's roundings are
+// bounded by (m+1)^2 * 2^-47 relative, the 2*uh*ul + ul^2 + e terms by 2^-46, the five reduction
+// levels by 5 * (m+6) * 2^-47; rel takes 8x that sum. abs covers products that reach the
+// subnormal range. If the best candidate beats the runner-up by more than both tolerances, it is
+// the oracle's arg-min. Otherwise (near ties, duplicate centers, non-finite values) the point's
+// candidates are evaluated exactly as the oracle does, one lane per candidate, in FP64.
+// Points with more candidates than recorded (or none) go to `over` for the full re-rank.
+__global__ void resolve_candidates_kernel(const int* __restrict__ list, const int* __restrict__ count,
+                                          long long max_list, const int* __restrict__ cand,
+                                          const int* __restrict__ cand_cnt,
+                                          const float* __restrict__ X, long long ldx,
+                                          const float* __restrict__ C, long long ldc,
+                                          const float* __restrict__ cn, int d,
+                                          int* __restrict__ labels, int* __restrict__ over,
+                                          int* __restrict__ over_count, const int* stop) {
+  if (stopped(stop)) return;
+  const long long cnt = min((long long)*(volatile const int*)count, max_list);
+  const int lane = threadIdx.x & 31;
+  const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const double m = (double)((d + 31) / 32);
+  const double rel = 8.0 * ((m + 1.0) * (m + 1.0) + 2.0 + 5.0 * (m + 6.0)) * 0x1p-47 +
+                     (double)(d + 2) * 0x1p-52;
+  const double abs_tol = (double)(d + 32) * 0x1p-118;
+  for (long long slot = w0; slot < cnt; slot += nw) {
+    const int pt = list[slot];
+    const int nc = cand_cnt[slot];
+    if (nc <= 0) {
+      if (lane == 0) over[atomicAdd(over_count, 1)] = pt;
+      continue;
+    }
+    const float* x = X + (size_t)pt * ldx;
+    // fast path: candidates in increasing index order, strict < keeps the lowest index
+    double v1 = INFINITY, v2 = INFINITY;
+    int i1 = -1;
+    bool finite = true;
+    for (int q = 0; q < nc; ++q) {
+      const int j = cand[slot * kMaxCand + q];
+      if (!(cn[j] < INFINITY)) continue;  // unusable center
+      float hi, lo;
+      ff_dist(x, C + (size_t)j * ldc, d, lane, hi, lo);
+      const double v = (double)hi + (double)lo;
+      if (!(v < 1.0e300)) finite = false;  // overflow, inf or NaN on the FP32 pipe
+      if (v < v1) {
+        v2 = v1;
+        v1 = v;
+        i1 = j;
+      } else if (v < v2) {
+        v2 = v;
+      }
+    }
+    if (i1 < 0) {  // no usable candidate
+      if (lane == 0) over[atomicAdd(over_count, 1)] = pt;
+      continue;
+    }
+    if (finite && (v2 - v1 > (v1 + v2) * rel + 2.0 * abs_tol)) {
+      if (lane == 0) labels[pt] = i1;
+      continue;
+    }
+    // exact path: the oracle's sequential FP64 evaluation, one lane per candidate
+    double best = INFINITY;
+    int bidx = -1;
+    if (lane < nc) {
+      const int j = cand[slot * kMaxCand + lane];
+      if (cn[j] < INFINITY) {
+        const float* c = C + (size_t)j * ldc;
+        double s = 0.0;
+        for (int t = 0; t < d; ++t) {
+          const double u = (double)__ldg(x + t) - (double)__ldg(c + t);
+          s = fma(u, u, s);
+        }
+        if (s < INFINITY) {  // the oracle never takes a NaN or infinite distance
+          best = s;
+          bidx = j;
+        }
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+      const bool take = (ob < best) || (ob == best && (unsigned)oi < (unsigned)bidx);
+      best = take ? ob : best;
+      bidx = take ? oi : bidx;
+    }
+    if (lane == 0) {
+      if (bidx < 0) over[atomicAdd(over_count, 1)] = pt;
+      else labels[pt] = bidx;
+    }
+  }
 }
 }  // namespace
 
-cudaError_t launch_count_stats(const int* counts, unsigned long long* stats, const int* stop,
-                               cudaStream_t s) {
-  count_stats_kernel<<<1, 1, 0, s>>>(counts, stats, stop);
+cudaError_t launch_gather_flagged(const int* list, const int* count, long long max_list,
+                                  const void* Xb, const void* Xl, long long ldb, const float* thr,
+                                  void* XbC, void* XlC, float* thrC, const int* stop,
+                                  cudaStream_t s) {
+  if ((ldb * 2) % 16) return cudaErrorInvalidValue;
+  gather_flagged_kernel<<<152 * 8, 256, 0, s>>>(
+      list, count, max_list, reinterpret_cast<const uint4*>(Xb), reinterpret_cast<const uint4*>(Xl),
+      ldb * 2 / 16, thr, reinterpret_cast<uint4*>(XbC), reinterpret_cast<uint4*>(XlC), thrC, stop);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_resolve_candidates(const int* list, const int* count, long long max_list,
+                                      const int* cand, const int* cand_cnt, const float* X,
+                                      long long ldx, const float* C, long long ldc, const float* cn,
+                                      int d, int* labels, int* over, int* over_count,
+                                      const int* stop, cudaStream_t s) {
+  resolve_candidates_kernel<<<152 * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt, X, ldx,
+                                                    C, ldc, cn, d, labels, over, over_count, stop);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long long* stats,
+                               const int* stop, cudaStream_t s) {
+  count_stats_kernel<<<1, 1, 0, s>>>(counts, full_idx, stats, stop);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -57,6 +57,27 @@ def test_near_ties_are_resolved_exactly(km, orc, torch_cuda, tier):
     assert res.reranked > 0
 
 
+@pytest.mark.parametrize("tier", TIERS)
+def test_duplicate_centers_take_the_lowest_index(km, orc, torch_cuda, tier):
+    # identical centers give identical FP64 distances: the label is the lowest index. Center 2
+    # has one copy (the candidate resolver's exact path), center 5 has 19 copies (more than the
+    # 16 recorded candidates: the full rescan).
+    rng = np.random.default_rng(23)
+    d, k = 40, 48
+    Cn = rng.uniform(-4, 4, size=(k, d)).astype(np.float32)
+    Cn[9] = Cn[2]
+    Cn[20:39] = Cn[5]
+    X = np.concatenate([Cn[rng.integers(0, k, 3000)] +
+                        rng.normal(0, 0.3, size=(3000, d)).astype(np.float32),
+                        Cn[[2, 5, 9, 25]]]).astype(np.float32)
+    res = km.lloyd(X, k, init=Cn, max_iters=1, assign_tier=tier)
+    ref = orc.lloyd(X, Cn, 1)
+    check_same(res, ref)
+    assert not np.isin(res.labels, [9] + list(range(20, 39))).any()
+    if tier != 0:
+        assert res.reranked_fp64 > 0  # the 19-copy points took the full rescan
+
+
 def test_reference_init_compute_kmeans_f(km, orc, torch_cuda):
     X, _, _ = mixture_numpy(50_000, 24, 40, seed=7)
     m, n, k = X.shape[0], X.shape[1], 40
