@@ -38,8 +38,9 @@ constexpr uint32_t KB_BYTES = BM * BK * 2;  // 16 KB: one tile k-block == one C 
 constexpr int MAX_STAGES = 8;
 constexpr int MAX_D = 256;
 constexpr uint32_t TMEM_COLS = 512;
-constexpr size_t SMEM_CAP = 227 * 1024;
-constexpr float kUnusable = -3.0e38f;      // accumulator start of padding / unusable centers  // upper bound; the device's opt-in limit is queried
+constexpr size_t SMEM_CAP = 227 * 1024;  // upper bound; the device's opt-in limit is queried
+constexpr float kUnusable = -3.0e38f;    // start value of padding / unusable centers
+static_assert(BN / 32 >= 2, "the epilogue releases a buffer while its last block is in flight");
 
 // UMMA instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, N>>3, M>>4.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -123,16 +124,18 @@ __device__ __forceinline__ float bound_acc(float xn, float cm, int d, int planes
   // operand error: plain (2ub + ub^2) |x||c|; split x = xh + xl + ex, c = ch + cl + ec with
   // |xl| <= ub|x|, |ex| <= ub^2|x|: dropping xl.cl and the residues leaves <= 3.03 ub^2 |x||c|
   const float op = planes > 1 ? 3.03f * ub * ub : 2.0f * ub + ub * ub;
-  // FP32 accumulation in TMEM: at most one rounding per 16-product MMA step plus the start
-  // value, (terms/16 + 2) 2^-21 relative to |start| + sum |products|. The measured worst case
-  // on GB300 is >= 6x below this (tests/test_gpu_tensor_numerics.py enforces >= 4x).
+  // FP32 accumulation in TMEM (from zero): at most one rounding per 16-product MMA step,
+  // modelled with margin as (terms/16 + 2) 2^-21 relative to |start| + sum |products|. The
+  // measured worst case on GB300 is >= 6x below this (tests/test_gpu_tensor_numerics.py
+  // enforces >= 4x on the keys, start value included).
   const int terms = planes > 1 ? 3 * d : d;
   const float gacc = (float)(terms / 16 + 2) * 4.76837158e-7f;
   const float pack = 3.81469727e-6f;        // 2^-18: 5 column bits in the mantissa
   const float cc = 0.5f * cm * cm;
   const float xc = xn * cm * 1.01f;
   const float s64 = (float)(d + 2) * 1.2e-16f * (xn + cm) * (xn + cm);
-  const float e = 0.5f * u * cm * cm + op * xc + (gacc + pack) * (cc + xc) + s64;
+  // the start value -||c||^2/2 is added to the accumulator with one more FP32 rounding
+  const float e = 0.5f * u * cm * cm + op * xc + (gacc + pack + u) * (cc + xc) + s64;
   return e * 1.02f + 1e-30f;
 }
 
@@ -157,6 +160,11 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nkb = (p.d + BK - 1) / BK;
   const int nchunks = (p.k + BN - 1) / BN;
+  // Each CTA visits the center chunks in its own rotated order, so that at any moment the CTAs
+  // stream different chunks of C from L2 (all CTAs requesting the same lines at once queues
+  // the loads on the same L2 slices and starves the C ring).
+  const int rot = (int)(blockIdx.x % (unsigned)nchunks);
+  auto chunk_of = [&](int c) { return c + rot < nchunks ? c + rot : c + rot - nchunks; };
   // rows of this launch: [row0, row0 + n_rows); a device count bounds them in candidate mode
   long long n_rows = p.n;
   if (p.n_dev) {
@@ -246,7 +254,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             mbar_arrive_expect_tx(cb, stage_bytes);
             for (int pl = 0; pl < planes; ++pl)
               tma_load_2d(smem_u32(cs + (size_t)stage * stage_bytes + pl * KB_BYTES),
-                          pl ? &tmCl : &tmC, cb, kb * BK, c * BN);
+                          pl ? &tmCl : &tmC, cb, kb * BK, chunk_of(c) * BN);
           }
         }
       }
@@ -292,7 +300,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
                 const uint32_t bbase = term == 1 ? cbase + KB_BYTES : cbase;
 #pragma unroll
                 for (int k16 = 0; k16 < BK / 16; ++k16)
-                  umma_bf16(dcol, sdesc_sw128(abase + k16 * 32), sdesc_sw128(bbase + k16 * 32), 1u);
+                  umma_bf16(dcol, sdesc_sw128(abase + k16 * 32), sdesc_sw128(bbase + k16 * 32),
+                            (kb | term | k16) ? 1u : 0u);  // the chunk's first product starts at 0
               }
             }
             umma_commit(smem_u32(&bars.c_empty[stage]));
@@ -313,36 +322,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16);
     const float cm = p.certify ? __ldg(p.cmax) : 0.0f;
 
-    // pre-load accumulator buffer (g & 1) with the chunk's accumulator start values
-    // (-||c||^2/2, or a huge negative number for padding / unusable centers; prepared once per
-    // iteration in p.cinit, padded to whole chunks)
-    auto init_buf = [&](long long g) {
-      const int c = (int)(g % nchunks);
-      const uint32_t base = lane_addr + (uint32_t)((g & 1) * (TILES * BN) + t * BN);
-      const float4* src = reinterpret_cast<const float4*>(p.cinit + (size_t)c * BN);
-#pragma unroll
-      for (int cb = 0; cb < BN / 32; ++cb) {
-        uint32_t v[32];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const float4 f = __ldg(src + cb * 8 + q);
-          v[4 * q + 0] = __float_as_uint(f.x);
-          v[4 * q + 1] = __float_as_uint(f.y);
-          v[4 * q + 2] = __float_as_uint(f.z);
-          v[4 * q + 3] = __float_as_uint(f.w);
-        }
-        tmem_st32(base + cb * 32, v);
-      }
-      tmem_st_wait();
-    };
-
     bool alive = true;
-    for (long long g0 = 0; g0 < 2 && g0 < total_chunks; ++g0) {
-      init_buf(g0);
-      tc_fence_before();
-      __syncwarp();
+    for (long long g0 = 0; g0 < 2 && g0 < total_chunks; ++g0)  // both buffers start free
       if (lane == 0) mbar_arrive(smem_u32(&bars.acc_empty[g0 & 1]));
-    }
     long long g = 0;
     for (long long u = blockIdx.x; u < n_units && alive; u += gridDim.x) {
       float b1 = -INFINITY, b2 = -INFINITY;
@@ -371,10 +353,32 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           uint32_t (&cur)[32] = (cb & 1) ? rb : ra;
           uint32_t (&nxt)[32] = (cb & 1) ? ra : rb;
           if (cb + 1 < BN / 32) tmem_ld32(base + (cb + 1) * 32, nxt);
-          if (p.dump) {  // diagnostic: raw accumulators of this point
+          // key = x.c - ||c||^2/2: the accumulator plus the column's start value (FMA pipe);
+          // padding and unusable centers carry a huge negative start value
+          {
+            const float4* hs =
+                reinterpret_cast<const float4*>(p.cinit + (size_t)chunk_of(c) * BN + cb * 32);
+#pragma unroll
+            for (int j4 = 0; j4 < 8; ++j4) {
+              const float4 h = __ldg(hs + j4);
+              cur[4 * j4 + 0] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 0]), h.x));
+              cur[4 * j4 + 1] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 1]), h.y));
+              cur[4 * j4 + 2] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 2]), h.z));
+              cur[4 * j4 + 3] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 3]), h.w));
+            }
+          }
+          if (cb + 2 == BN / 32) {
+            // the last block's load is in flight: wait for it and hand the buffer back to the
+            // MMA issuer before folding the last two blocks
+            tmem_ld_wait();
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&bars.acc_empty[b]));
+          }
+          if (p.dump) {  // diagnostic: keys of this point before the column bits are packed
             const long long pt = u * UNIT + t * BM + q * 32 + lane;
             if (pt < n_rows) {
-              float* dst = p.dump + (size_t)pt * (size_t)nchunks * BN + (size_t)c * BN + cb * 32;
+              float* dst = p.dump + (size_t)pt * (size_t)nchunks * BN + (size_t)chunk_of(c) * BN + cb * 32;
 #pragma unroll
               for (int j = 0; j < 32; ++j) dst[j] = __uint_as_float(cur[j]);
             }
@@ -386,11 +390,11 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               const float key = __uint_as_float((cur[j] & ~0x1Fu) | (uint32_t)j);
               if (key >= floor_key) {
                 if (ncand < kMaxCand)
-                  p.cand[(size_t)(p.row0 + prow) * kMaxCand + ncand] = c * BN + cb * 32 + j;
+                  p.cand[(size_t)(p.row0 + prow) * kMaxCand + ncand] = chunk_of(c) * BN + cb * 32 + j;
                 ++ncand;
               }
             }
-            if (cb + 1 < BN / 32) tmem_ld_wait();
+            if (cb + 1 < BN / 32 && cb + 2 != BN / 32) tmem_ld_wait();
             continue;
           }
           const float blk_before = b1;
@@ -403,13 +407,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             b2 = fmax3(b2, lo, fminf(b1, hi));
             b1 = fmaxf(b1, hi);
           }
-          if (b1 != blk_before) bblk = c * (BN / 32) + cb;  // 32-column block of the best
-          if (cb + 1 < BN / 32) tmem_ld_wait();
+          if (b1 != blk_before) bblk = chunk_of(c) * (BN / 32) + cb;  // 32-column block of the best
+          if (cb + 1 < BN / 32 && cb + 2 != BN / 32) tmem_ld_wait();
         }
-        if (g + 2 < total_chunks) init_buf(g + 2);
-        tc_fence_before();
-        __syncwarp();
-        if (lane == 0) mbar_arrive(smem_u32(&bars.acc_empty[b]));
       }
       if (!alive) break;
       if (cand_mode) {

@@ -257,6 +257,79 @@ __global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
   }
 }
 
+// FP32 rows whose width and stride are multiples of 4 (16-byte aligned): one warp per piece, a
+// lane owns 4 consecutive dimensions (one float4 per row, so a warp instruction reads a whole
+// 128-dimension row), the piece's point ids are read 32 at a time and broadcast by shuffles, and
+// 8 rows are in flight per warp. Every dimension still adds the piece's points in sorted order
+// with the same float-float TwoSum as the generic kernel: the sums are identical. The piece's
+// sum of ||x||^2 (SSE only) is added as a tree over 32 rows at a time.
+__global__ void piece_sums_vec4_kernel(const float* __restrict__ X, long long ldx,
+                                       const double* __restrict__ qn, const int* __restrict__ sorted,
+                                       const int* __restrict__ label_off, const int* __restrict__ pstart,
+                                       int k, int d, double* __restrict__ part,
+                                       double* __restrict__ partq, const int* stop) {
+  if (stopped(stop)) return;
+  const int ptot = pstart[k];
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long p = gw; p < ptot; p += nw) {
+    const int j = find_label(pstart, k, (int)p);
+    const int q = (int)p - pstart[j];
+    const int b = label_off[j] + q * kSumPiece;
+    const int e = min(b + kSumPiece, label_off[j + 1]);
+    for (int d0 = 0; d0 < d; d0 += 128) {
+      const int c = d0 + 4 * lane;
+      const bool on = c < d;
+      PieceAcc<float> a0, a1, a2, a3;
+      double qs = 0.0;
+      for (int t0 = b; t0 < e; t0 += 32) {
+        const int nt = min(32, e - t0);
+        const int my_i = lane < nt ? __ldg(sorted + t0 + lane) : 0;
+        if (qn && d0 == 0) {  // ||x||^2 of these 32 rows: one load per lane, tree sum (FP64)
+          double qv = lane < nt ? __ldg(qn + my_i) : 0.0;
+          for (int o = 16; o > 0; o >>= 1) qv += __shfl_xor_sync(0xffffffffu, qv, o);
+          qs += qv;
+        }
+        int tt = 0;
+        for (; tt + 8 <= nt; tt += 8) {
+          float4 v[8];
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            const int i = __shfl_sync(0xffffffffu, my_i, tt + r);
+            v[r] = on ? __ldg(reinterpret_cast<const float4*>(X + (size_t)i * ldx + c))
+                      : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+#pragma unroll
+          for (int r = 0; r < 8; ++r) {
+            a0.add(v[r].x);
+            a1.add(v[r].y);
+            a2.add(v[r].z);
+            a3.add(v[r].w);
+          }
+        }
+        for (; tt < nt; ++tt) {
+          const int i = __shfl_sync(0xffffffffu, my_i, tt);
+          const float4 v = on ? __ldg(reinterpret_cast<const float4*>(X + (size_t)i * ldx + c))
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+          a0.add(v.x);
+          a1.add(v.y);
+          a2.add(v.z);
+          a3.add(v.w);
+        }
+      }
+      if (on) {
+        double* o = part + (size_t)p * d + c;
+        o[0] = a0.value();
+        o[1] = a1.value();
+        o[2] = a2.value();
+        o[3] = a3.value();
+      }
+      if (d0 == 0 && lane == 0 && partq) partq[p] = qs;
+    }
+  }
+}
+
 // One warp per center.
 __global__ void finalize_kernel(const double* __restrict__ part, const double* __restrict__ partq,
                                 const int* __restrict__ label_off, const int* __restrict__ pstart,
@@ -389,8 +462,13 @@ cudaError_t launch_update(const float* X, const double* qn, const int* labels, f
   KMGB_CUDA_TRY(sort_by_label(labels, w, s));
   const long long max_pieces = w.max_pieces;
   long long warps = max_pieces < 152LL * 64 ? max_pieces : 152LL * 64;
-  piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-      X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq, w.stop); kmgb::count_launches(1);
+  if (w.ldx % 4 == 0 && w.d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
+    piece_sums_vec4_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq, w.stop);
+  else
+    piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq, w.stop);
+  kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   finalize_kernel<<<(unsigned)(((long long)k * 32 + 255) / 256), 256, 0, s>>>(
       w.part, qn ? w.partq : nullptr, w.label_off, w.piece_cnt, k, w.d, C, ldc, empty_policy,
