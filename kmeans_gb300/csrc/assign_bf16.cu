@@ -2,19 +2,29 @@
 //
 // Replaces the x.c contraction of the reference's assignment (main/cuda/ClosestCenters.cu:46-83,
 // cuBLAS option kmeans.cpp:918-955) with 5th-generation tensor cores; the N x K matrix is never
-// written. Per CTA (persistent, one per SM, 320 threads):
-//   warp 0      TMA producer: the unit's 256 points (two 128-row BF16 tiles, all k-blocks) once,
-//               then 128-center x 64-dim BF16 stages of C through a shared-memory ring
-//               (128-byte swizzle, mbarrier complete_tx);
-//   warp 1      TMEM owner + MMA issuer: tcgen05.mma.cta_group::1.kind::f16, M=128 N=128 K=16,
-//               one accumulator per point tile per chunk, two chunk buffers (4 x 128 of the 512
-//               TMEM columns) so the epilogue of chunk g overlaps the MMAs of chunk g+1;
-//   warps 2-9   epilogue: each thread owns one point (its TMEM lane) of one tile. Before a chunk
-//               is multiplied its accumulator is pre-loaded (tcgen05.st) with -||c_j||^2/2, so
-//               the MMA yields acc_j = x.c_j - ||c_j||^2/2 and arg-min distance = arg-max acc.
-//               The epilogue reads 32 columns at a time (tcgen05.ld), packs the column within
-//               the 32-column block into the 5 low mantissa bits and keeps the two largest keys
-//               per point with 3.5 ALU ops per element; the block of the best key is remembered.
+// written. The grid is persistent: one CTA per SM, CTAs paired in clusters of two that share one
+// tensor-core instruction stream (tcgen05 cta_group::2). A pair works on units of 256 points and
+// chunks of 256 centers:
+//   * CTA rank r holds points r*128 .. r*128+127 of the unit (the A rows of its half of the
+//     M=256 MMA) and centers r*128 .. r*128+127 of the chunk (its half of N=256), both in shared
+//     memory, so each SM streams only half of every center chunk and every MMA reads 8 KB of
+//     operands per SM per 128 cycles; measured on GB300, M=256 N=256 K=16 pair MMAs run at the
+//     full BF16 rate while the 128x128 single-CTA form is held to ~66% by its per-instruction cost.
+//   * warp 0 (both CTAs) TMA producer: the unit's points (double-buffered) and 64-dim k-blocks of
+//     the centers (both planes per stage) through a ring; every load completes on the leader's
+//     mbarrier (cta_group::2),
+//     the leader's producer posts the expected bytes of both CTAs.
+//   * warp 1 of the leader (rank 0) issues tcgen05.mma.cta_group::2.kind::f16 M=256 N=256 K=16
+//     into TMEM (two 256-column accumulator buffers: the epilogue of chunk g overlaps the MMAs of
+//     chunk g+1) and multicasts its commits (stage free, accumulator ready, points free) to both
+//     CTAs. Warp 1 of both CTAs allocates the 512 TMEM columns collectively.
+//   * warps 2-9 (both CTAs) epilogue: two warps per TMEM lane quadrant, each owning 32 points and
+//     128 of the chunk's 256 columns. A thread reads 32 columns at a time (tcgen05.ld), adds
+//     -||c_j||^2/2 (FP32, FMA pipe) so that arg-min distance = arg-max key, packs the column
+//     within the 32-column block into the 5 low mantissa bits and keeps the two largest keys with
+//     3.5 ALU ops per element. Accumulator buffers are handed back to the leader by remote
+//     mbarrier arrivals. At the end of a unit the two column halves of a point are merged through
+//     shared memory (bounded mbarrier handshake).
 // A point is certified when best - second > 2E, E the rigorous bound of the BF16 evaluation
 // (operand rounding, FP32 accumulation, norm rounding, key packing, FP64 reference error);
 // other points go to the exact re-rank list, so labels equal the FP64 arg-min.
@@ -27,24 +37,27 @@
 namespace kmgb {
 namespace {
 
-constexpr int BM = 128;                  // rows per M tile
-constexpr int TILES = 2;                 // M tiles per unit
-constexpr int UNIT = BM * TILES;         // points per unit
-constexpr int BN = 128;                  // centers per chunk (UMMA N)
+constexpr int BM = 128;                  // points per CTA per unit (A rows of one CTA)
+constexpr int UNIT = 2 * BM;             // points per pair unit (MMA M)
+constexpr int BN = 256;                  // centers per chunk (MMA N)
+constexpr int BNH = BN / 2;              // centers per CTA per chunk
 constexpr int BK = 64;                   // BF16 per k-block (one 128-byte swizzle row)
 constexpr int NUM_EPI_WARPS = 8;
 constexpr int NTHREADS = 64 + NUM_EPI_WARPS * 32;
-constexpr uint32_t KB_BYTES = BM * BK * 2;  // 16 KB: one tile k-block == one C stage
+constexpr uint32_t XKB_BYTES = BM * BK * 2;   // 16 KB: one k-block of one plane of the points
+constexpr uint32_t CKB_BYTES = BNH * BK * 2;  // 16 KB: one k-block of one plane of the centers
 constexpr int MAX_STAGES = 8;
 constexpr int MAX_D = 256;
-constexpr uint32_t TMEM_COLS = 512;
-constexpr size_t SMEM_CAP = 227 * 1024;  // upper bound; the device's opt-in limit is queried
-constexpr float kUnusable = -3.0e38f;    // start value of padding / unusable centers
-static_assert(BN / 32 >= 2, "the epilogue releases a buffer while its last block is in flight");
+constexpr uint32_t TMEM_COLS = 512;           // two 256-column accumulator buffers
+constexpr size_t SMEM_CAP = 227 * 1024;       // upper bound; the device's opt-in limit is queried
+constexpr float kUnusable = -3.0e38f;         // start value of padding / unusable centers
+constexpr int COLS_PER_WARP = BN / 2;         // epilogue: two warps per lane quadrant
+static_assert(2 * BN <= (int)TMEM_COLS, "two accumulator buffers");
+static_assert(kCenterPad % BN == 0, "start values are padded to whole chunks");
 
 // UMMA instruction descriptor, kind::f16: D=F32, A=B=BF16, both K-major, N>>3, M>>4.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+                           ((uint32_t)(UNIT >> 4) << 24);
 
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
@@ -62,22 +75,6 @@ __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
-      : "memory");
-}
-
-__device__ __forceinline__ void umma_commit(uint32_t bar) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
-      : "memory");
-}
-
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
@@ -91,24 +88,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
       : "r"(taddr));
 }
 
-__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, "
-      "%11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, "
-      "%28, %29, %30, %31, %32};" ::"r"(taddr),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
-      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
-      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
-      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
-      "r"(r[29]), "r"(r[30]), "r"(r[31])
-      : "memory");
-}
-
 __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_st_wait() {
-  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
@@ -139,31 +120,129 @@ __device__ __forceinline__ float bound_acc(float xn, float cm, int d, int planes
   return e * 1.02f + 1e-30f;
 }
 
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// Address of the same shared-memory object in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::
+                   : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
+               : "memory");
+}
+
+// 2-D TMA load into this CTA's shared memory, completing on an mbarrier of either CTA of the pair.
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map,
+                                                 uint32_t bar_cluster, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes.cta_group::2"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cluster), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// Pull a 2-D box of a tensor into L2 ahead of its TMA load.
+__device__ __forceinline__ void tma_prefetch_2d(const CUtensorMap* map, int c0, int c1) {
+  asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(c0), "r"(c1)
+               : "memory");
+}
+
+// Pair MMA: D[tmem, both CTAs] (+)= A[smem, 128 rows per CTA] . B[smem, 128 rows per CTA]^T.
+__device__ __forceinline__ void umma_pair(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+
+// The same with the A operand kept in the tensor core's collector for the next MMA (fill) and
+// taken from it (lastuse): one shared-memory read of A serves two products.
+__device__ __forceinline__ void umma_pair_a_fill(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                                 uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16.collector::a::fill [%0], %1, %2, %3, p;\n\t}" ::"r"(
+          tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_pair_a_lastuse(uint32_t tmem_d, uint64_t adesc,
+                                                    uint64_t bdesc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, 1, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16.collector::a::lastuse [%0], %1, %2, %3, p;\n\t}" ::"r"(
+          tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(IDESC)
+      : "memory");
+}
+
+// Arrive on the mbarrier at this offset in both CTAs once all prior pair MMAs have completed.
+__device__ __forceinline__ void umma_commit_pair(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;" ::"r"(bar),
+      "h"((uint16_t)3)
+      : "memory");
+}
+
 struct Bars {
   uint64_t x_full[2], x_empty[2], done;
   uint64_t c_full[MAX_STAGES], c_empty[MAX_STAGES];
   uint64_t acc_full[2], acc_empty[2];
+  uint64_t merge_full[4], merge_empty[4];
+};
+
+// the column half handed from warp (q, 1) to warp (q, 0) at the end of a unit
+struct MergeSlot {
+  float b1[4][32], b2[4][32];
+  int bblk[4][32], ncand[4][32];
 };
 
 __global__ void __launch_bounds__(NTHREADS, 1)
 assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmXl,
                    const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmCl,
                    AssignArgs p, int stages, int xbufs, int planes) {
-  if (stopped(p.stop)) return;
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                             ~static_cast<uintptr_t>(1023));
+  extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) Bars bars;
+  __shared__ MergeSlot merge;
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t rank = cluster_rank();
+  // the TMA boxes use the 128-byte swizzle: the dynamic area must start on a 1 KB boundary. The
+  // check is uniform over the grid, so every CTA of every pair returns together.
+  if ((smem_u32(smem) & 1023u) != 0) {
+    if (tid == 0 && blockIdx.x == 0) set_error(p.err, KMGB_DEV_BAD_SHAPE);
+    return;
+  }
+  const bool stop_now = stopped(p.stop);  // uniform: every CTA of the grid sees the same flag
+  if (stop_now) return;
   const int nkb = (p.d + BK - 1) / BK;
   const int nchunks = (p.k + BN - 1) / BN;
-  // Each CTA visits the center chunks in its own rotated order, so that at any moment the CTAs
-  // stream different chunks of C from L2 (all CTAs requesting the same lines at once queues
-  // the loads on the same L2 slices and starves the C ring).
-  const int rot = (int)(blockIdx.x % (unsigned)nchunks);
+  const long long pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
+  // Each pair visits the center chunks in its own rotated order, so that at any moment the pairs
+  // stream different chunks of C from L2.
+  const int rot = (int)(pair % nchunks);
   auto chunk_of = [&](int c) { return c + rot < nchunks ? c + rot : c + rot - nchunks; };
   // rows of this launch: [row0, row0 + n_rows); a device count bounds them in candidate mode
   long long n_rows = p.n;
@@ -174,14 +253,12 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const long long n_units = (n_rows + UNIT - 1) / UNIT;
   const bool cand_mode = p.thr_in != nullptr;
   long long my_units = 0;
-  if ((long long)blockIdx.x < n_units)
-    my_units = (n_units - 1 - blockIdx.x) / gridDim.x + 1;
+  if (pair < n_units) my_units = (n_units - 1 - pair) / npairs + 1;
   const long long total_chunks = my_units * nchunks;
-  // X buffer: [plane][tile][k-block] 16 KB boxes; C stage: [plane] 16 KB boxes of one
+  // points: [buffer][plane][k-block] 16 KB boxes; C stage: [plane] 16 KB boxes of one
   // (chunk, k-block). plane 0 = BF16 value, plane 1 = BF16 residual (split tier).
-  const size_t xbuf_bytes = (size_t)planes * TILES * nkb * KB_BYTES;
-  const uint32_t stage_bytes = (uint32_t)planes * KB_BYTES;
-  uint8_t* xs0 = smem;                       // X buffer b at xs0 + b * xbuf_bytes
+  const size_t xbuf_bytes = (size_t)planes * nkb * XKB_BYTES;
+  const uint32_t stage_bytes = (uint32_t)planes * CKB_BYTES;
   uint8_t* cs = smem + (size_t)xbufs * xbuf_bytes;
 
   if (tid == 0) {
@@ -189,15 +266,17 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     for (int b = 0; b < 2; ++b) {
       mbar_init(smem_u32(&bars.x_full[b]), 1);
       mbar_init(smem_u32(&bars.x_empty[b]), 1);
+      mbar_init(smem_u32(&bars.acc_full[b]), 1);
+      mbar_init(smem_u32(&bars.acc_empty[b]), 2 * NUM_EPI_WARPS);  // both CTAs' epilogue warps
     }
     mbar_init(smem_u32(&bars.done), 1);
     for (int s = 0; s < stages; ++s) {
       mbar_init(smem_u32(&bars.c_full[s]), 1);
       mbar_init(smem_u32(&bars.c_empty[s]), 1);
     }
-    for (int b = 0; b < 2; ++b) {
-      mbar_init(smem_u32(&bars.acc_full[b]), 1);
-      mbar_init(smem_u32(&bars.acc_empty[b]), NUM_EPI_WARPS);
+    for (int q = 0; q < 4; ++q) {
+      mbar_init(smem_u32(&bars.merge_full[q]), 32);
+      mbar_init(smem_u32(&bars.merge_empty[q]), 32);
     }
     fence_mbar_init();
     prefetch_tmap(&tmX);
@@ -207,41 +286,49 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       prefetch_tmap(&tmCl);
     }
   }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+  if (warp == 1) {  // both CTAs: one collective allocation of the pair's TMEM
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(&tmem_base_sh)),
                  "r"(TMEM_COLS)
                  : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
+  cluster_sync_all();  // the peer's barriers are initialised before any remote arrival
   tc_fence_after();
   const uint32_t tmem_base = tmem_base_sh;
 
   if (warp == 0) {
-    // ------------------------------ TMA producer ------------------------------
+    // ------------------------------ TMA producer (both CTAs) ------------------------------
     if (lane == 0 && total_chunks > 0) {
-      long long s = 0;
-      long long lu = 0;
+      long long s = 0, lu = 0;
       bool ok = true;
-      for (long long u = blockIdx.x; u < n_units && ok; u += gridDim.x, ++lu) {
-        // X buffer xi is used for the (use)-th time by this unit; wait until the MMAs of its
-        // previous user have completed
+      for (long long u = pair; u < n_units && ok; u += npairs, ++lu) {
         const int xi = (int)(lu % xbufs);
         const long long use = lu / xbufs;
+        // wait until the MMAs of the previous user of this buffer have completed
         if (use > 0 && !mbar_wait(smem_u32(&bars.x_empty[xi]), (uint32_t)((use - 1) & 1),
                                   &abort_flag, p.err, KMGB_DEV_TIMEOUT_EMPTY))
           break;
-        const uint32_t xb = smem_u32(&bars.x_full[xi]);
-        uint8_t* xs = xs0 + (size_t)xi * xbuf_bytes;
-        mbar_arrive_expect_tx(xb, (uint32_t)xbuf_bytes);
+        const uint32_t xb_local = smem_u32(&bars.x_full[xi]);
+        if (rank == 0) mbar_arrive_expect_tx(xb_local, (uint32_t)(2 * xbuf_bytes));
+        const uint32_t xb = map_to_rank(xb_local, 0);
+        uint8_t* xs = smem + (size_t)xi * xbuf_bytes;
+        const int xrow = (int)(p.row0 + u * UNIT + rank * BM);
         for (int pl = 0; pl < planes; ++pl)
-          for (int t = 0; t < TILES; ++t)
-            for (int kb = 0; kb < nkb; ++kb)
-              tma_load_2d(smem_u32(xs + (size_t)((pl * TILES + t) * nkb + kb) * KB_BYTES),
-                          pl ? &tmXl : &tmX, xb, kb * BK, (int)(p.row0 + u * UNIT + t * BM));
+          for (int kb = 0; kb < nkb; ++kb)
+            tma_load_2d_pair(smem_u32(xs + (size_t)(pl * nkb + kb) * XKB_BYTES), pl ? &tmXl : &tmX,
+                             xb, kb * BK, xrow);
+        // the next unit's points come from HBM: start them towards L2 now, so that their TMA
+        // load (queued behind the center stages) is an L2 hit
+        if (u + npairs < n_units) {
+          const int nrow = (int)(p.row0 + (u + npairs) * UNIT + rank * BM);
+          for (int pl = 0; pl < planes; ++pl)
+            for (int kb = 0; kb < nkb; ++kb) tma_prefetch_2d(pl ? &tmXl : &tmX, kb * BK, nrow);
+        }
         for (int c = 0; c < nchunks && ok; ++c) {
+          const int crow = chunk_of(c) * BN + (int)rank * BNH;
           for (int kb = 0; kb < nkb; ++kb, ++s) {
             const int stage = (int)(s % stages);
             if (s >= stages &&
@@ -250,28 +337,29 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               ok = false;
               break;
             }
-            const uint32_t cb = smem_u32(&bars.c_full[stage]);
-            mbar_arrive_expect_tx(cb, stage_bytes);
+            const uint32_t cb_local = smem_u32(&bars.c_full[stage]);
+            if (rank == 0) mbar_arrive_expect_tx(cb_local, 2 * stage_bytes);
+            const uint32_t cb = map_to_rank(cb_local, 0);
             for (int pl = 0; pl < planes; ++pl)
-              tma_load_2d(smem_u32(cs + (size_t)stage * stage_bytes + pl * KB_BYTES),
-                          pl ? &tmCl : &tmC, cb, kb * BK, chunk_of(c) * BN);
+              tma_load_2d_pair(smem_u32(cs + (size_t)stage * stage_bytes + pl * CKB_BYTES),
+                               pl ? &tmCl : &tmC, cb, kb * BK, crow);
           }
         }
       }
     }
   } else if (warp == 1) {
-    // ------------------------------ MMA issuer ------------------------------
-    if (lane == 0 && total_chunks > 0) {
+    // ------------------------------ MMA issuer (leader) ------------------------------
+    if (lane == 0 && rank == 0 && total_chunks > 0) {
       long long s = 0, g = 0, lu = 0;
       bool ok = true;
-      for (long long u = blockIdx.x; u < n_units && ok; u += gridDim.x, ++lu) {
+      for (long long u = pair; u < n_units && ok; u += npairs, ++lu) {
         const int xi = (int)(lu % xbufs);
         const long long use = lu / xbufs;
         if (!mbar_wait(smem_u32(&bars.x_full[xi]), (uint32_t)(use & 1), &abort_flag, p.err,
                        KMGB_DEV_TIMEOUT_FULL))
           break;
         tc_fence_after();
-        const uint8_t* xs = xs0 + (size_t)xi * xbuf_bytes;
+        const uint8_t* xs = smem + (size_t)xi * xbuf_bytes;
         for (int c = 0; c < nchunks && ok; ++c, ++g) {
           const int b = (int)(g & 1);
           if (!mbar_wait(smem_u32(&bars.acc_empty[b]), (uint32_t)((g >> 1) & 1), &abort_flag,
@@ -280,6 +368,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             break;
           }
           tc_fence_after();
+          const uint32_t dcol = tmem_base + (uint32_t)(b * BN);
           for (int kb = 0; kb < nkb; ++kb, ++s) {
             const int stage = (int)(s % stages);
             if (!mbar_wait(smem_u32(&bars.c_full[stage]), (uint32_t)((s / stages) & 1),
@@ -288,48 +377,52 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               break;
             }
             tc_fence_after();
-            const uint32_t cbase = smem_u32(cs + (size_t)stage * stage_bytes);
+            const uint32_t chi = smem_u32(cs + (size_t)stage * stage_bytes);
+            const uint32_t xhi = smem_u32(xs + (size_t)kb * XKB_BYTES);
 #pragma unroll
-            for (int t = 0; t < TILES; ++t) {
-              const uint32_t xhi = smem_u32(xs + (size_t)(t * nkb + kb) * KB_BYTES);
-              const uint32_t dcol = tmem_base + (uint32_t)(b * (TILES * BN) + t * BN);
-              // plain: x_hi.c_hi; split: + x_hi.c_lo + x_lo.c_hi (x_lo.c_lo is below the bound)
-              for (int term = 0; term < (planes > 1 ? 3 : 1); ++term) {
-                const uint32_t abase =
-                    term == 2 ? smem_u32(xs + (size_t)((TILES + t) * nkb + kb) * KB_BYTES) : xhi;
-                const uint32_t bbase = term == 1 ? cbase + KB_BYTES : cbase;
-#pragma unroll
-                for (int k16 = 0; k16 < BK / 16; ++k16)
-                  umma_bf16(dcol, sdesc_sw128(abase + k16 * 32), sdesc_sw128(bbase + k16 * 32),
-                            (kb | term | k16) ? 1u : 0u);  // the chunk's first product starts at 0
+            for (int k16 = 0; k16 < BK / 16; ++k16) {
+              const uint32_t acc = (kb | k16) ? 1u : 0u;  // the chunk's first product starts at 0
+              const uint64_t ahi = sdesc_sw128(xhi + k16 * 32);
+              const uint64_t bhi = sdesc_sw128(chi + k16 * 32);
+              if (planes == 1) {
+                umma_pair(dcol, ahi, bhi, acc);
+              } else {
+                // x_hi.c_hi, x_hi.c_lo (x_hi read once into the A collector), x_lo.c_hi;
+                // x_lo.c_lo is below the bound
+                umma_pair_a_fill(dcol, ahi, bhi, acc);
+                umma_pair_a_lastuse(dcol, ahi, sdesc_sw128(chi + CKB_BYTES + k16 * 32));
+                umma_pair(dcol, sdesc_sw128(xhi + (size_t)nkb * XKB_BYTES + k16 * 32), bhi, 1u);
               }
             }
-            umma_commit(smem_u32(&bars.c_empty[stage]));
+            umma_commit_pair(smem_u32(&bars.c_empty[stage]));
           }
-          if (ok) umma_commit(smem_u32(&bars.acc_full[b]));
+          if (ok) umma_commit_pair(smem_u32(&bars.acc_full[b]));
         }
-        if (ok) umma_commit(smem_u32(&bars.x_empty[xi]));
+        if (ok) umma_commit_pair(smem_u32(&bars.x_empty[xi]));
       }
-      // all MMAs issued by this thread have completed once `done` flips
-      umma_commit(smem_u32(&bars.done));
-      mbar_wait(smem_u32(&bars.done), 0u, &abort_flag, p.err, KMGB_DEV_TIMEOUT_ACC);
+      // both CTAs learn that every MMA issued here has completed once `done` flips
+      umma_commit_pair(smem_u32(&bars.done));
     }
+    if (lane == 0 && total_chunks > 0)
+      mbar_wait(smem_u32(&bars.done), 0u, &abort_flag, p.err, KMGB_DEV_TIMEOUT_ACC);
   } else {
-    // ------------------------------ epilogue ------------------------------
+    // ------------------------------ epilogue (both CTAs) ------------------------------
     const int e = warp - 2;
     const int q = warp & 3;       // TMEM lane quadrant this warp may access
-    const int t = e >> 2;         // point tile
+    const int h = e >> 2;         // column half of the chunk
     const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16);
     const float cm = p.certify ? __ldg(p.cmax) : 0.0f;
+    const uint32_t acc_empty_leader0 = map_to_rank(smem_u32(&bars.acc_empty[0]), 0);
+    const uint32_t acc_empty_leader1 = map_to_rank(smem_u32(&bars.acc_empty[1]), 0);
 
     bool alive = true;
     for (long long g0 = 0; g0 < 2 && g0 < total_chunks; ++g0)  // both buffers start free
-      if (lane == 0) mbar_arrive(smem_u32(&bars.acc_empty[g0 & 1]));
-    long long g = 0;
-    for (long long u = blockIdx.x; u < n_units && alive; u += gridDim.x) {
+      if (lane == 0) mbar_arrive_remote(g0 ? acc_empty_leader1 : acc_empty_leader0);
+    long long g = 0, lu = 0;
+    for (long long u = pair; u < n_units && alive; u += npairs, ++lu) {
       float b1 = -INFINITY, b2 = -INFINITY;
       int bblk = -1;  // global 32-column block holding the best key
-      const long long prow = u * UNIT + t * BM + q * 32 + lane;  // row within the launch
+      const long long prow = u * UNIT + rank * BM + q * 32 + lane;  // row within the launch
       float floor_key = INFINITY;  // candidate mode: record keys >= floor_key
       int ncand = 0;
       if (cand_mode && prow < n_rows) floor_key = __ldg(p.thr_in + p.row0 + prow);
@@ -342,80 +435,105 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           break;
         }
         tc_fence_after();
-        const uint32_t base = lane_addr + (uint32_t)(b * (TILES * BN) + t * BN);
-        // two 32-column register buffers: the load of block cb+1 is in flight while block cb
-        // is folded into (b1, b2)
-        uint32_t ra[32], rb[32];
-        tmem_ld32(base, ra);
-        tmem_ld_wait();
+        const int col0 = chunk_of(c) * BN + h * COLS_PER_WARP;  // first center of this warp
+        const uint32_t base = lane_addr + (uint32_t)(b * BN + h * COLS_PER_WARP);
+        // all of this warp's columns into registers at once, then the buffer goes straight back
+        // to the leader's MMA issuer and the folding below overlaps the next MMAs
+        uint32_t v[COLS_PER_WARP / 32][32];
 #pragma unroll
-        for (int cb = 0; cb < BN / 32; ++cb) {
-          uint32_t (&cur)[32] = (cb & 1) ? rb : ra;
-          uint32_t (&nxt)[32] = (cb & 1) ? ra : rb;
-          if (cb + 1 < BN / 32) tmem_ld32(base + (cb + 1) * 32, nxt);
+        for (int cb = 0; cb < COLS_PER_WARP / 32; ++cb) tmem_ld32(base + cb * 32, v[cb]);
+        tmem_ld_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive_remote(b ? acc_empty_leader1 : acc_empty_leader0);
+#pragma unroll
+        for (int cb = 0; cb < COLS_PER_WARP / 32; ++cb) {
+          uint32_t (&cur)[32] = v[cb];
           // key = x.c - ||c||^2/2: the accumulator plus the column's start value (FMA pipe);
           // padding and unusable centers carry a huge negative start value
           {
-            const float4* hs =
-                reinterpret_cast<const float4*>(p.cinit + (size_t)chunk_of(c) * BN + cb * 32);
+            const float4* hs = reinterpret_cast<const float4*>(p.cinit + (size_t)col0 + cb * 32);
 #pragma unroll
             for (int j4 = 0; j4 < 8; ++j4) {
-              const float4 h = __ldg(hs + j4);
-              cur[4 * j4 + 0] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 0]), h.x));
-              cur[4 * j4 + 1] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 1]), h.y));
-              cur[4 * j4 + 2] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 2]), h.z));
-              cur[4 * j4 + 3] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 3]), h.w));
+              const float4 hv = __ldg(hs + j4);
+              cur[4 * j4 + 0] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 0]), hv.x));
+              cur[4 * j4 + 1] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 1]), hv.y));
+              cur[4 * j4 + 2] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 2]), hv.z));
+              cur[4 * j4 + 3] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 3]), hv.w));
             }
           }
-          if (cb + 2 == BN / 32) {
-            // the last block's load is in flight: wait for it and hand the buffer back to the
-            // MMA issuer before folding the last two blocks
-            tmem_ld_wait();
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&bars.acc_empty[b]));
-          }
           if (p.dump) {  // diagnostic: keys of this point before the column bits are packed
-            const long long pt = u * UNIT + t * BM + q * 32 + lane;
-            if (pt < n_rows) {
-              float* dst = p.dump + (size_t)pt * (size_t)nchunks * BN + (size_t)chunk_of(c) * BN + cb * 32;
+            if (prow < n_rows) {
+              float* dst = p.dump + (size_t)prow * (size_t)((p.k + kCenterPad - 1) / kCenterPad * kCenterPad) + col0 + cb * 32;
 #pragma unroll
               for (int j = 0; j < 32; ++j) dst[j] = __uint_as_float(cur[j]);
             }
           }
           if (cand_mode) {
-            // second pass over flagged points: every key at or above the floor is a candidate
+            // second pass over flagged points: every key at or above the floor is a candidate;
+            // each column half records up to kMaxCand/2 in its own half of the point's list
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const float key = __uint_as_float((cur[j] & ~0x1Fu) | (uint32_t)j);
               if (key >= floor_key) {
-                if (ncand < kMaxCand)
-                  p.cand[(size_t)(p.row0 + prow) * kMaxCand + ncand] = chunk_of(c) * BN + cb * 32 + j;
+                if (ncand < kMaxCand / 2 && prow < n_rows)
+                  p.cand[(size_t)(p.row0 + prow) * kMaxCand + h * (kMaxCand / 2) + ncand] =
+                      col0 + cb * 32 + j;
                 ++ncand;
               }
             }
-            if (cb + 1 < BN / 32 && cb + 2 != BN / 32) tmem_ld_wait();
-            continue;
-          }
-          const float blk_before = b1;
+          } else {
+            const float blk_before = b1;
 #pragma unroll
-          for (int j = 0; j < 32; j += 2) {
-            const float k0 = __uint_as_float((cur[j] & ~0x1Fu) | (uint32_t)j);
-            const float k1 = __uint_as_float((cur[j + 1] & ~0x1Fu) | (uint32_t)(j + 1));
-            const float hi = fmaxf(k0, k1);
-            const float lo = fminf(k0, k1);
-            b2 = fmax3(b2, lo, fminf(b1, hi));
-            b1 = fmaxf(b1, hi);
+            for (int j = 0; j < 32; j += 2) {
+              const float k0 = __uint_as_float((cur[j] & ~0x1Fu) | (uint32_t)j);
+              const float k1 = __uint_as_float((cur[j + 1] & ~0x1Fu) | (uint32_t)(j + 1));
+              const float hi = fmaxf(k0, k1);
+              const float lo = fminf(k0, k1);
+              b2 = fmax3(b2, lo, fminf(b1, hi));
+              b1 = fmaxf(b1, hi);
+            }
+            if (b1 != blk_before) bblk = (col0 >> 5) + cb;  // 32-column block of the best
           }
-          if (b1 != blk_before) bblk = chunk_of(c) * (BN / 32) + cb;  // 32-column block of the best
-          if (cb + 1 < BN / 32 && cb + 2 != BN / 32) tmem_ld_wait();
         }
       }
       if (!alive) break;
-      if (cand_mode) {
-        if (prow < n_rows) p.cand_cnt[p.row0 + prow] = ncand > kMaxCand ? -1 : ncand;
+      // ---- merge the two column halves of each point: warp (q, 1) -> warp (q, 0) ----
+      const uint32_t mfull = smem_u32(&bars.merge_full[q]);
+      const uint32_t mempty = smem_u32(&bars.merge_empty[q]);
+      if (h == 1) {
+        bool ok = lu == 0 || mbar_wait(mempty, (uint32_t)((lu - 1) & 1), &abort_flag, p.err,
+                                       KMGB_DEV_TIMEOUT_ACC);
+        if (!__all_sync(0xffffffffu, ok)) break;
+        merge.b1[q][lane] = b1;
+        merge.b2[q][lane] = b2;
+        merge.bblk[q][lane] = bblk;
+        merge.ncand[q][lane] = ncand;
+        mbar_arrive(mfull);  // release: the writes above (and the candidate list) are visible
         continue;
       }
+      bool ok = mbar_wait(mfull, (uint32_t)(lu & 1), &abort_flag, p.err, KMGB_DEV_TIMEOUT_ACC);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      const float ob1 = merge.b1[q][lane], ob2 = merge.b2[q][lane];
+      const int obblk = merge.bblk[q][lane], oncand = merge.ncand[q][lane];
+      if (cand_mode) {
+        if (prow < n_rows) {
+          int* lst = p.cand + (size_t)(p.row0 + prow) * kMaxCand;
+          const bool over = ncand > kMaxCand / 2 || oncand > kMaxCand / 2;
+          if (!over)  // move the second half's candidates behind the first half's
+            for (int i = 0; i < oncand; ++i) lst[ncand + i] = lst[kMaxCand / 2 + i];
+          p.cand_cnt[p.row0 + prow] = over ? -1 : ncand + oncand;
+        }
+        mbar_arrive(mempty);
+        continue;
+      }
+      mbar_arrive(mempty);
+      // top-2 of the union; on equal best keys the first half's block is kept (such a point has
+      // a zero margin and is never certified)
+      const float nb2 = fmaxf(fminf(b1, ob1), fmaxf(b2, ob2));
+      if (ob1 > b1) bblk = obblk;
+      b1 = fmaxf(b1, ob1);
+      b2 = nb2;
       const long long pt = prow;
       if (pt < n_rows) {
         const bool none = !(b1 > -1.0e38f);  // no usable center at all
@@ -434,30 +552,34 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     }
   }
 
+  // every pair MMA has completed (done waited above); both CTAs free the pair's TMEM together
   tc_fence_before();
   __syncthreads();
+  cluster_sync_all();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_base),
                  "r"(TMEM_COLS)
                  : "memory");
   }
 }
 
 int g_num_sms = 0;
-size_t g_smem_budget = 0;  // dynamic shared memory a CTA of this kernel may use
+int g_max_pairs = 0;       // co-resident clusters of two CTAs
+size_t g_smem_budget = 0;  // dynamic shared memory a CTA of this kernel may use (1 KB aligned)
 
 }  // namespace
 
-// Shared memory of one X buffer for a dimension: planes x TILES x k-blocks x 16 KB.
+// Shared memory of one point buffer for a dimension: planes x k-blocks x 16 KB.
 static size_t xbuf_bytes_for(int d, int planes) {
-  return (size_t)planes * TILES * ((d + BK - 1) / BK) * KB_BYTES;
+  return (size_t)planes * ((d + BK - 1) / BK) * XKB_BYTES;
 }
 
 bool bf16_tc_supported(int d, int planes) {
   if (d <= 0 || d > MAX_D) return false;
-  // one X buffer and two C stages must fit the 227 KB a CTA can use
-  return xbuf_bytes_for(d, planes) + 2 * (size_t)planes * KB_BYTES + 1024 + 1024 <= SMEM_CAP;
+  // two point buffers and a 3-stage C ring must fit the shared memory of a CTA next to the
+  // 3 KB of static variables (barriers, merge slots)
+  return 2 * xbuf_bytes_for(d, planes) + 3 * (size_t)planes * CKB_BYTES + 3072 <= SMEM_CAP;
 }
 
 float assign_bf16_gamma(int d) {
@@ -480,40 +602,68 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
     KMGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fa;
     KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel));
-    size_t budget = (size_t)optin - fa.sharedSizeBytes;
+    // the dynamic area starts on the next 1 KB boundary after the static variables
+    const size_t static_bytes = (fa.sharedSizeBytes + 1023) / 1024 * 1024;
+    size_t budget = (size_t)optin > static_bytes ? (size_t)optin - static_bytes : 0;
     if (budget > SMEM_CAP) budget = SMEM_CAP;
     KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
     g_smem_budget = budget;
+    cudaLaunchConfig_t qc = {};
+    qc.gridDim = dim3((unsigned)(g_num_sms / 2 * 2));
+    qc.blockDim = dim3(NTHREADS);
+    qc.dynamicSmemBytes = budget;
+    cudaLaunchAttribute qa[1];
+    qa[0].id = cudaLaunchAttributeClusterDimension;
+    qa[0].val.clusterDim.x = 2;
+    qa[0].val.clusterDim.y = 1;
+    qa[0].val.clusterDim.z = 1;
+    qc.attrs = qa;
+    qc.numAttrs = 1;
+    KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&g_max_pairs, assign_bf16_kernel, &qc));
+    if (g_max_pairs <= 0) return cudaErrorInvalidConfiguration;
   }
   const size_t xbytes = xbuf_bytes_for(a.d, planes);
-  const size_t stage_bytes = (size_t)planes * KB_BYTES;
+  const size_t stage_bytes = (size_t)planes * CKB_BYTES;
   const size_t lim = g_smem_budget;
-  // double-buffer the unit's points when that still leaves a 4-stage ring for C
-  const int xbufs = (2 * xbytes + 4 * stage_bytes + 1024 <= lim) ? 2 : 1;
-  if (lim < xbufs * xbytes + 1024 + 2 * stage_bytes) return cudaErrorInvalidValue;
-  int stages = (int)((lim - 1024 - xbufs * xbytes) / stage_bytes);
+  // double-buffer the unit's points (needed to keep the tensor pipe busy across units)
+  const int xbufs = (2 * xbytes + 3 * stage_bytes <= lim) ? 2 : 1;
+  if (lim < xbufs * xbytes + 2 * stage_bytes) return cudaErrorInvalidValue;
+  int stages = (int)((lim - xbufs * xbytes) / stage_bytes);
   if (stages > MAX_STAGES) stages = MAX_STAGES;
-  const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes + 1024;
+  const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes;
   CUtensorMap tmX, tmC, tmXl, tmCl;
   KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmX, Xb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.d,
                                   (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
   KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmC, Cb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.d,
-                                  (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BN));
+                                  (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BNH));
   tmXl = tmX;
   tmCl = tmC;
   if (planes > 1) {
     KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmXl, Xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                                     (uint64_t)a.d, (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
     KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmCl, Cl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
-                                    (uint64_t)a.d, (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BN));
+                                    (uint64_t)a.d, (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BNH));
   }
   const long long n_units = (a.n + UNIT - 1) / UNIT;
-  const int grid = (int)(n_units < g_num_sms ? n_units : g_num_sms);
-  if (grid <= 0) return cudaSuccess;
-  assign_bf16_kernel<<<grid, NTHREADS, smem, s>>>(tmX, tmXl, tmC, tmCl, a, stages, xbufs, planes);
+  const long long pairs = n_units < g_max_pairs ? n_units : g_max_pairs;
+  if (pairs <= 0) return cudaSuccess;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(2 * pairs));
+  cfg.blockDim = dim3(NTHREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel, tmX, tmXl, tmC, tmCl, a, stages,
+                                   xbufs, planes));
   count_launches(1);
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 }  // namespace kmgb

@@ -1,9 +1,11 @@
 // Shared device/host helpers for the GB300 (sm_103a) Lloyd kernels.
 //
-// Every wait on an mbarrier is bounded: a wait gives up after KMGB_WAIT_NS nanoseconds of
-// %globaltimer, records an error code in the launch's error word and returns false; an abort
-// flag in shared memory then makes every later wait of the CTA return at once so the CTA
-// drains and exits (no unbounded spin, no __trap).
+// Every wait on an mbarrier is bounded: a wait gives up after KMGB_WAIT_CYCLES SM clock cycles
+// (about 2 s at 2 GHz), records an error code in the launch's error word and returns false; an
+// abort flag in shared memory then makes every later wait of the CTA return at once so the CTA
+// drains and exits (no unbounded spin, no __trap). The limit is counted with clock64, a cheap
+// register read: a %globaltimer read takes hundreds of cycles on GB300 and, inside the wait
+// loop, delayed every wake-up of the pipelines by about that much.
 #pragma once
 
 #include <cuda.h>
@@ -11,8 +13,8 @@
 #include <cuda_bf16.h>
 #include <stdint.h>
 
-#ifndef KMGB_WAIT_NS
-#define KMGB_WAIT_NS 2000000000ull  // 2 s per wait
+#ifndef KMGB_WAIT_CYCLES
+#define KMGB_WAIT_CYCLES 4000000000ull  // about 2 s per wait at a 2 GHz SM clock
 #endif
 
 // Error codes written to the device error word (first writer wins).
@@ -29,12 +31,6 @@ namespace kmgb {
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
 }
 
 __device__ __forceinline__ void set_error(int* err, int code) {
@@ -78,11 +74,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
                                           int* err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer();
+  const long long t0 = clock64();
   while (true) {
-    if (*abort_flag) return false;
     if (mbar_try_wait(bar, parity)) return true;
-    if (globaltimer() - t0 > KMGB_WAIT_NS) {
+    if (*abort_flag) return false;
+    if ((unsigned long long)(clock64() - t0) > KMGB_WAIT_CYCLES) {
       *abort_flag = 1;
       set_error(err, code);
       return false;

@@ -143,7 +143,7 @@ struct kmgb_handle {
   void* Cl = nullptr;
   float* cn = nullptr;
   float* cmax = nullptr;
-  float* cinit = nullptr;  // BF16 tier accumulator start values, padded to 128
+  float* cinit = nullptr;  // BF16 tier accumulator start values, padded to kCenterPad
   bool have_centers = false;
   // assignment
   int* labels = nullptr;
@@ -278,7 +278,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   if (split) KM_TRY(cudaMalloc(&h->Cl, (size_t)k * h->ldb * 2), (delete h, code));
   KM_TRY(dalloc(&h->cn, k), (delete h, code));
   KM_TRY(dalloc(&h->cmax, 1), (delete h, code));
-  if (bf16) KM_TRY(dalloc(&h->cinit, (size_t)(k + 127) / 128 * 128), (delete h, code));
+  if (bf16) KM_TRY(dalloc(&h->cinit, (size_t)round_up(k, kCenterPad)), (delete h, code));
   const long long na = h->n_act;
   KM_TRY(dalloc(&h->labels, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_list, na), (delete h, code));
@@ -794,7 +794,7 @@ int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int
   kmgb_handle* h = nullptr;
   int rc = create_handle(&h, n, d, k, &o);
   if (rc) return rc;
-  const int kpad = (k + 127) / 128 * 128;
+  const int kpad = (int)round_up(k, kCenterPad);
   float* dump = nullptr;
   std::vector<float> host;
   rc = set_data(h, X, false);

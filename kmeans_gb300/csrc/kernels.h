@@ -156,6 +156,9 @@ cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* 
 
 constexpr int kSumPiece = 128;
 constexpr int kMaxCand = 16;  // candidate centers recorded per flagged point
+// BF16 tiers: centers per tensor-core chunk; the start values and diagnostic accumulators are
+// padded to a whole number of chunks
+constexpr int kCenterPad = 256;
 
 // Message returned by kmgb_last_error() on the calling thread.
 void set_last_error(const char* msg);

@@ -150,7 +150,7 @@ cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, flo
                                 const int* stop, float* cinit, void* Cl) {
   if (k <= 0) return cudaSuccess;
   const int threads = 256;
-  const int kpad = (k + 127) / 128 * 128;
+  const int kpad = (k + kCenterPad - 1) / kCenterPad * kCenterPad;
   const int blocks = (int)(((long long)(cinit ? kpad : k) * 32 + threads - 1) / threads);
   prep_centers_kernel<<<blocks, threads, 0, s>>>(C, ldc, k, d, Cop,
                                                  reinterpret_cast<__nv_bfloat16*>(Cb), ldcb, cn,
