@@ -12,7 +12,9 @@ points; synthetic, generated on the device). Prints one JSON line.
 stream); `e2e` is the same metric through the public C-ABI one-shot call (kmgb_lloyd_f32) from
 pageable host memory, host<->device copies included; `roofline` covers the assignment kernel
 (2*N*K*D FLOP per launch, per-launch time from CUDA events bracketing it inside the timed
-region); `cpu_baseline` is the CPU restatement (oracle FP32 port, all host threads) on a sample.
+region; `tensor_*` counts the tensor-core products the tier actually issues, three per element
+in the split tier; `traffic` is the DRAM bytes of one launch from an ncu capture, scaled to N);
+`cpu_baseline` is the CPU restatement (oracle FP32 port, all host threads) on a sample.
 The reference arm (--impl reference) times that CPU path: the reference has no CPU
 implementation of its own and its GPU code cannot be built for this host.
 """
@@ -32,6 +34,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N, D, K = 4_000_000, 128, 1024
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one assignment launch per row of
+# X, from one ncu capture of the current split-tier kernel on the 1,000,000 x 128, K=1024 case
+# (517.0 MB read + 7.6 MB written). X is read once per launch and C stays in L2, so the traffic
+# of a launch grows in proportion to its rows.
+TRAFFIC_BYTES_PER_ROW = {"bf16x3": 524.64e6 / 1_000_000}
+# tensor-core products per distance element: the split tier evaluates x_hi.c_hi + x_hi.c_lo +
+# x_lo.c_hi
+TENSOR_PRODUCTS = {"bf16x3": 3, "bf16": 1}
 METRIC = "Lloyd iter/s (N=4M, D=128, K=1024), labels = FP64 arg-min"
 CPU_SAMPLE_ROWS = 65_536
 
@@ -193,11 +203,18 @@ def main():
     assign_ms = phase[1] / max(piters, 1)
     achieved = flop / (assign_ms / 1000.0) / 1e12
     bf16_peak, hbm_peak, src = peaks()
+    traffic = TRAFFIC_BYTES_PER_ROW.get(tier)
     roofline = {"bound": "tensor", "achieved": achieved, "peak": bf16_peak, "unit": "TFLOP/s",
-                "frac": achieved / bf16_peak, "traffic": None,
+                "frac": achieved / bf16_peak,
+                "traffic": traffic * n if traffic else None, "traffic_unit": "bytes",
                 "kernel": "assign_fp32_kernel" if tier == "fp32" else "assign_bf16_kernel",
                 "peak_source": f"{src} bf16 dense (MEASURED_PEAKS.json)",
                 "flop_per_launch": flop, "ms_per_launch": assign_ms}
+    if tier in TENSOR_PRODUCTS:
+        tf = TENSOR_PRODUCTS[tier] * flop
+        roofline["tensor_flop_per_launch"] = tf
+        roofline["tensor_tflops"] = tf / (assign_ms / 1000.0) / 1e12
+        roofline["tensor_frac"] = roofline["tensor_tflops"] / bf16_peak
 
     e2e = None
     if not args.no_e2e and rank == 0:

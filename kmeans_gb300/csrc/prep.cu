@@ -62,9 +62,18 @@ __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, 
   }
 }
 
-// One warp per point: qn = ||x||^2 in FP64, xn = FP32 upper bound of ||x||. Each lane sums its
-// squares as an error-free float-float value (exact products x*x = p + e by FMA, TwoSum
-// accumulation) on the FP32 pipe; the 32 lane sums are combined in FP64.
+__device__ __forceinline__ void ff_two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bp = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// One warp per point: qn = ||x||^2 (FP64), xn = FP32 upper bound of ||x||. GB300's FP64 pipe is
+// narrow, so the sum runs on the FP32 pipe as an error-free float-float value: exact squares
+// (p + e by FMA), TwoSum accumulation per lane, a float-float tree over the warp, and a single
+// FP64 addition per point. The float-float sum is within (d/32 + 8) 2^-46 of ||x||^2 relative;
+// xn adds 2^-20 before its upward-rounded square root. Rows whose squares leave the FP32 range
+// are summed in FP64 instead.
 __global__ void point_norms_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
                                    double* __restrict__ qn, float* __restrict__ xn) {
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -76,18 +85,35 @@ __global__ void point_norms_kernel(const float* __restrict__ X, long long ldx, l
     const float v = __ldg(x + t);
     const float p = __fmul_rn(v, v);
     const float e = __fmaf_rn(v, v, -p);  // v*v - p exactly
-    const float s1 = __fadd_rn(hi, p);
-    const float bp = __fsub_rn(s1, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s1, bp)), __fsub_rn(p, bp));
+    float s1, err;
+    ff_two_sum(hi, p, s1, err);
     hi = s1;
     lo = __fadd_rn(lo, __fadd_rn(err, e));
   }
-  double s = (double)hi + (double)lo;
-  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    float s1, err;
+    ff_two_sum(hi, oh, s1, err);
+    hi = s1;
+    lo = __fadd_rn(lo, __fadd_rn(ol, err));
+  }
+  if (!(fabsf(hi) < 1.0e37f)) {  // overflow (or NaN input): FP64 sum, same for every lane
+    double sd = 0.0;
+    for (int t = lane; t < d; t += 32) {
+      const double v = (double)__ldg(x + t);
+      sd = fma(v, v, sd);
+    }
+    for (int o = 16; o > 0; o >>= 1) sd += __shfl_xor_sync(0xffffffffu, sd, o);
+    if (lane == 0) {
+      if (qn) qn[warp] = sd;
+      if (xn) xn[warp] = __double2float_ru(sqrt(sd) * (1.0 + 1e-12));
+    }
+    return;
+  }
   if (lane == 0) {
-    if (qn) qn[warp] = s;
-    // the float-float sum is within ~2^-40 of ||x||^2; 1e-9 covers it
-    if (xn) xn[warp] = __double2float_ru(sqrt(s) * (1.0 + 1e-9));
+    if (qn) qn[warp] = (double)hi + (double)lo;
+    if (xn) xn[warp] = __fsqrt_ru(__fmul_ru(__fadd_ru(hi, fabsf(lo)), 1.0f + 0x1p-20f));
   }
 }
 
