@@ -16,7 +16,9 @@ region; `tensor_*` counts the tensor-core products the tier actually issues, thr
 in the split tier; `traffic` is the DRAM bytes of one launch from an ncu capture, scaled to N);
 `cpu_baseline` is the CPU restatement (oracle FP32 port, all host threads) on a sample.
 The reference arm (--impl reference) times that CPU path: the reference has no CPU
-implementation of its own and its GPU code cannot be built for this host.
+implementation of its own and its host code cannot be built for the GPU host. Its line also
+carries `reference_gpu`: the reference's own assignment kernels (compiled from its sources into
+oracle/_ref, launched as its ClosestCentersF does) timed on the same workload.
 """
 from __future__ import annotations
 
@@ -113,6 +115,57 @@ def cpu_baseline(steps: int = 1):
                       f"{len(times)}", "seconds_per_sample_iter": t}
 
 
+def reference_gpu_assign():
+    """The reference's own assignment kernels (main/cuda/ClosestCenters.cu, compiled from its
+    sources into oracle/_ref and launched as its ClosestCentersF does) on the same workload:
+    milliseconds per assignment pass, CUDA events on the legacy default stream. None when
+    oracle/_ref or a GPU is absent."""
+    try:
+        import torch
+        import oracle
+        if not torch.cuda.is_available():
+            return None
+        ref = oracle.ref_kernels()
+        if ref is None:
+            return None
+        from kmeans_gb300.synthetic import mixture_torch, sample_init
+        X, _, _ = mixture_torch(N, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+        C = X[torch.from_numpy(sample_init(N, K, seed=99)).cuda()]
+        rows_padded = (N + 63) // 64 * 64
+        # the reference's kernels read past the logical matrices (see oracle/ref_kernels.cpp)
+        A = torch.zeros((rows_padded + 1) * D + 16, dtype=torch.float32, device="cuda")
+        A[: N * D] = X.reshape(-1)
+        del X
+        B = torch.zeros((D + 16) * K, dtype=torch.float32, device="cuda")
+        B[: D * K] = C.t().contiguous().reshape(-1)
+        normB = (C * C).sum(1).contiguous()
+        ncolsc = (K + 63) // 64
+        part = torch.empty(ncolsc * N, dtype=torch.float32, device="cuda")
+        pidx = torch.empty(ncolsc * N, dtype=torch.int32, device="cuda")
+        labels = torch.empty(N, dtype=torch.int32, device="cuda")
+        args = (0, N, D, A.data_ptr(), K, B.data_ptr(), normB.data_ptr(), ncolsc, part.data_ptr(),
+                pidx.data_ptr(), labels.data_ptr())
+        for _ in range(2):
+            if ref.refk_closest_centers_f(*args) != 0:
+                return None
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        e0.record(torch.cuda.default_stream())
+        for _ in range(reps):
+            ref.refk_closest_centers_f(*args)
+        e1.record(torch.cuda.default_stream())
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        return {"kernels": "reference main/cuda/ClosestCenters.cu (ClosestCentersF), built from "
+                           "its sources for sm_103a", "assign_ms": ms,
+                "assign_tflops": 2.0 * N * K * D / (ms / 1000.0) / 1e12,
+                "note": "assignment pass only (FP32 labels); the reference's update and SSE "
+                        "kernels and host loop are not run"}
+    except Exception as e:  # noqa: BLE001 - an informational extra
+        return {"unavailable": str(e)[:200]}
+
+
 def reference_arm(args, rank: int):
     if rank != 0:
         return
@@ -126,7 +179,8 @@ def reference_arm(args, rank: int):
             "config": {"workload": "lloyd_4Mx128_K1024", "n": N, "d": D, "k": K},
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "iter/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "reference_gpu": reference_gpu_assign()}
     print(json.dumps(line), flush=True)
 
 

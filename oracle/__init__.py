@@ -39,6 +39,82 @@ def build(force: bool = False) -> str:
     return _SO
 
 
+_REF = os.path.join(_HERE, "_ref")
+_REF_CUBIN = os.path.join(_REF, "closest_centers.cubin")
+_REF_SO = os.path.join(_REF, "libref_kernels.so")
+_REF_LOADER_SRC = os.path.join(_HERE, "ref_kernels.cpp")
+_REF_SHIM = os.path.join(_HERE, "ref_shfl_shim.h")
+# The reference's CUDA sources; present only in the development container, never on the GPU host
+# (which uses the prebuilt cubin from oracle/_ref).
+_REFERENCE_CUDA_DIR = "/root/reference/main/cuda"
+
+
+def _cuda_home() -> str:
+    for cand in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if cand and os.path.isdir(os.path.join(cand, "include")):
+            return cand
+    return "/usr/local/cuda"
+
+
+def build_ref() -> bool:
+    """Recipe for oracle/_ref (git-ignored, test infrastructure).
+
+    1. Where the reference's sources are present, compile its main/cuda/ClosestCenters.cu, as it
+       lies, into a cubin for sm_103a with ref_shfl_shim.h force-included (the reference's
+       pre-Volta shuffles). Device code does not depend on the host architecture, so the cubin
+       built here runs on the Arm GPU host.
+    2. Wherever a CUDA toolkit is present, compile ref_kernels.cpp, the loader that plays the
+       reference's host side (the reference's own host code cannot be built for the GPU host).
+
+    Returns True when both the cubin and the loader exist.
+    """
+    os.makedirs(_REF, exist_ok=True)
+    cuda = _cuda_home()
+    src = os.path.join(_REFERENCE_CUDA_DIR, "ClosestCenters.cu")
+    if os.path.exists(src) and not os.path.exists(_REF_CUBIN):
+        nvcc = os.path.join(cuda, "bin", "nvcc")
+        subprocess.check_call([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                               "-w", "-include", _REF_SHIM, "-I", _REFERENCE_CUDA_DIR, src, "-o",
+                               _REF_CUBIN + ".tmp"])
+        os.replace(_REF_CUBIN + ".tmp", _REF_CUBIN)
+    if os.path.isdir(os.path.join(cuda, "include")) and (
+            not os.path.exists(_REF_SO)
+            or os.path.getmtime(_REF_SO) < os.path.getmtime(_REF_LOADER_SRC)):
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I",
+                               os.path.join(cuda, "include"), _REF_LOADER_SRC, "-o",
+                               _REF_SO + ".tmp", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+                               "-Wl,-rpath," + os.path.join(cuda, "lib64")])
+        os.replace(_REF_SO + ".tmp", _REF_SO)
+    return os.path.exists(_REF_CUBIN) and os.path.exists(_REF_SO)
+
+
+_ref_lib = None
+
+
+def ref_kernels():
+    """The reference's assignment kernels (cubin + loader), or None when oracle/_ref is absent."""
+    global _ref_lib
+    with _lock:
+        if _ref_lib is not None:
+            return _ref_lib
+        if not (os.path.exists(_REF_CUBIN) and os.path.exists(_REF_SO)):
+            return None
+        L = C.CDLL(_REF_SO)
+        P = C.c_void_p
+        L.refk_load.argtypes = [C.c_char_p]
+        L.refk_load.restype = C.c_int
+        L.refk_last_error.restype = C.c_char_p
+        L.refk_closest_centers_f.argtypes = [C.c_int, C.c_int, C.c_int, P, C.c_int, P, P, C.c_int,
+                                             P, P, P]
+        L.refk_closest_centers_f.restype = C.c_int
+        found = L.refk_load(_REF_CUBIN.encode())
+        if found != 17:
+            raise RuntimeError(f"reference cubin: found {found} of 17 kernels "
+                               f"({L.refk_last_error().decode()})")
+        _ref_lib = L
+        return L
+
+
 def lib():
     global _lib
     with _lock:
