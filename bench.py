@@ -10,7 +10,8 @@ points; synthetic, generated on the device). Prints one JSON line.
 
 `value` is Lloyd iterations/s with the data resident in HBM (CUDA events on the library's
 stream); `e2e` is the same metric through the public C-ABI one-shot call (kmgb_lloyd_f32) from
-pageable host memory, host<->device copies included; `roofline` covers the assignment kernel
+pageable host memory, host<->device copies included, one call running the workload's 30
+iterations; `roofline` covers the assignment kernel
 (2*N*K*D FLOP per launch, per-launch time from CUDA events bracketing it inside the timed
 region; `tensor_*` counts the tensor-core products the tier actually issues, three per element
 in the split tier; `traffic` is the DRAM bytes of one launch from an ncu capture, scaled to N);
@@ -44,6 +45,8 @@ TRAFFIC_BYTES_PER_ROW = {"bf16x3": 524.64e6 / 1_000_000}
 # tensor-core products per distance element: the split tier evaluates x_hi.c_hi + x_hi.c_lo +
 # x_lo.c_hi
 TENSOR_PRODUCTS = {"bf16x3": 3, "bf16": 1}
+# the workload's run is 30 Lloyd iterations: the end-to-end leg makes that one public call
+E2E_ITERS = 30
 METRIC = "Lloyd iter/s (N=4M, D=128, K=1024), labels = FP64 arg-min"
 CPU_SAMPLE_ROWS = 65_536
 
@@ -187,7 +190,7 @@ def reference_arm(args, rank: int):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--tier", default="bf16x3",
@@ -275,14 +278,19 @@ def main():
         Xh = X.cpu().numpy()
         del X
         torch.cuda.empty_cache()
+        # one untimed call first (module loading, allocator growth), like the device path's
+        # warm-up iterations; the timed call then includes all of its own host<->device copies
+        km.lloyd(Xh, K, init=init, max_iters=max(1, args.warmup), assign_tier=tier_id)
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        res = km.lloyd(Xh, K, init=init, max_iters=args.steps, assign_tier=tier_id)
+        res = km.lloyd(Xh, K, init=init, max_iters=E2E_ITERS, assign_tier=tier_id)
         t1 = time.perf_counter()
-        e2e = {"value": args.steps / (t1 - t0), "unit": "iter/s",
-               "h2d_bytes_per_step": (Xh.nbytes + init.nbytes) // args.steps,
+        e2e = {"value": E2E_ITERS / (t1 - t0), "unit": "iter/s",
+               "h2d_bytes_per_step": (Xh.nbytes + init.nbytes) // E2E_ITERS,
                "d2h_bytes_per_step": (res.centers.nbytes + res.labels.nbytes + res.sse.nbytes)
-               // args.steps,
-               "call": "kmgb_lloyd_f32 (host pageable X, init, centers/labels/SSE out)",
+               // E2E_ITERS, "iterations_per_call": E2E_ITERS,
+               "call": "kmgb_lloyd_f32 (host pageable X, init, centers/labels/SSE out); "
+                       "after one untimed call",
                "seconds": t1 - t0}
     cb = None
     if not args.no_cpu and rank == 0:

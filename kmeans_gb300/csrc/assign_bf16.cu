@@ -138,9 +138,12 @@ __device__ __forceinline__ void cluster_sync_all() {
                    : "memory");
 }
 
+// Arrive on an mbarrier of either CTA of the pair. Used only to hand an accumulator buffer back
+// to the leader's MMA issuer: no generic-memory data travels with it (the TMEM reads before it
+// are ordered by tcgen05.fence::before_thread_sync), so the default CTA-scope release suffices;
+// a cluster-scope release made every epilogue warp wait for its earlier global stores.
 __device__ __forceinline__ void mbar_arrive_remote(uint32_t cluster_addr) {
-  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr)
-               : "memory");
+  asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(cluster_addr) : "memory");
 }
 
 // 2-D TMA load into this CTA's shared memory, completing on an mbarrier of either CTA of the pair.
