@@ -319,7 +319,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(dalloc(&w.sorted, na), (delete h, code));
   KM_TRY(dalloc(&w.part, (size_t)w.max_pieces * d), (delete h, code));
   KM_TRY(dalloc(&w.partq, w.max_pieces), (delete h, code));
-  KM_TRY(dalloc(&w.sse_k, k), (delete h, code));
+  KM_TRY(dalloc(&w.sse_k, (size_t)k * ((d + 31) / 32)), (delete h, code));  // per (center, 32 dims)
   KM_TRY(dalloc(&w.counts, k), (delete h, code));
   w.err = h->err;
   w.stop = h->stop;

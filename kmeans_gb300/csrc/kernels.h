@@ -121,7 +121,7 @@ struct UpdateWork {
   int* sorted;          // [n]
   double* part;         // [max_pieces * d]
   double* partq;        // [max_pieces]
-  double* sse_k;        // [k]
+  double* sse_k;        // [k][ceil(d/32)] SSE terms per (center, group of 32 dimensions)
   long long* counts;    // [k]
   int* err;
   // stop rule (kmeans.cpp:1194-1237), evaluated on the device by the SSE reduction

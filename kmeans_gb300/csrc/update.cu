@@ -260,7 +260,7 @@ __global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
 // FP32 rows whose width and stride are multiples of 4 (16-byte aligned): one warp per piece, a
 // lane owns 4 consecutive dimensions (one float4 per row, so a warp instruction reads a whole
 // 128-dimension row), the piece's point ids are read 32 at a time and broadcast by shuffles, and
-// 8 rows are in flight per warp. Every dimension still adds the piece's points in sorted order
+// 16 rows are in flight per warp. Every dimension still adds the piece's points in sorted order
 // with the same float-float TwoSum as the generic kernel: the sums are identical. The piece's
 // sum of ||x||^2 (SSE only) is added as a tree over 32 rows at a time.
 __global__ void piece_sums_vec4_kernel(const float* __restrict__ X, long long ldx,
@@ -292,6 +292,22 @@ __global__ void piece_sums_vec4_kernel(const float* __restrict__ X, long long ld
           qs += qv;
         }
         int tt = 0;
+        for (; tt + 16 <= nt; tt += 16) {  // sixteen rows in flight
+          float4 v[16];
+#pragma unroll
+          for (int r = 0; r < 16; ++r) {
+            const int i = __shfl_sync(0xffffffffu, my_i, tt + r);
+            v[r] = on ? __ldg(reinterpret_cast<const float4*>(X + (size_t)i * ldx + c))
+                      : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+#pragma unroll
+          for (int r = 0; r < 16; ++r) {
+            a0.add(v[r].x);
+            a1.add(v[r].y);
+            a2.add(v[r].z);
+            a3.add(v[r].w);
+          }
+        }
         for (; tt + 8 <= nt; tt += 8) {
           float4 v[8];
 #pragma unroll
@@ -330,26 +346,40 @@ __global__ void piece_sums_vec4_kernel(const float* __restrict__ X, long long ld
   }
 }
 
-// One warp per center.
+// One warp per (center j, group g of 32 dimensions): lane c of group g owns dimension
+// g*32 + c, adds the center's piece sums in piece order (the canonical order: centers are
+// unchanged by the split), divides in FP64 and rounds once. The group's SSE term
+// sum_c (n mu^2 - 2 mu s) lands in sse_k[j * G + g]; group 0 adds the members' sum of ||x||^2.
 __global__ void finalize_kernel(const double* __restrict__ part, const double* __restrict__ partq,
                                 const int* __restrict__ label_off, const int* __restrict__ pstart,
                                 int k, int d, float* __restrict__ C, long long ldc,
                                 int empty_policy, double* __restrict__ sse_k, const int* stop) {
   if (stopped(stop)) return;
-  const int j = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int groups = (d + 31) / 32;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (j >= k) return;
+  if (wid >= (long long)k * groups) return;
+  const int j = (int)(wid / groups), g = (int)(wid - (long long)j * groups);
+  const int c = g * 32 + lane;
   const long long n = (long long)label_off[j + 1] - label_off[j];
   const int p0 = pstart[j], p1 = pstart[j + 1];
   double sse = 0.0;
-  for (int c = lane; c < d; c += 32) {
+  if (c < d) {
     double s = 0.0;
-    for (int p = p0; p < p1; ++p) s += part[(size_t)p * d + c];
+    int p = p0;
+    for (; p + 8 <= p1; p += 8) {  // eight loads in flight, additions in piece order
+      double v[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) v[i] = __ldg(part + (size_t)(p + i) * d + c);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) s += v[i];
+    }
+    for (; p < p1; ++p) s += __ldg(part + (size_t)p * d + c);
     float mu;
     if (n > 0) {
       mu = __double2float_rn(__ddiv_rn(s, (double)n));
       const double m = (double)mu;
-      sse += fma((double)n * m, m, -2.0 * m * s);
+      sse = fma((double)n * m, m, -2.0 * m * s);
     } else if (empty_policy == 1) {
       mu = C[(size_t)j * ldc + c];
     } else {
@@ -360,9 +390,9 @@ __global__ void finalize_kernel(const double* __restrict__ part, const double* _
   for (int o = 16; o > 0; o >>= 1) sse += __shfl_xor_sync(0xffffffffu, sse, o);
   if (lane == 0 && sse_k) {
     double q = 0.0;
-    if (partq && n > 0)
-      for (int p = p0; p < p1; ++p) q += partq[p];
-    sse_k[j] = (n > 0) ? sse + q : 0.0;
+    if (g == 0 && partq && n > 0)
+      for (int pp = p0; pp < p1; ++pp) q += partq[pp];
+    sse_k[(size_t)j * groups + g] = (n > 0) ? sse + q : 0.0;
   }
 }
 
@@ -470,13 +500,14 @@ cudaError_t launch_update(const float* X, const double* qn, const int* labels, f
         X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq, w.stop);
   kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
-  finalize_kernel<<<(unsigned)(((long long)k * 32 + 255) / 256), 256, 0, s>>>(
+  const long long fin_warps = (long long)k * ((w.d + 31) / 32);
+  finalize_kernel<<<(unsigned)((fin_warps * 32 + 255) / 256), 256, 0, s>>>(
       w.part, qn ? w.partq : nullptr, w.label_off, w.piece_cnt, k, w.d, C, ldc, empty_policy,
       w.sse_k, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   if (sse_out) {
-    sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, k, sse_out, w.stop, w.criterion, w.sse_prev,
-                                         w.rel_out, w.iters_done); kmgb::count_launches(1);
+    sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, (int)fin_warps, sse_out, w.stop, w.criterion,
+                                         w.sse_prev, w.rel_out, w.iters_done); kmgb::count_launches(1);
     KMGB_CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;
