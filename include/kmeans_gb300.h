@@ -200,7 +200,11 @@ typedef struct kmgb_options {
   int max_iters;             /* iterations (upper bound when criterion >= 0) */
   double criterion;          /* stop when |dSSE|/SSE <= criterion; < 0: run max_iters */
   float mini_batch_fraction; /* < 1: reference mini-batch windows of (int)(f*m) rows */
-  int reserved[8];
+  int stream_tile_rows;      /* > 0 and < n: host-streamed tiles (the reference's out-of-memory
+                                path): X stays in host memory and passes through two device
+                                tile buffers of this many rows every iteration; the host array
+                                must stay valid while the handle runs. 0: X resident in HBM */
+  int reserved[7];
 } kmgb_options;
 
 typedef struct kmgb_stats {

@@ -64,7 +64,8 @@ class KmeansError(RuntimeError):
 class kmgb_options(C.Structure):
     _fields_ = [("assign_tier", C.c_int), ("certify", C.c_int), ("empty_policy", C.c_int),
                 ("max_iters", C.c_int), ("criterion", C.c_double),
-                ("mini_batch_fraction", C.c_float), ("reserved", C.c_int * 8)]
+                ("mini_batch_fraction", C.c_float), ("stream_tile_rows", C.c_int),
+                ("reserved", C.c_int * 7)]
 
 
 class kmgb_stats(C.Structure):
@@ -315,9 +316,10 @@ class LloydResult:
 
 def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
           assign_tier: int = ASSIGN_FP32, certify: bool = True, empty_policy: int = EMPTY_NAN,
-          mini_batch_fraction: float = 1.0) -> LloydResult:
+          mini_batch_fraction: float = 1.0, stream_tile_rows: int = 0) -> LloydResult:
     """One-shot Lloyd run through kmgb_lloyd_f32. X: numpy (host) or torch (device) n x d
-    float32; init: k x d float32 or None (reference initialisation)."""
+    float32; init: k x d float32 or None (reference initialisation). stream_tile_rows > 0 keeps
+    a host X in host memory and streams it through the GPU in tiles of that many rows."""
     if isinstance(X, np.ndarray):
         X = np.ascontiguousarray(X, dtype=np.float32)
     n, d = X.shape
@@ -325,7 +327,8 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
         init = np.ascontiguousarray(init, dtype=np.float32)
     opt = default_options(assign_tier=assign_tier, certify=int(certify),
                           empty_policy=empty_policy, max_iters=max_iters, criterion=criterion,
-                          mini_batch_fraction=mini_batch_fraction)
+                          mini_batch_fraction=mini_batch_fraction,
+                          stream_tile_rows=stream_tile_rows)
     cen = np.empty((k, d), dtype=np.float32)
     lab = np.empty(n, dtype=np.int32)
     sse = np.zeros(max(max_iters, 1), dtype=np.float64)

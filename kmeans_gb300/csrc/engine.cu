@@ -122,6 +122,19 @@ struct kmgb_handle {
   long long n_act = 0; // rows processed per iteration
   int iter_base = 0;   // iterations already run (mini-batch window index)
 
+  // host-streamed tiles (opt.stream_tile_rows): X stays in host memory and passes through two
+  // device tile buffers (X, X2) every iteration; labels cover all n rows, the update adds every
+  // tile's canonical sums to FP64 accumulators
+  bool streaming = false;
+  long long tile_rows = 0;
+  const float* Xhost = nullptr;
+  float* X2 = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_copied[2] = {nullptr, nullptr};
+  cudaEvent_t ev_free[2] = {nullptr, nullptr};
+  double* accS = nullptr;
+  double* accQ = nullptr;
+  int* accN = nullptr;
   // data set
   float* X = nullptr;
   void* Xb = nullptr;
@@ -161,6 +174,7 @@ struct kmgb_handle {
   void* XlC = nullptr;
   int* cand = nullptr;
   int* cand_cnt = nullptr;
+  long long cand_cap = 0;  // rows of the compact buffers for the candidate pass
   unsigned long long* rr_stats = nullptr;
   int* err = nullptr;
   // device-side loop state: stop flag, previous SSE, last relErr, iterations done
@@ -204,9 +218,14 @@ struct kmgb_handle {
                     rr_list, rr_count, rr_over, rr_list2, rr_hi2, thr_full, thr_c, XbC, XlC, cand,
                     cand_cnt, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
                     uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
-                    stop, loopf, iters_done};
+                    stop, loopf, iters_done, X2, accS, accQ, accN};
     for (void* p : ptrs)
       if (p) cudaFree(p);
+    for (int b = 0; b < 2; ++b) {
+      if (ev_copied[b]) cudaEventDestroy(ev_copied[b]);
+      if (ev_free[b]) cudaEventDestroy(ev_free[b]);
+    }
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     if (sse_pinned) cudaFreeHost(sse_pinned);
     if (loop_init) cudaFreeHost(loop_init);
     if (ev0) cudaEventDestroy(ev0);
@@ -252,18 +271,40 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
       return KMEANS_ERROR_TILING;
     }
   }
-  h->n_act = h->mini ? h->m_mb : n;
+  h->streaming = h->opt.stream_tile_rows > 0 && h->opt.stream_tile_rows < n;
+  if (h->streaming && h->mini) {
+    delete h;
+    set_err("kmgb_create: host-streamed tiles run full-batch Lloyd (mini_batch_fraction 1)");
+    return KMEANS_ERROR_TILING;
+  }
+  h->tile_rows = h->streaming ? h->opt.stream_tile_rows : n;
+  h->n_act = h->mini ? h->m_mb : h->tile_rows;
+  const long long nx = h->tile_rows;  // rows of a device data buffer
   const bool bf16 = h->opt.assign_tier != KMGB_ASSIGN_FP32;
   const bool split = h->opt.assign_tier == KMGB_ASSIGN_BF16X3;
   const int code = KMEANS_ERROR_BUILDDATA;
   KM_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), (delete h, code));
   KM_TRY(cudaEventCreate(&h->ev0), (delete h, code));
   KM_TRY(cudaEventCreate(&h->ev1), (delete h, code));
-  KM_TRY(dalloc(&h->X, (size_t)n * h->ldx), (delete h, code));
-  KM_TRY(dalloc(&h->qn, n), (delete h, code));
-  KM_TRY(dalloc(&h->xn, n), (delete h, code));
-  if (bf16) KM_TRY(cudaMalloc(&h->Xb, (size_t)n * h->ldb * 2), (delete h, code));
-  if (split) KM_TRY(cudaMalloc(&h->Xl, (size_t)n * h->ldb * 2), (delete h, code));
+  KM_TRY(dalloc(&h->X, (size_t)nx * h->ldx), (delete h, code));
+  KM_TRY(dalloc(&h->qn, nx), (delete h, code));
+  KM_TRY(dalloc(&h->xn, nx), (delete h, code));
+  if (bf16) KM_TRY(cudaMalloc(&h->Xb, (size_t)nx * h->ldb * 2), (delete h, code));
+  if (split) KM_TRY(cudaMalloc(&h->Xl, (size_t)nx * h->ldb * 2), (delete h, code));
+  if (h->streaming) {
+    KM_TRY(dalloc(&h->X2, (size_t)nx * h->ldx), (delete h, code));
+    // the copies write d of ldx columns: the padding stays zero
+    KM_TRY(cudaMemset(h->X, 0, sizeof(float) * (size_t)nx * h->ldx), (delete h, code));
+    KM_TRY(cudaMemset(h->X2, 0, sizeof(float) * (size_t)nx * h->ldx), (delete h, code));
+    KM_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), (delete h, code));
+    for (int b = 0; b < 2; ++b) {
+      KM_TRY(cudaEventCreateWithFlags(&h->ev_copied[b], cudaEventDisableTiming), (delete h, code));
+      KM_TRY(cudaEventCreateWithFlags(&h->ev_free[b], cudaEventDisableTiming), (delete h, code));
+    }
+    KM_TRY(dalloc(&h->accS, (size_t)k * d), (delete h, code));
+    KM_TRY(dalloc(&h->accQ, k), (delete h, code));
+    KM_TRY(dalloc(&h->accN, k), (delete h, code));
+  }
   if (h->mini) {
     KM_TRY(dalloc(&h->perm, n), (delete h, code));
     KM_TRY(dalloc(&h->Xw, (size_t)h->m_mb * h->ldx), (delete h, code));
@@ -280,26 +321,32 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(dalloc(&h->cmax, 1), (delete h, code));
   if (bf16) KM_TRY(dalloc(&h->cinit, (size_t)round_up(k, kCenterPad)), (delete h, code));
   const long long na = h->n_act;
-  KM_TRY(dalloc(&h->labels, na), (delete h, code));
+  const long long nl = h->streaming ? n : na;  // labels of every row when streaming
+  KM_TRY(dalloc(&h->labels, nl), (delete h, code));
   KM_TRY(dalloc(&h->rr_list, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_count, 3), (delete h, code));
   KM_TRY(dalloc(&h->rr_list2, na), (delete h, code));
   KM_TRY(dalloc(&h->rr_hi2, na), (delete h, code));
   if (bf16) {
+    // flagged points are ~1-2% of the rows for the split tier and ~1/3 for plain BF16; the
+    // compact copies hold an eighth (split) or half (plain) of the rows, at least 1024, and any
+    // excess takes the full rescan
+    h->cand_cap = std::min(na, std::max<long long>(1024, split ? na / 8 : na / 2));
+    const long long cc = h->cand_cap;
     KM_TRY(dalloc(&h->rr_over, na), (delete h, code));
     KM_TRY(dalloc(&h->thr_full, na), (delete h, code));
-    KM_TRY(dalloc(&h->thr_c, na), (delete h, code));
-    KM_TRY(cudaMalloc(&h->XbC, (size_t)na * h->ldb * 2), (delete h, code));
-    if (split) KM_TRY(cudaMalloc(&h->XlC, (size_t)na * h->ldb * 2), (delete h, code));
-    KM_TRY(dalloc(&h->cand, (size_t)na * kMaxCand), (delete h, code));
-    KM_TRY(dalloc(&h->cand_cnt, na), (delete h, code));
+    KM_TRY(dalloc(&h->thr_c, cc), (delete h, code));
+    KM_TRY(cudaMalloc(&h->XbC, (size_t)cc * h->ldb * 2), (delete h, code));
+    if (split) KM_TRY(cudaMalloc(&h->XlC, (size_t)cc * h->ldb * 2), (delete h, code));
+    KM_TRY(dalloc(&h->cand, (size_t)cc * kMaxCand), (delete h, code));
+    KM_TRY(dalloc(&h->cand_cnt, cc), (delete h, code));
   }
   KM_TRY(dalloc(&h->rr_stats, 2), (delete h, code));
   KM_TRY(dalloc(&h->err, 1), (delete h, code));
   KM_TRY(dalloc(&h->stop, 1), (delete h, code));
   KM_TRY(dalloc(&h->loopf, 2), (delete h, code));
   KM_TRY(dalloc(&h->iters_done, 1), (delete h, code));
-  KM_TRY(cudaMemset(h->labels, 0, sizeof(int) * na), (delete h, code));
+  KM_TRY(cudaMemset(h->labels, 0, sizeof(int) * nl), (delete h, code));
   KM_TRY(cudaMemset(h->rr_stats, 0, sizeof(unsigned long long) * 2), (delete h, code));
   KM_TRY(cudaMemset(h->err, 0, sizeof(int)), (delete h, code));
   // update work space
@@ -349,6 +396,16 @@ cudaError_t order_after_default_stream(kmgb_handle* h) {
 // Upload (or copy) the data set and compute its per-point norms and BF16 copy.
 int set_data(kmgb_handle* h, const float* X, bool on_device) {
   const int code = KMEANS_ERROR_BUILDDATA;
+  if (h->streaming) {
+    if (on_device) {
+      set_err("kmgb_set_data: host-streamed tiles read the data set from host memory");
+      return code;
+    }
+    h->Xhost = X;  // read tile by tile during every run
+    h->have_data = true;
+    h->iter_base = 0;
+    return 0;
+  }
   if (on_device) KM_TRY(order_after_default_stream(h), code);
   const size_t row_bytes = sizeof(float) * h->d;
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
@@ -469,10 +526,12 @@ int step(kmgb_handle* h, int slot) {
       // BF16 tiers: a second tensor-core pass over the flagged rows records every center whose
       // key reaches the point's floor (best - 2E); those few candidates are resolved in FP64.
       // Points with more than kMaxCand candidates take the full rescan below.
-      KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, na, Xba, Xla, h->ldb, h->thr_full,
-                                   h->XbC, Xla ? h->XlC : nullptr, h->thr_c, h->stop, s),
+      KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, Xba, Xla, h->ldb,
+                                   h->thr_full, h->XbC, Xla ? h->XlC : nullptr, h->thr_c,
+                                   h->rr_over, h->rr_count + 1, h->stop, s),
              KMEANS_ERROR_CLOSEST_CENTERS);
       AssignArgs c2 = a;
+      c2.n = h->cand_cap;
       c2.labels = nullptr;
       c2.certify = 0;
       c2.thr_out = nullptr;
@@ -484,7 +543,7 @@ int step(kmgb_handle* h, int slot) {
       KM_TRY(launch_assign_bf16(h->XbC, Xla ? h->XlC : nullptr, h->ldb, h->Cb, h->Cl, h->ldb, c2,
                                 s),
              KMEANS_ERROR_CLOSEST_CENTERS);
-      KM_TRY(launch_resolve_candidates(h->rr_list, h->rr_count, na, h->cand, h->cand_cnt, Xa,
+      KM_TRY(launch_resolve_candidates(h->rr_list, h->rr_count, h->cand_cap, h->cand, h->cand_cnt, Xa,
                                        h->ldx, h->Cop, h->ldx, h->cn, h->d, h->labels, h->rr_over,
                                        h->rr_count + 1, h->stop, s),
              KMEANS_ERROR_CLOSEST_CENTERS);
@@ -505,6 +564,140 @@ int step(kmgb_handle* h, int slot) {
   // cluster centers + compactness (kmeans.cpp:1018-1104)
   KM_TRY(launch_update(Xa, qna, h->labels, h->C, h->ldx, h->opt.empty_policy, h->uw,
                        h->sse_dev + slot, s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  KM_TRY(h->pmark(4), KMEANS_ERROR_CLUSTER_CENTERS);
+  if (h->prof) ++h->pused;
+  return 0;
+}
+
+// One Lloyd iteration over host-streamed tiles: the centers are prepared once, then every tile
+// is copied (copy stream, two buffers), normed, converted, assigned, re-ranked and accumulated
+// (canonical per-tile sums into FP64); the centers, SSE and stop rule come from the totals.
+int step_stream(kmgb_handle* h, int slot) {
+  cudaStream_t s = h->stream, cs = h->copy_stream;
+  const bool tc = h->opt.assign_tier != KMGB_ASSIGN_FP32;
+  KM_TRY(h->pmark(0), KMEANS_ERROR_RESET);
+  KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
+  KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
+                             h->stop, h->cinit, h->Cl),
+         KMEANS_ERROR_RESET);
+  KM_TRY(cudaMemsetAsync(h->accS, 0, sizeof(double) * (size_t)h->k * h->d, s), KMEANS_ERROR_RESET);
+  KM_TRY(cudaMemsetAsync(h->accQ, 0, sizeof(double) * h->k, s), KMEANS_ERROR_RESET);
+  KM_TRY(cudaMemsetAsync(h->accN, 0, sizeof(int) * h->k, s), KMEANS_ERROR_RESET);
+  KM_TRY(h->pmark(1), KMEANS_ERROR_RESET);
+  const long long T = h->tile_rows;
+  const long long ntiles = (h->n + T - 1) / T;
+  const size_t row_bytes = sizeof(float) * h->d;
+  for (long long t = 0; t < ntiles; ++t) {
+    const long long r0 = t * T;
+    const long long nt = std::min(T, h->n - r0);
+    const int b = (int)(t & 1);
+    float* Xt = b ? h->X2 : h->X;
+    // copy the tile once the buffer's previous tile has been consumed
+    KM_TRY(cudaStreamWaitEvent(cs, h->ev_free[b], 0), KMEANS_ERROR_COPY_TILE);
+    if (h->ldx == h->d)
+      KM_TRY(cudaMemcpyAsync(Xt, h->Xhost + (size_t)r0 * h->d, row_bytes * nt,
+                             cudaMemcpyHostToDevice, cs),
+             KMEANS_ERROR_COPY_TILE);
+    else
+      KM_TRY(cudaMemcpy2DAsync(Xt, sizeof(float) * h->ldx, h->Xhost + (size_t)r0 * h->d, row_bytes,
+                               row_bytes, nt, cudaMemcpyHostToDevice, cs),
+             KMEANS_ERROR_COPY_TILE);
+    KM_TRY(cudaEventRecord(h->ev_copied[b], cs), KMEANS_ERROR_COPY_TILE);
+    KM_TRY(cudaStreamWaitEvent(s, h->ev_copied[b], 0), KMEANS_ERROR_COPY_TILE);
+    KM_TRY(launch_point_norms(Xt, h->ldx, nt, h->d, h->qn, h->xn, s), KMEANS_ERROR_COPY_TILE);
+    if (tc)
+      KM_TRY(launch_to_bf16(Xt, h->ldx, nt, h->d, h->Xb, h->ldb, s, h->stop, h->Xl),
+             KMEANS_ERROR_COPY_TILE);
+    KM_TRY(cudaMemsetAsync(h->rr_count, 0, 3 * sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS);
+    int* lab = h->labels + r0;
+    AssignArgs a{};
+    a.cn = h->cn;
+    a.xnorm = h->xn;
+    a.cmax = h->cmax;
+    a.labels = lab;
+    a.rerank_list = h->rr_list;
+    a.rerank_count = h->rr_count;
+    a.err = h->err;
+    a.n = nt;
+    a.k = h->k;
+    a.d = h->d;
+    a.certify = h->opt.certify;
+    a.stop = h->stop;
+    a.cinit = h->cinit;
+    if (tc) {
+      a.gamma = assign_bf16_gamma(h->d);
+      a.thr_out = h->opt.certify ? h->thr_full : nullptr;
+      KM_TRY(launch_assign_bf16(h->Xb, h->Xl, h->ldb, h->Cb, h->Cl, h->ldb, a, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+    } else {
+      a.gamma = assign_fp32_gamma(h->d);
+      KM_TRY(launch_assign_fp32(Xt, h->ldx, h->Cop, h->ldx, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
+    }
+    if (h->opt.certify) {
+      RerankArgs r{};
+      r.X = Xt;
+      r.ldx = h->ldx;
+      r.C = h->Cop;
+      r.ldc = h->ldx;
+      r.cn = h->cn;
+      r.list = h->rr_list;
+      r.count = h->rr_count;
+      r.labels = lab;
+      r.stats = h->rr_stats;
+      r.n = nt;
+      r.k = h->k;
+      r.d = h->d;
+      r.mode = 0;
+      r.max_list = h->n_act;
+      r.stop = h->stop;
+      if (tc) {
+        KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, h->Xb, h->Xl, h->ldb,
+                                     h->thr_full, h->XbC, h->Xl ? h->XlC : nullptr, h->thr_c,
+                                     h->rr_over, h->rr_count + 1, h->stop, s),
+               KMEANS_ERROR_CLOSEST_CENTERS);
+        AssignArgs c2 = a;
+        c2.n = h->cand_cap;
+        c2.labels = nullptr;
+        c2.certify = 0;
+        c2.thr_out = nullptr;
+        c2.n_dev = h->rr_count;
+        c2.row0 = 0;
+        c2.thr_in = h->thr_c;
+        c2.cand = h->cand;
+        c2.cand_cnt = h->cand_cnt;
+        KM_TRY(launch_assign_bf16(h->XbC, h->Xl ? h->XlC : nullptr, h->ldb, h->Cb, h->Cl, h->ldb,
+                                  c2, s),
+               KMEANS_ERROR_CLOSEST_CENTERS);
+        KM_TRY(launch_resolve_candidates(h->rr_list, h->rr_count, h->cand_cap, h->cand, h->cand_cnt,
+                                         Xt, h->ldx, h->Cop, h->ldx, h->cn, h->d, lab, h->rr_over,
+                                         h->rr_count + 1, h->stop, s),
+               KMEANS_ERROR_CLOSEST_CENTERS);
+        r.list = h->rr_over;
+        r.count = h->rr_count + 1;
+      }
+      KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 2, h->rr_hi2, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+      r.list = h->rr_list2;
+      r.count = h->rr_count + 2;
+      r.stats = nullptr;
+      KM_TRY(launch_rerank_exact(r, h->rr_hi2, s), KMEANS_ERROR_CLOSEST_CENTERS);
+      KM_TRY(launch_count_stats(h->rr_count, tc ? 1 : 0, h->rr_stats, h->stop, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+    }
+    // this tile's canonical sums into the run's FP64 totals (tiles in order)
+    UpdateWork w = h->uw;
+    w.n = nt;
+    plan_update_tiles(nt, h->k, &w.tile_pts, &w.ntiles);
+    w.max_pieces = nt / kSumPiece + h->k + 1;
+    KM_TRY(launch_stream_accumulate(Xt, h->ldx, h->qn, lab, w, h->accS, h->accN, h->accQ, s),
+           KMEANS_ERROR_CLUSTER_CENTERS);
+    KM_TRY(cudaEventRecord(h->ev_free[b], s), KMEANS_ERROR_CLUSTER_CENTERS);
+  }
+  KM_TRY(h->pmark(2), KMEANS_ERROR_CLOSEST_CENTERS);
+  KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
+  KM_TRY(launch_stream_finalize(h->accS, h->accN, h->accQ, h->C, h->ldx, h->opt.empty_policy,
+                                h->uw, h->sse_dev + slot, s),
          KMEANS_ERROR_CLUSTER_CENTERS);
   KM_TRY(h->pmark(4), KMEANS_ERROR_CLUSTER_CENTERS);
   if (h->prof) ++h->pused;
@@ -541,6 +734,18 @@ int run(kmgb_handle* h, int iters, double criterion) {
   // Every iteration is enqueued; the SSE reduction evaluates the stop rule on the device and
   // the kernels of later iterations return at once after it fires.
   for (int it = 0; it < iters; ++it) {
+    if (h->streaming) {
+      // a streamed iteration copies the whole data set: look at the stop flag between
+      // iterations so that a converged run issues no further copies
+      int rc = step_stream(h, it);
+      if (rc) return rc;
+      int stop = 0;
+      KM_TRY(cudaMemcpyAsync(&stop, h->stop, sizeof(int), cudaMemcpyDeviceToHost, h->stream),
+             KMEANS_ERROR_COMPUTE);
+      KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);
+      if (stop) break;
+      continue;
+    }
     int rc = step(h, it);
     if (rc) return rc;
   }

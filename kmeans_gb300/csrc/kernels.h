@@ -73,12 +73,13 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, fl
                                 cudaStream_t s);
 // FP64 stage over list2 (one CTA per point), candidates bounded by hi2.
 cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s);
-// Candidate re-rank of the BF16 tiers: compact copy of the flagged rows, then FP64 resolution
-// of their recorded candidates (overflowing points are appended to `over`).
-cudaError_t launch_gather_flagged(const int* list, const int* count, long long max_list,
+// Candidate re-rank of the BF16 tiers: compact copy of up to `cap` flagged rows (the rest go to
+// `over`), then FP64 resolution of their recorded candidates (overflowing points are appended
+// to `over`).
+cudaError_t launch_gather_flagged(const int* list, const int* count, long long cap,
                                   const void* Xb, const void* Xl, long long ldb, const float* thr,
-                                  void* XbC, void* XlC, float* thrC, const int* stop,
-                                  cudaStream_t s);
+                                  void* XbC, void* XlC, float* thrC, int* over, int* over_count,
+                                  const int* stop, cudaStream_t s);
 cudaError_t launch_resolve_candidates(const int* list, const int* count, long long max_list,
                                       const int* cand, const int* cand_cnt, const float* X,
                                       long long ldx, const float* C, long long ldc, const float* cn,
@@ -145,6 +146,15 @@ template <typename T>
 cudaError_t launch_finalize_acc(const double* acc, const int* acc_counts, int k, int d, T* centers,
                                 int* counts, cudaStream_t s);
 void plan_update_tiles(long long n, int k, int* tile_pts, int* ntiles);
+// Host-streamed tiles: per tile, label sort + canonical piece sums (with sum of ||x||^2) added to
+// FP64 accumulators accS[k][d], accN[k], accQ[k]; after the last tile, centers, SSE and the stop
+// rule from the accumulators.
+cudaError_t launch_stream_accumulate(const float* X, long long ldx, const double* qn,
+                                     const int* labels, const UpdateWork& w, double* accS,
+                                     int* accN, double* accQ, cudaStream_t s);
+cudaError_t launch_stream_finalize(const double* accS, const int* accN, const double* accQ,
+                                   float* C, long long ldc, int empty_policy, const UpdateWork& w,
+                                   double* sse_out, cudaStream_t s);
 
 // Mini-batch gather: rows perm[(start + r) mod m] of Xsrc into Xdst (m_mb rows).
 cudaError_t launch_gather_rows(const float* Xsrc, long long ldx, const int* perm, long long m,

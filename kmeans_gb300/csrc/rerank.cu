@@ -344,18 +344,24 @@ __global__ void count_stats_kernel(const int* counts, int full_idx, unsigned lon
 }
 
 // Copies the BF16 rows (and residual rows) of the flagged points into a compact buffer, row
-// `slot` for list[slot], with the point's candidate floor. One warp per row, 16-byte moves.
+// `slot` for list[slot], with the point's candidate floor. One warp per row, 16-byte moves. The
+// compact buffer holds `cap` rows; flagged points beyond it go straight to `over` (the full
+// rescan), so any number of flagged points is settled exactly.
 __global__ void gather_flagged_kernel(const int* __restrict__ list, const int* __restrict__ count,
-                                      long long max_list, const uint4* __restrict__ Xb,
+                                      long long cap, const uint4* __restrict__ Xb,
                                       const uint4* __restrict__ Xl, long long row_vec,
                                       const float* __restrict__ thr, uint4* __restrict__ XbC,
                                       uint4* __restrict__ XlC, float* __restrict__ thrC,
+                                      int* __restrict__ over, int* __restrict__ over_count,
                                       const int* stop) {
   if (stopped(stop)) return;
-  const long long cnt = min((long long)*(volatile const int*)count, max_list);
+  const long long total = *(volatile const int*)count;
+  const long long cnt = min(total, cap);
   const int lane = threadIdx.x & 31;
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long slot = cap + w0 * 32 + lane; slot < total; slot += nw * 32)
+    over[atomicAdd(over_count, 1)] = list[slot];
   for (long long slot = w0; slot < cnt; slot += nw) {
     const long long pt = list[slot];
     for (long long v = lane; v < row_vec; v += 32) {
@@ -500,14 +506,15 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
 }
 }  // namespace
 
-cudaError_t launch_gather_flagged(const int* list, const int* count, long long max_list,
+cudaError_t launch_gather_flagged(const int* list, const int* count, long long cap,
                                   const void* Xb, const void* Xl, long long ldb, const float* thr,
-                                  void* XbC, void* XlC, float* thrC, const int* stop,
-                                  cudaStream_t s) {
+                                  void* XbC, void* XlC, float* thrC, int* over, int* over_count,
+                                  const int* stop, cudaStream_t s) {
   if ((ldb * 2) % 16) return cudaErrorInvalidValue;
   gather_flagged_kernel<<<152 * 8, 256, 0, s>>>(
-      list, count, max_list, reinterpret_cast<const uint4*>(Xb), reinterpret_cast<const uint4*>(Xl),
-      ldb * 2 / 16, thr, reinterpret_cast<uint4*>(XbC), reinterpret_cast<uint4*>(XlC), thrC, stop);
+      list, count, cap, reinterpret_cast<const uint4*>(Xb), reinterpret_cast<const uint4*>(Xl),
+      ldb * 2 / 16, thr, reinterpret_cast<uint4*>(XbC), reinterpret_cast<uint4*>(XlC), thrC, over,
+      over_count, stop);
   count_launches(1);
   return cudaGetLastError();
 }

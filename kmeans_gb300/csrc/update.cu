@@ -531,6 +531,66 @@ __global__ void accumulate_kernel(const double* __restrict__ part, const int* __
   if (lane == 0) acc_counts[j] += label_off[j + 1] - label_off[j];
 }
 
+// Host-streamed tiles: add this tile's canonical per-center sums, member counts and sum of
+// ||x||^2 to the run's FP64 accumulators (the tile's pieces in piece order, then one addition per
+// tile, tiles in order).
+__global__ void accumulate_stream_kernel(const double* __restrict__ part,
+                                         const double* __restrict__ partq,
+                                         const int* __restrict__ label_off,
+                                         const int* __restrict__ pstart, int k, int d,
+                                         double* __restrict__ accS, int* __restrict__ accN,
+                                         double* __restrict__ accQ, const int* stop) {
+  if (stopped(stop)) return;
+  const int j = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (j >= k) return;
+  const int p0 = pstart[j], p1 = pstart[j + 1];
+  for (int c = lane; c < d; c += 32) {
+    double s = 0.0;
+    for (int p = p0; p < p1; ++p) s += part[(size_t)p * d + c];
+    accS[(size_t)j * d + c] += s;
+  }
+  if (lane == 0) {
+    double q = 0.0;
+    for (int p = p0; p < p1; ++p) q += partq[p];
+    accQ[j] += q;
+    accN[j] += label_off[j + 1] - label_off[j];
+  }
+}
+
+// Host-streamed tiles: centers and SSE terms from the run's accumulators, one warp per (center,
+// group of 32 dimensions) as finalize_kernel.
+__global__ void finalize_stream_kernel(const double* __restrict__ accS, const int* __restrict__ accN,
+                                       const double* __restrict__ accQ, int k, int d,
+                                       float* __restrict__ C, long long ldc, int empty_policy,
+                                       double* __restrict__ sse_k, const int* stop) {
+  if (stopped(stop)) return;
+  const int groups = (d + 31) / 32;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= (long long)k * groups) return;
+  const int j = (int)(wid / groups), g = (int)(wid - (long long)j * groups);
+  const int c = g * 32 + lane;
+  const long long n = accN[j];
+  double sse = 0.0;
+  if (c < d) {
+    const double s = accS[(size_t)j * d + c];
+    float mu;
+    if (n > 0) {
+      mu = __double2float_rn(__ddiv_rn(s, (double)n));
+      const double m = (double)mu;
+      sse = fma((double)n * m, m, -2.0 * m * s);
+    } else if (empty_policy == 1) {
+      mu = C[(size_t)j * ldc + c];
+    } else {
+      mu = __int_as_float(0x7fc00000);
+    }
+    C[(size_t)j * ldc + c] = mu;
+  }
+  for (int o = 16; o > 0; o >>= 1) sse += __shfl_xor_sync(0xffffffffu, sse, o);
+  if (lane == 0) sse_k[(size_t)j * groups + g] = (n > 0) ? sse + (g == 0 ? accQ[j] : 0.0) : 0.0;
+}
+
 template <typename T>
 __global__ void finalize_acc_kernel(const double* __restrict__ acc, const int* __restrict__ acc_counts,
                                     int k, int d, T* __restrict__ centers, int* __restrict__ counts) {
@@ -571,6 +631,41 @@ template <typename T>
 cudaError_t launch_finalize_acc(const double* acc, const int* acc_counts, int k, int d, T* centers,
                                 int* counts, cudaStream_t s) {
   finalize_acc_kernel<T><<<152 * 4, 256, 0, s>>>(acc, acc_counts, k, d, centers, counts); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stream_accumulate(const float* X, long long ldx, const double* qn,
+                                     const int* labels, const UpdateWork& w, double* accS,
+                                     int* accN, double* accQ, cudaStream_t s) {
+  if (w.n <= 0 || w.k <= 0) return cudaSuccess;
+  KMGB_CUDA_TRY(sort_by_label(labels, w, s));
+  long long warps = w.max_pieces < 152LL * 64 ? w.max_pieces : 152LL * 64;
+  if (w.ldx % 4 == 0 && w.d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
+    piece_sums_vec4_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, w.partq, w.stop);
+  else
+    piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, w.partq, w.stop);
+  kmgb::count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  accumulate_stream_kernel<<<(unsigned)(((long long)w.k * 32 + 255) / 256), 256, 0, s>>>(
+      w.part, w.partq, w.label_off, w.piece_cnt, w.k, w.d, accS, accN, accQ, w.stop);
+  kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stream_finalize(const double* accS, const int* accN, const double* accQ,
+                                   float* C, long long ldc, int empty_policy, const UpdateWork& w,
+                                   double* sse_out, cudaStream_t s) {
+  const int k = w.k;
+  const long long fin_warps = (long long)k * ((w.d + 31) / 32);
+  finalize_stream_kernel<<<(unsigned)((fin_warps * 32 + 255) / 256), 256, 0, s>>>(
+      accS, accN, accQ, k, w.d, C, ldc, empty_policy, w.sse_k, w.stop);
+  kmgb::count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, (int)fin_warps, sse_out, w.stop, w.criterion,
+                                       w.sse_prev, w.rel_out, w.iters_done);
+  kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

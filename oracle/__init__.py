@@ -141,6 +141,8 @@ def lib():
         L.orc_sse_d.restype = f64
         L.orc_lloyd_d.argtypes = [P, i64, i32, i32, P, i32, f64, f32, i32, i32, P, P, P, P]
         L.orc_lloyd_d.restype = i32
+        L.orc_lloyd_tiled.argtypes = [P, i64, i32, i32, P, i32, f64, i32, i32, i64, P, P, P, P]
+        L.orc_lloyd_tiled.restype = i32
         L.orc_closest_expansion.argtypes = [P, i32, i32, P, i32, P, P]
         L.orc_closest_expansion_d.argtypes = [P, i32, i32, P, i32, P, P]
         L.orc_row_transform_min_f.argtypes = [i32, i32, i32, P, P, P, P]
@@ -212,6 +214,22 @@ def sse(X, labels, centers) -> float:
     m, d = X.shape
     labels = np.ascontiguousarray(labels, dtype=np.int32)
     return float(lib().orc_sse(_p(X), m, d, _p(labels), _p(centers)))
+
+
+def lloyd_tiled(X, init, max_iters, tile_rows, criterion=-1.0, empty_policy=0, piece=PIECE):
+    """Full-batch loop with the host-streamed tiles' update order (tiles of `tile_rows` rows).
+    Returns (status, centers KxD, labels, sse[iters], iters)."""
+    X, init = _f32(X), _f32(init)
+    m, d = X.shape
+    k = init.shape[0]
+    cen = np.empty((k, d), dtype=np.float32)
+    lab = np.empty(m, dtype=np.int32)
+    sse_ = np.zeros(max(max_iters, 1), dtype=np.float64)
+    its = C.c_int(0)
+    st = lib().orc_lloyd_tiled(_p(X), m, d, k, _p(init), max_iters, float(criterion),
+                               empty_policy, piece, int(tile_rows), _p(cen), _p(lab), _p(sse_),
+                               C.byref(its))
+    return st, cen, lab, sse_[:its.value], its.value
 
 
 def lloyd(X, init, max_iters, criterion=-1.0, mb_fraction=1.0, empty_policy=0, piece=PIECE):

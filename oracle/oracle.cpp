@@ -293,7 +293,67 @@ int lloyd(const T* X, long long m, int d, int k, const T* init, int max_iters, d
   return (rel <= criterion) ? 0 : 13;
 }
 
+// Host-streamed tiles (the reference's out-of-memory path, kmeans.cpp:301-536, 699-818, with
+// one pass per iteration): rows [t*tile, (t+1)*tile) form tile t; each tile's canonical per-center
+// sums (update_rows on the tile: pieces of its label-sorted members, summed from zero in piece
+// order) are added to the FP64 totals one tile at a time, tiles in order; the center is the total
+// over the count, rounded once.
+template <typename T>
+void update_tiled(const T* X, long long m, int d, const int* labels, int k, int piece,
+                  long long tile, const T* old_centers, int empty_policy, T* new_centers) {
+  std::vector<double> total((size_t)k * d, 0.0), sums((size_t)k * d);
+  std::vector<long long> cnt(k, 0), tcnt(k);
+  std::vector<T> scratch((size_t)k * d);
+  for (long long r0 = 0; r0 < m; r0 += tile) {
+    const long long nt = std::min(tile, m - r0);
+    update_rows<T>(X + (size_t)r0 * d, nt, nullptr, d, labels + r0, k, piece, nullptr, 0,
+                   scratch.data(), tcnt.data(), sums.data());
+    for (size_t e = 0; e < total.size(); ++e) total[e] += sums[e];
+    for (int j = 0; j < k; ++j) cnt[j] += tcnt[j];
+  }
+  for (int j = 0; j < k; ++j)
+    for (int t = 0; t < d; ++t) {
+      T v;
+      if (cnt[j] > 0) v = (T)(total[(size_t)j * d + t] / (double)cnt[j]);
+      else if (empty_policy == 1 && old_centers) v = old_centers[(size_t)j * d + t];
+      else v = std::numeric_limits<T>::quiet_NaN();
+      new_centers[(size_t)j * d + t] = v;
+    }
+}
+
+// Full-batch Lloyd loop with the host-streamed tiles' update order.
+template <typename T>
+int lloyd_tiled(const T* X, long long m, int d, int k, const T* init, int max_iters,
+                double criterion, int empty_policy, int piece, long long tile, T* centers_out,
+                int* labels_out, double* sse_out, int* iters_out) {
+  std::vector<T> cur(init, init + (size_t)k * d), nxt((size_t)k * d);
+  std::vector<int> labels(m);
+  double sse_old = 0.0, rel = 1.0;
+  int it = 0;
+  while (it < max_iters && rel > criterion) {
+    assign_rows<T>(X, m, nullptr, d, cur.data(), k, labels.data(), nullptr);
+    update_tiled<T>(X, m, d, labels.data(), k, piece, tile, cur.data(), empty_policy, nxt.data());
+    const double sse = sse_rows<T>(X, m, nullptr, d, labels.data(), nxt.data());
+    rel = std::fabs(sse - sse_old) / std::fabs(sse);
+    sse_old = sse;
+    if (sse_out) sse_out[it] = sse;
+    cur.swap(nxt);
+    ++it;
+  }
+  std::memcpy(centers_out, cur.data(), sizeof(T) * (size_t)k * d);
+  if (labels_out) std::memcpy(labels_out, labels.data(), sizeof(int) * (size_t)m);
+  if (iters_out) *iters_out = it;
+  return (rel <= criterion) ? 0 : 13;
+}
+
 extern "C" {
+
+int orc_lloyd_tiled(const float* X, long long m, int d, int k, const float* init, int max_iters,
+                    double criterion, int empty_policy, int piece, long long tile,
+                    float* centers_out, int* labels_out, double* sse_out, int* iters_out) {
+  return lloyd_tiled<float>(X, m, d, k, init, max_iters, criterion, empty_policy, piece, tile,
+                            centers_out, labels_out, sse_out, iters_out);
+}
 
 void orc_assign(const float* X, long long m, int d, const float* C, int k, int* labels,
                 double* best_out) {

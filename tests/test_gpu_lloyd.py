@@ -55,6 +55,10 @@ def test_near_ties_are_resolved_exactly(km, orc, torch_cuda, tier):
     res = km.lloyd(X, k, init=Cn, max_iters=1, assign_tier=tier)
     check_same(res, orc.lloyd(X, Cn, 1))
     assert res.reranked > 0
+    if tier != 0:
+        # nearly every point is flagged: more than the candidate pass's compact buffer holds
+        # (1024 rows at this size), the excess takes the full rescan
+        assert res.reranked > 2100 and res.reranked_fp64 > 0
 
 
 @pytest.mark.parametrize("tier", TIERS)
@@ -235,3 +239,34 @@ def test_split_tier_certifies_more_than_plain_bf16(km, orc, torch_cuda):
     check_same(r1, ref)
     check_same(r2, ref)
     assert r2.reranked * 5 < r1.reranked
+
+
+@pytest.mark.parametrize("tier", TIERS)
+@pytest.mark.parametrize("tile", [997, 4096, 12000])
+def test_host_streamed_tiles(km, orc, torch_cuda, tier, tile):
+    # the reference's out-of-memory path: X stays in host memory and passes through the GPU in
+    # tiles every iteration; centers follow the tiled canonical order (per-tile sums, tiles in
+    # order), labels are the FP64 arg-min
+    X, _, _ = mixture_numpy(20000, 48, 40, seed=61)
+    init = X[sample_init(len(X), 40, seed=62)]
+    res = km.lloyd(X, 40, init=init, max_iters=5, assign_tier=tier, stream_tile_rows=tile)
+    check_same(res, orc.lloyd_tiled(X, init, 5, tile_rows=tile))
+
+
+def test_host_streamed_tiles_stop_rule_and_odd_width(km, orc, torch_cuda):
+    X, _, _ = mixture_numpy(9000, 37, 20, seed=63)  # width not a multiple of 4: padded rows
+    init = X[sample_init(len(X), 20, seed=64)]
+    res = km.lloyd(X, 20, init=init, max_iters=50, criterion=1e-4, assign_tier=km.ASSIGN_BF16,
+                   stream_tile_rows=2500)
+    ref = orc.lloyd_tiled(X, init, 50, tile_rows=2500, criterion=1e-4)
+    check_same(res, ref)
+    assert res.iterations < 50
+
+
+def test_host_streamed_tiles_reject_device_data_and_mini_batch(km, torch_cuda):
+    X, _, _ = mixture_numpy(5000, 16, 8, seed=65)
+    init = X[sample_init(len(X), 8, seed=66)]
+    with pytest.raises(km.KmeansError):
+        km.lloyd(torch_cuda.from_numpy(X).cuda(), 8, init=init, max_iters=2, stream_tile_rows=1000)
+    with pytest.raises(km.KmeansError):
+        km.lloyd(X, 8, init=init, max_iters=2, stream_tile_rows=1000, mini_batch_fraction=0.5)

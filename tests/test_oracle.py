@@ -134,3 +134,17 @@ def test_port_close_to_oracle(orc):
     _, c2, lab2, sse2, _ = orc.lloyd(X, init, 3)
     assert (lab != lab2).mean() < 1e-3
     np.testing.assert_allclose(sse, sse2, rtol=1e-5)
+
+
+def test_tiled_oracle_with_one_tile_is_the_untiled_loop(orc):
+    from kmeans_gb300.synthetic import mixture_numpy, sample_init
+    X, _, _ = mixture_numpy(3000, 12, 9, seed=44)
+    init = X[sample_init(3000, 9, seed=45)]
+    a = orc.lloyd(X, init, 4)
+    b = orc.lloyd_tiled(X, init, 4, tile_rows=3000)
+    assert a[0] == b[0] and a[4] == b[4]
+    assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+    assert np.array_equal(a[3], b[3])
+    c = orc.lloyd_tiled(X, init, 4, tile_rows=700)  # same labels, centers within rounding
+    assert np.array_equal(a[2], c[2])
+    np.testing.assert_allclose(a[1], c[1], rtol=1e-6)
