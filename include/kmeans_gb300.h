@@ -185,7 +185,7 @@ KMGB_EXPORT kmeansCudaErrorStatus colNormalizeD(const int m, const int n, const 
 enum kmgb_assign_tier {
   KMGB_ASSIGN_FP32 = 0,  /* plain FP32 fused kernel (TMA + FFMA) */
   KMGB_ASSIGN_BF16 = 1,  /* tcgen05 BF16 tensor cores, FP32 accumulate in TMEM (D <= 256) */
-  KMGB_ASSIGN_BF16X3 = 2 /* tcgen05 split BF16: x.c = xh.ch + xh.cl + xl.ch (D <= 128) */
+  KMGB_ASSIGN_BF16X3 = 2 /* tcgen05 split BF16: x.c = xh.ch + xh.cl + xl.ch (D <= 256) */
 };
 
 enum kmgb_empty_policy {

@@ -580,9 +580,9 @@ static size_t xbuf_bytes_for(int d, int planes) {
 
 bool bf16_tc_supported(int d, int planes) {
   if (d <= 0 || d > MAX_D) return false;
-  // two point buffers and a 3-stage C ring must fit the shared memory of a CTA next to the
-  // 3 KB of static variables (barriers, merge slots)
-  return 2 * xbuf_bytes_for(d, planes) + 3 * (size_t)planes * CKB_BYTES + 3072 <= SMEM_CAP;
+  // one point buffer (two when they fit) and a 3-stage C ring must fit the shared memory of a
+  // CTA next to the 3 KB of static variables (barriers, merge slots): D <= 256 in both tiers
+  return xbuf_bytes_for(d, planes) + 3 * (size_t)planes * CKB_BYTES + 3072 <= SMEM_CAP;
 }
 
 float assign_bf16_gamma(int d) {
@@ -629,9 +629,10 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   const size_t xbytes = xbuf_bytes_for(a.d, planes);
   const size_t stage_bytes = (size_t)planes * CKB_BYTES;
   const size_t lim = g_smem_budget;
-  // double-buffer the unit's points (needed to keep the tensor pipe busy across units)
+  // double-buffer the unit's points when that still leaves a 3-stage ring (a single buffer
+  // measured no slower on GB300: the next unit's points are prefetched into L2)
   const int xbufs = (2 * xbytes + 3 * stage_bytes <= lim) ? 2 : 1;
-  if (lim < xbufs * xbytes + 2 * stage_bytes) return cudaErrorInvalidValue;
+  if (lim < xbufs * xbytes + 3 * stage_bytes) return cudaErrorInvalidValue;
   int stages = (int)((lim - xbufs * xbytes) / stage_bytes);
   if (stages > MAX_STAGES) stages = MAX_STAGES;
   const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes;

@@ -34,8 +34,8 @@ def test_c1_config(km, orc, torch_cuda, tier):
                                    (20000, 128, 256), (3001, 17, 1), (2000, 256, 300)])
 @pytest.mark.parametrize("tier", TIERS)
 def test_odd_shapes(km, orc, torch_cuda, n, d, k, tier):
-    if tier == 2 and d > 128:
-        pytest.skip("the split BF16 tier covers D <= 128")
+    if tier != 0 and d > 256:
+        pytest.skip("the tensor-core tiers cover D <= 256")
     X, _, _ = mixture_numpy(n, d, max(k, 1), seed=n + d + k)
     init = X[sample_init(n, k, seed=3)]
     res = km.lloyd(X, k, init=init, max_iters=6, assign_tier=tier)

@@ -25,6 +25,10 @@ def cases():
     X3 = rng.uniform(-1, 1, (n, 64)).astype(np.float32)
     C3 = rng.uniform(-1, 1, (k, 64)).astype(np.float32)
     yield "d64", X3, C3
+    # the widest rows the tiers take (3 x 256 products per element in the split tier)
+    X4 = (rng.standard_normal((n, 256)) * 3 + 20).astype(np.float32)
+    C4 = (X4[rng.integers(0, n, k)] + rng.standard_normal((k, 256)).astype(np.float32))
+    yield "d256", X4, C4.astype(np.float32)
 
 
 @pytest.mark.parametrize("use_split", [False, True])
