@@ -18,12 +18,12 @@
 //     into TMEM (two 256-column accumulator buffers: the epilogue of chunk g overlaps the MMAs of
 //     chunk g+1) and multicasts its commits (stage free, accumulator ready, points free) to both
 //     CTAs. Warp 1 of both CTAs allocates the 512 TMEM columns collectively.
-//   * warps 2-9 (both CTAs) epilogue: two warps per TMEM lane quadrant, each owning 32 points and
-//     128 of the chunk's 256 columns. A thread reads 32 columns at a time (tcgen05.ld), adds
+//   * warps 2.. (both CTAs) epilogue: EPQ warps per TMEM lane quadrant (2 in the split tier, 4 in
+//     the plain tier), each owning 32 points and 256/EPQ of the chunk's 256 columns. A thread reads 32 columns at a time (tcgen05.ld), adds
 //     -||c_j||^2/2 (FP32, FMA pipe) so that arg-min distance = arg-max key, packs the column
 //     within the 32-column block into the 5 low mantissa bits and keeps the two largest keys with
 //     3.5 ALU ops per element. Accumulator buffers are handed back to the leader by remote
-//     mbarrier arrivals. At the end of a unit the two column halves of a point are merged through
+//     mbarrier arrivals. At the end of a unit the column slices of a point are merged through
 //     shared memory (bounded mbarrier handshake).
 // A point is certified when best - second > 2E, E the rigorous bound of the BF16 evaluation
 // (operand rounding, FP32 accumulation, norm rounding, key packing, FP64 reference error);
@@ -42,8 +42,11 @@ constexpr int UNIT = 2 * BM;             // points per pair unit (MMA M)
 constexpr int BN = 256;                  // centers per chunk (MMA N)
 constexpr int BNH = BN / 2;              // centers per CTA per chunk
 constexpr int BK = 64;                   // BF16 per k-block (one 128-byte swizzle row)
-constexpr int NUM_EPI_WARPS = 8;
-constexpr int NTHREADS = 64 + NUM_EPI_WARPS * 32;
+// The epilogue has EPQ warps per TMEM lane quadrant (a template parameter): 2 for the split tier,
+// whose three products per element leave the tensor pipe the longer task (more epilogue warps
+// only take issue slots from the MMA and TMA threads), 4 for the plain tier, whose epilogue is
+// the longer task.
+constexpr int threads_for(int epq) { return 64 + 4 * epq * 32; }
 constexpr uint32_t XKB_BYTES = BM * BK * 2;   // 16 KB: one k-block of one plane of the points
 constexpr uint32_t CKB_BYTES = BNH * BK * 2;  // 16 KB: one k-block of one plane of the centers
 constexpr int MAX_STAGES = 8;
@@ -51,7 +54,7 @@ constexpr int MAX_D = 256;
 constexpr uint32_t TMEM_COLS = 512;           // two 256-column accumulator buffers
 constexpr size_t SMEM_CAP = 227 * 1024;       // upper bound; the device's opt-in limit is queried
 constexpr float kUnusable = -3.0e38f;         // start value of padding / unusable centers
-constexpr int COLS_PER_WARP = BN / 2;         // epilogue: two warps per lane quadrant
+
 static_assert(2 * BN <= (int)TMEM_COLS, "two accumulator buffers");
 static_assert(kCenterPad % BN == 0, "start values are padded to whole chunks");
 
@@ -214,19 +217,26 @@ struct Bars {
   uint64_t merge_full[4], merge_empty[4];
 };
 
-// the column half handed from warp (q, 1) to warp (q, 0) at the end of a unit
+// the column slices handed from warps (q, 1..EPQ-1) to warp (q, 0) at the end of a unit
+template <int EPQ>
 struct MergeSlot {
-  float b1[4][32], b2[4][32];
-  int bblk[4][32], ncand[4][32];
+  float b1[EPQ - 1][4][32], b2[EPQ - 1][4][32];
+  int bblk[EPQ - 1][4][32], ncand[EPQ - 1][4][32];
 };
 
-__global__ void __launch_bounds__(NTHREADS, 1)
+template <int EPQ>
+__global__ void __launch_bounds__(threads_for(EPQ), 1)
 assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmXl,
                    const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmCl,
                    AssignArgs p, int stages, int xbufs, int planes) {
+  constexpr int NUM_EPI_WARPS = 4 * EPQ;
+  constexpr int EPI_PER_QUAD = EPQ;
+  constexpr int COLS_PER_WARP = BN / EPQ;           // columns of a chunk per epilogue warp
+  constexpr int CAND_PER_WARP = kMaxCand / EPQ;     // candidate slots per column slice
+  static_assert(EPQ >= 2 && COLS_PER_WARP % 32 == 0 && CAND_PER_WARP >= 1, "epilogue split");
   extern __shared__ __align__(1024) uint8_t smem[];
   __shared__ __align__(8) Bars bars;
-  __shared__ MergeSlot merge;
+  __shared__ MergeSlot<EPQ> merge;
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_flag;
 
@@ -278,7 +288,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       mbar_init(smem_u32(&bars.c_empty[s]), 1);
     }
     for (int q = 0; q < 4; ++q) {
-      mbar_init(smem_u32(&bars.merge_full[q]), 32);
+      mbar_init(smem_u32(&bars.merge_full[q]), (EPI_PER_QUAD - 1) * 32);
       mbar_init(smem_u32(&bars.merge_empty[q]), 32);
     }
     fence_mbar_init();
@@ -412,7 +422,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     // ------------------------------ epilogue (both CTAs) ------------------------------
     const int e = warp - 2;
     const int q = warp & 3;       // TMEM lane quadrant this warp may access
-    const int h = e >> 2;         // column half of the chunk
+    const int h = e >> 2;         // column slice of the chunk (0 .. EPI_PER_QUAD-1)
     const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16);
     const float cm = p.certify ? __ldg(p.cmax) : 0.0f;
     const uint32_t acc_empty_leader0 = map_to_rank(smem_u32(&bars.acc_empty[0]), 0);
@@ -429,6 +439,10 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       float floor_key = INFINITY;  // candidate mode: record keys >= floor_key
       int ncand = 0;
       if (cand_mode && prow < n_rows) floor_key = __ldg(p.thr_in + p.row0 + prow);
+      // the point's norm bound is needed only after the last chunk: load it now so that its
+      // HBM latency hides behind the unit's chunks
+      const float xn_pt = (p.certify && !cand_mode && h == 0 && prow < n_rows)
+                              ? __ldg(p.xnorm + prow) : 0.0f;
       for (int c = 0; c < nchunks; ++c, ++g) {
         const int b = (int)(g & 1);
         bool ok = mbar_wait(smem_u32(&bars.acc_full[b]), (uint32_t)((g >> 1) & 1), &abort_flag,
@@ -474,13 +488,13 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           }
           if (cand_mode) {
             // second pass over flagged points: every key at or above the floor is a candidate;
-            // each column half records up to kMaxCand/2 in its own half of the point's list
+            // each column slice records up to CAND_PER_WARP in its own part of the point's list
 #pragma unroll
             for (int j = 0; j < 32; ++j) {
               const float key = __uint_as_float((cur[j] & ~0x1Fu) | (uint32_t)j);
               if (key >= floor_key) {
-                if (ncand < kMaxCand / 2 && prow < n_rows)
-                  p.cand[(size_t)(p.row0 + prow) * kMaxCand + h * (kMaxCand / 2) + ncand] =
+                if (ncand < CAND_PER_WARP && prow < n_rows)
+                  p.cand[(size_t)(p.row0 + prow) * kMaxCand + h * CAND_PER_WARP + ncand] =
                       col0 + cb * 32 + j;
                 ++ncand;
               }
@@ -501,49 +515,65 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         }
       }
       if (!alive) break;
-      // ---- merge the two column halves of each point: warp (q, 1) -> warp (q, 0) ----
+      // ---- merge the column slices of each point: warps (q, 1..) -> warp (q, 0) ----
       const uint32_t mfull = smem_u32(&bars.merge_full[q]);
       const uint32_t mempty = smem_u32(&bars.merge_empty[q]);
-      if (h == 1) {
+      if (h > 0) {
         bool ok = lu == 0 || mbar_wait(mempty, (uint32_t)((lu - 1) & 1), &abort_flag, p.err,
                                        KMGB_DEV_TIMEOUT_ACC);
         if (!__all_sync(0xffffffffu, ok)) break;
-        merge.b1[q][lane] = b1;
-        merge.b2[q][lane] = b2;
-        merge.bblk[q][lane] = bblk;
-        merge.ncand[q][lane] = ncand;
+        merge.b1[h - 1][q][lane] = b1;
+        merge.b2[h - 1][q][lane] = b2;
+        merge.bblk[h - 1][q][lane] = bblk;
+        merge.ncand[h - 1][q][lane] = ncand;
         mbar_arrive(mfull);  // release: the writes above (and the candidate list) are visible
         continue;
       }
       bool ok = mbar_wait(mfull, (uint32_t)(lu & 1), &abort_flag, p.err, KMGB_DEV_TIMEOUT_ACC);
       if (!__all_sync(0xffffffffu, ok)) break;
-      const float ob1 = merge.b1[q][lane], ob2 = merge.b2[q][lane];
-      const int obblk = merge.bblk[q][lane], oncand = merge.ncand[q][lane];
+      float ob1[EPI_PER_QUAD - 1], ob2[EPI_PER_QUAD - 1];
+      int obblk[EPI_PER_QUAD - 1], oncand[EPI_PER_QUAD - 1];
+#pragma unroll
+      for (int o = 0; o < EPI_PER_QUAD - 1; ++o) {
+        ob1[o] = merge.b1[o][q][lane];
+        ob2[o] = merge.b2[o][q][lane];
+        obblk[o] = merge.bblk[o][q][lane];
+        oncand[o] = merge.ncand[o][q][lane];
+      }
+      mbar_arrive(mempty);
       if (cand_mode) {
         if (prow < n_rows) {
           int* lst = p.cand + (size_t)(p.row0 + prow) * kMaxCand;
-          const bool over = ncand > kMaxCand / 2 || oncand > kMaxCand / 2;
-          if (!over)  // move the second half's candidates behind the first half's
-            for (int i = 0; i < oncand; ++i) lst[ncand + i] = lst[kMaxCand / 2 + i];
-          p.cand_cnt[p.row0 + prow] = over ? -1 : ncand + oncand;
+          bool over = ncand > CAND_PER_WARP;
+          int total = over ? 0 : ncand;
+#pragma unroll
+          for (int o = 0; o < EPI_PER_QUAD - 1; ++o) {
+            over = over || oncand[o] > CAND_PER_WARP;
+            if (!over) {  // move slice o+1's candidates behind the earlier slices' (dst <= src)
+              for (int i = 0; i < oncand[o]; ++i) lst[total + i] = lst[(o + 1) * CAND_PER_WARP + i];
+              total += oncand[o];
+            }
+          }
+          p.cand_cnt[p.row0 + prow] = over ? -1 : total;
         }
-        mbar_arrive(mempty);
         continue;
       }
-      mbar_arrive(mempty);
-      // top-2 of the union; on equal best keys the first half's block is kept (such a point has
-      // a zero margin and is never certified)
-      const float nb2 = fmaxf(fminf(b1, ob1), fmaxf(b2, ob2));
-      if (ob1 > b1) bblk = obblk;
-      b1 = fmaxf(b1, ob1);
-      b2 = nb2;
+      // top-2 of the union, slices in order; on equal best keys the earlier slice's block is
+      // kept (such a point has a zero margin and is never certified)
+#pragma unroll
+      for (int o = 0; o < EPI_PER_QUAD - 1; ++o) {
+        const float nb2 = fmaxf(fminf(b1, ob1[o]), fmaxf(b2, ob2[o]));
+        if (ob1[o] > b1) bblk = obblk[o];
+        b1 = fmaxf(b1, ob1[o]);
+        b2 = nb2;
+      }
       const long long pt = prow;
       if (pt < n_rows) {
         const bool none = !(b1 > -1.0e38f);  // no usable center at all
         const int label = (bblk < 0 || none) ? 0 : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
         p.labels[pt] = label;
         if (p.certify) {
-          const float eb = bound_acc(__ldg(p.xnorm + pt), cm, p.d, planes);
+          const float eb = bound_acc(xn_pt, cm, p.d, planes);
           if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
             p.rerank_list[slot] = (int)pt;
@@ -567,9 +597,53 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   }
 }
 
+// per kernel variant: co-resident clusters of two CTAs and the dynamic shared memory a CTA may use
+struct VariantInfo {
+  bool ready = false;
+  int max_pairs = 0;
+  size_t smem_budget = 0;  // 1 KB aligned
+  size_t static_bytes = 0;
+};
+VariantInfo g_variant[5];
 int g_num_sms = 0;
-int g_max_pairs = 0;       // co-resident clusters of two CTAs
-size_t g_smem_budget = 0;  // dynamic shared memory a CTA of this kernel may use (1 KB aligned)
+
+template <int EPQ>
+cudaError_t prepare_variant(VariantInfo& vi) {
+  if (vi.ready) return cudaSuccess;
+  int dev = 0, optin = 0;
+  KMGB_CUDA_TRY(cudaGetDevice(&dev));
+  KMGB_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+  KMGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel<EPQ>));
+  // the dynamic area starts on the next 1 KB boundary after the static variables
+  vi.static_bytes = (fa.sharedSizeBytes + 1023) / 1024 * 1024;
+  size_t budget = (size_t)optin > vi.static_bytes ? (size_t)optin - vi.static_bytes : 0;
+  if (budget > SMEM_CAP) budget = SMEM_CAP;
+  KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel<EPQ>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
+  vi.smem_budget = budget;
+  cudaLaunchConfig_t qc = {};
+  qc.gridDim = dim3((unsigned)(g_num_sms / 2 * 2));
+  qc.blockDim = dim3(threads_for(EPQ));
+  qc.dynamicSmemBytes = budget;
+  cudaLaunchAttribute qa[1];
+  qa[0].id = cudaLaunchAttributeClusterDimension;
+  qa[0].val.clusterDim.x = 2;
+  qa[0].val.clusterDim.y = 1;
+  qa[0].val.clusterDim.z = 1;
+  qc.attrs = qa;
+  qc.numAttrs = 1;
+  KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&vi.max_pairs, assign_bf16_kernel<EPQ>, &qc));
+  if (vi.max_pairs <= 0) return cudaErrorInvalidConfiguration;
+  vi.ready = true;
+  return cudaSuccess;
+}
+
+// epilogue warps per lane quadrant for a tier
+constexpr int epq_for(int planes) { return planes > 1 ? 2 : 4; }
+// static shared memory of a variant: barriers + merge slots (+ slack), 1 KB aligned
+constexpr size_t static_smem_for(int epq) { return epq > 2 ? 7168 : 3072; }
 
 }  // namespace
 
@@ -580,9 +654,10 @@ static size_t xbuf_bytes_for(int d, int planes) {
 
 bool bf16_tc_supported(int d, int planes) {
   if (d <= 0 || d > MAX_D) return false;
-  // one point buffer (two when they fit) and a 3-stage C ring must fit the shared memory of a
-  // CTA next to the 3 KB of static variables (barriers, merge slots): D <= 256 in both tiers
-  return xbuf_bytes_for(d, planes) + 3 * (size_t)planes * CKB_BYTES + 3072 <= SMEM_CAP;
+  // one point buffer (two when they fit) and a C ring of at least two stages must fit the shared
+  // memory of a CTA next to the static variables (barriers, merge slots): D <= 256 in both tiers
+  return xbuf_bytes_for(d, planes) + 2 * (size_t)planes * CKB_BYTES +
+             static_smem_for(epq_for(planes)) <= SMEM_CAP;
 }
 
 float assign_bf16_gamma(int d) {
@@ -598,41 +673,17 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
       (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15) ||
       (reinterpret_cast<uintptr_t>(Xl) & 15) || (reinterpret_cast<uintptr_t>(Cl) & 15))
     return cudaErrorInvalidValue;
-  if (g_num_sms == 0) {
-    int dev = 0, optin = 0;
-    KMGB_CUDA_TRY(cudaGetDevice(&dev));
-    KMGB_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
-    KMGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    cudaFuncAttributes fa;
-    KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel));
-    // the dynamic area starts on the next 1 KB boundary after the static variables
-    const size_t static_bytes = (fa.sharedSizeBytes + 1023) / 1024 * 1024;
-    size_t budget = (size_t)optin > static_bytes ? (size_t)optin - static_bytes : 0;
-    if (budget > SMEM_CAP) budget = SMEM_CAP;
-    KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
-    g_smem_budget = budget;
-    cudaLaunchConfig_t qc = {};
-    qc.gridDim = dim3((unsigned)(g_num_sms / 2 * 2));
-    qc.blockDim = dim3(NTHREADS);
-    qc.dynamicSmemBytes = budget;
-    cudaLaunchAttribute qa[1];
-    qa[0].id = cudaLaunchAttributeClusterDimension;
-    qa[0].val.clusterDim.x = 2;
-    qa[0].val.clusterDim.y = 1;
-    qa[0].val.clusterDim.z = 1;
-    qc.attrs = qa;
-    qc.numAttrs = 1;
-    KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&g_max_pairs, assign_bf16_kernel, &qc));
-    if (g_max_pairs <= 0) return cudaErrorInvalidConfiguration;
-  }
+  const int epq = epq_for(planes);
+  VariantInfo& vi = g_variant[epq];
+  if (epq == 2) KMGB_CUDA_TRY(prepare_variant<2>(vi));
+  else KMGB_CUDA_TRY(prepare_variant<4>(vi));
   const size_t xbytes = xbuf_bytes_for(a.d, planes);
   const size_t stage_bytes = (size_t)planes * CKB_BYTES;
-  const size_t lim = g_smem_budget;
+  const size_t lim = vi.smem_budget;
   // double-buffer the unit's points when that still leaves a 3-stage ring (a single buffer
   // measured no slower on GB300: the next unit's points are prefetched into L2)
   const int xbufs = (2 * xbytes + 3 * stage_bytes <= lim) ? 2 : 1;
-  if (lim < xbufs * xbytes + 3 * stage_bytes) return cudaErrorInvalidValue;
+  if (lim < xbufs * xbytes + 2 * stage_bytes) return cudaErrorInvalidValue;
   int stages = (int)((lim - xbufs * xbytes) / stage_bytes);
   if (stages > MAX_STAGES) stages = MAX_STAGES;
   const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes;
@@ -650,11 +701,11 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
                                     (uint64_t)a.d, (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BNH));
   }
   const long long n_units = (a.n + UNIT - 1) / UNIT;
-  const long long pairs = n_units < g_max_pairs ? n_units : g_max_pairs;
+  const long long pairs = n_units < vi.max_pairs ? n_units : vi.max_pairs;
   if (pairs <= 0) return cudaSuccess;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(2 * pairs));
-  cfg.blockDim = dim3(NTHREADS);
+  cfg.blockDim = dim3(threads_for(epq));
   cfg.dynamicSmemBytes = smem;
   cfg.stream = s;
   cudaLaunchAttribute at[1];
@@ -664,8 +715,12 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel, tmX, tmXl, tmC, tmCl, a, stages,
-                                   xbufs, planes));
+  if (epq == 2)
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2>, tmX, tmXl, tmC, tmCl, a, stages,
+                                     xbufs, planes));
+  else
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4>, tmX, tmXl, tmC, tmCl, a, stages,
+                                     xbufs, planes));
   count_launches(1);
   return cudaSuccess;
 }
