@@ -37,6 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N, D, K = 4_000_000, 128, 1024
+NUM_CENTERS = K
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one assignment launch per row of
 # X, from one ncu capture of the current split-tier kernel on the 1,000,000 x 128, K=1024 case
 # (517.0 MB read + 7.6 MB written). X is read once per launch and C stays in L2, so the traffic
@@ -187,6 +188,30 @@ def reference_arm(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
+def time_kmeanspp(km, torch, h, n, k, reps=1):
+    """k-means++ initialisation on the handle's resident data (outside the Lloyd timed region):
+    one untimed call, then `reps` calls bracketed by CUDA events on the handle's stream. Each
+    draw reads X once (N*D*4 bytes) and D^2 three times and writes it once (4 * N*4 bytes)."""
+    stream = torch.cuda.ExternalStream(h.stream)
+    h.init_kmeanspp(1000)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = km.launch_count()
+    e0.record(stream)
+    for r in range(reps):
+        h.init_kmeanspp(r)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    launches = (km.launch_count() - l0) // reps
+    draw_bytes = n * D * 4 + 4 * n * 4
+    gbs = draw_bytes * (k - 1) / (ms / 1000.0) / 1e9
+    _, hbm, src = peaks()
+    return {"ms": ms, "draws": k, "us_per_draw": ms * 1000.0 / k, "launches": launches,
+            "bytes_per_draw": draw_bytes, "achieved_GBs": gbs, "peak_GBs": hbm,
+            "frac": gbs / hbm, "peak_source": f"{src} HBM copy (MEASURED_PEAKS.json)"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -199,6 +224,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=N, help="rows (default: the 4M workload); smaller "
                     "values are for profiling captures only")
+    ap.add_argument("--k", type=int, default=NUM_CENTERS, help="centers (default 1024); other values are "
+                    "for profiling captures only")
+    ap.add_argument("--no-init", action="store_true", help="skip the k-means++ timing")
+    ap.add_argument("--only-init", action="store_true",
+                    help="time only the k-means++ initialisation (profiling captures)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -221,8 +251,16 @@ def main():
     tier = args.tier
     tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3}[tier]
 
-    n = args.n
+    n, K = args.n, args.k
     X, _, _ = mixture_torch(n, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+    if args.only_init:
+        h = km.Handle(n, D, K, assign_tier=km.ASSIGN_FP32)
+        h.set_data(X, True)
+        line = {"metric": f"k-means++ initialisation (N={n}, D={D}, K={K})",
+                "init_kmeanspp": time_kmeanspp(km, torch, h, n, K, reps=max(1, args.steps))}
+        print(json.dumps(line), flush=True)
+        h.close()
+        return
     idx = torch.from_numpy(sample_init(n, K, seed=99)).cuda()
     init = X[idx].cpu().numpy()
     h = km.Handle(n, D, K, assign_tier=tier_id, max_iters=args.steps + args.warmup)
@@ -273,6 +311,10 @@ def main():
         roofline["tensor_tflops"] = tf / (assign_ms / 1000.0) / 1e12
         roofline["tensor_frac"] = roofline["tensor_tflops"] / bf16_peak
 
+    init_pp = None
+    if not args.no_init and rank == 0:
+        init_pp = time_kmeanspp(km, torch, h, n, K, reps=1)
+
     e2e = None
     if not args.no_e2e and rank == 0:
         Xh = X.cpu().numpy()
@@ -312,6 +354,7 @@ def main():
                                       zip(["prep", "assign", "rerank", "update"], phase)},
                 "reranked_points_total": st.reranked, "reranked_fp64_total": st.reranked_fp64,
                 "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+                "init_kmeanspp": init_pp,
                 "gpu_launches": launches, "clocks": cl}
         print(json.dumps(line), flush=True)
     h.close()

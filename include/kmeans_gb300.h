@@ -60,8 +60,10 @@ KMGB_EXPORT const char* kmeansGetErrorString(kmeansErrorStatus err);
  * data: host, m x n row-major. result: host, n x k with result[j*k + i] = dim j of center i;
  * it receives the initial centers, then the final centers. The data are shuffled with
  * std::shuffle(default_random_engine(0)) and the initial centers picked with srand(42)/rand()
- * exactly as the reference does. numRetries and initAlgorithm are accepted and ignored (the
- * reference ignores them too); doFullSGEMM (0/1/2) and matrixFormat (0/1) are accepted and
+ * exactly as the reference does when initAlgorithm is 0 (numRetries is then ignored, as in the
+ * reference). initAlgorithm 1 (an extension) draws k-means++ centers with seeds 0 ..
+ * numRetries-1 and keeps the run with the lowest final SSE; result then receives that run's
+ * initial centers before its final ones. doFullSGEMM (0/1/2) and matrixFormat (0/1) are accepted and
  * all map to the same fused assignment. miniBatchFraction < 1 selects the reference's
  * sliding mini-batch windows. Returns KMEANS_NONCONVERGENCE (13) when the relative SSE change
  * is still above `criterion` after maxIters iterations (criterion < 0 always runs maxIters). */
@@ -193,6 +195,13 @@ enum kmgb_empty_policy {
   KMGB_EMPTY_KEEP = 1 /* keep the previous center */
 };
 
+/* Initialisation when no initial centers are given. initAlgorithm of computeKmeansF/D takes the
+ * same values. */
+enum kmgb_init_algorithm {
+  KMGB_INIT_REFERENCE = 0, /* the reference's shuffle + srand(42) picks (kmeans.cpp:554-557, 876-888) */
+  KMGB_INIT_KMEANSPP = 1   /* k-means++: D^2-weighted seeded draws, see kmgb_kmeanspp_f32 */
+};
+
 typedef struct kmgb_options {
   int assign_tier;           /* kmgb_assign_tier */
   int certify;               /* 1: labels equal the FP64 arg-min (margin test + re-rank) */
@@ -204,7 +213,11 @@ typedef struct kmgb_options {
                                 path): X stays in host memory and passes through two device
                                 tile buffers of this many rows every iteration; the host array
                                 must stay valid while the handle runs. 0: X resident in HBM */
-  int reserved[7];
+  int init_algorithm;        /* initial centers when none are given: kmgb_init_algorithm */
+  int num_retries;           /* k-means++: runs seeded seed, seed+1, ...; the run with the lowest
+                                final SSE is returned (< 1 counts as 1) */
+  unsigned long long seed;   /* k-means++ seed */
+  int reserved[4];
 } kmgb_options;
 
 typedef struct kmgb_stats {
@@ -226,11 +239,25 @@ typedef struct kmgb_stats {
 KMGB_EXPORT int kmgb_reference_init(const float* data, int m, int d, int k, float* centers,
                                     int* perm, int* picks);
 
-/* Defaults: FP32 tier, certify on, NaN policy, 20 iterations, criterion -1, full batch. */
+/* k-means++ initial centers (Arthur & Vassilvitskii, 2007), reproducible bit for bit for a seed:
+ * draw 0 is uniform; draw r picks a point with probability proportional to its weight
+ * q = trunc(D^2 * 2^31 / max D^2), D^2 = squared distance (in the data's precision) to the
+ * nearest center drawn so far, from the 53-bit number u = splitmix64(splitmix64(seed) + r) >> 11
+ * as the point whose interval of the running sum of q holds (u * sum q) >> 53.
+ * X: n x d row-major (host or device); centers: k x d row-major (host or device, nullable);
+ * picks: the k chosen rows (host, nullable). Runs on the GPU; the data set must fit in HBM. */
+KMGB_EXPORT int kmgb_kmeanspp_f32(const float* X, long long n, int d, int k, unsigned long long seed,
+                                  float* centers, int* picks);
+KMGB_EXPORT int kmgb_kmeanspp_f64(const double* X, long long n, int d, int k,
+                                  unsigned long long seed, double* centers, int* picks);
+
+/* Defaults: FP32 tier, certify on, NaN policy, 20 iterations, criterion -1, full batch,
+ * reference initialisation, one retry, seed 0. */
 KMGB_EXPORT void kmgb_default_options(kmgb_options* opt);
 
 /* One-shot Lloyd run. X: n x d row-major FP32 (host or device pointer). init: k x d row-major
- * initial centers (host or device), or NULL for the reference initialisation. Outputs (host or
+ * initial centers (host or device), or NULL for opt->init_algorithm (with opt->num_retries runs
+ * for k-means++, keeping the lowest final SSE). Outputs (host or
  * device, each may be NULL): centers k x d row-major, labels[n] of the last assignment
  * (source-row order; -1 outside the last mini-batch window), sse[max_iters] per iteration
  * (FP64, against the updated centers, as the reference's compactness). */
@@ -243,6 +270,9 @@ typedef struct kmgb_handle kmgb_handle;
 KMGB_EXPORT int kmgb_create(kmgb_handle** h, long long n, int d, int k, const kmgb_options* opt);
 KMGB_EXPORT int kmgb_set_data(kmgb_handle* h, const float* X, int x_on_device);
 KMGB_EXPORT int kmgb_set_centers(kmgb_handle* h, const float* C, int c_on_device); /* NULL: reference init */
+/* k-means++ centers from the resident data (not for host-streamed handles); picks: k rows (host,
+ * nullable). Resets the mini-batch window to the first one. */
+KMGB_EXPORT int kmgb_init_kmeanspp(kmgb_handle* h, unsigned long long seed, int* picks);
 /* Runs up to `iters` iterations from the current centers (asynchronous when criterion < 0). */
 KMGB_EXPORT int kmgb_run(kmgb_handle* h, int iters, double criterion);
 KMGB_EXPORT int kmgb_synchronize(kmgb_handle* h);

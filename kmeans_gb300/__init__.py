@@ -36,6 +36,8 @@ ASSIGN_BF16 = 1
 ASSIGN_BF16X3 = 2
 EMPTY_NAN = 0
 EMPTY_KEEP = 1
+INIT_REFERENCE = 0
+INIT_KMEANSPP = 1
 
 ERROR_STRINGS = {
     1: "error in building the data",
@@ -65,7 +67,8 @@ class kmgb_options(C.Structure):
     _fields_ = [("assign_tier", C.c_int), ("certify", C.c_int), ("empty_policy", C.c_int),
                 ("max_iters", C.c_int), ("criterion", C.c_double),
                 ("mini_batch_fraction", C.c_float), ("stream_tile_rows", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("init_algorithm", C.c_int), ("num_retries", C.c_int),
+                ("seed", C.c_ulonglong), ("reserved", C.c_int * 4)]
 
 
 class kmgb_stats(C.Structure):
@@ -132,6 +135,9 @@ def lib():
             "kmgb_reference_init": (i32, [P, i32, i32, i32, P, P, P]),
             "kmgb_tc_accumulators": (i32, [P, i64, i32, P, i32, i32, P]),
             "kmgb_version": (C.c_char_p, []),
+            "kmgb_kmeanspp_f32": (i32, [P, i64, i32, i32, C.c_ulonglong, P, P]),
+            "kmgb_kmeanspp_f64": (i32, [P, i64, i32, i32, C.c_ulonglong, P, P]),
+            "kmgb_init_kmeanspp": (i32, [P, C.c_ulonglong, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -203,6 +209,22 @@ def reference_init(data: np.ndarray, k: int):
     if rc:
         raise KmeansError(rc, last_error())
     return cen, perm, picks
+
+
+def kmeanspp(X, k: int, seed: int = 0):
+    """k-means++ initial centers through kmgb_kmeanspp_f32/_f64. X: numpy (host) or torch (device)
+    n x d, float32 or float64. Returns (centers k x d numpy, picks int32[k])."""
+    dbl = str(getattr(X, "dtype", "")).endswith("float64")
+    if isinstance(X, np.ndarray):
+        X = np.ascontiguousarray(X, dtype=np.float64 if dbl else np.float32)
+    n, d = X.shape
+    cen = np.empty((k, d), np.float64 if dbl else np.float32)
+    picks = np.empty(k, np.int32)
+    fn = lib().kmgb_kmeanspp_f64 if dbl else lib().kmgb_kmeanspp_f32
+    rc = fn(_ptr(X), n, d, k, seed, _ptr(cen), _ptr(picks))
+    if rc:
+        raise KmeansError(rc, last_error())
+    return cen, picks
 
 
 def tc_accumulators(X: np.ndarray, C: np.ndarray, split: bool) -> np.ndarray:
@@ -316,10 +338,13 @@ class LloydResult:
 
 def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
           assign_tier: int = ASSIGN_FP32, certify: bool = True, empty_policy: int = EMPTY_NAN,
-          mini_batch_fraction: float = 1.0, stream_tile_rows: int = 0) -> LloydResult:
+          mini_batch_fraction: float = 1.0, stream_tile_rows: int = 0,
+          init_algorithm: int = INIT_REFERENCE, num_retries: int = 1,
+          seed: int = 0) -> LloydResult:
     """One-shot Lloyd run through kmgb_lloyd_f32. X: numpy (host) or torch (device) n x d
-    float32; init: k x d float32 or None (reference initialisation). stream_tile_rows > 0 keeps
-    a host X in host memory and streams it through the GPU in tiles of that many rows."""
+    float32; init: k x d float32, or None for init_algorithm (the reference initialisation, or
+    k-means++ with num_retries seeded runs keeping the lowest final SSE). stream_tile_rows > 0
+    keeps a host X in host memory and streams it through the GPU in tiles of that many rows."""
     if isinstance(X, np.ndarray):
         X = np.ascontiguousarray(X, dtype=np.float32)
     n, d = X.shape
@@ -328,7 +353,8 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
     opt = default_options(assign_tier=assign_tier, certify=int(certify),
                           empty_policy=empty_policy, max_iters=max_iters, criterion=criterion,
                           mini_batch_fraction=mini_batch_fraction,
-                          stream_tile_rows=stream_tile_rows)
+                          stream_tile_rows=stream_tile_rows, init_algorithm=init_algorithm,
+                          num_retries=num_retries, seed=seed)
     cen = np.empty((k, d), dtype=np.float32)
     lab = np.empty(n, dtype=np.int32)
     sse = np.zeros(max(max_iters, 1), dtype=np.float64)
@@ -361,6 +387,12 @@ class Handle:
 
     def set_centers(self, Cn=None, on_device: bool = False):
         self._chk(lib().kmgb_set_centers(self._h, _ptr(Cn), int(on_device)))
+
+    def init_kmeanspp(self, seed: int = 0) -> np.ndarray:
+        """k-means++ centers from the resident data; returns the picked rows."""
+        picks = np.empty(self.k, np.int32)
+        self._chk(lib().kmgb_init_kmeanspp(self._h, seed, _ptr(picks)))
+        return picks
 
     def run(self, iters: int, criterion: float = -1.0):
         self._chk(lib().kmgb_run(self._h, iters, criterion))

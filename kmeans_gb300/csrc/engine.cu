@@ -177,6 +177,11 @@ struct kmgb_handle {
   long long cand_cap = 0;  // rows of the compact buffers for the candidate pass
   unsigned long long* rr_stats = nullptr;
   int* err = nullptr;
+  // k-means++ work space (allocated on first use): D^2, block weight sums, max/pick, picks
+  float* kpp_d2 = nullptr;
+  unsigned long long* kpp_blk = nullptr;
+  unsigned long long* kpp_sc = nullptr;
+  int* kpp_picks = nullptr;
   // device-side loop state: stop flag, previous SSE, last relErr, iterations done
   int* stop = nullptr;
   double* loopf = nullptr;  // [0] SSE_old, [1] relErr
@@ -218,7 +223,8 @@ struct kmgb_handle {
                     rr_list, rr_count, rr_over, rr_list2, rr_hi2, thr_full, thr_c, XbC, XlC, cand,
                     cand_cnt, rr_stats, err, uw.hist, uw.scan_tmp, uw.label_off,
                     uw.piece_cnt, uw.sorted, uw.part, uw.partq, uw.sse_k, uw.counts, sse_dev,
-                    stop, loopf, iters_done, X2, accS, accQ, accN};
+                    stop, loopf, iters_done, X2, accS, accQ, accN, kpp_d2, kpp_blk, kpp_sc,
+                    kpp_picks};
     for (void* p : ptrs)
       if (p) cudaFree(p);
     for (int b = 0; b < 2; ++b) {
@@ -816,6 +822,44 @@ int set_centers(kmgb_handle* h, const float* C, bool on_device) {
   return 0;
 }
 
+// k-means++ centers from the resident data into h->C (launch_kmeanspp); picks_out: host, k.
+int init_kmeanspp(kmgb_handle* h, unsigned long long seed, int* picks_out) {
+  const int code = KMEANS_ERROR_INITIALIZE;
+  if (h->streaming || !h->have_data) {
+    set_err(h->streaming ? "k-means++ needs the data set resident in device memory"
+                         : "k-means++ needs the data set first");
+    return code;
+  }
+  if (h->k > h->n) {
+    set_err("k-means++ needs 0 < k <= n");
+    return code;
+  }
+  if (!h->kpp_d2) {
+    KM_TRY(dalloc(&h->kpp_d2, (size_t)kmeanspp_d2_elems(h->n)), code);
+    KM_TRY(dalloc(&h->kpp_blk, (size_t)kmeanspp_blocks(h->n)), code);
+    KM_TRY(dalloc(&h->kpp_sc, 3), code);
+    KM_TRY(dalloc(&h->kpp_picks, (size_t)h->k), code);
+  }
+  KM_TRY(cudaMemsetAsync(h->C, 0, sizeof(float) * h->ldx * h->k, h->stream), code);
+  KM_TRY(launch_kmeanspp(h->X, h->ldx, h->n, h->d, h->k, seed, h->C, h->ldx, h->kpp_picks,
+                         h->kpp_d2, h->kpp_blk, h->kpp_sc, h->err, h->stream),
+         code);
+  if (picks_out)
+    KM_TRY(cudaMemcpyAsync(picks_out, h->kpp_picks, sizeof(int) * h->k, cudaMemcpyDeviceToHost,
+                           h->stream),
+           code);
+  KM_TRY(cudaStreamSynchronize(h->stream), code);
+  int e = 0;
+  KM_TRY(cudaMemcpy(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost), code);
+  if (e) {
+    set_err("k-means++: a bounded wait in the D^2 kernel gave up (device error word set)");
+    return code;
+  }
+  h->have_centers = true;
+  h->iter_base = 0;
+  return 0;
+}
+
 int get_centers(kmgb_handle* h, float* out, bool on_device) {
   const size_t row_bytes = sizeof(float) * h->d;
   KM_TRY(cudaMemcpy2DAsync(out, row_bytes, h->C, sizeof(float) * h->ldx, row_bytes, h->k,
@@ -853,6 +897,39 @@ int get_labels(kmgb_handle* h, int* out, bool on_device) {
   return 0;
 }
 
+
+// k-means++ with opt.num_retries seeds (seed, seed+1, ...), a full Lloyd run each; the handle ends
+// holding the run with the lowest final SSE (the first on ties; a NaN SSE never wins over a
+// number). A losing last run is replaced by running the winner's seed again, which reproduces it
+// bit for bit. init_out (host, k x d, nullable): the winner's initial centers.
+int run_kmeanspp_retries(kmgb_handle* h, const kmgb_options& o, float* init_out) {
+  const int retries = std::max(1, o.num_retries);
+  std::vector<float> cur(init_out ? (size_t)h->k * h->d : 0), keep(cur.size());
+  int best = 0;
+  double best_sse = std::nan("");
+  for (int r = 0; r < retries; ++r) {
+    int rc = init_kmeanspp(h, o.seed + (unsigned long long)r, nullptr);
+    if (!rc && init_out) rc = get_centers(h, cur.data(), false);
+    if (!rc) rc = run(h, o.max_iters, o.criterion);
+    if (!rc) rc = finish(h);
+    if (rc) return rc;
+    const double sse = h->iterations > 0 ? h->sse_host[h->iterations - 1] : std::nan("");
+    if (r == 0 || sse < best_sse || (std::isnan(best_sse) && !std::isnan(sse))) {
+      best = r;
+      best_sse = sse;
+      keep.swap(cur);
+    }
+  }
+  if (best != retries - 1) {
+    int rc = init_kmeanspp(h, o.seed + (unsigned long long)best, nullptr);
+    if (!rc) rc = run(h, o.max_iters, o.criterion);
+    if (!rc) rc = finish(h);
+    if (rc) return rc;
+  }
+  if (init_out) std::memcpy(init_out, keep.data(), sizeof(float) * keep.size());
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -865,6 +942,9 @@ void kmgb_default_options(kmgb_options* opt) {
   opt->max_iters = 20;
   opt->criterion = -1.0;
   opt->mini_batch_fraction = 1.0f;
+  opt->init_algorithm = KMGB_INIT_REFERENCE;
+  opt->num_retries = 1;
+  opt->seed = 0;
 }
 
 const char* kmgb_last_error(void) { return g_last_error.c_str(); }
@@ -912,6 +992,91 @@ int kmgb_set_centers(kmgb_handle* h, const float* C, int c_on_device) {
                       sizeof(float) * h->d, cudaMemcpyDeviceToHost),
            KMEANS_ERROR_INITIALIZE);
   return set_centers(h, init.data(), false);
+}
+
+int kmgb_init_kmeanspp(kmgb_handle* h, unsigned long long seed, int* picks) {
+  if (!h) return KMEANS_ERROR_INITIALIZE;
+  return init_kmeanspp(h, seed, picks);
+}
+
+}  // extern "C"
+
+namespace {
+template <typename T>
+int kmeanspp_oneshot(const T* X, long long n, int d, int k, unsigned long long seed, T* centers,
+                     int* picks) {
+  const int code = KMEANS_ERROR_INITIALIZE;
+  if (!X || n <= 0 || d <= 0 || k <= 0 || k > n || n >= 0x7fffffffLL) {
+    set_err("k-means++: needs X, d > 0 and 0 < k <= n < 2^31-1");
+    return code;
+  }
+  const bool x_dev = is_device_ptr(X);
+  T *Xd = nullptr, *Cd = nullptr, *d2 = nullptr;
+  unsigned long long *blk = nullptr, *sc = nullptr;
+  int *kp = nullptr, *err = nullptr;
+  int rc = 0;
+  // host data is uploaded with 16-byte aligned rows (the bulk-copy D^2 kernel's layout)
+  const long long ldx = x_dev ? d : round_up(d, (long long)(16 / sizeof(T)));
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return code;
+  auto fail = [&](cudaError_t e, const char* where) {
+    if (e != cudaSuccess && !rc) {
+      set_err(where, e);
+      rc = code;
+    }
+  };
+  if (x_dev) {
+    fail(cudaStreamSynchronize(nullptr), "k-means++ (legacy stream)");
+  } else {
+    fail(dalloc(&Xd, (size_t)n * ldx), "k-means++ (data)");
+    if (!rc)
+      fail(cudaMemcpy2DAsync(Xd, sizeof(T) * ldx, X, sizeof(T) * d, sizeof(T) * d, n,
+                             cudaMemcpyHostToDevice, s),
+           "k-means++ (upload)");
+  }
+  if (!rc) fail(dalloc(&Cd, (size_t)k * d), "k-means++ (centers)");
+  if (!rc) fail(dalloc(&d2, (size_t)kmeanspp_d2_elems(n)), "k-means++ (D^2)");
+  if (!rc) fail(dalloc(&blk, (size_t)kmeanspp_blocks(n)), "k-means++ (sums)");
+  if (!rc) fail(dalloc(&sc, 3), "k-means++ (scalars)");
+  if (!rc) fail(dalloc(&kp, (size_t)k), "k-means++ (picks)");
+  if (!rc) fail(dalloc(&err, 1), "k-means++ (error word)");
+  if (!rc) fail(cudaMemsetAsync(err, 0, sizeof(int), s), "k-means++ (error word)");
+  if (!rc)
+    fail(launch_kmeanspp(x_dev ? X : Xd, ldx, n, d, k, seed, Cd, d, kp, d2, blk, sc, err, s),
+         "k-means++ (kernels)");
+  if (!rc && centers)
+    fail(cudaMemcpyAsync(centers, Cd, sizeof(T) * (size_t)k * d,
+                         is_device_ptr(centers) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                         s),
+         "k-means++ (centers out)");
+  if (!rc && picks)
+    fail(cudaMemcpyAsync(picks, kp, sizeof(int) * k, cudaMemcpyDeviceToHost, s),
+         "k-means++ (picks out)");
+  if (!rc) fail(cudaStreamSynchronize(s), "k-means++");
+  int e = 0;
+  if (!rc) fail(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost), "k-means++ (error word)");
+  if (!rc && e) {
+    set_err("k-means++: a bounded wait in the D^2 kernel gave up (device error word set)");
+    rc = code;
+  }
+  cudaStreamSynchronize(s);
+  for (void* p : {(void*)Xd, (void*)Cd, (void*)d2, (void*)blk, (void*)sc, (void*)kp, (void*)err})
+    if (p) cudaFree(p);
+  cudaStreamDestroy(s);
+  return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int kmgb_kmeanspp_f32(const float* X, long long n, int d, int k, unsigned long long seed,
+                      float* centers, int* picks) {
+  return kmeanspp_oneshot<float>(X, n, d, k, seed, centers, picks);
+}
+
+int kmgb_kmeanspp_f64(const double* X, long long n, int d, int k, unsigned long long seed,
+                      double* centers, int* picks) {
+  return kmeanspp_oneshot<double>(X, n, d, k, seed, centers, picks);
 }
 
 int kmgb_run(kmgb_handle* h, int iters, double criterion) {
@@ -1059,10 +1224,13 @@ int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
   int rc = create_handle(&h, n, d, k, &o);
   if (rc) return rc;
   const bool x_dev = is_device_ptr(X);
+  const bool kpp = !init && o.init_algorithm == KMGB_INIT_KMEANSPP;
   rc = set_data(h, X, x_dev);
   if (!rc) {
     if (init) {
       rc = set_centers(h, init, is_device_ptr(init));
+    } else if (kpp) {
+      rc = run_kmeanspp_retries(h, o, nullptr);
     } else if (!x_dev) {
       std::vector<float> ini;
       rc = reference_init_host(h, X, ini);
@@ -1071,8 +1239,8 @@ int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
       rc = kmgb_set_centers(h, nullptr, 0);
     }
   }
-  if (!rc) rc = run(h, o.max_iters, o.criterion);
-  if (!rc) rc = finish(h);
+  if (!rc && !kpp) rc = run(h, o.max_iters, o.criterion);
+  if (!rc && !kpp) rc = finish(h);
   if (!rc && centers) rc = get_centers(h, centers, is_device_ptr(centers));
   if (!rc && labels) rc = get_labels(h, labels, is_device_ptr(labels));
   if (!rc && sse) kmgb_get_sse(h, sse, o.max_iters);
@@ -1110,8 +1278,6 @@ kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, co
                                  const int numRetries, const int initAlgorithm,
                                  const int doFullSGEMM, const int matrixFormat, float* result,
                                  const float miniBatchFraction) {
-  (void)numRetries;
-  (void)initAlgorithm;
   if (!data || !result || m <= 0 || n <= 0 || k <= 0) return KMEANS_ERROR_BUILDDATA;
   if (doFullSGEMM < 0 || doFullSGEMM > 2 || matrixFormat < 0 || matrixFormat > 1)
     return KMEANS_ERROR_BUILDDATA;
@@ -1127,16 +1293,23 @@ kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, co
   int rc = create_handle(&h, m, n, k, &o);
   if (rc) return (kmeansErrorStatus)rc;
   rc = set_data(h, data, false);
-  std::vector<float> init;
-  if (!rc) rc = reference_init_host(h, data, init);
+  std::vector<float> init((size_t)k * n);
+  const bool kpp = initAlgorithm == KMGB_INIT_KMEANSPP;  // the reference ignores numRetries
+  if (kpp) {
+    o.num_retries = numRetries;
+    o.seed = 0;
+    if (!rc) rc = run_kmeanspp_retries(h, o, init.data());
+  } else if (!rc) {
+    rc = reference_init_host(h, data, init);
+    if (!rc) rc = set_centers(h, init.data(), false);
+  }
   if (!rc) {
     // the reference writes the initial centers into result (kmeans.cpp:886-888)
     for (int i = 0; i < k; ++i)
       for (int j = 0; j < n; ++j) result[(size_t)j * k + i] = init[(size_t)i * n + j];
-    rc = set_centers(h, init.data(), false);
   }
-  if (!rc) rc = run(h, o.max_iters, (double)criterion);
-  if (!rc) rc = finish(h);
+  if (!rc && !kpp) rc = run(h, o.max_iters, (double)criterion);
+  if (!rc && !kpp) rc = finish(h);
   std::vector<float> fin;
   if (!rc) {
     fin.resize((size_t)k * n);

@@ -129,8 +129,12 @@ struct DevBufs {
     if ((expr) != cudaSuccess) return (code); \
   } while (0)
 
+// One FP64 run. kpp_seed < 0: the reference initialisation; else k-means++ with that seed (on the
+// device, from the uploaded data). result receives the initial then the final centers (D x K);
+// *final_sse the SSE of the last iteration (NaN when none ran).
 kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterion, int maxIters,
-                        double* result, double fraction) {
+                        double* result, double fraction, long long kpp_seed, double* final_sse) {
+  *final_sse = std::nan("");
   const bool mini = fraction < 1.0;
   const long long m_mb = mini ? (long long)(int)((float)fraction * (float)m) : m;
   if (m_mb <= 0) return KMEANS_ERROR_TILING;
@@ -142,7 +146,7 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
     std::shuffle(perm.begin(), perm.end(), std::default_random_engine(seed));
   }
   std::vector<int> picks;
-  {
+  if (kpp_seed < 0) {
     struct random_data rd;
     std::memset(&rd, 0, sizeof(rd));
     std::vector<char> state(128, 0);
@@ -159,11 +163,12 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
     }
   }
   std::vector<double> C((size_t)k * n);
-  for (int i = 0; i < k; ++i)
-    for (int j = 0; j < n; ++j) {
-      C[(size_t)i * n + j] = data[(size_t)perm[picks[i]] * n + j];
-      result[(size_t)j * k + i] = C[(size_t)i * n + j];
-    }
+  if (kpp_seed < 0)
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < n; ++j) {
+        C[(size_t)i * n + j] = data[(size_t)perm[picks[i]] * n + j];
+        result[(size_t)j * k + i] = C[(size_t)i * n + j];
+      }
 
   DevBufs B;
   double *X = nullptr, *Xw = nullptr, *Cd = nullptr, *CT = nullptr, *acc = nullptr, *part = nullptr,
@@ -186,7 +191,29 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
   const int sse_blocks = 152 * 4;
   KD_TRY(B.alloc(&part, sse_blocks), E);
   KD_TRY(B.alloc(&sse, 1), E);
-  KD_TRY(cudaMemcpy(Cd, C.data(), sizeof(double) * C.size(), cudaMemcpyHostToDevice), E);
+  if (kpp_seed < 0) {
+    KD_TRY(cudaMemcpy(Cd, C.data(), sizeof(double) * C.size(), cudaMemcpyHostToDevice), E);
+  } else {
+    double* d2 = nullptr;
+    unsigned long long *blk = nullptr, *sc = nullptr;
+    int *kp = nullptr, *err = nullptr;
+    const kmeansErrorStatus EI = KMEANS_ERROR_INITIALIZE;
+    KD_TRY(B.alloc(&d2, kmeanspp_d2_elems(m)), EI);
+    KD_TRY(B.alloc(&blk, kmeanspp_blocks(m)), EI);
+    KD_TRY(B.alloc(&sc, 3), EI);
+    KD_TRY(B.alloc(&kp, k), EI);
+    KD_TRY(B.alloc(&err, 1), EI);
+    KD_TRY(cudaMemset(err, 0, sizeof(int)), EI);
+    KD_TRY(launch_kmeanspp(X, n, m, n, k, (unsigned long long)kpp_seed, Cd, n, kp, d2, blk, sc, err,
+                           s),
+           EI);
+    KD_TRY(cudaMemcpy(C.data(), Cd, sizeof(double) * C.size(), cudaMemcpyDeviceToHost), EI);
+    int e = 0;
+    KD_TRY(cudaMemcpy(&e, err, sizeof(int), cudaMemcpyDeviceToHost), EI);
+    if (e) return EI;
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < n; ++j) result[(size_t)j * k + i] = C[(size_t)i * n + j];
+  }
   UpdateWork w{};
   w.n = m_mb;
   w.k = k;
@@ -232,6 +259,7 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
     KD_TRY(cudaMemcpy(&h, sse, sizeof(double), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPACTNESS);
     rel = std::fabs(h - sse_old) / std::fabs(h);
     sse_old = h;
+    *final_sse = h;
     ++it;
     if (mini) {
       start += m_mb;
@@ -254,11 +282,29 @@ extern "C" kmeansErrorStatus computeKmeansD(const double* data, const int m, con
                                             const int initAlgorithm, const int doFullSGEMM,
                                             const int matrixFormat, double* result,
                                             const double miniBatchFraction) {
-  (void)numRetries;
-  (void)initAlgorithm;
   if (!data || !result || m <= 0 || n <= 0 || k <= 0) return KMEANS_ERROR_BUILDDATA;
   if (doFullSGEMM < 0 || doFullSGEMM > 2 || matrixFormat < 0 || matrixFormat > 1)
     return KMEANS_ERROR_BUILDDATA;
   if (k > m) return KMEANS_ERROR_INITIALIZE;
-  return run_d(data, m, n, k, criterion, maxIters < 0 ? 0 : maxIters, result, miniBatchFraction);
+  const int iters = maxIters < 0 ? 0 : maxIters;
+  double sse = 0.0;
+  if (initAlgorithm != KMGB_INIT_KMEANSPP)  // the reference ignores numRetries
+    return run_d(data, m, n, k, criterion, iters, result, miniBatchFraction, -1, &sse);
+  // k-means++ with seeds 0 .. numRetries-1; the lowest final SSE wins (the first on ties)
+  const int retries = numRetries < 1 ? 1 : numRetries;
+  double best_sse = std::nan("");
+  kmeansErrorStatus best_st = KMEANS_SUCCESS;
+  std::vector<double> tmp((size_t)n * k), keep((size_t)n * k);
+  for (int r = 0; r < retries; ++r) {
+    const kmeansErrorStatus st =
+        run_d(data, m, n, k, criterion, iters, tmp.data(), miniBatchFraction, r, &sse);
+    if (st != KMEANS_SUCCESS && st != KMEANS_NONCONVERGENCE) return st;
+    if (r == 0 || sse < best_sse || (std::isnan(best_sse) && !std::isnan(sse))) {
+      best_sse = sse;
+      best_st = st;
+      keep.swap(tmp);
+    }
+  }
+  std::memcpy(result, keep.data(), sizeof(double) * keep.size());
+  return best_st;
 }

@@ -164,6 +164,20 @@ cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* 
                               long long m, long long start, long long m_mb, double* qdst,
                               float* xdst, cudaStream_t s, const int* stop = nullptr);
 
+// k-means++ (D^2-weighted draws, seeded): k centers from X (n x d, row stride ldx) into C (k x d,
+// row stride ldc); picks[k] receives the chosen rows. Work space: d2[kmeanspp_d2_elems(n)],
+// blocksum[kmeanspp_blocks(n)], scalars[3]; err: device error word (a bounded wait that gave up).
+long long kmeanspp_blocks(long long n);
+long long kmeanspp_d2_elems(long long n);
+cudaError_t launch_kmeanspp(const float* X, long long ldx, long long n, int d, int k,
+                            unsigned long long seed, float* C, long long ldc, int* picks,
+                            float* d2, unsigned long long* blocksum, unsigned long long* scalars,
+                            int* err, cudaStream_t s);
+cudaError_t launch_kmeanspp(const double* X, long long ldx, long long n, int d, int k,
+                            unsigned long long seed, double* C, long long ldc, int* picks,
+                            double* d2, unsigned long long* blocksum, unsigned long long* scalars,
+                            int* err, cudaStream_t s);
+
 constexpr int kSumPiece = 128;
 constexpr int kMaxCand = 16;  // candidate centers recorded per flagged point
 // BF16 tiers: centers per tensor-core chunk; the start values and diagnostic accumulators are

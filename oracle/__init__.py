@@ -150,6 +150,10 @@ def lib():
         L.orc_port_lloyd.argtypes = [P, i64, i32, i32, P, i32, i32, P, P, P]
         L.orc_port_lloyd.restype = i32
         L.orc_num_threads.restype = i32
+        L.orc_kmeanspp.argtypes = [P, i64, i32, i32, C.c_ulonglong, P, P]
+        L.orc_kmeanspp.restype = i32
+        L.orc_kmeanspp_d.argtypes = [P, i64, i32, i32, C.c_ulonglong, P, P]
+        L.orc_kmeanspp_d.restype = i32
         _lib = L
         return L
 
@@ -306,6 +310,20 @@ def port_lloyd(X, init, iters, piece=PIECE):
     s = np.zeros(max(iters, 1), dtype=np.float64)
     lib().orc_port_lloyd(_p(X), m, d, k, _p(init), iters, piece, _p(cen), _p(lab), _p(s))
     return cen, lab, s[:iters]
+
+
+def kmeanspp(X: np.ndarray, k: int, seed: int = 0):
+    """k-means++ picks (k row indices) and centers (k x d) of X (float32 or float64)."""
+    dbl = X.dtype == np.float64
+    X = np.ascontiguousarray(X, dtype=np.float64 if dbl else np.float32)
+    n, d = X.shape
+    picks = np.empty(k, np.int32)
+    cen = np.empty((k, d), X.dtype)
+    fn = lib().orc_kmeanspp_d if dbl else lib().orc_kmeanspp
+    rc = fn(_p(X), n, d, k, seed, _p(picks), _p(cen))
+    if rc != 0:
+        raise ValueError("kmeanspp: needs 0 < k <= n")
+    return picks, cen
 
 
 def num_threads() -> int:

@@ -530,6 +530,111 @@ int orc_port_lloyd(const float* X, long long m, int d, int k, const float* init,
   return iters;
 }
 
+// k-means++ initialisation restated from the library's documented draw rule (an extension: the
+// reference declares initAlgorithm/numRetries, main/cpp/kmeans.hpp:94-95, and never reads them).
+// D^2 per point in T: 32 lane partials (lane l takes dims l, l+32, ... as an fma chain of
+// (x-c)^2), then the xor butterfly s_l += s_(l^o) for o = 16..1; D^2 = fmin over the centers
+// drawn so far. Weights q = saturating truncation of D^2 * (2^31 / M) in T, M = max D^2.
+// Draw r: u = splitmix64(splitmix64(seed) + r) >> 11; target = (u * sum q) >> 53; the point
+// whose [prefix, prefix + q) holds target. Draw 0, or a zero total, picks (u * n) >> 53.
+}  // extern "C"
+
+namespace {
+
+inline uint64_t orc_splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+template <typename T>
+T kpp_dist(const T* x, const T* c, int d) {
+  T lanes[32];
+  for (int l = 0; l < 32; ++l) {
+    T s = T(0);
+    for (int t = l; t < d; t += 32) {
+      const T u = x[t] - c[t];
+      s = std::fma(u, u, s);
+    }
+    lanes[l] = s;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    T nx[32];
+    for (int l = 0; l < 32; ++l) nx[l] = lanes[l] + lanes[l ^ o];
+    std::memcpy(lanes, nx, sizeof(lanes));
+  }
+  return lanes[0];
+}
+
+template <typename T>
+uint32_t kpp_weight(T v, T scale) {
+  const T p = v * scale;
+  if (!(p > T(0))) return 0u;  // NaN, zero
+  if (p >= T(4294967296.0)) return 0xffffffffu;
+  return (uint32_t)p;
+}
+
+template <typename T>
+int kmeanspp(const T* X, long long n, int d, int k, unsigned long long seed, int* picks, T* centers) {
+  if (n <= 0 || d <= 0 || k <= 0 || k > n) return -1;
+  std::vector<T> d2(n);
+  std::vector<uint32_t> q(n);
+  const uint64_t s0 = orc_splitmix64(seed);
+  for (int r = 0; r < k; ++r) {
+    unsigned long long total = 0;
+    if (r > 0) {
+      const T* c = X + (size_t)picks[r - 1] * d;
+      const bool first = r == 1;
+#pragma omp parallel for schedule(static)
+      for (long long i = 0; i < n; ++i) {
+        const T s = kpp_dist(X + (size_t)i * d, c, d);
+        d2[i] = first ? s : std::fmin(d2[i], s);
+      }
+      T M = T(0);
+      for (long long i = 0; i < n; ++i)
+        if (d2[i] > M) M = d2[i];
+      const T scale = M > T(0) ? T(2147483648.0) / M : T(0);
+      for (long long i = 0; i < n; ++i) {
+        q[i] = kpp_weight(d2[i], scale);
+        total += q[i];
+      }
+    }
+    const uint64_t u = orc_splitmix64(s0 + (uint64_t)r) >> 11;
+    long long chosen = (long long)(((unsigned __int128)u * (unsigned long long)n) >> 53);
+    if (total > 0) {
+      const unsigned long long target = (unsigned long long)(((unsigned __int128)u * total) >> 53);
+      unsigned long long ex = 0;
+      for (long long i = 0; i < n; ++i) {
+        if (q[i] > 0 && target < ex + q[i]) {
+          chosen = i;
+          break;
+        }
+        ex += q[i];
+      }
+    }
+    picks[r] = (int)chosen;
+  }
+  if (centers)
+    for (int j = 0; j < k; ++j)
+      std::memcpy(centers + (size_t)j * d, X + (size_t)picks[j] * d, sizeof(T) * d);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_kmeanspp(const float* X, long long n, int d, int k, unsigned long long seed, int* picks,
+                 float* centers) {
+  return kmeanspp<float>(X, n, d, k, seed, picks, centers);
+}
+
+int orc_kmeanspp_d(const double* X, long long n, int d, int k, unsigned long long seed, int* picks,
+                   double* centers) {
+  return kmeanspp<double>(X, n, d, k, seed, picks, centers);
+}
+
 int orc_num_threads() {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -90,9 +90,10 @@ def test_reference_init_compute_kmeans_f(km, orc, torch_cuda):
     assert rc == 13
     st, c, lab, sse, it = orc.lloyd(X, orc.reference_init(X, k), 12)
     assert np.array_equal(result.reshape(n, k), c.T, equal_nan=True)  # D x K, K fastest
-    # doFullSGEMM / matrixFormat map to the same implementation
+    # doFullSGEMM / matrixFormat map to the same implementation; numRetries is ignored with
+    # the reference initialisation (initAlgorithm 0)
     r2 = np.zeros_like(result)
-    assert km.computeKmeansF(X, m, n, k, -1.0, 12, 3, 1, 1, 1, r2, 1.0) == 13
+    assert km.computeKmeansF(X, m, n, k, -1.0, 12, 3, 0, 1, 1, r2, 1.0) == 13
     assert np.array_equal(r2, result, equal_nan=True)
 
 
