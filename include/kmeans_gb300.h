@@ -265,6 +265,33 @@ KMGB_EXPORT int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const 
                    const kmgb_options* opt, float* centers, int* labels, double* sse,
                    kmgb_stats* stats);
 
+/* Batched Lloyd: many independent problems in one call (e.g. 10,000 problems of 256..200,000
+ * points, D 16..128, K up to a few hundred). Problems of the same dimension share device
+ * buffers and every phase of an iteration is one launch over all of them; each problem follows
+ * exactly the single-problem semantics (kmgb_lloyd_f32 with the FP32 tier: FP64 arg-min labels,
+ * canonical FP64 center sums, FP64 SSE, its own stop rule). */
+typedef struct kmgb_problem {
+  const float* X;     /* n x d row-major FP32 (host or device) */
+  long long n;
+  int d;
+  int k;
+  const float* init;  /* k x d initial centers (host or device), or NULL: the reference
+                         initialisation of this problem (needs k <= n) */
+  float* centers;     /* out, host, nullable: k x d final centers */
+  int* labels;        /* out, host, nullable: n labels of the last assignment */
+  double* sse;        /* out, host, nullable: SSE per iteration (opt->max_iters entries) */
+  int iterations;     /* out: iterations run */
+  int status;         /* out: KMEANS_SUCCESS or KMEANS_NONCONVERGENCE */
+  long long reserved[4];
+} kmgb_problem;
+
+/* opt: max_iters, criterion, empty_policy and certify are used; the tier must be
+ * KMGB_ASSIGN_FP32, mini_batch_fraction 1, stream_tile_rows 0, init_algorithm
+ * KMGB_INIT_REFERENCE. stats (nullable): iterations = the largest over the problems, reranked =
+ * rows settled by the exact re-rank, ms_total = wall time of the call. */
+KMGB_EXPORT int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const kmgb_options* opt,
+                                       kmgb_stats* stats);
+
 /* Resident handle: data uploaded once, iterations run on the handle's own stream. */
 typedef struct kmgb_handle kmgb_handle;
 KMGB_EXPORT int kmgb_create(kmgb_handle** h, long long n, int d, int k, const kmgb_options* opt);

@@ -71,6 +71,13 @@ class kmgb_options(C.Structure):
                 ("seed", C.c_ulonglong), ("reserved", C.c_int * 4)]
 
 
+class kmgb_problem(C.Structure):
+    _fields_ = [("X", C.c_void_p), ("n", C.c_longlong), ("d", C.c_int), ("k", C.c_int),
+                ("init", C.c_void_p), ("centers", C.c_void_p), ("labels", C.c_void_p),
+                ("sse", C.c_void_p), ("iterations", C.c_int), ("status", C.c_int),
+                ("reserved", C.c_longlong * 4)]
+
+
 class kmgb_stats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("status", C.c_int), ("reranked", C.c_ulonglong),
                 ("reranked_fp64", C.c_ulonglong), ("empty_clusters", C.c_longlong),
@@ -138,6 +145,7 @@ def lib():
             "kmgb_kmeanspp_f32": (i32, [P, i64, i32, i32, C.c_ulonglong, P, P]),
             "kmgb_kmeanspp_f64": (i32, [P, i64, i32, i32, C.c_ulonglong, P, P]),
             "kmgb_init_kmeanspp": (i32, [P, C.c_ulonglong, P]),
+            "kmgb_lloyd_batched_f32": (i32, [P, i32, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -365,6 +373,42 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
         raise KmeansError(rc, last_error())
     return LloydResult(rc, cen, lab, sse[:st.iterations], st.iterations, st.reranked,
                        st.reranked_fp64, st.empty_clusters, st.ms_total)
+
+
+def lloyd_batched(problems, max_iters: int = 20, criterion: float = -1.0,
+                  empty_policy: int = EMPTY_NAN, certify: bool = True):
+    """Many independent Lloyd runs in one kmgb_lloyd_batched_f32 call. problems: sequence of
+    (X, k) or (X, k, init) with X numpy n x d float32 (init k x d, or None for the reference
+    initialisation). Returns (list of LloydResult, kmgb_stats)."""
+    arr = (kmgb_problem * len(problems))()
+    keep = []
+    outs = []
+    for i, p in enumerate(problems):
+        X, k = p[0], int(p[1])
+        init = p[2] if len(p) > 2 else None
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        if init is not None:
+            init = np.ascontiguousarray(init, dtype=np.float32)
+        n, d = X.shape
+        cen = np.empty((k, d), np.float32)
+        lab = np.empty(n, np.int32)
+        sse = np.zeros(max(max_iters, 1), np.float64)
+        keep += [X, init]
+        outs.append((cen, lab, sse))
+        arr[i].X, arr[i].n, arr[i].d, arr[i].k = _ptr(X), n, d, k
+        arr[i].init = _ptr(init)
+        arr[i].centers, arr[i].labels, arr[i].sse = _ptr(cen), _ptr(lab), _ptr(sse)
+    opt = default_options(max_iters=max_iters, criterion=criterion, empty_policy=empty_policy,
+                          certify=int(certify))
+    st = kmgb_stats()
+    rc = lib().kmgb_lloyd_batched_f32(arr, len(problems), C.byref(opt), C.byref(st))
+    if rc:
+        raise KmeansError(rc, last_error())
+    res = []
+    for i, (cen, lab, sse) in enumerate(outs):
+        it = arr[i].iterations
+        res.append(LloydResult(arr[i].status, cen, lab, sse[:it], it, 0, 0, 0, 0.0))
+    return res, st
 
 
 class Handle:

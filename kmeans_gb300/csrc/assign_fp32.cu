@@ -42,10 +42,24 @@ __device__ __forceinline__ float bound_e(float xn, float cm, float gamma, int d)
   return e * 1.01f + 1e-30f;
 }
 
+// GROUPED: many problems of one dimension in one launch. Tile t (rows 128t .. 128t+127) belongs
+// to problem g.tile_prob[t], whose centers are rows c_off .. c_off + k - 1 of the shared center
+// matrix; labels are written as global center indices and rows past the problem's end (padding
+// up to its next 128-row boundary) are left alone.
+template <bool GROUPED>
 __global__ void __launch_bounds__(NTHREADS, 1)
 assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmC,
-                   AssignArgs p) {
+                   AssignArgs p, GroupArgs g) {
   if (stopped(p.stop)) return;
+  int cbeg = 0, kp = p.k;
+  long long rend = p.n;
+  if (GROUPED) {
+    const int prob = g.tile_prob[blockIdx.x];
+    if (g.done && g.done[prob]) return;
+    cbeg = g.c_off[prob];
+    kp = g.k[prob];
+    rend = g.row_end[prob];
+  }
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
@@ -56,7 +70,7 @@ assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const int tid = threadIdx.x;
   const long long row0 = (long long)blockIdx.x * BM;
   const int nkb = (p.d + BKF - 1) / BKF;
-  const int nchunks = (p.k + BN - 1) / BN;
+  const int nchunks = (kp + BN - 1) / BN;
   const int total = nchunks * nkb;
 
   // Thread 0 doubles as the TMA producer: it fills the ring, then refills each stage as soon
@@ -68,7 +82,7 @@ assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     const uint32_t bar = smem_u32(&full_bar[stage]);
     mbar_arrive_expect_tx(bar, STAGE_BYTES);
     tma_load_2d(dst, &tmX, bar, kb * BKF, (int)row0);
-    tma_load_2d(dst + TILE_BYTES, &tmC, bar, kb * BKF, chunk * BN);
+    tma_load_2d(dst + TILE_BYTES, &tmC, bar, kb * BKF, cbeg + chunk * BN);
   };
 
   if (tid == 0) {
@@ -159,7 +173,7 @@ assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int c = chunk * BN + tx + 16 * j;
-      cnv[j] = (c < p.k) ? __ldg(p.cn + c) : INFINITY;
+      cnv[j] = (c < kp) ? __ldg(p.cn + cbeg + c) : INFINITY;
     }
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
@@ -197,8 +211,8 @@ assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
       const long long pt = row0 + ty + 16 * i;
-      if (pt < p.n) {
-        p.labels[pt] = i1[i] < 0 ? 0 : i1[i];
+      if (pt < rend) {
+        p.labels[pt] = cbeg + (i1[i] < 0 ? 0 : i1[i]);
         if (p.certify) {
           const float e = bound_e(__ldg(p.xnorm + pt), cm, p.gamma, p.d);
           const float margin = b2[i] - b1[i];
@@ -221,7 +235,8 @@ float assign_fp32_gamma(int d) {
 }
 
 cudaError_t launch_assign_fp32(const float* X, long long ldx, const float* Cop, long long ldc,
-                               const AssignArgs& a, cudaStream_t s) {
+                               const AssignArgs& a, cudaStream_t s, const GroupArgs* grp,
+                               long long tiles) {
   if (a.n <= 0 || a.k <= 0 || a.d <= 0) return cudaSuccess;
   if ((ldx % 4) || (ldc % 4) || (reinterpret_cast<uintptr_t>(X) & 15) ||
       (reinterpret_cast<uintptr_t>(Cop) & 15))
@@ -233,14 +248,23 @@ cudaError_t launch_assign_fp32(const float* X, long long ldx, const float* Cop, 
                                   (uint64_t)a.k, (uint64_t)ldc * 4, BKF, BN));
   static bool attr_set = false;
   if (!attr_set) {
-    KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_fp32_kernel,
+    KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_fp32_kernel<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)SMEM_BYTES));
+    KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_fp32_kernel<true>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)SMEM_BYTES));
     attr_set = true;
   }
-  const long long grid = (a.n + BM - 1) / BM;
-  if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  assign_fp32_kernel<<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(tmX, tmC, a); kmgb::count_launches(1);
+  const long long grid = grp ? tiles : (a.n + BM - 1) / BM;
+  if (grid <= 0) return cudaSuccess;
+  if (grid > 0x7fffffffLL || (grp && tiles * BM > a.n)) return cudaErrorInvalidConfiguration;
+  if (grp)
+    assign_fp32_kernel<true><<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(tmX, tmC, a, *grp);
+  else
+    assign_fp32_kernel<false><<<(unsigned)grid, NTHREADS, SMEM_BYTES, s>>>(tmX, tmC, a,
+                                                                          GroupArgs{});
+  kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,472 @@
+// Batched Lloyd (kmgb_lloyd_batched_f32): many independent problems per call.
+//
+// The reference runs one problem per computeKmeansF call (main/cpp/kmeans.cpp:1316-1361), each
+// with its own allocations, shuffle, initialisation and loop; thousands of small problems are
+// then bound by launches and allocations. Here problems of the same dimension form one group
+// that shares device buffers:
+//   * X: every problem's rows start on a 128-row boundary of one matrix (zero rows in between),
+//     so each 128-row assignment tile belongs to exactly one problem;
+//   * centers: one matrix, problem p owning rows c_off[p] .. c_off[p] + k[p] - 1;
+//   * labels: global center indices.
+// An iteration is then a fixed number of launches for the whole group: center preparation,
+// the grouped FP32 assignment (each tile against its own problem's centers, certified
+// margins), the grouped exact re-rank of uncertified rows, the counting sort with tiles that
+// never cross a problem (the single-problem stable order, problem after problem), the
+// canonical piece sums and the finalize step over all centers, and one warp per problem for
+// its SSE and stop rule. A problem whose loop stopped is skipped by the assignment; its update
+// recomputes the same centers from the same labels. Results per problem are those of the
+// single-problem FP32 tier (and of the oracle) bit for bit: labels, centers, iteration count;
+// SSE to FP64 rounding.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/kmeans_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+using namespace kmgb;
+
+namespace {
+
+constexpr int kTileRows = 128;       // assignment tile (rows of one problem)
+constexpr int kSortTile = 4096;      // counting-sort tile (rows of one problem)
+constexpr long long kMaxRows = 1LL << 30;
+constexpr long long kMaxHist = 60LL << 20;  // scan capacity of the counting sort
+constexpr long long kMaxXBytes = 32LL << 30;
+
+long long rup(long long v, long long m) { return (v + m - 1) / m * m; }
+
+bool on_device(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+struct DevPool {
+  std::vector<void*> ptrs;
+  ~DevPool() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  cudaError_t alloc(T** p, size_t count) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * (count ? count : 1));
+    if (e == cudaSuccess) ptrs.push_back(*p);
+    return e;
+  }
+  template <typename T>
+  cudaError_t upload(T** p, const std::vector<T>& v, cudaStream_t s) {
+    cudaError_t e = alloc(p, v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(*p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, s);
+  }
+};
+
+struct Fail {
+  int code = 0;
+  std::string msg;
+  bool set(cudaError_t e, int c, const char* where) {
+    if (e == cudaSuccess) return false;
+    if (!code) {
+      code = c;
+      msg = std::string("kmgb_lloyd_batched_f32: ") + where + ": " + cudaGetErrorString(e);
+    }
+    return true;
+  }
+};
+
+// Initial centers (k x d each, packed) of the group's problems: the given ones, or the
+// reference initialisation (shuffle + srand(42) picks), computed on all host cores.
+bool initial_centers(const kmgb_problem* pr, const std::vector<int>& ids, int d,
+                     std::vector<float>& C0, const std::vector<int>& c_off, Fail& f) {
+  const int P = (int)ids.size();
+  std::vector<int> bad(P, 0);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  auto work = [&](int lo, int hi) {
+    cudaSetDevice(dev);  // worker threads use the caller's device
+    std::vector<int> perm, picks;
+    for (int i = lo; i < hi; ++i) {
+      const kmgb_problem& q = pr[ids[i]];
+      float* dst = C0.data() + (size_t)c_off[i] * d;
+      if (q.init) {
+        if (on_device(q.init)) {
+          if (cudaMemcpy(dst, q.init, sizeof(float) * (size_t)q.k * d, cudaMemcpyDeviceToHost) !=
+              cudaSuccess)
+            bad[i] = 2;
+        } else {
+          std::memcpy(dst, q.init, sizeof(float) * (size_t)q.k * d);
+        }
+        continue;
+      }
+      if (!reference_picks((int)q.n, q.k, picks)) {
+        bad[i] = 1;
+        continue;
+      }
+      reference_perm((int)q.n, perm);
+      const bool x_dev = on_device(q.X);
+      for (int j = 0; j < q.k; ++j) {
+        const float* src = q.X + (size_t)perm[picks[j]] * d;
+        if (x_dev) {
+          if (cudaMemcpy(dst + (size_t)j * d, src, sizeof(float) * d, cudaMemcpyDeviceToHost) !=
+              cudaSuccess)
+            bad[i] = 2;
+        } else {
+          std::memcpy(dst + (size_t)j * d, src, sizeof(float) * d);
+        }
+      }
+    }
+  };
+  int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  nth = std::min(nth, P);
+  std::vector<std::thread> th;
+  for (int t = 0; t < nth; ++t)
+    th.emplace_back(work, (int)((long long)P * t / nth), (int)((long long)P * (t + 1) / nth));
+  for (auto& t : th) t.join();
+  for (int i = 0; i < P; ++i) {
+    if (bad[i] == 1) {
+      f.code = KMEANS_ERROR_INITIALIZE;
+      f.msg = "kmgb_lloyd_batched_f32: the reference initialisation needs 0 < k <= n";
+      return false;
+    }
+    if (bad[i] == 2) {
+      f.code = KMEANS_ERROR_INITIALIZE;
+      f.msg = "kmgb_lloyd_batched_f32: copying initial centers failed";
+      return false;
+    }
+  }
+  return true;
+}
+
+// One group: problems `ids` (all of dimension d).
+int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_options& o,
+              cudaStream_t s, unsigned long long* reranked, Fail& f) {
+  const int P = (int)ids.size();
+  const long long ldx = rup(d, 4);
+  const int max_iters = std::max(0, o.max_iters);
+  // layout
+  std::vector<long long> rbeg(P), rend(P), hoff(P);
+  std::vector<int> coff(P), kk(P), nt(P);
+  long long rows = 0, nvalid = 0, hist = 0, stiles = 0;
+  long long K = 0;
+  for (int i = 0; i < P; ++i) {
+    const kmgb_problem& q = pr[ids[i]];
+    rbeg[i] = rows;
+    rend[i] = rows + q.n;
+    rows += rup(q.n, kTileRows);
+    nvalid += q.n;
+    coff[i] = (int)K;
+    kk[i] = q.k;
+    K += q.k;
+    nt[i] = (int)((q.n + kSortTile - 1) / kSortTile);
+    hoff[i] = hist;
+    hist += (long long)q.k * nt[i];
+    stiles += nt[i];
+  }
+  const long long tiles = rows / kTileRows;
+  std::vector<int> tile_prob(tiles), stile_prob(stiles), stile_local(stiles), cprob(K);
+  for (int i = 0, st = 0; i < P; ++i) {
+    const long long t0 = rbeg[i] / kTileRows, t1 = t0 + rup(rend[i] - rbeg[i], kTileRows) / kTileRows;
+    for (long long t = t0; t < t1; ++t) tile_prob[t] = i;
+    for (int t = 0; t < nt[i]; ++t, ++st) {
+      stile_prob[st] = i;
+      stile_local[st] = t;
+    }
+    for (int j = 0; j < kk[i]; ++j) cprob[coff[i] + j] = i;
+  }
+  std::vector<float> C0((size_t)K * d);
+  if (!initial_centers(pr, ids, d, C0, coff, f)) return f.code;
+
+  DevPool m;
+  const int E = KMEANS_ERROR_BUILDDATA;
+  float *X = nullptr, *xn = nullptr, *C = nullptr, *Cop = nullptr, *cn = nullptr, *cmax = nullptr;
+  double* qn = nullptr;
+  int *labels = nullptr, *rr_list = nullptr, *rr_count = nullptr, *err = nullptr;
+  unsigned long long* rr_stats = nullptr;
+  if (f.set(m.alloc(&X, (size_t)rows * ldx), E, "data") ||
+      f.set(cudaMemsetAsync(X, 0, sizeof(float) * (size_t)rows * ldx, s), E, "data") ||
+      f.set(m.alloc(&xn, rows), E, "norms") || f.set(m.alloc(&qn, rows), E, "norms") ||
+      f.set(m.alloc(&C, (size_t)K * ldx), E, "centers") ||
+      f.set(m.alloc(&Cop, (size_t)K * ldx), E, "centers") || f.set(m.alloc(&cn, K), E, "centers") ||
+      f.set(m.alloc(&cmax, 1), E, "centers") || f.set(m.alloc(&labels, rows), E, "labels") ||
+      f.set(m.alloc(&rr_list, nvalid), E, "re-rank") || f.set(m.alloc(&rr_count, 1), E, "re-rank") ||
+      f.set(m.alloc(&rr_stats, 2), E, "re-rank") || f.set(m.alloc(&err, 1), E, "error word") ||
+      f.set(cudaMemsetAsync(rr_stats, 0, 2 * sizeof(unsigned long long), s), E, "re-rank") ||
+      f.set(cudaMemsetAsync(err, 0, sizeof(int), s), E, "error word") ||
+      f.set(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)K * ldx, s), E, "centers"))
+    return f.code;
+  // data and initial centers
+  for (int i = 0; i < P; ++i) {
+    const kmgb_problem& q = pr[ids[i]];
+    if (f.set(cudaMemcpy2DAsync(X + (size_t)rbeg[i] * ldx, sizeof(float) * ldx, q.X,
+                                sizeof(float) * d, sizeof(float) * d, q.n,
+                                on_device(q.X) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                s),
+              E, "data upload"))
+      return f.code;
+  }
+  if (f.set(cudaMemcpy2DAsync(C, sizeof(float) * ldx, C0.data(), sizeof(float) * d,
+                              sizeof(float) * d, K, cudaMemcpyHostToDevice, s),
+            KMEANS_ERROR_INITIALIZE, "initial centers"))
+    return f.code;
+  if (f.set(launch_point_norms(X, ldx, rows, d, qn, xn, s), E, "norms")) return f.code;
+
+  // problem tables
+  GroupArgs g{};
+  BatchUpdate b{};
+  int *d_tile_prob = nullptr, *d_coff = nullptr, *d_k = nullptr, *d_nt = nullptr,
+      *d_cprob = nullptr, *d_sprob = nullptr, *d_slocal = nullptr, *d_done = nullptr,
+      *d_iters = nullptr;
+  long long *d_rbeg = nullptr, *d_rend = nullptr, *d_hoff = nullptr;
+  double *d_prev = nullptr, *d_rel = nullptr, *d_hist = nullptr;
+  const int EU = KMEANS_ERROR_CLUSTER_CENTERS;
+  if (f.set(m.upload(&d_tile_prob, tile_prob, s), E, "tables") ||
+      f.set(m.upload(&d_coff, coff, s), E, "tables") || f.set(m.upload(&d_k, kk, s), E, "tables") ||
+      f.set(m.upload(&d_nt, nt, s), E, "tables") || f.set(m.upload(&d_cprob, cprob, s), E, "tables") ||
+      f.set(m.upload(&d_sprob, stile_prob, s), E, "tables") ||
+      f.set(m.upload(&d_slocal, stile_local, s), E, "tables") ||
+      f.set(m.upload(&d_rbeg, rbeg, s), E, "tables") || f.set(m.upload(&d_rend, rend, s), E, "tables") ||
+      f.set(m.upload(&d_hoff, hoff, s), E, "tables") || f.set(m.alloc(&d_done, P), E, "tables") ||
+      f.set(m.alloc(&d_iters, P), E, "tables") || f.set(m.alloc(&d_prev, P), E, "tables") ||
+      f.set(m.upload(&d_rel, std::vector<double>(P, 1.0), s), E, "tables") ||
+      f.set(m.alloc(&d_hist, (size_t)P * std::max(1, max_iters)), E, "tables") ||
+      f.set(cudaMemsetAsync(d_done, 0, sizeof(int) * P, s), E, "tables") ||
+      f.set(cudaMemsetAsync(d_iters, 0, sizeof(int) * P, s), E, "tables") ||
+      f.set(cudaMemsetAsync(d_prev, 0, sizeof(double) * P, s), E, "tables"))
+    return f.code;
+  g.tile_prob = d_tile_prob;
+  g.c_off = d_coff;
+  g.k = d_k;
+  g.row_end = d_rend;
+  g.done = d_done;
+  b.P = P;
+  b.K = (int)K;
+  b.n_valid = nvalid;
+  b.row_beg = d_rbeg;
+  b.row_end = d_rend;
+  b.c_off = d_coff;
+  b.k = d_k;
+  b.hoff = d_hoff;
+  b.ntiles = d_nt;
+  b.cprob = d_cprob;
+  b.stiles = stiles;
+  b.stile_prob = d_sprob;
+  b.stile_local = d_slocal;
+  b.tile_pts = kSortTile;
+  b.hist_elems = hist;
+  b.done = d_done;
+  b.sse_prev = d_prev;
+  b.rel = d_rel;
+  b.iters = d_iters;
+  b.sse_hist = d_hist;
+  b.max_iters = std::max(1, max_iters);
+  b.criterion = o.criterion;
+
+  UpdateWork w{};
+  w.n = nvalid;
+  w.k = (int)K;
+  w.d = d;
+  w.ldx = ldx;
+  w.max_pieces = nvalid / kSumPiece + K + 1;
+  w.err = err;
+  if (f.set(m.alloc(&w.hist, hist), EU, "update") ||
+      f.set(m.alloc(&w.scan_tmp, update_scan_tmp_elems(std::max<long long>(hist, K + 1))), EU,
+            "update") ||
+      f.set(m.alloc(&w.label_off, K + 1), EU, "update") ||
+      f.set(m.alloc(&w.piece_cnt, K + 1), EU, "update") ||
+      f.set(m.alloc(&w.sorted, nvalid), EU, "update") ||
+      f.set(m.alloc(&w.part, (size_t)w.max_pieces * d), EU, "update") ||
+      f.set(m.alloc(&w.partq, w.max_pieces), EU, "update") ||
+      f.set(m.alloc(&w.sse_k, (size_t)K * ((d + 31) / 32)), EU, "update") ||
+      f.set(m.alloc(&w.counts, K), EU, "update"))
+    return f.code;
+
+  AssignArgs a{};
+  a.cn = cn;
+  a.xnorm = xn;
+  a.cmax = cmax;
+  a.labels = labels;
+  a.rerank_list = rr_list;
+  a.rerank_count = rr_count;
+  a.err = err;
+  a.n = rows;
+  a.k = (int)K;
+  a.d = d;
+  a.certify = o.certify ? 1 : 0;
+  a.gamma = assign_fp32_gamma(d);
+  RerankArgs ra{};
+  ra.X = X;
+  ra.ldx = ldx;
+  ra.C = Cop;
+  ra.ldc = ldx;
+  ra.cn = cn;
+  ra.list = rr_list;
+  ra.count = rr_count;
+  ra.labels = labels;
+  ra.stats = rr_stats;
+  ra.n = rows;
+  ra.k = (int)K;
+  ra.d = d;
+  ra.mode = 0;
+  ra.max_list = nvalid;
+  for (int it = 0; it < max_iters; ++it) {
+    if (f.set(cudaMemsetAsync(cmax, 0, sizeof(float), s), EU, "centers") ||
+        f.set(launch_prep_centers(C, ldx, (int)K, d, Cop, nullptr, 0, cn, cmax, s), EU,
+              "center preparation") ||
+        f.set(cudaMemsetAsync(rr_count, 0, sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS,
+              "re-rank") ||
+        f.set(launch_assign_fp32(X, ldx, Cop, ldx, a, s, &g, tiles), KMEANS_ERROR_CLOSEST_CENTERS,
+              "assignment") ||
+        (o.certify && f.set(launch_rerank_grouped(ra, g, s), KMEANS_ERROR_CLOSEST_CENTERS,
+                            "re-rank")) ||
+        f.set(launch_update_batched(X, ldx, d, qn, labels, C, ldx, o.empty_policy, w, b, it, s),
+              EU, "update"))
+      return f.code;
+    if (o.criterion >= 0.0) {  // stop early once every problem's rule has fired
+      std::vector<int> done(P);
+      if (f.set(cudaMemcpyAsync(done.data(), d_done, sizeof(int) * P, cudaMemcpyDeviceToHost, s),
+                EU, "stop flags") ||
+          f.set(cudaStreamSynchronize(s), EU, "stop flags"))
+        return f.code;
+      if (std::all_of(done.begin(), done.end(), [](int v) { return v != 0; })) break;
+    }
+  }
+  // results
+  std::vector<int> lab(rows), iters(P);
+  std::vector<float> Ch((size_t)K * d);
+  std::vector<double> rel(P), sh((size_t)P * std::max(1, max_iters));
+  int e = 0;
+  const int EG = KMEANS_ERROR_GET_CENTERS;
+  if (f.set(cudaMemcpyAsync(lab.data(), labels, sizeof(int) * rows, cudaMemcpyDeviceToHost, s), EG,
+            "labels") ||
+      f.set(cudaMemcpy2DAsync(Ch.data(), sizeof(float) * d, C, sizeof(float) * ldx,
+                              sizeof(float) * d, K, cudaMemcpyDeviceToHost, s),
+            EG, "centers") ||
+      f.set(cudaMemcpyAsync(iters.data(), d_iters, sizeof(int) * P, cudaMemcpyDeviceToHost, s), EG,
+            "iterations") ||
+      f.set(cudaMemcpyAsync(rel.data(), d_rel, sizeof(double) * P, cudaMemcpyDeviceToHost, s), EG,
+            "relErr") ||
+      f.set(cudaMemcpyAsync(sh.data(), d_hist, sizeof(double) * sh.size(), cudaMemcpyDeviceToHost,
+                            s),
+            EG, "SSE") ||
+      f.set(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, s), EG, "error word") ||
+      f.set(cudaStreamSynchronize(s), EG, "results"))
+    return f.code;
+  unsigned long long rs[2] = {0, 0};
+  if (f.set(cudaMemcpy(rs, rr_stats, sizeof(rs), cudaMemcpyDeviceToHost), EG, "statistics"))
+    return f.code;
+  *reranked += rs[0];
+  if (e) {
+    f.code = e == KMGB_DEV_BAD_LABEL ? KMEANS_ERROR_CLUSTER_CENTERS : KMEANS_ERROR_CLOSEST_CENTERS;
+    f.msg = "kmgb_lloyd_batched_f32: device error word " + std::to_string(e);
+    return f.code;
+  }
+  for (int i = 0; i < P; ++i) {
+    kmgb_problem& q = pr[ids[i]];
+    if (q.labels)
+      for (long long r = 0; r < q.n; ++r) q.labels[r] = lab[rbeg[i] + r] - coff[i];
+    if (q.centers) std::memcpy(q.centers, Ch.data() + (size_t)coff[i] * d, sizeof(float) * q.k * d);
+    q.iterations = iters[i];
+    if (q.sse)
+      for (int t = 0; t < iters[i]; ++t) q.sse[t] = sh[(size_t)i * b.max_iters + t];
+    // kmeans.hpp:198-200: success only when relErr (1 before the first iteration) <= criterion
+    q.status = (rel[i] <= o.criterion) ? KMEANS_SUCCESS : KMEANS_NONCONVERGENCE;
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const kmgb_options* opt,
+                                      kmgb_stats* stats) {
+  const auto t0 = std::chrono::steady_clock::now();
+  kmgb_options o;
+  if (opt) o = *opt;
+  else kmgb_default_options(&o);
+  auto reject = [](int code, const char* msg) {
+    set_last_error(msg);
+    return code;
+  };
+  if (!problems || count <= 0) return reject(KMEANS_ERROR_BUILDDATA, "kmgb_lloyd_batched_f32: no problems");
+  if (o.assign_tier != KMGB_ASSIGN_FP32 || o.mini_batch_fraction < 1.0f || o.stream_tile_rows > 0 ||
+      o.init_algorithm == KMGB_INIT_KMEANSPP)
+    return reject(KMEANS_ERROR_BUILDDATA,
+                  "kmgb_lloyd_batched_f32: batched problems use the FP32 tier, full batches, "
+                  "resident data and the reference or given initialisation");
+  for (int i = 0; i < count; ++i) {
+    const kmgb_problem& q = problems[i];
+    if (!q.X || q.n <= 0 || q.d <= 0 || q.k <= 0 || q.n >= kMaxRows || q.k > (1 << 24))
+      return reject(KMEANS_ERROR_BUILDDATA,
+                    "kmgb_lloyd_batched_f32: every problem needs X, 0 < n < 2^30, d > 0, k > 0");
+    if (!q.init && q.k > q.n)
+      return reject(KMEANS_ERROR_INITIALIZE,
+                    "kmgb_lloyd_batched_f32: the reference initialisation needs k <= n");
+  }
+  for (int i = 0; i < count; ++i) {
+    problems[i].iterations = 0;
+    problems[i].status = KMEANS_NONCONVERGENCE;
+  }
+  // groups: problems of one dimension, split so that every group fits the index and scan limits
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return problems[x].d < problems[y].d; });
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+    return reject(KMEANS_ERROR_BUILDDATA, "kmgb_lloyd_batched_f32: stream creation failed");
+  Fail f;
+  unsigned long long reranked = 0;
+  size_t i = 0;
+  while (i < order.size() && !f.code) {
+    const int d = problems[order[i]].d;
+    const long long ldx = rup(d, 4);
+    std::vector<int> ids;
+    long long rows = 0, hist = 0, K = 0;
+    while (i < order.size() && problems[order[i]].d == d) {
+      const kmgb_problem& q = problems[order[i]];
+      const long long r = rup(q.n, kTileRows);
+      const long long h = (long long)q.k * ((q.n + kSortTile - 1) / kSortTile);
+      if (!ids.empty() && (rows + r > kMaxRows || hist + h > kMaxHist || K + q.k > (1LL << 30) ||
+                           (rows + r) * ldx * 4 > kMaxXBytes))
+        break;
+      if (h > kMaxHist) {
+        f.code = KMEANS_ERROR_BUILDDATA;
+        f.msg = "kmgb_lloyd_batched_f32: a problem's k x ceil(n/4096) exceeds the sort capacity";
+        break;
+      }
+      ids.push_back(order[i]);
+      rows += r;
+      hist += h;
+      K += q.k;
+      ++i;
+    }
+    if (f.code) break;
+    run_group(problems, ids, d, o, s, &reranked, f);
+  }
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  if (stats) {
+    std::memset(stats, 0, sizeof(*stats));
+    int it = 0;
+    for (int j = 0; j < count; ++j) it = std::max(it, problems[j].iterations);
+    stats->iterations = it;
+    stats->status = f.code;
+    stats->reranked = reranked;
+    stats->ms_total =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  }
+  if (f.code) {
+    set_last_error(f.msg.c_str());
+    return f.code;
+  }
+  return 0;
+}

@@ -77,7 +77,7 @@ bool is_device_ptr(const void* p) {
 void kmgb::set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 
 // Reference shuffle permutation (kmeans.cpp:554-557): perm[i] = source row of shuffled row i.
-static void reference_perm(int m, std::vector<int>& perm) {
+void kmgb::reference_perm(int m, std::vector<int>& perm) {
   perm.resize(m);
   for (int i = 0; i < m; ++i) perm[i] = i;
   unsigned seed = 0;
@@ -88,7 +88,7 @@ static void reference_perm(int m, std::vector<int>& perm) {
 // binary_search over the unsorted pick list finds the index. glibc random_r with a private
 // TYPE_3 state seeded with 42 yields the srand(42)/rand() stream without touching the
 // process-wide generator.
-static bool reference_picks(int m, int k, std::vector<int>& picks) {
+bool kmgb::reference_picks(int m, int k, std::vector<int>& picks) {
   if (m <= 0 || k <= 0 || k > m) return false;
   struct random_data rd;
   std::memset(&rd, 0, sizeof(rd));

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace kmgb {
 
 // Certified assignment: labels plus a list of points whose top-2 margin does not prove the
@@ -35,9 +37,22 @@ struct AssignArgs {
   const int* stop;        // device stop flag of the run (nullable)
 };
 
+// Many problems of one dimension in one launch (batched Lloyd): problem p owns rows
+// R_p .. row_end[p]-1 of X (R_p a multiple of 128) and centers c_off[p] .. c_off[p]+k[p]-1.
+struct GroupArgs {
+  const int* tile_prob;       // [tiles] problem of each 128-row tile
+  const int* c_off;           // [P] first center of the problem (global index)
+  const int* k;               // [P] centers of the problem
+  const long long* row_end;   // [P] one past the problem's last row
+  const int* done;            // [P] nullable: problems whose loop has stopped (skipped)
+};
+
 // FP32 SIMT assignment. X: [n][ldx] FP32, Cop: [k][ldc] FP32 (ld multiples of 4 floats).
+// With grp: `tiles` 128-row tiles of grouped problems (a.n = rows of X, a.k = all centers);
+// labels are global center indices.
 cudaError_t launch_assign_fp32(const float* X, long long ldx, const float* Cop, long long ldc,
-                               const AssignArgs& a, cudaStream_t s);
+                               const AssignArgs& a, cudaStream_t s,
+                               const GroupArgs* grp = nullptr, long long tiles = 0);
 float assign_fp32_gamma(int d);
 
 // tcgen05 BF16 assignment. Xb: [n][ldb] BF16, Cb: [k][ldb] BF16, ldb a multiple of 8. With the
@@ -71,6 +86,9 @@ cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s);
 // hi2[slot] receives the FP32 upper end of the best center of every point passed on.
 cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, float* hi2,
                                 cudaStream_t s);
+// Grouped problems (batched Lloyd): one CTA per flagged row over its own problem's centers
+// (FP32 band, then FP64); a.C / a.cn cover all problems' centers, a.stats (nullable) counts.
+cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaStream_t s);
 // FP64 stage over list2 (one CTA per point), candidates bounded by hi2.
 cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s);
 // Candidate re-rank of the BF16 tiers: compact copy of up to `cap` flagged rows (the rest go to
@@ -156,6 +174,38 @@ cudaError_t launch_stream_finalize(const double* accS, const int* accN, const do
                                    float* C, long long ldc, int empty_policy, const UpdateWork& w,
                                    double* sse_out, cudaStream_t s);
 
+// Batched Lloyd update (problems of one dimension sharing X and one center matrix; labels are
+// global center indices). Device arrays; see launch_update_batched.
+struct BatchUpdate {
+  int P;                        // problems
+  int K;                        // centers of all problems
+  long long n_valid;            // rows of all problems (padding rows excluded)
+  const long long* row_beg;     // [P] first row of the problem
+  const long long* row_end;     // [P] one past its last row
+  const int* c_off;             // [P] first center
+  const int* k;                 // [P] centers
+  const long long* hoff;        // [P] first counter of the problem in hist
+  const int* ntiles;            // [P] sort tiles of the problem
+  const int* cprob;             // [K] problem of each center
+  long long stiles;             // sort tiles of all problems
+  const int* stile_prob;        // [stiles]
+  const int* stile_local;       // [stiles] tile index inside its problem
+  int tile_pts;                 // rows per sort tile
+  long long hist_elems;         // sum over problems of k * ntiles
+  // per-problem loop state (device)
+  int* done;                    // [P] 1 once the problem's stop rule fired
+  double* sse_prev;             // [P]
+  double* rel;                  // [P] last relErr
+  int* iters;                   // [P] iterations recorded
+  double* sse_hist;             // [P][max_iters]
+  int max_iters;
+  double criterion;
+};
+cudaError_t launch_update_batched(const float* X, long long ldx, int d, const double* qn,
+                                  const int* labels, float* C, long long ldc, int empty_policy,
+                                  const UpdateWork& w, const BatchUpdate& b, int iter,
+                                  cudaStream_t s);
+
 // Mini-batch gather: rows perm[(start + r) mod m] of Xsrc into Xdst (m_mb rows).
 cudaError_t launch_gather_rows(const float* Xsrc, long long ldx, const int* perm, long long m,
                                long long start, long long m_mb, int d, float* Xdst,
@@ -183,6 +233,11 @@ constexpr int kMaxCand = 16;  // candidate centers recorded per flagged point
 // BF16 tiers: centers per tensor-core chunk; the start values and diagnostic accumulators are
 // padded to a whole number of chunks
 constexpr int kCenterPad = 256;
+
+// Host: the reference's shuffle permutation (perm[i] = source row of shuffled row i) and its
+// initial picks (srand(42) / rand() % m, kmeans.cpp:554-557, 876-883); engine.cu.
+void reference_perm(int m, std::vector<int>& perm);
+bool reference_picks(int m, int k, std::vector<int>& picks);
 
 // Message returned by kmgb_last_error() on the calling thread.
 void set_last_error(const char* msg);

@@ -333,6 +333,78 @@ rerank_exact_kernel(RerankArgs a, const float* __restrict__ hi2) {
   }
 }
 
+// Grouped (batched Lloyd) re-rank, one CTA per flagged row of any problem: the row's own
+// problem (tile_prob[row / 128]) gives its center range. Pass 1 finds the smallest FP32
+// direct-form value over the usable centers and its upper end; pass 2 evaluates in FP64 (as the
+// oracle does) every center whose FP32 lower end is within it. Labels are global indices.
+__global__ void __launch_bounds__(256)
+rerank_grouped_kernel(RerankArgs a, GroupArgs g) {
+  if (stopped(a.stop)) return;
+  extern __shared__ float xsm[];
+  __shared__ float rf[8];
+  __shared__ double rb[8];
+  __shared__ int ri[8];
+  const long long cnt = min((long long)*(volatile const int*)a.count, a.max_list);
+  const float u = 5.9604645e-8f;
+  const float gam = (float)(a.d + 4) * 2.0f * u * 1.01f;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nw = (int)(blockDim.x >> 5);
+  for (long long slot = blockIdx.x; slot < cnt; slot += gridDim.x) {
+    __syncthreads();
+    const int pt = a.list[slot];
+    const int prob = g.tile_prob[pt >> 7];
+    const int cbeg = g.c_off[prob], kp = g.k[prob];
+    const float* x = a.X + (size_t)pt * a.ldx;
+    for (int t = threadIdx.x; t < a.d; t += blockDim.x) xsm[t] = x[t];
+    __syncthreads();
+    float lo = INFINITY;
+    for (int j = threadIdx.x; j < kp; j += blockDim.x) {
+      if (!(a.cn[cbeg + j] < INFINITY)) continue;
+      lo = fminf(lo, approx_value(0, xsm, a.C + (size_t)(cbeg + j) * a.ldc, a.d, 0.0f));
+    }
+    for (int o = 16; o > 0; o >>= 1) lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    if (lane == 0) rf[w] = lo;
+    __syncthreads();
+    float best_lo = rf[0];
+    for (int ww = 1; ww < nw; ++ww) best_lo = fminf(best_lo, rf[ww]);
+    const float best_hi = best_lo * (1.0f + gam) + 1e-30f;
+    double best = INFINITY;
+    int bidx = -1;
+    for (int j = threadIdx.x; j < kp; j += blockDim.x) {
+      if (!(a.cn[cbeg + j] < INFINITY)) continue;
+      const float* c = a.C + (size_t)(cbeg + j) * a.ldc;
+      const float v = approx_value(0, xsm, c, a.d, 0.0f);
+      if (!(v * (1.0f - gam) - 1e-30f <= best_hi)) continue;
+      const double ex = exact_value(0, xsm, c, a.d, 0.0f);
+      if (ex < best) {
+        best = ex;
+        bidx = j;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
+      const bool take = (ob < best) || (ob == best && (unsigned)oi < (unsigned)bidx);
+      best = take ? ob : best;
+      bidx = take ? oi : bidx;
+    }
+    if (lane == 0) {
+      rb[w] = best;
+      ri[w] = bidx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int ww = 1; ww < nw; ++ww) {
+        const bool take = (rb[ww] < best) || (rb[ww] == best && (unsigned)ri[ww] < (unsigned)bidx);
+        best = take ? rb[ww] : best;
+        bidx = take ? ri[ww] : bidx;
+      }
+      a.labels[pt] = cbeg + (bidx < 0 ? 0 : bidx);
+      if (a.stats) atomicAdd(a.stats, 1ull);
+    }
+  }
+}
+
 }  // namespace
 
 namespace {
@@ -559,6 +631,18 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, fl
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_tiled_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   rerank_tiled_kernel<<<152 * 2, 256, smem, s>>>(a, list2, count2, hi2);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaStream_t s) {
+  if (a.n <= 0 || a.k <= 0) return cudaSuccess;
+  const size_t smem = sizeof(float) * (size_t)a.d;
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024)
+    KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_grouped_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  rerank_grouped_kernel<<<152 * 4, 256, smem, s>>>(a, g);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -396,6 +396,46 @@ __global__ void finalize_kernel(const double* __restrict__ part, const double* _
   }
 }
 
+// Clusters whose identity SSE (Q - 2 mu.S + n |mu|^2, summed over the groups) is within
+// 1e-9 Q of zero -- singletons, duplicates, variance far below the magnitude of the points --
+// get their SSE again in the direct form sum_i sum_d ((double)x - (double)mu)^2 over the
+// members (exactly 0 when every member equals the center, as the reference's compactness,
+// Compactness.cu:3-59, gives); the identity's cancellation error is of the order of 1e-15 Q.
+// One warp per center; the direct sum only runs for flagged clusters.
+__global__ void sse_fixup_kernel(double* __restrict__ sse_k, int groups,
+                                 const double* __restrict__ partq, const int* __restrict__ label_off,
+                                 const int* __restrict__ pstart, int k, int d,
+                                 const float* __restrict__ X, long long ldx,
+                                 const int* __restrict__ sorted, const float* __restrict__ C,
+                                 long long ldc, const int* stop) {
+  if (stopped(stop)) return;
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= k) return;
+  const int j = (int)wid;
+  const int m0 = label_off[j], m1 = label_off[j + 1];
+  if (m1 <= m0) return;
+  double t = 0.0, q = 0.0;
+  for (int g = lane; g < groups; g += 32) t += sse_k[(size_t)j * groups + g];
+  for (int p = pstart[j] + lane; p < pstart[j + 1]; p += 32) q += partq[p];
+  for (int o = 16; o > 0; o >>= 1) {
+    t += __shfl_xor_sync(0xffffffffu, t, o);
+    q += __shfl_xor_sync(0xffffffffu, q, o);
+  }
+  if (!(fabs(t) <= 1e-9 * q)) return;
+  const float* mu = C + (size_t)j * ldc;
+  double s = 0.0;
+  for (int m = m0; m < m1; ++m) {
+    const float* x = X + (size_t)sorted[m] * ldx;
+    for (int c = lane; c < d; c += 32) {
+      const double u = (double)x[c] - (double)mu[c];
+      s = fma(u, u, s);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  for (int g = lane; g < groups; g += 32) sse_k[(size_t)j * groups + g] = (g == 0) ? s : 0.0;
+}
+
 // Second level of the SSE reduction plus the loop's stop rule (kmeans.cpp:1234-1237,1194):
 // relErr = |SSE - SSE_old| / |SSE|; the run stops once !(relErr > criterion), NaN included.
 __global__ void sse_reduce_kernel(const double* __restrict__ sse_k, int k, double* __restrict__ out,
@@ -505,6 +545,13 @@ cudaError_t launch_update(const float* X, const double* qn, const int* labels, f
       w.part, qn ? w.partq : nullptr, w.label_off, w.piece_cnt, k, w.d, C, ldc, empty_policy,
       w.sse_k, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
+  if (qn) {
+    sse_fixup_kernel<<<(unsigned)((k * 32LL + 255) / 256), 256, 0, s>>>(
+        w.sse_k, (w.d + 31) / 32, w.partq, w.label_off, w.piece_cnt, k, w.d, X, w.ldx, w.sorted, C,
+        ldc, w.stop);
+    kmgb::count_launches(1);
+    KMGB_CUDA_TRY(cudaGetLastError());
+  }
   if (sse_out) {
     sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, (int)fin_warps, sse_out, w.stop, w.criterion,
                                          w.sse_prev, w.rel_out, w.iters_done); kmgb::count_launches(1);
@@ -677,5 +724,165 @@ template cudaError_t launch_finalize_acc<float>(const double*, const int*, int, 
                                                 cudaStream_t);
 template cudaError_t launch_finalize_acc<double>(const double*, const int*, int, int, double*, int*,
                                                  cudaStream_t);
+
+// ---------------------------------------------------------------------------------------
+// Batched Lloyd: many problems of one dimension share X (problem p: rows row_beg[p] ..
+// row_end[p]-1) and one center matrix (problem p: centers c_off[p] .. c_off[p]+k[p]-1), labels
+// being global center indices. The counting sort uses tiles of tile_pts rows that never cross a
+// problem; problem p's counters are hist[hoff[p] + j * ntiles[p] + t] (center j, tile t), so the
+// exclusive scan of hist in memory order is the stable order by global label, i.e. problem by
+// problem, each sorted exactly as a single problem would be. Piece sums and the finalize step
+// are the single-problem kernels over all K centers.
+namespace {
+
+__global__ void hist_batched_kernel(const int* __restrict__ labels, BatchUpdate b,
+                                    int* __restrict__ hist, int* err) {
+  const long long st = blockIdx.x;
+  const int prob = b.stile_prob[st];
+  const int tl = b.stile_local[st];
+  const long long i0 = b.row_beg[prob] + (long long)tl * b.tile_pts;
+  const long long i1 = min(b.row_end[prob], i0 + b.tile_pts);
+  const int cb = b.c_off[prob], kp = b.k[prob], nt = b.ntiles[prob];
+  int* h = hist + b.hoff[prob];
+  const int lane = threadIdx.x & 31;
+  for (long long base = i0; base < i1; base += blockDim.x) {
+    const long long i = base + threadIdx.x;
+    int l = -1;
+    if (i < i1) {
+      l = labels[i] - cb;
+      if (l < 0 || l >= kp) {
+        set_error(err, KMGB_DEV_BAD_LABEL);
+        l = -1;
+      }
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    const int leader = __ffs(peers) - 1;
+    if (l >= 0 && lane == leader) atomicAdd(&h[(size_t)l * nt + tl], __popc(peers));
+  }
+}
+
+// label_off[g] = first sorted position of global center g (label_off[K] = rows), piece counts
+// and member counts, from the scanned counters.
+__global__ void label_offsets_batched_kernel(const int* __restrict__ hist, BatchUpdate b,
+                                             int* __restrict__ label_off, int* __restrict__ piece_cnt,
+                                             long long* __restrict__ counts) {
+  const int gc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gc > b.K) return;
+  auto start = [&](int c) -> int {
+    if (c >= b.K) return (int)b.n_valid;
+    const int prob = b.cprob[c];
+    return hist[b.hoff[prob] + (size_t)(c - b.c_off[prob]) * b.ntiles[prob]];
+  };
+  if (gc == b.K) {
+    label_off[b.K] = (int)b.n_valid;
+    piece_cnt[b.K] = 0;
+    return;
+  }
+  const int a0 = start(gc), a1 = start(gc + 1);
+  label_off[gc] = a0;
+  piece_cnt[gc] = (a1 - a0 + kSumPiece - 1) / kSumPiece;
+  if (counts) counts[gc] = a1 - a0;
+}
+
+__global__ void scatter_batched_kernel(const int* __restrict__ labels, BatchUpdate b, int* pos,
+                                       int* __restrict__ sorted) {
+  const long long st = blockIdx.x;
+  const int prob = b.stile_prob[st];
+  const int tl = b.stile_local[st];
+  const long long i0 = b.row_beg[prob] + (long long)tl * b.tile_pts;
+  const long long i1 = min(b.row_end[prob], i0 + b.tile_pts);
+  const int cb = b.c_off[prob], kp = b.k[prob], nt = b.ntiles[prob];
+  volatile int* vpos = pos + b.hoff[prob];
+  const int lane = threadIdx.x;
+  for (long long base = i0; base < i1; base += 32) {
+    const long long i = base + lane;
+    int l = -1;
+    if (i < i1) {
+      l = labels[i] - cb;
+      if (l < 0 || l >= kp) l = -1;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    const int leader = __ffs(peers) - 1;
+    const int rank = __popc(peers & lanemask_lt());
+    int bs = 0;
+    if (l >= 0 && lane == leader) bs = vpos[(size_t)l * nt + tl];
+    bs = __shfl_sync(0xffffffffu, bs, leader);
+    if (l >= 0) sorted[bs + rank] = (int)i;
+    if (l >= 0 && lane == leader) vpos[(size_t)l * nt + tl] = bs + __popc(peers);
+    __syncwarp();
+  }
+}
+
+// One warp per problem: SSE = sum of its centers' terms; the reference's stop rule per problem
+// (kmeans.cpp:1194-1237). A problem that has stopped keeps its history; its centers are
+// recomputed from unchanged labels, which reproduces them bit for bit.
+__global__ void sse_batched_kernel(const double* __restrict__ sse_k, int groups, BatchUpdate b,
+                                   int iter) {
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wid >= b.P) return;
+  const int prob = (int)wid;
+  if (b.done[prob]) return;
+  const long long e0 = (long long)b.c_off[prob] * groups;
+  const long long e1 = e0 + (long long)b.k[prob] * groups;
+  double s = 0.0;
+  for (long long e = e0 + lane; e < e1; e += 32) s += sse_k[e];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const double rel = fabs(s - b.sse_prev[prob]) / fabs(s);
+    b.sse_prev[prob] = s;
+    b.rel[prob] = rel;
+    b.sse_hist[(size_t)prob * b.max_iters + iter] = s;
+    b.iters[prob] = iter + 1;
+    if (!(rel > b.criterion)) b.done[prob] = 1;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_update_batched(const float* X, long long ldx, int d, const double* qn,
+                                  const int* labels, float* C, long long ldc, int empty_policy,
+                                  const UpdateWork& w, const BatchUpdate& b, int iter,
+                                  cudaStream_t s) {
+  if (b.P <= 0 || b.K <= 0 || b.n_valid <= 0) return cudaSuccess;
+  KMGB_CUDA_TRY(cudaMemsetAsync(w.hist, 0, sizeof(int) * b.hist_elems, s));
+  hist_batched_kernel<<<(unsigned)b.stiles, 256, 0, s>>>(labels, b, w.hist, w.err);
+  count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  KMGB_CUDA_TRY(excl_scan(w.hist, b.hist_elems, w.scan_tmp, s, nullptr));
+  label_offsets_batched_kernel<<<(b.K + 1 + 255) / 256, 256, 0, s>>>(w.hist, b, w.label_off,
+                                                                    w.piece_cnt, w.counts);
+  count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  KMGB_CUDA_TRY(excl_scan(w.piece_cnt, b.K + 1, w.scan_tmp, s, nullptr));
+  scatter_batched_kernel<<<(unsigned)b.stiles, 32, 0, s>>>(labels, b, w.hist, w.sorted);
+  count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  const long long max_pieces = w.max_pieces;
+  const long long warps = max_pieces < 152LL * 64 ? max_pieces : 152LL * 64;
+  if (ldx % 4 == 0 && d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
+    piece_sums_vec4_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+        X, ldx, qn, w.sorted, w.label_off, w.piece_cnt, b.K, d, w.part, w.partq, nullptr);
+  else
+    piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
+        X, ldx, qn, w.sorted, w.label_off, w.piece_cnt, b.K, d, w.part, w.partq, nullptr);
+  count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  const int groups = (d + 31) / 32;
+  const long long fin_warps = (long long)b.K * groups;
+  finalize_kernel<<<(unsigned)((fin_warps * 32 + 255) / 256), 256, 0, s>>>(
+      w.part, w.partq, w.label_off, w.piece_cnt, b.K, d, C, ldc, empty_policy, w.sse_k, nullptr);
+  count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  sse_fixup_kernel<<<(unsigned)((b.K * 32LL + 255) / 256), 256, 0, s>>>(
+      w.sse_k, groups, w.partq, w.label_off, w.piece_cnt, b.K, d, X, ldx, w.sorted, C, ldc,
+      nullptr);
+  count_launches(1);
+  KMGB_CUDA_TRY(cudaGetLastError());
+  sse_batched_kernel<<<(unsigned)((b.P * 32LL + 255) / 256), 256, 0, s>>>(w.sse_k, groups, b,
+                                                                         iter);
+  count_launches(1);
+  return cudaGetLastError();
+}
 
 }  // namespace kmgb

@@ -1,0 +1,101 @@
+"""GPU parity of batched Lloyd (kmgb_lloyd_batched_f32): every problem of a batch equals the
+oracle's single-problem loop -- labels and centers bit-exact, SSE within 1e-10 relative,
+iteration count and status equal -- for mixed dimensions, sizes, inits, stop rules and empty
+clusters."""
+import numpy as np
+import pytest
+
+from kmeans_gb300.synthetic import mixture_numpy, sample_init
+
+pytestmark = pytest.mark.gpu
+SSE_RTOL = 1e-10
+
+
+def check(res, ref):
+    st, c, lab, sse, it = ref
+    assert res.iterations == it
+    assert res.status == st
+    assert np.array_equal(res.labels, lab)
+    assert np.array_equal(res.centers, c, equal_nan=True)
+    np.testing.assert_allclose(res.sse, sse, rtol=SSE_RTOL)
+
+
+def make_batch(count, seed, dims=(3, 16, 32, 64, 128, 130), nmax=20_000, kmax=316):
+    rng = np.random.default_rng(seed)
+    probs = []
+    for i in range(count):
+        d = int(rng.choice(dims))
+        n = int(np.exp(rng.uniform(np.log(1), np.log(nmax))))
+        k = int(max(1, min(n, kmax, round(np.sqrt(max(n, 1) / 2)) + int(rng.integers(0, 3)))))
+        X, _, _ = mixture_numpy(n, d, max(1, k), seed=seed * 1000 + i)
+        init = None
+        if i % 3 == 1:  # explicit, point-sampled init
+            init = X[sample_init(n, k, seed=i)]
+        probs.append((X, k, init))
+    return probs
+
+
+def test_mixed_batch_matches_oracle(km, orc, torch_cuda):
+    probs = make_batch(40, 5)
+    res, st = km.lloyd_batched(probs, max_iters=6)
+    for (X, k, init), r in zip(probs, res):
+        ini = orc.reference_init(X, k) if init is None else init
+        check(r, orc.lloyd(X, ini, 6))
+    assert st.iterations == 6
+
+
+def test_per_problem_stop_rule(km, orc, torch_cuda):
+    probs = make_batch(24, 9, dims=(8, 32), nmax=5000, kmax=20)
+    res, st = km.lloyd_batched(probs, max_iters=60, criterion=1e-4)
+    iters = set()
+    for (X, k, init), r in zip(probs, res):
+        ini = orc.reference_init(X, k) if init is None else init
+        ref = orc.lloyd(X, ini, 60, criterion=1e-4)
+        check(r, ref)
+        iters.add(r.iterations)
+    assert len(iters) > 1  # the problems stopped at different iterations
+
+
+@pytest.mark.parametrize("policy", [0, 1])
+def test_empty_clusters(km, orc, torch_cuda, policy):
+    probs = []
+    for i, d in enumerate((4, 33)):
+        X, _, _ = mixture_numpy(3000, d, 6, seed=40 + i)
+        init = X[sample_init(len(X), 9, seed=i)].copy()
+        init[5] = init[2]  # duplicate centers: one of each pair stays empty
+        init[7] = 1e6      # far away: empty
+        probs.append((X, 9, init))
+    res, _ = km.lloyd_batched(probs, max_iters=4, empty_policy=policy)
+    for (X, k, init), r in zip(probs, res):
+        check(r, orc.lloyd(X, init, 4, empty_policy=policy))
+
+
+def test_matches_single_problem_calls(km, orc, torch_cuda):
+    probs = make_batch(6, 13, dims=(24,), nmax=30_000, kmax=64)
+    res, _ = km.lloyd_batched(probs, max_iters=5)
+    for (X, k, init), r in zip(probs, res):
+        one = km.lloyd(X, k, init=init, max_iters=5)
+        assert np.array_equal(one.labels, r.labels)
+        assert np.array_equal(one.centers, r.centers, equal_nan=True)
+
+
+def test_many_small_problems(km, orc, torch_cuda):
+    probs = make_batch(2000, 21, dims=(16, 32, 64, 128), nmax=3000, kmax=40)
+    res, st = km.lloyd_batched(probs, max_iters=3)
+    rng = np.random.default_rng(0)
+    for i in rng.choice(len(probs), 60, replace=False):
+        X, k, init = probs[i]
+        ini = orc.reference_init(X, k) if init is None else init
+        check(res[i], orc.lloyd(X, ini, 3))
+
+
+def test_rejections(km, torch_cuda):
+    X, _, _ = mixture_numpy(500, 8, 4, seed=3)
+    with pytest.raises(km.KmeansError):
+        km.lloyd_batched([(X, 501)])  # reference init needs k <= n
+    arr = (km.kmgb_problem * 1)()
+    arr[0].X, arr[0].n, arr[0].d, arr[0].k = X.ctypes.data, 500, 8, 4
+    for kw in ({"assign_tier": km.ASSIGN_BF16X3}, {"mini_batch_fraction": 0.5},
+               {"init_algorithm": km.INIT_KMEANSPP}):
+        opt = km.default_options(**kw)
+        assert km.lib().kmgb_lloyd_batched_f32(arr, 1, km.C.byref(opt), None) == 1
