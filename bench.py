@@ -212,6 +212,68 @@ def time_kmeanspp(km, torch, h, n, k, reps=1):
             "frac": gbs / hbm, "peak_source": f"{src} HBM copy (MEASURED_PEAKS.json)"}
 
 
+def batched_problems(count, seed=2024):
+    """The many-problems workload: N_i log-uniform in [256, 2e5], D_i uniform in {16,32,64,128},
+    K_i = clamp(round(sqrt(N_i/2)), 4, 512), K_i isotropic unit-variance Gaussians with means
+    U[-10,10]^D, equal weights (seeded, synthetic)."""
+    rng = np.random.default_rng(seed)
+    probs = []
+    for _ in range(count):
+        n = int(np.exp(rng.uniform(np.log(256), np.log(2e5))))
+        d = int(rng.choice([16, 32, 64, 128]))
+        k = int(min(512, max(4, round(np.sqrt(n / 2)))))
+        means = rng.uniform(-10, 10, (k, d)).astype(np.float32)
+        X = means[rng.integers(0, k, n)] + rng.standard_normal((n, d), dtype=np.float32)
+        probs.append((X, k))
+    return probs
+
+
+def batched_workload(args):
+    """15 Lloyd iterations of every problem in one kmgb_lloyd_batched_f32 call (host data,
+    reference initialisation per problem, uploads and result copies inside the call)."""
+    import kmeans_gb300 as km
+    km.build()
+    iters = 15
+    t0 = time.perf_counter()
+    probs = batched_problems(args.problems)
+    gen_s = time.perf_counter() - t0
+    rows = sum(len(p[0]) for p in probs)
+    flop = sum(2.0 * len(X) * k * X.shape[1] for X, k in probs)
+    km.lloyd_batched(probs[:64], max_iters=2)  # warm-up: module loading, allocator
+    t0 = time.perf_counter()
+    km.lloyd_batched(probs, max_iters=1)
+    one = time.perf_counter() - t0
+    l0 = km.launch_count()
+    t0 = time.perf_counter()
+    _, st = km.lloyd_batched(probs, max_iters=iters)
+    full = time.perf_counter() - t0
+    launches = km.launch_count() - l0
+    per_iter = st.ms_total / 1000.0 / iters  # CUDA events around the iteration loops
+    sample = probs[: min(200, len(probs))]
+    km.lloyd(sample[0][0], sample[0][1], max_iters=1)
+    t0 = time.perf_counter()
+    for X, k in sample:
+        km.lloyd(X, k, max_iters=iters)
+    loop = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    km.lloyd_batched(sample, max_iters=iters)
+    bsample = time.perf_counter() - t0
+    line = {"metric": f"batched Lloyd, {len(probs)} problems x {iters} iterations (s per call)",
+            "value": full, "unit": "s", "higher_is_better": False, "n_gpus": 1,
+            "data": "synthetic", "dtype": "f32",
+            "config": {"workload": f"batched_{len(probs)}_problems", "rows": rows,
+                       "gflop_per_iteration": flop / 1e9, "iterations": iters,
+                       "tier": "fp32", "certified_labels": True},
+            "ms_per_iteration": per_iter * 1000.0,
+            "setup_s": full - st.ms_total / 1000.0,
+            "assign_tflops_per_iteration": flop / per_iter / 1e12,
+            "setup_and_one_iteration_s": one, "generation_s": gen_s,
+            "reranked_points_total": st.reranked, "gpu_launches": launches,
+            "single_call_loop": {"problems": len(sample), "loop_s": loop, "batched_s": bsample,
+                                 "speedup": loop / bsample}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -229,12 +291,19 @@ def main():
     ap.add_argument("--no-init", action="store_true", help="skip the k-means++ timing")
     ap.add_argument("--only-init", action="store_true",
                     help="time only the k-means++ initialisation (profiling captures)")
+    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "batched"],
+                    help="batched: the many-problems workload through kmgb_lloyd_batched_f32 "
+                         "(its own JSON line; not the headline)")
+    ap.add_argument("--problems", type=int, default=10_000,
+                    help="problems of the batched workload")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
         return reference_arm(args, rank)
+    if args.workload == "batched":
+        return batched_workload(args)
 
     import torch
     import kmeans_gb300 as km

@@ -288,7 +288,9 @@ typedef struct kmgb_problem {
 /* opt: max_iters, criterion, empty_policy and certify are used; the tier must be
  * KMGB_ASSIGN_FP32, mini_batch_fraction 1, stream_tile_rows 0, init_algorithm
  * KMGB_INIT_REFERENCE. stats (nullable): iterations = the largest over the problems, reranked =
- * rows settled by the exact re-rank, ms_total = wall time of the call. */
+ * rows settled by the exact re-rank, ms_total = GPU time of the iterations (CUDA events, summed
+ * over the groups of one dimension), reserved[0] = wall time of the whole call in microseconds
+ * (uploads, initialisation and result copies included). */
 KMGB_EXPORT int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const kmgb_options* opt,
                                        kmgb_stats* stats);
 

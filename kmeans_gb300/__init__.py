@@ -378,15 +378,17 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
 def lloyd_batched(problems, max_iters: int = 20, criterion: float = -1.0,
                   empty_policy: int = EMPTY_NAN, certify: bool = True):
     """Many independent Lloyd runs in one kmgb_lloyd_batched_f32 call. problems: sequence of
-    (X, k) or (X, k, init) with X numpy n x d float32 (init k x d, or None for the reference
-    initialisation). Returns (list of LloydResult, kmgb_stats)."""
+    (X, k) or (X, k, init) with X numpy (host) or a contiguous torch tensor (device), n x d
+    float32 (init k x d, or None for the reference initialisation). Returns (list of
+    LloydResult, kmgb_stats)."""
     arr = (kmgb_problem * len(problems))()
     keep = []
     outs = []
     for i, p in enumerate(problems):
         X, k = p[0], int(p[1])
         init = p[2] if len(p) > 2 else None
-        X = np.ascontiguousarray(X, dtype=np.float32)
+        if isinstance(X, np.ndarray):
+            X = np.ascontiguousarray(X, dtype=np.float32)
         if init is not None:
             init = np.ascontiguousarray(init, dtype=np.float32)
         n, d = X.shape

@@ -34,7 +34,7 @@ using namespace kmgb;
 namespace {
 
 constexpr int kTileRows = 128;       // assignment tile (rows of one problem)
-constexpr int kSortTile = 4096;      // counting-sort tile (rows of one problem)
+constexpr int kSortTile = 2048;      // counting-sort tile (rows of one problem)
 constexpr long long kMaxRows = 1LL << 30;
 constexpr long long kMaxHist = 60LL << 20;  // scan capacity of the counting sort
 constexpr long long kMaxXBytes = 32LL << 30;
@@ -147,9 +147,85 @@ bool initial_centers(const kmgb_problem* pr, const std::vector<int>& ids, int d,
   return true;
 }
 
+// Host problems' rows into X (rows x ldx): chunks of rows are packed into two alternating
+// pinned buffers by host threads (zeros for padding rows and columns) and copied with
+// cudaMemcpyAsync while the next chunk is packed.
+bool upload_host_rows(const kmgb_problem* pr, const std::vector<int>& ids, int d, long long ldx,
+                      long long rows, const std::vector<long long>& rbeg,
+                      const std::vector<long long>& rend, const std::vector<char>& is_dev,
+                      float* X, cudaStream_t s, Fail& f) {
+  const int E = KMEANS_ERROR_BUILDDATA;
+  const long long chunk_rows = std::max<long long>(1, (256LL << 20) / (ldx * 4));
+  float* buf[2] = {nullptr, nullptr};
+  cudaEvent_t freed[2] = {nullptr, nullptr};
+  bool ok = true;
+  for (int b = 0; b < 2 && ok; ++b) {
+    ok = !f.set(cudaHostAlloc(reinterpret_cast<void**>(&buf[b]),
+                              sizeof(float) * chunk_rows * ldx, cudaHostAllocDefault),
+                E, "pinned staging") &&
+         !f.set(cudaEventCreateWithFlags(&freed[b], cudaEventDisableTiming), E, "staging event");
+  }
+  const int P = (int)ids.size();
+  // problem i's padded region is rows [rbeg[i], pend(i)); the regions tile [0, rows)
+  auto pend = [&](int i) { return rbeg[i] + rup(rend[i] - rbeg[i], kTileRows); };
+  const int nth = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+  int first = 0;  // first problem whose region ends after the chunk's first row
+  for (long long r0 = 0, c = 0; ok && r0 < rows; r0 += chunk_rows, ++c) {
+    const long long r1 = std::min(rows, r0 + chunk_rows);
+    const int b = (int)(c & 1);
+    if (c >= 2 && f.set(cudaEventSynchronize(freed[b]), E, "staging")) {
+      ok = false;
+      break;
+    }
+    while (first < P && pend(first) <= r0) ++first;
+    float* out = buf[b];
+    auto fill = [&](long long a0, long long a1) {  // rows [a0, a1) of X
+      int i = first;
+      for (long long r = a0; r < a1;) {
+        while (pend(i) <= r) ++i;  // r < rows, so some region holds it
+        float* dst = out + (size_t)(r - r0) * ldx;
+        if (r < rend[i] && !is_dev[i]) {
+          const long long stop = std::min(a1, rend[i]);
+          const float* src = pr[ids[i]].X + (size_t)(r - rbeg[i]) * d;
+          if (ldx == d) {
+            std::memcpy(dst, src, sizeof(float) * (size_t)(stop - r) * d);
+          } else {
+            for (long long t = 0; t < stop - r; ++t) {
+              std::memcpy(dst + (size_t)t * ldx, src + (size_t)t * d, sizeof(float) * d);
+              std::memset(dst + (size_t)t * ldx + d, 0, sizeof(float) * (ldx - d));
+            }
+          }
+          r = stop;
+        } else {  // padding rows (and device problems, copied afterwards) up to the region's end
+          const long long stop = std::min(a1, pend(i));
+          std::memset(dst, 0, sizeof(float) * (size_t)(stop - r) * ldx);
+          r = stop;
+        }
+      }
+    };
+    std::vector<std::thread> th;
+    const long long n = r1 - r0;
+    for (int t = 0; t < nth; ++t) {
+      const long long a0 = r0 + n * t / nth, a1 = r0 + n * (t + 1) / nth;
+      if (a1 > a0) th.emplace_back(fill, a0, a1);
+    }
+    for (auto& t : th) t.join();
+    ok = !f.set(cudaMemcpyAsync(X + (size_t)r0 * ldx, out, sizeof(float) * (size_t)n * ldx,
+                                cudaMemcpyHostToDevice, s),
+                E, "data upload") &&
+         !f.set(cudaEventRecord(freed[b], s), E, "staging event");
+  }
+  if (ok) ok = !f.set(cudaStreamSynchronize(s), E, "data upload");
+  for (int b = 0; b < 2; ++b) {
+    if (freed[b]) cudaEventDestroy(freed[b]);
+    if (buf[b]) cudaFreeHost(buf[b]);
+  }
+  return ok;
+}
+
 // One group: problems `ids` (all of dimension d).
 int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_options& o,
-              cudaStream_t s, unsigned long long* reranked, Fail& f) {
+              cudaStream_t s, unsigned long long* reranked, double* loop_ms, Fail& f) {
   const int P = (int)ids.size();
   const long long ldx = rup(d, 4);
   const int max_iters = std::max(0, o.max_iters);
@@ -204,14 +280,24 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       f.set(cudaMemsetAsync(err, 0, sizeof(int), s), E, "error word") ||
       f.set(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)K * ldx, s), E, "centers"))
     return f.code;
-  // data and initial centers
+  // data: host problems are packed by host threads into two pinned staging buffers in the
+  // device layout (rows of ldx floats, zero padding rows and columns) while the previous buffer
+  // is copied; device problems are copied on the device
+  std::vector<char> is_dev(P);
+  bool any_host = false;
+  for (int i = 0; i < P; ++i) {
+    is_dev[i] = on_device(pr[ids[i]].X) ? 1 : 0;
+    any_host |= !is_dev[i];
+  }
+  if (any_host && !upload_host_rows(pr, ids, d, ldx, rows, rbeg, rend, is_dev, X, s, f))
+    return f.code;
   for (int i = 0; i < P; ++i) {
     const kmgb_problem& q = pr[ids[i]];
-    if (f.set(cudaMemcpy2DAsync(X + (size_t)rbeg[i] * ldx, sizeof(float) * ldx, q.X,
+    if (is_dev[i] &&
+        f.set(cudaMemcpy2DAsync(X + (size_t)rbeg[i] * ldx, sizeof(float) * ldx, q.X,
                                 sizeof(float) * d, sizeof(float) * d, q.n,
-                                on_device(q.X) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
-                                s),
-              E, "data upload"))
+                                cudaMemcpyDeviceToDevice, s),
+              E, "data copy"))
       return f.code;
   }
   if (f.set(cudaMemcpy2DAsync(C, sizeof(float) * ldx, C0.data(), sizeof(float) * d,
@@ -262,6 +348,7 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
   b.stile_prob = d_sprob;
   b.stile_local = d_slocal;
   b.tile_pts = kSortTile;
+  b.kmax = *std::max_element(kk.begin(), kk.end());
   b.hist_elems = hist;
   b.done = d_done;
   b.sse_prev = d_prev;
@@ -318,6 +405,20 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
   ra.d = d;
   ra.mode = 0;
   ra.max_list = nvalid;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  if (f.set(cudaEventCreate(&ev[0]), EU, "events") || f.set(cudaEventCreate(&ev[1]), EU, "events") ||
+      f.set(cudaEventRecord(ev[0], s), EU, "events")) {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    return f.code;
+  }
+  struct EvGuard {
+    cudaEvent_t* e;
+    ~EvGuard() {
+      cudaEventDestroy(e[0]);
+      cudaEventDestroy(e[1]);
+    }
+  } ev_guard{ev};
   for (int it = 0; it < max_iters; ++it) {
     if (f.set(cudaMemsetAsync(cmax, 0, sizeof(float), s), EU, "centers") ||
         f.set(launch_prep_centers(C, ldx, (int)K, d, Cop, nullptr, 0, cn, cmax, s), EU,
@@ -340,6 +441,12 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       if (std::all_of(done.begin(), done.end(), [](int v) { return v != 0; })) break;
     }
   }
+  float ms = 0.f;
+  if (f.set(cudaEventRecord(ev[1], s), EU, "events") ||
+      f.set(cudaEventSynchronize(ev[1]), EU, "events") ||
+      f.set(cudaEventElapsedTime(&ms, ev[0], ev[1]), EU, "events"))
+    return f.code;
+  *loop_ms += ms;
   // results
   std::vector<int> lab(rows), iters(P);
   std::vector<float> Ch((size_t)K * d);
@@ -425,6 +532,7 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     return reject(KMEANS_ERROR_BUILDDATA, "kmgb_lloyd_batched_f32: stream creation failed");
   Fail f;
   unsigned long long reranked = 0;
+  double loop_ms = 0.0;
   size_t i = 0;
   while (i < order.size() && !f.code) {
     const int d = problems[order[i]].d;
@@ -450,7 +558,7 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
       ++i;
     }
     if (f.code) break;
-    run_group(problems, ids, d, o, s, &reranked, f);
+    run_group(problems, ids, d, o, s, &reranked, &loop_ms, f);
   }
   cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
@@ -461,8 +569,10 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     stats->iterations = it;
     stats->status = f.code;
     stats->reranked = reranked;
-    stats->ms_total =
-        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    stats->ms_total = loop_ms;
+    stats->reserved[0] = (long long)std::chrono::duration<double, std::micro>(
+                             std::chrono::steady_clock::now() - t0)
+                             .count();
   }
   if (f.code) {
     set_last_error(f.msg.c_str());

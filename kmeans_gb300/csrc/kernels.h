@@ -191,6 +191,7 @@ struct BatchUpdate {
   const int* stile_prob;        // [stiles]
   const int* stile_local;       // [stiles] tile index inside its problem
   int tile_pts;                 // rows per sort tile
+  int kmax;                     // largest k of the problems
   long long hist_elems;         // sum over problems of k * ntiles
   // per-problem loop state (device)
   int* done;                    // [P] 1 once the problem's stop rule fired

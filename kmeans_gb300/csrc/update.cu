@@ -784,8 +784,11 @@ __global__ void label_offsets_batched_kernel(const int* __restrict__ hist, Batch
   if (counts) counts[gc] = a1 - a0;
 }
 
+// One warp per sort tile. SMEM: the tile's k counters live in shared memory (k <= smem_k).
+template <bool SMEM>
 __global__ void scatter_batched_kernel(const int* __restrict__ labels, BatchUpdate b, int* pos,
                                        int* __restrict__ sorted) {
+  extern __shared__ int cnt_s[];
   const long long st = blockIdx.x;
   const int prob = b.stile_prob[st];
   const int tl = b.stile_local[st];
@@ -794,21 +797,30 @@ __global__ void scatter_batched_kernel(const int* __restrict__ labels, BatchUpda
   const int cb = b.c_off[prob], kp = b.k[prob], nt = b.ntiles[prob];
   volatile int* vpos = pos + b.hoff[prob];
   const int lane = threadIdx.x;
+  if (SMEM) {
+    for (int j = lane; j < kp; j += 32) cnt_s[j] = vpos[(size_t)j * nt + tl];
+    __syncwarp();
+  }
+  int lnext = (i0 + lane < i1) ? labels[i0 + lane] : 0;
   for (long long base = i0; base < i1; base += 32) {
     const long long i = base + lane;
     int l = -1;
     if (i < i1) {
-      l = labels[i] - cb;
+      l = lnext - cb;
       if (l < 0 || l >= kp) l = -1;
     }
+    if (base + 32 + lane < i1) lnext = labels[base + 32 + lane];  // next batch in flight
     const unsigned peers = __match_any_sync(0xffffffffu, l);
     const int leader = __ffs(peers) - 1;
     const int rank = __popc(peers & lanemask_lt());
     int bs = 0;
-    if (l >= 0 && lane == leader) bs = vpos[(size_t)l * nt + tl];
+    if (l >= 0 && lane == leader) bs = SMEM ? cnt_s[l] : vpos[(size_t)l * nt + tl];
     bs = __shfl_sync(0xffffffffu, bs, leader);
     if (l >= 0) sorted[bs + rank] = (int)i;
-    if (l >= 0 && lane == leader) vpos[(size_t)l * nt + tl] = bs + __popc(peers);
+    if (l >= 0 && lane == leader) {
+      if (SMEM) cnt_s[l] = bs + __popc(peers);
+      else vpos[(size_t)l * nt + tl] = bs + __popc(peers);
+    }
     __syncwarp();
   }
 }
@@ -855,7 +867,11 @@ cudaError_t launch_update_batched(const float* X, long long ldx, int d, const do
   count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   KMGB_CUDA_TRY(excl_scan(w.piece_cnt, b.K + 1, w.scan_tmp, s, nullptr));
-  scatter_batched_kernel<<<(unsigned)b.stiles, 32, 0, s>>>(labels, b, w.hist, w.sorted);
+  if (b.kmax <= 12288)
+    scatter_batched_kernel<true><<<(unsigned)b.stiles, 32, sizeof(int) * (size_t)b.kmax, s>>>(
+        labels, b, w.hist, w.sorted);
+  else
+    scatter_batched_kernel<false><<<(unsigned)b.stiles, 32, 0, s>>>(labels, b, w.hist, w.sorted);
   count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   const long long max_pieces = w.max_pieces;

@@ -89,6 +89,16 @@ def test_many_small_problems(km, orc, torch_cuda):
         check(res[i], orc.lloyd(X, ini, 3))
 
 
+def test_device_and_host_problems_mixed(km, orc, torch_cuda):
+    probs = make_batch(12, 31, dims=(5, 32), nmax=8000, kmax=30)
+    mixed = [((torch_cuda.from_numpy(X).cuda() if i % 2 else X), k, init)
+             for i, (X, k, init) in enumerate(probs)]
+    res, _ = km.lloyd_batched(mixed, max_iters=4)
+    for (X, k, init), r in zip(probs, res):
+        ini = orc.reference_init(X, k) if init is None else init
+        check(r, orc.lloyd(X, ini, 4))
+
+
 def test_rejections(km, torch_cuda):
     X, _, _ = mixture_numpy(500, 8, 4, seed=3)
     with pytest.raises(km.KmeansError):
