@@ -200,6 +200,11 @@ struct kmgb_handle {
   bool pending = false;
   double ms_total = 0.0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // one iteration captured as a CUDA graph (resident data, full batches, profiling off),
+  // replayed for every iteration while the buffers it was captured with are in place
+  cudaGraphExec_t gexec = nullptr;
+  const double* g_sse = nullptr;
+  long long g_launches = 0;
   // phase profiling: 5 events per iteration
   bool prof = false;
   std::vector<cudaEvent_t> pev;
@@ -234,6 +239,7 @@ struct kmgb_handle {
     if (copy_stream) cudaStreamDestroy(copy_stream);
     if (sse_pinned) cudaFreeHost(sse_pinned);
     if (loop_init) cudaFreeHost(loop_init);
+    if (gexec) cudaGraphExecDestroy(gexec);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -379,6 +385,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   w.sse_prev = h->loopf;
   w.rel_out = h->loopf + 1;
   w.iters_done = h->iters_done;
+  w.sse_indexed = h->streaming ? 0 : 1;  // host-streamed iterations write their own slot
   h->sse_cap = std::max(1, h->opt.max_iters);
   KM_TRY(dalloc(&h->sse_dev, h->sse_cap), (delete h, code));
   KM_TRY(cudaMallocHost(&h->sse_pinned, sizeof(double)), (delete h, code));
@@ -568,8 +575,9 @@ int step(kmgb_handle* h, int slot) {
   }
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
   // cluster centers + compactness (kmeans.cpp:1018-1104)
+  // the SSE lands in sse_dev[iteration of the run] (device-side index)
   KM_TRY(launch_update(Xa, qna, h->labels, h->C, h->ldx, h->opt.empty_policy, h->uw,
-                       h->sse_dev + slot, s),
+                       h->uw.sse_indexed ? h->sse_dev : h->sse_dev + slot, s),
          KMEANS_ERROR_CLUSTER_CENTERS);
   KM_TRY(h->pmark(4), KMEANS_ERROR_CLUSTER_CENTERS);
   if (h->prof) ++h->pused;
@@ -710,6 +718,55 @@ int step_stream(kmgb_handle* h, int slot) {
   return 0;
 }
 
+// Enqueues `iters` iterations as launches of one captured CUDA graph holding a whole iteration
+// (resident data, full batches): every iteration issues the same kernels with the same
+// parameters -- the SSE slot and the stop rule are indexed on the device -- so the graph is
+// captured once and replayed until a buffer it uses is replaced. Returns 0 when launched, -1 when
+// the iteration cannot be captured (it is then launched kernel by kernel), else an error code.
+int run_graph(kmgb_handle* h, int iters) {
+  if (!(h->gexec && h->g_sse == h->sse_dev)) {
+    if (h->gexec) {
+      cudaGraphExecDestroy(h->gexec);
+      h->gexec = nullptr;
+    }
+    if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      return -1;
+    }
+    const long long l0 = launch_count();
+    const int rc = step(h, 0);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    const long long captured = launch_count() - l0;
+    count_launches(-captured);  // recorded into the graph, not launched
+    if (rc || e != cudaSuccess || !g) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return -1;
+    }
+    cudaGraphExec_t ex = nullptr;
+    const cudaError_t ei = cudaGraphInstantiate(&ex, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) {
+      cudaGetLastError();
+      return -1;
+    }
+    h->gexec = ex;
+    h->g_sse = h->sse_dev;
+    h->g_launches = captured;
+  }
+  for (int it = 0; it < iters; ++it) {
+    KM_TRY(cudaGraphLaunch(h->gexec, h->stream), KMEANS_ERROR_COMPUTE);
+    count_launches(h->g_launches);
+  }
+  return 0;
+}
+
+bool graphs_enabled() {
+  const char* v = std::getenv("KMGB_GRAPHS");
+  return !(v && std::strcmp(v, "0") == 0);
+}
+
 int run(kmgb_handle* h, int iters, double criterion) {
   if (!h->have_data || !h->have_centers) {
     set_err("kmgb_run: data and centers must be set first");
@@ -739,7 +796,12 @@ int run(kmgb_handle* h, int iters, double criterion) {
   KM_TRY(cudaEventRecord(h->ev0, h->stream), KMEANS_ERROR_COMPUTE);
   // Every iteration is enqueued; the SSE reduction evaluates the stop rule on the device and
   // the kernels of later iterations return at once after it fires.
-  for (int it = 0; it < iters; ++it) {
+  int graph_rc = -1;
+  if (!h->streaming && !h->mini && !h->prof && iters > 0 && graphs_enabled()) {
+    graph_rc = run_graph(h, iters);
+    if (graph_rc > 0) return graph_rc;
+  }
+  for (int it = 0; it < iters && graph_rc != 0; ++it) {
     if (h->streaming) {
       // a streamed iteration copies the whole data set: look at the stop flag between
       // iterations so that a converged run issues no further copies

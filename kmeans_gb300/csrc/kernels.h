@@ -149,6 +149,8 @@ struct UpdateWork {
   double* sse_prev;     // previous SSE (0 before the first iteration)
   double* rel_out;      // last relErr
   int* iters_done;      // iterations completed
+  int sse_indexed;      // 1: the SSE lands in sse_out[*iters_done] (a run's iteration index,
+                        // so one captured iteration serves every iteration of the run)
 };
 size_t update_scan_tmp_elems(long long elems);
 cudaError_t launch_update(const float* X, const double* qn, const int* labels, float* C,

@@ -440,7 +440,7 @@ __global__ void sse_fixup_kernel(double* __restrict__ sse_k, int groups,
 // relErr = |SSE - SSE_old| / |SSE|; the run stops once !(relErr > criterion), NaN included.
 __global__ void sse_reduce_kernel(const double* __restrict__ sse_k, int k, double* __restrict__ out,
                                   int* stop, double criterion, double* sse_prev, double* rel_out,
-                                  int* iters_done) {
+                                  int* iters_done, int indexed) {
   if (stopped(stop)) return;
   __shared__ double red[1024];
   const int per = (k + blockDim.x - 1) / blockDim.x;
@@ -454,7 +454,8 @@ __global__ void sse_reduce_kernel(const double* __restrict__ sse_k, int k, doubl
   }
   if (threadIdx.x == 0) {
     const double sse = red[0];
-    *out = sse;
+    if (indexed && iters_done) out[*iters_done] = sse;
+    else *out = sse;
     if (sse_prev) {
       const double rel = fabs(sse - *sse_prev) / fabs(sse);
       *sse_prev = sse;
@@ -554,7 +555,7 @@ cudaError_t launch_update(const float* X, const double* qn, const int* labels, f
   }
   if (sse_out) {
     sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, (int)fin_warps, sse_out, w.stop, w.criterion,
-                                         w.sse_prev, w.rel_out, w.iters_done); kmgb::count_launches(1);
+                                         w.sse_prev, w.rel_out, w.iters_done, w.sse_indexed); kmgb::count_launches(1);
     KMGB_CUDA_TRY(cudaGetLastError());
   }
   return cudaSuccess;
@@ -711,7 +712,7 @@ cudaError_t launch_stream_finalize(const double* accS, const int* accN, const do
   kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   sse_reduce_kernel<<<1, 1024, 0, s>>>(w.sse_k, (int)fin_warps, sse_out, w.stop, w.criterion,
-                                       w.sse_prev, w.rel_out, w.iters_done);
+                                       w.sse_prev, w.rel_out, w.iters_done, w.sse_indexed);
   kmgb::count_launches(1);
   return cudaGetLastError();
 }
