@@ -119,11 +119,11 @@ def cpu_baseline(steps: int = 1):
                       f"{len(times)}", "seconds_per_sample_iter": t}
 
 
-def reference_gpu_assign():
+def reference_gpu_assign(N=N, D=D, K=K, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0)):
     """The reference's own assignment kernels (main/cuda/ClosestCenters.cu, compiled from its
-    sources into oracle/_ref and launched as its ClosestCentersF does) on the same workload:
-    milliseconds per assignment pass, CUDA events on the legacy default stream. None when
-    oracle/_ref or a GPU is absent."""
+    sources into oracle/_ref and launched as its ClosestCentersF does) on an N x D, K workload
+    (default: the 4M x 128, K=1024 one): milliseconds per assignment pass, CUDA events on the
+    legacy default stream. None when oracle/_ref or a GPU is absent."""
     try:
         import torch
         import oracle
@@ -133,7 +133,7 @@ def reference_gpu_assign():
         if ref is None:
             return None
         from kmeans_gb300.synthetic import mixture_torch, sample_init
-        X, _, _ = mixture_torch(N, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+        X, _, _ = mixture_torch(N, D, K, seed=1234, mean_lo=mean_lo, mean_hi=mean_hi, std=std)
         C = X[torch.from_numpy(sample_init(N, K, seed=99)).cuda()]
         rows_padded = (N + 63) // 64 * 64
         # the reference's kernels read past the logical matrices (see oracle/ref_kernels.cpp)
@@ -154,7 +154,7 @@ def reference_gpu_assign():
                 return None
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = 5
+        reps = 5 if N * K * D > 1e10 else 50
         e0.record(torch.cuda.default_stream())
         for _ in range(reps):
             ref.refk_closest_centers_f(*args)
@@ -184,7 +184,9 @@ def reference_arm(args, rank: int):
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "reference_gpu": reference_gpu_assign()}
+            "reference_gpu": reference_gpu_assign(),
+            "reference_gpu_100kx32_K64": reference_gpu_assign(100_000, 32, 64, -10.0, 10.0,
+                                                                (1.0, 1.0))}
     print(json.dumps(line), flush=True)
 
 
@@ -274,6 +276,77 @@ def batched_workload(args):
     print(json.dumps(line), flush=True)
 
 
+def large_k_workload(args, n=16_000_000, d=256, k=65_536):
+    """Large-K workload: 16M points, D=256, K=65,536 clusters with Zipf(1.1) sizes, unit-variance
+    Gaussians around means drawn from N(0, 25 I), values rounded to BF16 (BF16 points);
+    initial centers a seeded sample of points. Times split-BF16 iterations against one plain
+    FP32 iteration from the same centers and checks that both give the same labels (both are
+    the FP64 arg-min)."""
+    import torch
+    import kmeans_gb300 as km
+    from kmeans_gb300.synthetic import sample_init
+    km.build()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(77)
+    w = 1.0 / torch.arange(1, k + 1, device="cuda", dtype=torch.float64) ** 1.1
+    lab = torch.multinomial((w / w.sum()).float(), n, replacement=True, generator=g)
+    means = torch.randn((k, d), device="cuda", generator=g) * 5.0
+    X = torch.empty((n, d), device="cuda", dtype=torch.float32)
+    for r0 in range(0, n, 1 << 21):
+        r1 = min(n, r0 + (1 << 21))
+        X[r0:r1] = (means[lab[r0:r1]] + torch.randn((r1 - r0, d), device="cuda", generator=g)
+                    ).to(torch.bfloat16).float()
+    del lab, means
+    init = X[torch.from_numpy(sample_init(n, k, seed=5)).cuda()].cpu().numpy()
+    flop = 2.0 * n * k * d
+    out = {"metric": f"Lloyd iteration, N={n}, D={d}, K={k} (ms)", "unit": "ms",
+           "higher_is_better": False, "data": "synthetic (Zipf 1.1 cluster sizes, BF16 points)",
+           "config": {"workload": "lloyd_16Mx256_K65536", "n": n, "d": d, "k": k}}
+    labels = {}
+    for tier, iters in (("bf16x3", 3), ("fp32", 1)):
+        if tier not in args.tiers.split(","):
+            continue
+        tid = km.ASSIGN_BF16X3 if tier == "bf16x3" else km.ASSIGN_FP32
+        h = km.Handle(n, d, k, assign_tier=tid, max_iters=iters + 1)
+        h.set_data(X, True)
+        h.set_centers(init, False)
+        if tier == "bf16x3":
+            h.run(1)  # warm-up
+            h.synchronize()
+            h.set_centers(init, False)
+        stream = torch.cuda.ExternalStream(h.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        h.set_profiling(True)
+        e0.record(stream)
+        h.run(iters)
+        e1.record(stream)
+        h.synchronize()
+        ms = e0.elapsed_time(e1) / iters
+        phase, pit = h.phase_ms()
+        st = h.stats()
+        out[tier] = {"ms_per_iteration": ms, "assign_ms": phase[1] / max(pit, 1),
+                     "assign_tflops": flop / (phase[1] / max(pit, 1) / 1000.0) / 1e12,
+                     "phase_ms_per_iter": {nm: p / max(pit, 1) for nm, p in
+                                           zip(["prep", "assign", "rerank", "update"], phase)},
+                     "iterations": iters, "reranked_points": st.reranked,
+                     "full_rescan_points": st.reranked_fp64}
+        if tier == "fp32":
+            labels[tier] = h.labels()
+        else:
+            # labels after the first iteration from the same initial centers
+            h.set_centers(init, False)
+            h.run(1)
+            h.synchronize()
+            labels[tier] = h.labels()
+        h.close()
+    if "bf16x3" in out:
+        out["value"] = out["bf16x3"]["ms_per_iteration"]
+    if "bf16x3" in out and "fp32" in out:
+        out["speedup_vs_fp32"] = out["fp32"]["ms_per_iteration"] / out["bf16x3"]["ms_per_iteration"]
+        out["labels_identical"] = bool(np.array_equal(labels["fp32"], labels["bf16x3"]))
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -291,11 +364,13 @@ def main():
     ap.add_argument("--no-init", action="store_true", help="skip the k-means++ timing")
     ap.add_argument("--only-init", action="store_true",
                     help="time only the k-means++ initialisation (profiling captures)")
-    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "batched"],
-                    help="batched: the many-problems workload through kmgb_lloyd_batched_f32 "
-                         "(its own JSON line; not the headline)")
+    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "batched", "large_k"],
+                    help="batched: the many-problems workload through kmgb_lloyd_batched_f32; "
+                         "large_k: 16M x 256, K=65536 split BF16 vs FP32 (own JSON lines; not "
+                         "the headline)")
     ap.add_argument("--problems", type=int, default=10_000,
                     help="problems of the batched workload")
+    ap.add_argument("--tiers", default="bf16x3,fp32", help="tiers of the large_k workload")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -304,6 +379,8 @@ def main():
         return reference_arm(args, rank)
     if args.workload == "batched":
         return batched_workload(args)
+    if args.workload == "large_k":
+        return large_k_workload(args)
 
     import torch
     import kmeans_gb300 as km

@@ -341,9 +341,10 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(dalloc(&h->rr_hi2, na), (delete h, code));
   if (bf16) {
     // flagged points are ~1-2% of the rows for the split tier and ~1/3 for plain BF16; the
-    // compact copies hold an eighth (split) or half (plain) of the rows, at least 1024, and any
-    // excess takes the full rescan
-    h->cand_cap = std::min(na, std::max<long long>(1024, split ? na / 8 : na / 2));
+    // compact copies hold half of the rows, at least 1024 and at most 8M; any excess takes the
+    // full rescan. (With many near-equal centers -- K=65,536 drawn from Zipf-sized clusters --
+    // a third of the points can miss the certificate after the first update.)
+    h->cand_cap = std::min(na, std::min<long long>(8LL << 20, std::max<long long>(1024, na / 2)));
     const long long cc = h->cand_cap;
     KM_TRY(dalloc(&h->rr_over, na), (delete h, code));
     KM_TRY(dalloc(&h->thr_full, na), (delete h, code));

@@ -232,7 +232,7 @@ cudaError_t launch_kmeanspp(const double* X, long long ldx, long long n, int d, 
                             int* err, cudaStream_t s);
 
 constexpr int kSumPiece = 128;
-constexpr int kMaxCand = 16;  // candidate centers recorded per flagged point
+constexpr int kMaxCand = 32;  // candidate centers recorded per flagged point
 // BF16 tiers: centers per tensor-core chunk; the start values and diagnostic accumulators are
 // padded to a whole number of chunks
 constexpr int kCenterPad = 256;

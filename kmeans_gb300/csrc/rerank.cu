@@ -277,58 +277,141 @@ rerank_tiled_kernel(RerankArgs a, int* __restrict__ list2, int* __restrict__ cou
   }
 }
 
-// Exact stage of the Lloyd re-rank (mode 0), one CTA per residual point: every usable center
-// whose FP32 lower end is within the point's best upper end (from the FP32 stage) is evaluated
-// in FP64 exactly as the oracle does; the smallest value wins, lowest index on ties.
+// Exact stage of the Lloyd re-rank (mode 0), tiled like the FP32 stage: 32 residual points per
+// CTA iteration against 64-center blocks staged in shared memory. Every (point, usable center)
+// pair whose FP32 direct-form lower end is within the point's best upper end (hi2, from the FP32
+// stage) is evaluated in FP64 in the oracle's order (sequential fma over the dimensions); the
+// smallest value wins, lowest index on ties. Centers are read once per 32 points, so the cost
+// stays that of one tiled FP32 scan however many points reach this stage.
 __global__ void __launch_bounds__(256)
 rerank_exact_kernel(RerankArgs a, const float* __restrict__ hi2) {
   if (stopped(a.stop)) return;
-  extern __shared__ float xsm[];
-  __shared__ double rb[8];
-  __shared__ int ri[8];
+  extern __shared__ float4 sm4[];
+  const int dq = (a.d + 3) >> 2;
+  const int rs = dq + 1;
+  float4* xs = sm4;                       // [TP][rs]
+  float4* cs = xs + TP * rs;              // [TC][rs]
+  float* cflag = reinterpret_cast<float*>(cs + TC * rs);  // [TC] 0 usable, +inf unusable
+  __shared__ double mb[8][TP];
+  __shared__ int mi[8][TP];
+  __shared__ float hs[TP];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int pq = tid & 7;                 // points pq*4 .. pq*4+3
+  const int cq = tid >> 3;                // centers cq*2, cq*2+1 of the block
   const long long cnt = min((long long)*(volatile const int*)a.count, a.max_list);
   const float u = 5.9604645e-8f;
   const float gam = (float)(a.d + 4) * 2.0f * u * 1.01f;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (long long slot = blockIdx.x; slot < cnt; slot += gridDim.x) {
+
+  for (long long g0 = (long long)blockIdx.x * TP; g0 < cnt; g0 += (long long)gridDim.x * TP) {
     __syncthreads();
-    const int pt = a.list[slot];
-    const float* x = a.X + (size_t)pt * a.ldx;
-    for (int t = threadIdx.x; t < a.d; t += blockDim.x) xsm[t] = x[t];
-    __syncthreads();
-    const float best_hi = hi2[slot];
-    double best = INFINITY;
-    int bidx = -1;
-    for (int j = threadIdx.x; j < a.k; j += blockDim.x) {
-      if (!(a.cn[j] < INFINITY)) continue;
-      const float* c = a.C + (size_t)j * a.ldc;
-      const float v = approx_value(0, xsm, c, a.d, 0.0f);
-      if (!(v * (1.0f - gam) - 1e-30f <= best_hi)) continue;
-      const double ex = exact_value(0, xsm, c, a.d, 0.0f);
-      if (ex < best) {
-        best = ex;
-        bidx = j;
+    for (int e = tid; e < TP * dq; e += blockDim.x) {
+      const int r = e / dq, q = e % dq;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (g0 + r < cnt) {
+        const float* x = a.X + (size_t)a.list[g0 + r] * a.ldx;
+        const int c0 = q * 4;
+        v.x = c0 < a.d ? x[c0] : 0.f;
+        v.y = c0 + 1 < a.d ? x[c0 + 1] : 0.f;
+        v.z = c0 + 2 < a.d ? x[c0 + 2] : 0.f;
+        v.w = c0 + 3 < a.d ? x[c0 + 3] : 0.f;
+      }
+      xs[r * rs + q] = v;
+    }
+    if (tid < TP) hs[tid] = (g0 + tid < cnt) ? hi2[g0 + tid] : -INFINITY;
+    double be[4];
+    int bi[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      be[i] = INFINITY;
+      bi[i] = -1;
+    }
+    for (int j0 = 0; j0 < a.k; j0 += TC) {
+      __syncthreads();
+      for (int e = tid; e < TC * dq; e += blockDim.x) {
+        const int r = e / dq, q = e % dq;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (j0 + r < a.k) v = *reinterpret_cast<const float4*>(a.C + (size_t)(j0 + r) * a.ldc + q * 4);
+        cs[r * rs + q] = v;
+      }
+      if (tid < TC) {
+        const int j = j0 + tid;
+        cflag[tid] = (j < a.k && a.cn[j] < INFINITY) ? 0.0f : INFINITY;
+      }
+      __syncthreads();
+      float acc[4][2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i][0] = acc[i][1] = 0.0f;
+      for (int q = 0; q < dq; ++q) {
+        const float4 c0 = cs[(cq * 2) * rs + q];
+        const float4 c1 = cs[(cq * 2 + 1) * rs + q];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float4 x = xs[(pq * 4 + i) * rs + q];
+          float t;
+          t = x.x - c0.x; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.y - c0.y; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.z - c0.z; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.w - c0.w; acc[i][0] = fmaf(t, t, acc[i][0]);
+          t = x.x - c1.x; acc[i][1] = fmaf(t, t, acc[i][1]);
+          t = x.y - c1.y; acc[i][1] = fmaf(t, t, acc[i][1]);
+          t = x.z - c1.z; acc[i][1] = fmaf(t, t, acc[i][1]);
+          t = x.w - c1.w; acc[i][1] = fmaf(t, t, acc[i][1]);
+        }
+      }
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {
+        const int cl = cq * 2 + jj;
+        const int j = j0 + cl;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int pl = pq * 4 + i;
+          if (cflag[cl] != 0.0f) continue;  // unusable (empty-cluster) or padding center
+          const float v = acc[i][jj];
+          if (!(v * (1.0f - gam) - 1e-30f <= hs[pl])) continue;
+          // FP64 in the oracle's order: dimensions 0 .. d-1 (padding dimensions are zero)
+          double ex = 0.0;
+          for (int q = 0; q < dq; ++q) {
+            const float4 x = xs[pl * rs + q];
+            const float4 c = cs[cl * rs + q];
+            double dd;
+            dd = (double)x.x - (double)c.x; ex = fma(dd, dd, ex);
+            dd = (double)x.y - (double)c.y; ex = fma(dd, dd, ex);
+            dd = (double)x.z - (double)c.z; ex = fma(dd, dd, ex);
+            dd = (double)x.w - (double)c.w; ex = fma(dd, dd, ex);
+          }
+          if (ex < INFINITY && (ex < be[i] || (ex == be[i] && (unsigned)j < (unsigned)bi[i]))) {
+            be[i] = ex;
+            bi[i] = j;
+          }
+        }
       }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int oi = __shfl_xor_sync(0xffffffffu, bidx, o);
-      const bool take = (ob < best) || (ob == best && (unsigned)oi < (unsigned)bidx);
-      best = take ? ob : best;
-      bidx = take ? oi : bidx;
-    }
-    if (lane == 0) {
-      rb[w] = best;
-      ri[w] = bidx;
+    // merge the 32 threads of each point: lanes pq, pq+8, pq+16, pq+24 of every warp
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+      for (int off = 8; off < 32; off <<= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, be[i], off);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi[i], off);
+        const bool take = (ob < be[i]) || (ob == be[i] && (unsigned)oi < (unsigned)bi[i]);
+        be[i] = take ? ob : be[i];
+        bi[i] = take ? oi : bi[i];
+      }
+      if (lane < 8) {
+        mb[w][pq * 4 + i] = be[i];
+        mi[w][pq * 4 + i] = bi[i];
+      }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int ww = 1; ww < (int)(blockDim.x >> 5); ++ww) {
-        const bool take = (rb[ww] < best) || (rb[ww] == best && (unsigned)ri[ww] < (unsigned)bidx);
-        best = take ? rb[ww] : best;
-        bidx = take ? ri[ww] : bidx;
+    if (tid < TP && g0 + tid < cnt) {
+      double fb = mb[0][tid];
+      int fi = mi[0][tid];
+      for (int ww = 1; ww < 8; ++ww) {
+        const bool take = (mb[ww][tid] < fb) || (mb[ww][tid] == fb && (unsigned)mi[ww][tid] < (unsigned)fi);
+        fb = take ? mb[ww][tid] : fb;
+        fi = take ? mi[ww][tid] : fi;
       }
-      a.labels[pt] = bidx < 0 ? 0 : bidx;
+      a.labels[a.list[g0 + tid]] = fi < 0 ? 0 : fi;
     }
   }
 }
@@ -518,7 +601,8 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
       continue;
     }
     const float* x = X + (size_t)pt * ldx;
-    // fast path: candidates in increasing index order, strict < keeps the lowest index
+    // fast path: certifies only a strict separation, so the list order (column slice by column
+    // slice) does not matter
     double v1 = INFINITY, v2 = INFINITY;
     int i1 = -1;
     bool finite = true;
@@ -545,11 +629,12 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
       if (lane == 0) labels[pt] = i1;
       continue;
     }
-    // exact path: the oracle's sequential FP64 evaluation, one lane per candidate
+    // exact path: the oracle's sequential FP64 evaluation, lane l taking candidates l, l+32, ...;
+    // equal values go to the lowest center index, within a lane and across lanes
     double best = INFINITY;
     int bidx = -1;
-    if (lane < nc) {
-      const int j = cand[slot * kMaxCand + lane];
+    for (int q = lane; q < nc; q += 32) {
+      const int j = cand[slot * kMaxCand + q];
       if (cn[j] < INFINITY) {
         const float* c = C + (size_t)j * ldc;
         double s = 0.0;
@@ -557,8 +642,8 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
           const double u = (double)__ldg(x + t) - (double)__ldg(c + t);
           s = fma(u, u, s);
         }
-        if (s < INFINITY) {  // the oracle never takes a NaN or infinite distance
-          best = s;
+        if (s < INFINITY && (s < best || (s == best && (unsigned)j < (unsigned)bidx))) {
+          best = s;  // the oracle never takes a NaN or infinite distance
           bidx = j;
         }
       }
@@ -611,12 +696,13 @@ cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long lo
 
 cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s) {
   if (a.n <= 0 || a.k <= 0) return cudaSuccess;
-  const size_t smem = sizeof(float) * (size_t)a.d;
+  const int dq = (a.d + 3) / 4;
+  const size_t smem = sizeof(float4) * (size_t)(TP + TC) * (dq + 1) + sizeof(float) * TC;
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   if (smem > 48 * 1024)
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  rerank_exact_kernel<<<152 * 4, 256, smem, s>>>(a, hi2);
+  rerank_exact_kernel<<<152 * 2, 256, smem, s>>>(a, hi2);
   count_launches(1);
   return cudaGetLastError();
 }
