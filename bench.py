@@ -347,6 +347,65 @@ def large_k_workload(args, n=16_000_000, d=256, k=65_536):
     print(json.dumps(out), flush=True)
 
 
+def streamed_workload(args, n=200_000_000, d=96, k=4096, iters=10, tile=4_000_000):
+    """Host-resident data set: 200M x 96 (76.8 GB of host memory), K=4096 isotropic Gaussians
+    (sigma 1.5, means U[-15,15]^96, equal weights), initial centers a seeded sample of points;
+    10 Lloyd iterations of the split BF16 tier through kmgb_lloyd_f32, (a) streamed through the
+    GPU in 4M-row tiles every iteration (the reference's out-of-memory path), (b) uploaded once
+    and resident in HBM. Both give the FP64 arg-min labels, so they must be identical."""
+    import torch
+    import kmeans_gb300 as km
+    from kmeans_gb300.synthetic import sample_init
+    km.build()
+    if args.n != N:
+        n = args.n
+    t0 = time.perf_counter()
+    Xh = np.empty((n, d), np.float32)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(31)
+    means = torch.empty((k, d), device="cuda").uniform_(-15.0, 15.0, generator=g)
+    for r0 in range(0, n, 1 << 22):
+        r1 = min(n, r0 + (1 << 22))
+        lab = torch.randint(0, k, (r1 - r0,), device="cuda", generator=g)
+        Xh[r0:r1] = (means[lab] + 1.5 * torch.randn((r1 - r0, d), device="cuda", generator=g)
+                     ).cpu().numpy()
+    del means
+    torch.cuda.empty_cache()
+    gen_s = time.perf_counter() - t0
+    init = Xh[sample_init(n, k, seed=17)]
+    # one host-to-device pass of X in tiles (pageable source), the floor of a streamed iteration
+    buf = torch.empty((tile, d), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r0 in range(0, n, tile):
+        r1 = min(n, r0 + tile)
+        buf[: r1 - r0].copy_(torch.from_numpy(Xh[r0:r1]))
+    torch.cuda.synchronize()
+    h2d_s = time.perf_counter() - t0
+    del buf
+    torch.cuda.empty_cache()
+    out = {"metric": f"Lloyd iteration, host data N={n}, D={d}, K={k} (s)", "unit": "s",
+           "higher_is_better": False, "data": "synthetic", "dtype": "bf16",
+           "config": {"workload": f"lloyd_{n}x{d}_K{k}_host", "n": n, "d": d, "k": k,
+                      "iterations": iters, "tier": "bf16x3", "tile_rows": tile},
+           "generation_s": gen_s, "h2d_pass_s": h2d_s, "h2d_GBs": Xh.nbytes / h2d_s / 1e9}
+    labels = {}
+    for mode, rows in (("streamed", tile), ("resident", 0)):
+        km.lloyd(Xh[:tile], k, init=init, max_iters=1, assign_tier=km.ASSIGN_BF16X3)  # warm-up
+        t0 = time.perf_counter()
+        res = km.lloyd(Xh, k, init=init, max_iters=iters, assign_tier=km.ASSIGN_BF16X3,
+                       stream_tile_rows=rows)
+        wall = time.perf_counter() - t0
+        out[mode] = {"call_s": wall, "s_per_iteration": wall / iters,
+                     "gpu_iterations_ms": res.ms_total, "reranked_points": res.reranked,
+                     "sse_last": float(res.sse[-1])}
+        labels[mode] = res.labels
+        del res
+    out["value"] = out["streamed"]["s_per_iteration"]
+    out["labels_identical"] = bool(np.array_equal(labels["streamed"], labels["resident"]))
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -364,10 +423,12 @@ def main():
     ap.add_argument("--no-init", action="store_true", help="skip the k-means++ timing")
     ap.add_argument("--only-init", action="store_true",
                     help="time only the k-means++ initialisation (profiling captures)")
-    ap.add_argument("--workload", default="lloyd", choices=["lloyd", "batched", "large_k"],
+    ap.add_argument("--workload", default="lloyd",
+                    choices=["lloyd", "batched", "large_k", "streamed"],
                     help="batched: the many-problems workload through kmgb_lloyd_batched_f32; "
-                         "large_k: 16M x 256, K=65536 split BF16 vs FP32 (own JSON lines; not "
-                         "the headline)")
+                         "large_k: 16M x 256, K=65536 split BF16 vs FP32; streamed: 200M x 96, "
+                         "K=4096 host data, streamed tiles vs resident (own JSON lines; not the "
+                         "headline)")
     ap.add_argument("--problems", type=int, default=10_000,
                     help="problems of the batched workload")
     ap.add_argument("--tiers", default="bf16x3,fp32", help="tiers of the large_k workload")
@@ -381,6 +442,8 @@ def main():
         return batched_workload(args)
     if args.workload == "large_k":
         return large_k_workload(args)
+    if args.workload == "streamed":
+        return streamed_workload(args)
 
     import torch
     import kmeans_gb300 as km
