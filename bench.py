@@ -190,6 +190,75 @@ def reference_arm(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
+def accuracy_and_plain_fp32(km, torch, h, X, n, k):
+    """Outside the timed region. One more iteration of the measured handle from its current
+    centers C gives labels L, centers C' and SSE s. Checked against an independent FP64
+    evaluation on the GPU (torch, float64): L on a 65,536-row sample against the arg-min of the
+    direct squared distances to C (first index on ties; NaN centers of empty clusters never
+    win), C' against the FP64 means of the rows
+    of each label, s against the FP64 sum of ||x - C'[label]||^2 over all rows. Then the plain
+    FP32 tier from the same C: its labels must equal L, and its iteration rate is the
+    denominator of the tensor-core speed-up."""
+    d = X.shape[1]
+    C = torch.from_numpy(h.centers()).cuda()
+    h.run(1)
+    h.synchronize()
+    L = torch.from_numpy(h.labels()).cuda().long()
+    C1 = torch.from_numpy(h.centers()).cuda()
+    sse = float(h.sse(1)[-1])  # the SSE of this run's single iteration
+    C64 = C.double()
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    idx = torch.randperm(n, device="cuda", generator=g)[:65536]
+    mism = 0
+    for r0 in range(0, idx.numel(), 1024):
+        xs = X[idx[r0:r0 + 1024]].double()
+        dist = ((xs[:, None, :] - C64[None, :, :]) ** 2).sum(-1)
+        # an empty cluster's NaN center never wins (torch's argmin would return it)
+        dist = torch.nan_to_num(dist, nan=float("inf"))
+        mism += int((dist.argmin(1) != L[idx[r0:r0 + 1024]]).sum())
+        del xs, dist
+    sums = torch.zeros((k, d), dtype=torch.float64, device="cuda")
+    sq = torch.zeros((), dtype=torch.float64, device="cuda")
+    for r0 in range(0, n, 1 << 20):
+        sums.index_add_(0, L[r0:r0 + (1 << 20)], X[r0:r0 + (1 << 20)].double())
+    cnt = torch.bincount(L, minlength=k).double()
+    means = sums / cnt[:, None]
+    used = cnt > 0
+    cerr = ((C1.double() - means).abs() / means.abs().clamp_min(1e-30))[used].max()
+    C164 = C1.double()
+    for r0 in range(0, n, 1 << 20):
+        diff = X[r0:r0 + (1 << 20)].double() - C164[L[r0:r0 + (1 << 20)]]
+        sq += (diff * diff).sum()
+    sse64 = float(sq)
+    acc = {"sample_rows": int(idx.numel()), "label_mismatches": mism,
+           "label_mismatch_rate": mism / idx.numel(),
+           "center_max_rel_err": float(cerr), "sse_rel_err": abs(sse - sse64) / abs(sse64),
+           "reference": "torch float64 on the GPU (direct squared distances, FP64 means and SSE)"}
+    # plain FP32 tier from the same centers
+    h32 = km.Handle(n, d, k, assign_tier=km.ASSIGN_FP32, max_iters=8)
+    h32.set_data(X, True)
+    h32.set_centers(C.cpu().numpy(), False)
+    h32.run(1)
+    h32.synchronize()
+    same = bool(torch.equal(torch.from_numpy(h32.labels()).cuda().long(), L))
+    stream = torch.cuda.ExternalStream(h32.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h32.set_profiling(True)
+    e0.record(stream)
+    h32.run(5)
+    e1.record(stream)
+    h32.synchronize()
+    ms = e0.elapsed_time(e1) / 5
+    phase, pit = h32.phase_ms()
+    h32.close()
+    a_ms = phase[1] / max(pit, 1)
+    plain = {"iter_per_s": 1000.0 / ms, "ms_per_iteration": ms, "assign_ms": a_ms,
+             "assign_tflops": 2.0 * n * k * d / (a_ms / 1000.0) / 1e12,
+             "labels_equal": same}
+    return {"accuracy": acc, "plain_fp32": plain}
+
+
 def time_kmeanspp(km, torch, h, n, k, reps=1):
     """k-means++ initialisation on the handle's resident data (outside the Lloyd timed region):
     one untimed call, then `reps` calls bracketed by CUDA events on the handle's stream. Each
@@ -421,6 +490,8 @@ def main():
     ap.add_argument("--k", type=int, default=NUM_CENTERS, help="centers (default 1024); other values are "
                     "for profiling captures only")
     ap.add_argument("--no-init", action="store_true", help="skip the k-means++ timing")
+    ap.add_argument("--no-checks", action="store_true",
+                    help="skip the FP64 accuracy checks and the plain-FP32 comparison")
     ap.add_argument("--only-init", action="store_true",
                     help="time only the k-means++ initialisation (profiling captures)")
     ap.add_argument("--workload", default="lloyd",
@@ -520,6 +591,10 @@ def main():
         roofline["tensor_tflops"] = tf / (assign_ms / 1000.0) / 1e12
         roofline["tensor_frac"] = roofline["tensor_tflops"] / bf16_peak
 
+    checks = None
+    if not args.no_checks and rank == 0:
+        checks = accuracy_and_plain_fp32(km, torch, h, X, n, K)
+
     init_pp = None
     if not args.no_init and rank == 0:
         init_pp = time_kmeanspp(km, torch, h, n, K, reps=1)
@@ -564,6 +639,10 @@ def main():
                 "reranked_points_total": st.reranked, "reranked_fp64_total": st.reranked_fp64,
                 "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
                 "init_kmeanspp": init_pp,
+                "accuracy": checks["accuracy"] if checks else None,
+                "plain_fp32": checks["plain_fp32"] if checks else None,
+                "speedup_vs_plain_fp32": (value / checks["plain_fp32"]["iter_per_s"]
+                                          if checks else None),
                 "gpu_launches": launches, "clocks": cl}
         print(json.dumps(line), flush=True)
     h.close()
