@@ -310,13 +310,14 @@ def batched_workload(args):
     gen_s = time.perf_counter() - t0
     rows = sum(len(p[0]) for p in probs)
     flop = sum(2.0 * len(X) * k * X.shape[1] for X, k in probs)
-    km.lloyd_batched(probs[:64], max_iters=2)  # warm-up: module loading, allocator
+    tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3}[args.tier]
+    km.lloyd_batched(probs[:64], max_iters=2, assign_tier=tier_id)  # warm-up: module loading
     t0 = time.perf_counter()
-    km.lloyd_batched(probs, max_iters=1)
+    km.lloyd_batched(probs, max_iters=1, assign_tier=tier_id)
     one = time.perf_counter() - t0
     l0 = km.launch_count()
     t0 = time.perf_counter()
-    _, st = km.lloyd_batched(probs, max_iters=iters)
+    _, st = km.lloyd_batched(probs, max_iters=iters, assign_tier=tier_id)
     full = time.perf_counter() - t0
     launches = km.launch_count() - l0
     per_iter = st.ms_total / 1000.0 / iters  # CUDA events around the iteration loops
@@ -324,18 +325,20 @@ def batched_workload(args):
     km.lloyd(sample[0][0], sample[0][1], max_iters=1)
     t0 = time.perf_counter()
     for X, k in sample:
-        km.lloyd(X, k, max_iters=iters)
+        km.lloyd(X, k, max_iters=iters, assign_tier=tier_id)
     loop = time.perf_counter() - t0
     t0 = time.perf_counter()
-    km.lloyd_batched(sample, max_iters=iters)
+    km.lloyd_batched(sample, max_iters=iters, assign_tier=tier_id)
     bsample = time.perf_counter() - t0
     line = {"metric": f"batched Lloyd, {len(probs)} problems x {iters} iterations (s per call)",
             "value": full, "unit": "s", "higher_is_better": False, "n_gpus": 1,
-            "data": "synthetic", "dtype": "f32",
+            "data": "synthetic", "dtype": "f32" if args.tier == "fp32" else "bf16",
             "config": {"workload": f"batched_{len(probs)}_problems", "rows": rows,
                        "gflop_per_iteration": flop / 1e9, "iterations": iters,
-                       "tier": "fp32", "certified_labels": True},
+                       "tier": args.tier, "certified_labels": True},
             "ms_per_iteration": per_iter * 1000.0,
+            "phase_ms_per_iteration": {nm: st.reserved[1 + i] / 1000.0 / iters for i, nm in
+                                       enumerate(["prep", "assign", "rerank", "update"])},
             "setup_s": full - st.ms_total / 1000.0,
             "assign_tflops_per_iteration": flop / per_iter / 1e12,
             "setup_and_one_iteration_s": one, "generation_s": gen_s,

@@ -290,7 +290,8 @@ typedef struct kmgb_problem {
  * KMGB_INIT_REFERENCE. stats (nullable): iterations = the largest over the problems, reranked =
  * rows settled by the exact re-rank, ms_total = GPU time of the iterations (CUDA events, summed
  * over the groups of one dimension), reserved[0] = wall time of the whole call in microseconds
- * (uploads, initialisation and result copies included). */
+ * (uploads, initialisation and result copies included), reserved[1..4] = microseconds of center
+ * preparation, assignment, re-rank and update summed over the iterations (CUDA events). */
 KMGB_EXPORT int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const kmgb_options* opt,
                                        kmgb_stats* stats);
 

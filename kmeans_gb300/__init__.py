@@ -376,7 +376,8 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
 
 
 def lloyd_batched(problems, max_iters: int = 20, criterion: float = -1.0,
-                  empty_policy: int = EMPTY_NAN, certify: bool = True):
+                  empty_policy: int = EMPTY_NAN, certify: bool = True,
+                  assign_tier: int = ASSIGN_FP32):
     """Many independent Lloyd runs in one kmgb_lloyd_batched_f32 call. problems: sequence of
     (X, k) or (X, k, init) with X numpy (host) or a contiguous torch tensor (device), n x d
     float32 (init k x d, or None for the reference initialisation). Returns (list of
@@ -401,7 +402,7 @@ def lloyd_batched(problems, max_iters: int = 20, criterion: float = -1.0,
         arr[i].init = _ptr(init)
         arr[i].centers, arr[i].labels, arr[i].sse = _ptr(cen), _ptr(lab), _ptr(sse)
     opt = default_options(max_iters=max_iters, criterion=criterion, empty_policy=empty_policy,
-                          certify=int(certify))
+                          certify=int(certify), assign_tier=assign_tier)
     st = kmgb_stats()
     rc = lib().kmgb_lloyd_batched_f32(arr, len(problems), C.byref(opt), C.byref(st))
     if rc:

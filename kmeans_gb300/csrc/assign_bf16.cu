@@ -253,10 +253,6 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const int nkb = (p.d + BK - 1) / BK;
   const int nchunks = (p.k + BN - 1) / BN;
   const long long pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
-  // Each pair visits the center chunks in its own rotated order, so that at any moment the pairs
-  // stream different chunks of C from L2.
-  const int rot = (int)(pair % nchunks);
-  auto chunk_of = [&](int c) { return c + rot < nchunks ? c + rot : c + rot - nchunks; };
   // rows of this launch: [row0, row0 + n_rows); a device count bounds them in candidate mode
   long long n_rows = p.n;
   if (p.n_dev) {
@@ -265,9 +261,37 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   }
   const long long n_units = (n_rows + UNIT - 1) / UNIT;
   const bool cand_mode = p.thr_in != nullptr;
-  long long my_units = 0;
-  if (pair < n_units) my_units = (n_units - 1 - pair) / npairs + 1;
-  const long long total_chunks = my_units * nchunks;
+  const bool grouped = p.u_prob != nullptr;
+  // A unit's chunks: how many, the first center, the rows that exist, and a rotation -- each pair
+  // visits the chunks in its own rotated order so that at any moment the pairs stream different
+  // chunks of C from L2. Every role of both CTAs derives the same sequence (false: skipped unit).
+  struct UnitInfo {
+    int nch, rot, cbase;
+    long long rend;
+  };
+  auto unit_info = [&](long long u, UnitInfo& ui) -> bool {
+    if (!grouped) {
+      ui.nch = nchunks;
+      ui.cbase = 0;
+      ui.rend = n_rows;
+    } else {
+      const int pr = p.u_prob[u];
+      if (p.g_done && p.g_done[pr]) return false;
+      ui.nch = (p.g_k[pr] + BN - 1) / BN;
+      ui.cbase = p.g_coff[pr];
+      ui.rend = p.g_rend[pr];
+    }
+    ui.rot = (int)(pair % ui.nch);
+    return true;
+  };
+  auto chunk_of = [](const UnitInfo& ui, int c) {
+    return c + ui.rot < ui.nch ? c + ui.rot : c + ui.rot - ui.nch;
+  };
+  long long total_chunks = 0;
+  for (long long u = pair; u < n_units; u += npairs) {
+    UnitInfo ui;
+    if (unit_info(u, ui)) total_chunks += ui.nch;
+  }
   // points: [buffer][plane][k-block] 16 KB boxes; C stage: [plane] 16 KB boxes of one
   // (chunk, k-block). plane 0 = BF16 value, plane 1 = BF16 residual (split tier).
   const size_t xbuf_bytes = (size_t)planes * nkb * XKB_BYTES;
@@ -317,9 +341,12 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     if (lane == 0 && total_chunks > 0) {
       long long s = 0, lu = 0;
       bool ok = true;
-      for (long long u = pair; u < n_units && ok; u += npairs, ++lu) {
+      for (long long u = pair; u < n_units && ok; u += npairs) {
+        UnitInfo ui;
+        if (!unit_info(u, ui)) continue;
         const int xi = (int)(lu % xbufs);
         const long long use = lu / xbufs;
+        ++lu;
         // wait until the MMAs of the previous user of this buffer have completed
         if (use > 0 && !mbar_wait(smem_u32(&bars.x_empty[xi]), (uint32_t)((use - 1) & 1),
                                   &abort_flag, p.err, KMGB_DEV_TIMEOUT_EMPTY))
@@ -340,8 +367,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           for (int pl = 0; pl < planes; ++pl)
             for (int kb = 0; kb < nkb; ++kb) tma_prefetch_2d(pl ? &tmXl : &tmX, kb * BK, nrow);
         }
-        for (int c = 0; c < nchunks && ok; ++c) {
-          const int crow = chunk_of(c) * BN + (int)rank * BNH;
+        for (int c = 0; c < ui.nch && ok; ++c) {
+          const int crow = ui.cbase + chunk_of(ui, c) * BN + (int)rank * BNH;
           for (int kb = 0; kb < nkb; ++kb, ++s) {
             const int stage = (int)(s % stages);
             if (s >= stages &&
@@ -365,15 +392,18 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     if (lane == 0 && rank == 0 && total_chunks > 0) {
       long long s = 0, g = 0, lu = 0;
       bool ok = true;
-      for (long long u = pair; u < n_units && ok; u += npairs, ++lu) {
+      for (long long u = pair; u < n_units && ok; u += npairs) {
+        UnitInfo ui;
+        if (!unit_info(u, ui)) continue;
         const int xi = (int)(lu % xbufs);
         const long long use = lu / xbufs;
+        ++lu;
         if (!mbar_wait(smem_u32(&bars.x_full[xi]), (uint32_t)(use & 1), &abort_flag, p.err,
                        KMGB_DEV_TIMEOUT_FULL))
           break;
         tc_fence_after();
         const uint8_t* xs = smem + (size_t)xi * xbuf_bytes;
-        for (int c = 0; c < nchunks && ok; ++c, ++g) {
+        for (int c = 0; c < ui.nch && ok; ++c, ++g) {
           const int b = (int)(g & 1);
           if (!mbar_wait(smem_u32(&bars.acc_empty[b]), (uint32_t)((g >> 1) & 1), &abort_flag,
                          p.err, KMGB_DEV_TIMEOUT_ACC)) {
@@ -431,8 +461,12 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     bool alive = true;
     for (long long g0 = 0; g0 < 2 && g0 < total_chunks; ++g0)  // both buffers start free
       if (lane == 0) mbar_arrive_remote(g0 ? acc_empty_leader1 : acc_empty_leader0);
-    long long g = 0, lu = 0;
-    for (long long u = pair; u < n_units && alive; u += npairs, ++lu) {
+    long long g = 0, lu_next = 0;
+    for (long long u = pair; u < n_units && alive; u += npairs) {
+      UnitInfo ui;
+      if (!unit_info(u, ui)) continue;
+      const long long lu = lu_next++;    // units this warp has processed before this one
+      const long long n_rows = ui.rend;  // rows of this unit that exist end here
       float b1 = -INFINITY, b2 = -INFINITY;
       int bblk = -1;  // global 32-column block holding the best key
       const long long prow = u * UNIT + rank * BM + q * 32 + lane;  // row within the launch
@@ -443,7 +477,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       // HBM latency hides behind the unit's chunks
       const float xn_pt = (p.certify && !cand_mode && h == 0 && prow < n_rows)
                               ? __ldg(p.xnorm + prow) : 0.0f;
-      for (int c = 0; c < nchunks; ++c, ++g) {
+      for (int c = 0; c < ui.nch; ++c, ++g) {
         const int b = (int)(g & 1);
         bool ok = mbar_wait(smem_u32(&bars.acc_full[b]), (uint32_t)((g >> 1) & 1), &abort_flag,
                             p.err, KMGB_DEV_TIMEOUT_ACC);
@@ -452,7 +486,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           break;
         }
         tc_fence_after();
-        const int col0 = chunk_of(c) * BN + h * COLS_PER_WARP;  // first center of this warp
+        const int col0 = ui.cbase + chunk_of(ui, c) * BN + h * COLS_PER_WARP;  // first center
         const uint32_t base = lane_addr + (uint32_t)(b * BN + h * COLS_PER_WARP);
         // all of this warp's columns into registers at once, then the buffer goes straight back
         // to the leader's MMA issuer and the folding below overlaps the next MMAs
@@ -570,7 +604,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       const long long pt = prow;
       if (pt < n_rows) {
         const bool none = !(b1 > -1.0e38f);  // no usable center at all
-        const int label = (bblk < 0 || none) ? 0 : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
+        // no usable center at all: the first center of the point's problem
+        const int label =
+            (bblk < 0 || none) ? ui.cbase : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
         p.labels[pt] = label;
         if (p.certify) {
           const float eb = bound_acc(xn_pt, cm, p.d, planes);

@@ -21,6 +21,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <thread>
 #include <vector>
@@ -151,7 +152,7 @@ bool initial_centers(const kmgb_problem* pr, const std::vector<int>& ids, int d,
 // pinned buffers by host threads (zeros for padding rows and columns) and copied with
 // cudaMemcpyAsync while the next chunk is packed.
 bool upload_host_rows(const kmgb_problem* pr, const std::vector<int>& ids, int d, long long ldx,
-                      long long rows, const std::vector<long long>& rbeg,
+                      long long rows, long long row_pad, const std::vector<long long>& rbeg,
                       const std::vector<long long>& rend, const std::vector<char>& is_dev,
                       float* X, cudaStream_t s, Fail& f) {
   const int E = KMEANS_ERROR_BUILDDATA;
@@ -167,7 +168,7 @@ bool upload_host_rows(const kmgb_problem* pr, const std::vector<int>& ids, int d
   }
   const int P = (int)ids.size();
   // problem i's padded region is rows [rbeg[i], pend(i)); the regions tile [0, rows)
-  auto pend = [&](int i) { return rbeg[i] + rup(rend[i] - rbeg[i], kTileRows); };
+  auto pend = [&](int i) { return rbeg[i] + rup(rend[i] - rbeg[i], row_pad); };
   const int nth = (int)std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
   int first = 0;  // first problem whose region ends after the chunk's first row
   for (long long r0 = 0, c = 0; ok && r0 < rows; r0 += chunk_rows, ++c) {
@@ -225,10 +226,18 @@ bool upload_host_rows(const kmgb_problem* pr, const std::vector<int>& ids, int d
 
 // One group: problems `ids` (all of dimension d).
 int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_options& o,
-              cudaStream_t s, unsigned long long* reranked, double* loop_ms, Fail& f) {
+              cudaStream_t s, unsigned long long* reranked, double* loop_ms, double* phase_ms,
+              Fail& f) {
   const int P = (int)ids.size();
   const long long ldx = rup(d, 4);
+  const long long ldb = rup(d, 8);
   const int max_iters = std::max(0, o.max_iters);
+  // tensor-core tiers: a problem's rows fill whole 256-row pair units and its centers whole
+  // 256-center chunks (padding centers are NaN, which the center preparation marks unusable)
+  const bool tc = o.assign_tier != KMGB_ASSIGN_FP32;
+  const bool split = o.assign_tier == KMGB_ASSIGN_BF16X3;
+  const long long row_pad = tc ? 256 : kTileRows;
+  const long long cen_pad = tc ? 256 : 1;
   // layout
   std::vector<long long> rbeg(P), rend(P), hoff(P);
   std::vector<int> coff(P), kk(P), nt(P);
@@ -238,28 +247,36 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
     const kmgb_problem& q = pr[ids[i]];
     rbeg[i] = rows;
     rend[i] = rows + q.n;
-    rows += rup(q.n, kTileRows);
+    rows += rup(q.n, row_pad);
     nvalid += q.n;
     coff[i] = (int)K;
     kk[i] = q.k;
-    K += q.k;
+    const long long kspan = rup(q.k, cen_pad);  // the problem's centers plus padding
+    K += kspan;
     nt[i] = (int)((q.n + kSortTile - 1) / kSortTile);
     hoff[i] = hist;
-    hist += (long long)q.k * nt[i];
+    hist += kspan * nt[i];
     stiles += nt[i];
   }
   const long long tiles = rows / kTileRows;
   std::vector<int> tile_prob(tiles), stile_prob(stiles), stile_local(stiles), cprob(K);
+  std::vector<int> unit_prob(tc ? rows / 256 : 0);
   for (int i = 0, st = 0; i < P; ++i) {
-    const long long t0 = rbeg[i] / kTileRows, t1 = t0 + rup(rend[i] - rbeg[i], kTileRows) / kTileRows;
-    for (long long t = t0; t < t1; ++t) tile_prob[t] = i;
+    const long long span = rup(rend[i] - rbeg[i], row_pad);
+    for (long long t = rbeg[i] / kTileRows; t < (rbeg[i] + span) / kTileRows; ++t) tile_prob[t] = i;
+    if (tc)
+      for (long long u = rbeg[i] / 256; u < (rbeg[i] + span) / 256; ++u) unit_prob[u] = i;
     for (int t = 0; t < nt[i]; ++t, ++st) {
       stile_prob[st] = i;
       stile_local[st] = t;
     }
-    for (int j = 0; j < kk[i]; ++j) cprob[coff[i] + j] = i;
   }
-  std::vector<float> C0((size_t)K * d);
+  for (int i = 0; i < P; ++i) {
+    const long long c1 = (i + 1 < P) ? coff[i + 1] : K;
+    for (long long j = coff[i]; j < c1; ++j) cprob[j] = i;
+  }
+  // initial centers; padding centers are NaN (unusable, never a label, never updated)
+  std::vector<float> C0((size_t)K * d, std::numeric_limits<float>::quiet_NaN());
   if (!initial_centers(pr, ids, d, C0, coff, f)) return f.code;
 
   DevPool m;
@@ -280,6 +297,20 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       f.set(cudaMemsetAsync(err, 0, sizeof(int), s), E, "error word") ||
       f.set(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)K * ldx, s), E, "centers"))
     return f.code;
+  // tensor-core tiers: BF16 planes of the points and centers, the centers' start values
+  void *Xb = nullptr, *Xl = nullptr, *Cb = nullptr, *Cl = nullptr;
+  float* cinit = nullptr;
+  int* d_unit_prob = nullptr;
+  if (tc &&
+      (f.set(m.alloc(reinterpret_cast<uint16_t**>(&Xb), (size_t)rows * ldb), E, "BF16 data") ||
+       (split && f.set(m.alloc(reinterpret_cast<uint16_t**>(&Xl), (size_t)rows * ldb), E,
+                       "BF16 data")) ||
+       f.set(m.alloc(reinterpret_cast<uint16_t**>(&Cb), (size_t)K * ldb), E, "BF16 centers") ||
+       (split && f.set(m.alloc(reinterpret_cast<uint16_t**>(&Cl), (size_t)K * ldb), E,
+                       "BF16 centers")) ||
+       f.set(m.alloc(&cinit, (size_t)rup(K, kCenterPad)), E, "BF16 centers") ||
+       f.set(m.upload(&d_unit_prob, unit_prob, s), E, "tables")))
+    return f.code;
   // data: host problems are packed by host threads into two pinned staging buffers in the
   // device layout (rows of ldx floats, zero padding rows and columns) while the previous buffer
   // is copied; device problems are copied on the device
@@ -289,7 +320,7 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
     is_dev[i] = on_device(pr[ids[i]].X) ? 1 : 0;
     any_host |= !is_dev[i];
   }
-  if (any_host && !upload_host_rows(pr, ids, d, ldx, rows, rbeg, rend, is_dev, X, s, f))
+  if (any_host && !upload_host_rows(pr, ids, d, ldx, rows, row_pad, rbeg, rend, is_dev, X, s, f))
     return f.code;
   for (int i = 0; i < P; ++i) {
     const kmgb_problem& q = pr[ids[i]];
@@ -305,6 +336,8 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
             KMEANS_ERROR_INITIALIZE, "initial centers"))
     return f.code;
   if (f.set(launch_point_norms(X, ldx, rows, d, qn, xn, s), E, "norms")) return f.code;
+  if (tc && f.set(launch_to_bf16(X, ldx, rows, d, Xb, ldb, s, nullptr, Xl), E, "BF16 data"))
+    return f.code;
 
   // problem tables
   GroupArgs g{};
@@ -389,7 +422,15 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
   a.k = (int)K;
   a.d = d;
   a.certify = o.certify ? 1 : 0;
-  a.gamma = assign_fp32_gamma(d);
+  a.gamma = tc ? assign_bf16_gamma(d) : assign_fp32_gamma(d);
+  if (tc) {
+    a.cinit = cinit;
+    a.u_prob = d_unit_prob;
+    a.g_coff = d_coff;
+    a.g_k = d_k;
+    a.g_rend = d_rend;
+    a.g_done = d_done;
+  }
   RerankArgs ra{};
   ra.X = X;
   ra.ldx = ldx;
@@ -419,18 +460,38 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       cudaEventDestroy(e[1]);
     }
   } ev_guard{ev};
+  // phase events of every iteration: centers | assignment | re-rank | update
+  std::vector<cudaEvent_t> pev;
+  struct PevGuard {
+    std::vector<cudaEvent_t>* v;
+    ~PevGuard() {
+      for (cudaEvent_t e : *v) cudaEventDestroy(e);
+    }
+  } pev_guard{&pev};
+  auto mark = [&]() -> bool {
+    cudaEvent_t e = nullptr;
+    if (f.set(cudaEventCreate(&e), EU, "events")) return false;
+    pev.push_back(e);
+    return !f.set(cudaEventRecord(e, s), EU, "events");
+  };
   for (int it = 0; it < max_iters; ++it) {
-    if (f.set(cudaMemsetAsync(cmax, 0, sizeof(float), s), EU, "centers") ||
-        f.set(launch_prep_centers(C, ldx, (int)K, d, Cop, nullptr, 0, cn, cmax, s), EU,
-              "center preparation") ||
+    if (!mark() || f.set(cudaMemsetAsync(cmax, 0, sizeof(float), s), EU, "centers") ||
+        f.set(launch_prep_centers(C, ldx, (int)K, d, Cop, Cb, ldb, cn, cmax, s, nullptr, cinit,
+                                  Cl),
+              EU, "center preparation") ||
         f.set(cudaMemsetAsync(rr_count, 0, sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS,
               "re-rank") ||
-        f.set(launch_assign_fp32(X, ldx, Cop, ldx, a, s, &g, tiles), KMEANS_ERROR_CLOSEST_CENTERS,
-              "assignment") ||
+        !mark() ||
+        f.set(tc ? launch_assign_bf16(Xb, Xl, ldb, Cb, Cl, ldb, a, s)
+                 : launch_assign_fp32(X, ldx, Cop, ldx, a, s, &g, tiles),
+              KMEANS_ERROR_CLOSEST_CENTERS, "assignment") ||
+        !mark() ||
         (o.certify && f.set(launch_rerank_grouped(ra, g, s), KMEANS_ERROR_CLOSEST_CENTERS,
                             "re-rank")) ||
+        !mark() ||
         f.set(launch_update_batched(X, ldx, d, qn, labels, C, ldx, o.empty_policy, w, b, it, s),
-              EU, "update"))
+              EU, "update") ||
+        !mark())
       return f.code;
     if (o.criterion >= 0.0) {  // stop early once every problem's rule has fired
       std::vector<int> done(P);
@@ -447,6 +508,11 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       f.set(cudaEventElapsedTime(&ms, ev[0], ev[1]), EU, "events"))
     return f.code;
   *loop_ms += ms;
+  for (size_t e = 0; e + 5 <= pev.size(); e += 5)  // five events per iteration
+    for (int ph = 0; ph < 4; ++ph) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, pev[e + ph], pev[e + ph + 1]) == cudaSuccess) phase_ms[ph] += t;
+    }
   // results
   std::vector<int> lab(rows), iters(P);
   std::vector<float> Ch((size_t)K * d);
@@ -504,11 +570,11 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     return code;
   };
   if (!problems || count <= 0) return reject(KMEANS_ERROR_BUILDDATA, "kmgb_lloyd_batched_f32: no problems");
-  if (o.assign_tier != KMGB_ASSIGN_FP32 || o.mini_batch_fraction < 1.0f || o.stream_tile_rows > 0 ||
+  if (o.mini_batch_fraction < 1.0f || o.stream_tile_rows > 0 ||
       o.init_algorithm == KMGB_INIT_KMEANSPP)
     return reject(KMEANS_ERROR_BUILDDATA,
-                  "kmgb_lloyd_batched_f32: batched problems use the FP32 tier, full batches, "
-                  "resident data and the reference or given initialisation");
+                  "kmgb_lloyd_batched_f32: batched problems use full batches, resident data and "
+                  "the reference or given initialisation");
   for (int i = 0; i < count; ++i) {
     const kmgb_problem& q = problems[i];
     if (!q.X || q.n <= 0 || q.d <= 0 || q.k <= 0 || q.n >= kMaxRows || q.k > (1 << 24))
@@ -517,6 +583,10 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     if (!q.init && q.k > q.n)
       return reject(KMEANS_ERROR_INITIALIZE,
                     "kmgb_lloyd_batched_f32: the reference initialisation needs k <= n");
+    if (o.assign_tier != KMGB_ASSIGN_FP32 &&
+        !bf16_tc_supported(q.d, o.assign_tier == KMGB_ASSIGN_BF16X3 ? 2 : 1))
+      return reject(KMEANS_ERROR_BUILDDATA,
+                    "kmgb_lloyd_batched_f32: the BF16 tensor-core tiers support D <= 256");
   }
   for (int i = 0; i < count; ++i) {
     problems[i].iterations = 0;
@@ -533,7 +603,10 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
   Fail f;
   unsigned long long reranked = 0;
   double loop_ms = 0.0;
+  double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
   size_t i = 0;
+  const bool tc = o.assign_tier != KMGB_ASSIGN_FP32;
+  const long long row_pad = tc ? 256 : kTileRows, cen_pad = tc ? 256 : 1;
   while (i < order.size() && !f.code) {
     const int d = problems[order[i]].d;
     const long long ldx = rup(d, 4);
@@ -541,24 +614,25 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     long long rows = 0, hist = 0, K = 0;
     while (i < order.size() && problems[order[i]].d == d) {
       const kmgb_problem& q = problems[order[i]];
-      const long long r = rup(q.n, kTileRows);
-      const long long h = (long long)q.k * ((q.n + kSortTile - 1) / kSortTile);
-      if (!ids.empty() && (rows + r > kMaxRows || hist + h > kMaxHist || K + q.k > (1LL << 30) ||
+      const long long r = rup(q.n, row_pad);
+      const long long kspan = rup(q.k, cen_pad);
+      const long long h = kspan * ((q.n + kSortTile - 1) / kSortTile);
+      if (!ids.empty() && (rows + r > kMaxRows || hist + h > kMaxHist || K + kspan > (1LL << 30) ||
                            (rows + r) * ldx * 4 > kMaxXBytes))
         break;
       if (h > kMaxHist) {
         f.code = KMEANS_ERROR_BUILDDATA;
-        f.msg = "kmgb_lloyd_batched_f32: a problem's k x ceil(n/4096) exceeds the sort capacity";
+        f.msg = "kmgb_lloyd_batched_f32: a problem's k x ceil(n/2048) exceeds the sort capacity";
         break;
       }
       ids.push_back(order[i]);
       rows += r;
       hist += h;
-      K += q.k;
+      K += kspan;
       ++i;
     }
     if (f.code) break;
-    run_group(problems, ids, d, o, s, &reranked, &loop_ms, f);
+    run_group(problems, ids, d, o, s, &reranked, &loop_ms, phase_ms, f);
   }
   cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
@@ -570,6 +644,8 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     stats->status = f.code;
     stats->reranked = reranked;
     stats->ms_total = loop_ms;
+    // reserved[1..4]: microseconds of center preparation, assignment, re-rank and update
+    for (int ph = 0; ph < 4; ++ph) stats->reserved[1 + ph] = (long long)(phase_ms[ph] * 1000.0);
     stats->reserved[0] = (long long)std::chrono::duration<double, std::micro>(
                              std::chrono::steady_clock::now() - t0)
                              .count();

@@ -35,6 +35,15 @@ struct AssignArgs {
   int certify;            // 0: write arg-min labels only
   float gamma;
   const int* stop;        // device stop flag of the run (nullable)
+  // BF16 tiers, grouped problems (batched Lloyd; null otherwise): unit u (rows 256u .. 256u+255)
+  // belongs to problem u_prob[u], whose centers are rows g_coff[p] .. g_coff[p] + g_k[p] - 1 (a
+  // multiple of 256 apart, padding centers unusable); labels are global center indices; rows at
+  // or past g_rend[p] are not written; units of problems with g_done[p] set are skipped
+  const int* u_prob;
+  const int* g_coff;
+  const int* g_k;
+  const long long* g_rend;
+  const int* g_done;
 };
 
 // Many problems of one dimension in one launch (batched Lloyd): problem p owns rows

@@ -416,50 +416,78 @@ rerank_exact_kernel(RerankArgs a, const float* __restrict__ hi2) {
   }
 }
 
-// Grouped (batched Lloyd) re-rank, one CTA per flagged row of any problem: the row's own
-// problem (tile_prob[row / 128]) gives its center range. Pass 1 finds the smallest FP32
-// direct-form value over the usable centers and its upper end; pass 2 evaluates in FP64 (as the
-// oracle does) every center whose FP32 lower end is within it. Labels are global indices.
-__global__ void __launch_bounds__(256)
+// Grouped (batched Lloyd) re-rank, one warp per flagged row of any problem; the row's own
+// problem (tile_prob[row / 128]) gives its center range. Pass 1, FP32 direct form: the lanes
+// split the dimensions of four centers at a time (coalesced rows, a tree sum per center -- like
+// any order it stays within the (d+4) 2u relative bound of a sum of non-negative terms); the
+// values of up to RG_VCAP centers stay in shared memory. Pass 2: every usable center whose FP32
+// lower end is within the smallest upper end is evaluated in FP64 in the oracle's order
+// (sequential fma over the dimensions), the smallest value winning, lowest index on ties.
+// Labels are global center indices.
+constexpr int RG_VCAP = 512;
+constexpr int RG_WARPS = 8;
+
+__global__ void __launch_bounds__(RG_WARPS * 32)
 rerank_grouped_kernel(RerankArgs a, GroupArgs g) {
   if (stopped(a.stop)) return;
-  extern __shared__ float xsm[];
-  __shared__ float rf[8];
-  __shared__ double rb[8];
-  __shared__ int ri[8];
+  extern __shared__ float rg_smem[];  // [warps][RG_VCAP] values, then [warps][d] rows
   const long long cnt = min((long long)*(volatile const int*)a.count, a.max_list);
   const float u = 5.9604645e-8f;
   const float gam = (float)(a.d + 4) * 2.0f * u * 1.01f;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int nw = (int)(blockDim.x >> 5);
-  for (long long slot = blockIdx.x; slot < cnt; slot += gridDim.x) {
-    __syncthreads();
+  float* vals = rg_smem + (size_t)w * RG_VCAP;
+  float* xs = rg_smem + (size_t)RG_WARPS * RG_VCAP + (size_t)w * a.d;
+  for (long long slot = (long long)blockIdx.x * RG_WARPS + w; slot < cnt;
+       slot += (long long)gridDim.x * RG_WARPS) {
     const int pt = a.list[slot];
     const int prob = g.tile_prob[pt >> 7];
     const int cbeg = g.c_off[prob], kp = g.k[prob];
+    const bool keep = kp <= RG_VCAP;
     const float* x = a.X + (size_t)pt * a.ldx;
-    for (int t = threadIdx.x; t < a.d; t += blockDim.x) xsm[t] = x[t];
-    __syncthreads();
+    __syncwarp();
+    for (int t = lane; t < a.d; t += 32) xs[t] = x[t];
+    __syncwarp();
     float lo = INFINITY;
-    for (int j = threadIdx.x; j < kp; j += blockDim.x) {
-      if (!(a.cn[cbeg + j] < INFINITY)) continue;
-      lo = fminf(lo, approx_value(0, xsm, a.C + (size_t)(cbeg + j) * a.ldc, a.d, 0.0f));
+    for (int j0 = 0; j0 < kp; j0 += 4) {
+      float sv[4] = {0.f, 0.f, 0.f, 0.f};
+      const float* cr[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+        cr[r] = a.C + (size_t)(cbeg + min(j0 + r, kp - 1)) * a.ldc;
+      for (int t = lane; t < a.d; t += 32) {
+        const float xt = xs[t];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const float df = xt - __ldg(cr[r] + t);
+          sv[r] = fmaf(df, df, sv[r]);
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) sv[r] += __shfl_xor_sync(0xffffffffu, sv[r], o);
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const int j = j0 + r;
+        if (j < kp) {
+          const float v = (a.cn[cbeg + j] < INFINITY) ? sv[r] : INFINITY;  // unusable center
+          lo = fminf(lo, v);
+          if (keep && lane == 0) vals[j] = v;
+        }
+      }
     }
-    for (int o = 16; o > 0; o >>= 1) lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-    if (lane == 0) rf[w] = lo;
-    __syncthreads();
-    float best_lo = rf[0];
-    for (int ww = 1; ww < nw; ++ww) best_lo = fminf(best_lo, rf[ww]);
-    const float best_hi = best_lo * (1.0f + gam) + 1e-30f;
+    __syncwarp();
+    const float best_hi = lo * (1.0f + gam) + 1e-30f;
     double best = INFINITY;
     int bidx = -1;
-    for (int j = threadIdx.x; j < kp; j += blockDim.x) {
+    for (int j = lane; j < kp; j += 32) {
       if (!(a.cn[cbeg + j] < INFINITY)) continue;
       const float* c = a.C + (size_t)(cbeg + j) * a.ldc;
-      const float v = approx_value(0, xsm, c, a.d, 0.0f);
+      const float v = keep ? vals[j] : approx_value(0, xs, c, a.d, 0.0f);
       if (!(v * (1.0f - gam) - 1e-30f <= best_hi)) continue;
-      const double ex = exact_value(0, xsm, c, a.d, 0.0f);
-      if (ex < best) {
+      const double ex = exact_value(0, xs, c, a.d, 0.0f);
+      if (ex < best) {  // a lane's centers come in increasing index order
         best = ex;
         bidx = j;
       }
@@ -472,16 +500,6 @@ rerank_grouped_kernel(RerankArgs a, GroupArgs g) {
       bidx = take ? oi : bidx;
     }
     if (lane == 0) {
-      rb[w] = best;
-      ri[w] = bidx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      for (int ww = 1; ww < nw; ++ww) {
-        const bool take = (rb[ww] < best) || (rb[ww] == best && (unsigned)ri[ww] < (unsigned)bidx);
-        best = take ? rb[ww] : best;
-        bidx = take ? ri[ww] : bidx;
-      }
       a.labels[pt] = cbeg + (bidx < 0 ? 0 : bidx);
       if (a.stats) atomicAdd(a.stats, 1ull);
     }
@@ -723,12 +741,12 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, fl
 
 cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaStream_t s) {
   if (a.n <= 0 || a.k <= 0) return cudaSuccess;
-  const size_t smem = sizeof(float) * (size_t)a.d;
+  const size_t smem = sizeof(float) * (size_t)RG_WARPS * (RG_VCAP + (size_t)a.d);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   if (smem > 48 * 1024)
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_grouped_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  rerank_grouped_kernel<<<152 * 4, 256, smem, s>>>(a, g);
+  rerank_grouped_kernel<<<152 * 4, RG_WARPS * 32, smem, s>>>(a, g);
   count_launches(1);
   return cudaGetLastError();
 }

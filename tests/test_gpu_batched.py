@@ -35,18 +35,23 @@ def make_batch(count, seed, dims=(3, 16, 32, 64, 128, 130), nmax=20_000, kmax=31
     return probs
 
 
-def test_mixed_batch_matches_oracle(km, orc, torch_cuda):
+TIERS = [0, 1, 2]  # FP32 grouped kernel, tcgen05 BF16, tcgen05 split BF16 (pair units)
+
+
+@pytest.mark.parametrize("tier", TIERS)
+def test_mixed_batch_matches_oracle(km, orc, torch_cuda, tier):
     probs = make_batch(40, 5)
-    res, st = km.lloyd_batched(probs, max_iters=6)
+    res, st = km.lloyd_batched(probs, max_iters=6, assign_tier=tier)
     for (X, k, init), r in zip(probs, res):
         ini = orc.reference_init(X, k) if init is None else init
         check(r, orc.lloyd(X, ini, 6))
     assert st.iterations == 6
 
 
-def test_per_problem_stop_rule(km, orc, torch_cuda):
+@pytest.mark.parametrize("tier", TIERS)
+def test_per_problem_stop_rule(km, orc, torch_cuda, tier):
     probs = make_batch(24, 9, dims=(8, 32), nmax=5000, kmax=20)
-    res, st = km.lloyd_batched(probs, max_iters=60, criterion=1e-4)
+    res, st = km.lloyd_batched(probs, max_iters=60, criterion=1e-4, assign_tier=tier)
     iters = set()
     for (X, k, init), r in zip(probs, res):
         ini = orc.reference_init(X, k) if init is None else init
@@ -56,8 +61,9 @@ def test_per_problem_stop_rule(km, orc, torch_cuda):
     assert len(iters) > 1  # the problems stopped at different iterations
 
 
+@pytest.mark.parametrize("tier", TIERS)
 @pytest.mark.parametrize("policy", [0, 1])
-def test_empty_clusters(km, orc, torch_cuda, policy):
+def test_empty_clusters(km, orc, torch_cuda, policy, tier):
     probs = []
     for i, d in enumerate((4, 33)):
         X, _, _ = mixture_numpy(3000, d, 6, seed=40 + i)
@@ -65,7 +71,7 @@ def test_empty_clusters(km, orc, torch_cuda, policy):
         init[5] = init[2]  # duplicate centers: one of each pair stays empty
         init[7] = 1e6      # far away: empty
         probs.append((X, 9, init))
-    res, _ = km.lloyd_batched(probs, max_iters=4, empty_policy=policy)
+    res, _ = km.lloyd_batched(probs, max_iters=4, empty_policy=policy, assign_tier=tier)
     for (X, k, init), r in zip(probs, res):
         check(r, orc.lloyd(X, init, 4, empty_policy=policy))
 
@@ -79,9 +85,10 @@ def test_matches_single_problem_calls(km, orc, torch_cuda):
         assert np.array_equal(one.centers, r.centers, equal_nan=True)
 
 
-def test_many_small_problems(km, orc, torch_cuda):
+@pytest.mark.parametrize("tier", [0, 2])
+def test_many_small_problems(km, orc, torch_cuda, tier):
     probs = make_batch(2000, 21, dims=(16, 32, 64, 128), nmax=3000, kmax=40)
-    res, st = km.lloyd_batched(probs, max_iters=3)
+    res, st = km.lloyd_batched(probs, max_iters=3, assign_tier=tier)
     rng = np.random.default_rng(0)
     for i in rng.choice(len(probs), 60, replace=False):
         X, k, init = probs[i]
@@ -89,11 +96,12 @@ def test_many_small_problems(km, orc, torch_cuda):
         check(res[i], orc.lloyd(X, ini, 3))
 
 
-def test_device_and_host_problems_mixed(km, orc, torch_cuda):
+@pytest.mark.parametrize("tier", [0, 2])
+def test_device_and_host_problems_mixed(km, orc, torch_cuda, tier):
     probs = make_batch(12, 31, dims=(5, 32), nmax=8000, kmax=30)
     mixed = [((torch_cuda.from_numpy(X).cuda() if i % 2 else X), k, init)
              for i, (X, k, init) in enumerate(probs)]
-    res, _ = km.lloyd_batched(mixed, max_iters=4)
+    res, _ = km.lloyd_batched(mixed, max_iters=4, assign_tier=tier)
     for (X, k, init), r in zip(probs, res):
         ini = orc.reference_init(X, k) if init is None else init
         check(r, orc.lloyd(X, ini, 4))
@@ -103,9 +111,11 @@ def test_rejections(km, torch_cuda):
     X, _, _ = mixture_numpy(500, 8, 4, seed=3)
     with pytest.raises(km.KmeansError):
         km.lloyd_batched([(X, 501)])  # reference init needs k <= n
+    Xw, _, _ = mixture_numpy(300, 300, 4, seed=4)
+    with pytest.raises(km.KmeansError):  # the tensor-core tiers cover D <= 256
+        km.lloyd_batched([(Xw, 4)], assign_tier=km.ASSIGN_BF16X3)
     arr = (km.kmgb_problem * 1)()
     arr[0].X, arr[0].n, arr[0].d, arr[0].k = X.ctypes.data, 500, 8, 4
-    for kw in ({"assign_tier": km.ASSIGN_BF16X3}, {"mini_batch_fraction": 0.5},
-               {"init_algorithm": km.INIT_KMEANSPP}):
+    for kw in ({"mini_batch_fraction": 0.5}, {"init_algorithm": km.INIT_KMEANSPP}):
         opt = km.default_options(**kw)
         assert km.lib().kmgb_lloyd_batched_f32(arr, 1, km.C.byref(opt), None) == 1
