@@ -4,13 +4,14 @@
 // tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker. The
 // product library (kmeans_gb300/) never links, loads or calls it.
 //
-// Parity status: the reference has no CPU path and ships no golden vectors; its GPU code
-// cannot run in the development container (no GPU) and cannot be built for the GPU host
-// (no aarch64 cross compiler). The oracle is therefore pinned to the reference's own
-// known-answer procedure (test/python/distance.py.in:75-79, arg-min of the norm expansion
-// with numpy) through the committed fixtures in tests/golden/, and otherwise follows the
-// reference source line by line as cited below ("parity unpinned" against reference
-// outputs).
+// Parity status: the reference has no CPU path and ships no golden vectors. The oracle is
+// pinned (1) to the reference's own known-answer procedure (test/python/distance.py.in:75-79,
+// arg-min of the norm expansion with numpy) and to independent restatements of its host-side
+// random streams through the committed fixtures in tests/golden/, and (2) to the reference's
+// own assignment kernels (main/cuda/ClosestCenters.cu built from its sources for the GPU and
+// launched with its grid; tests/test_gpu_reference_kernels.py): their labels equal the
+// oracle's on the test mixtures. The reference's host loop, update and SSE kernels are not run;
+// those rules follow its source line by line as cited below.
 //
 // Semantics restated here:
 //  * shuffle   : std::shuffle of row indices with std::default_random_engine(0)
