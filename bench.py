@@ -506,6 +506,9 @@ def main():
     ap.add_argument("--problems", type=int, default=10_000,
                     help="problems of the batched workload")
     ap.add_argument("--tiers", default="bf16x3,fp32", help="tiers of the large_k workload")
+    ap.add_argument("--bf16-data", action="store_true",
+                    help="the workload's points stored as BF16 values (the configuration's BF16 "
+                         "storage variant)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -536,6 +539,8 @@ def main():
 
     n, K = args.n, args.k
     X, _, _ = mixture_torch(n, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+    if args.bf16_data:
+        X = X.to(torch.bfloat16).float()
     if args.only_init:
         h = km.Handle(n, D, K, assign_tier=km.ASSIGN_FP32)
         h.set_data(X, True)
@@ -631,9 +636,11 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32" if tier == "fp32" else "bf16", "data": "synthetic",
-                "config": {"workload": "lloyd_4Mx128_K1024" if n == N else f"lloyd_{n}x128_K1024",
+                "config": {"workload": ("lloyd_4Mx128_K1024" if n == N else f"lloyd_{n}x128_K1024")
+                           + ("_bf16" if args.bf16_data else ""),
                            "n": n, "d": D, "k": K,
                            "tier": tier, "certified_labels": True,
+                           "storage": "bf16 values" if args.bf16_data else "fp32",
                            "l2": "inputs larger than L2 (X: 2.05 GB FP32 per pass)",
                            "parallelism": "replicas" if world > 1 else "single"},
                 "assign_tflops": achieved,

@@ -314,7 +314,8 @@ KMGB_EXPORT void* kmgb_stream(kmgb_handle* h); /* cudaStream_t of the handle */
 KMGB_EXPORT int kmgb_destroy(kmgb_handle* h);
 
 /* Diagnostic: raw tcgen05 accumulators x.c_j - ||c_j||^2/2 for every point and center, as the
- * BF16 (split = 0) or split BF16 (split = 1) assignment kernel computes them. X: n x d, C: k x d,
+ * BF16 (split = 0), split BF16 (split = 1) or split BF16 with BF16-valued X (split = 2: the two
+ * products x.c_hi + x.c_lo; X must hold BF16 numbers) assignment kernel computes them. X: n x d, C: k x d,
  * host row-major FP32; out: host n x k. For validating the accumulation-error model on a
  * device; allocates device memory, small problems only. */
 KMGB_EXPORT int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int k,

@@ -235,8 +235,9 @@ def kmeanspp(X, k: int, seed: int = 0):
     return cen, picks
 
 
-def tc_accumulators(X: np.ndarray, C: np.ndarray, split: bool) -> np.ndarray:
-    """Raw tcgen05 accumulators x.c_j - ||c_j||^2/2 (n x k) of the BF16 / split BF16 kernel."""
+def tc_accumulators(X: np.ndarray, C: np.ndarray, split) -> np.ndarray:
+    """Raw tcgen05 accumulators x.c_j - ||c_j||^2/2 (n x k) of the BF16 (split 0), split BF16
+    (1) or two-product split kernel for BF16-valued X (2)."""
     X = np.ascontiguousarray(X, dtype=np.float32)
     C = np.ascontiguousarray(C, dtype=np.float32)
     n, d = X.shape

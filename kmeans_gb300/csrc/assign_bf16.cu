@@ -102,17 +102,20 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
 }
 
 // Rigorous bound (in accumulator units) of |key - (x.c - ||c||^2/2)| for any usable center.
-__device__ __forceinline__ float bound_acc(float xn, float cm, int d, int planes) {
+// mode: 1 plain BF16 (x_hi.c_hi), 2 split (x_hi.c_hi + x_hi.c_lo + x_lo.c_hi), 3 split with every x
+// a BF16 number (x.c_hi + x.c_lo).
+__device__ __forceinline__ float bound_acc(float xn, float cm, int d, int mode) {
   const float u = 5.9604645e-8f;            // 2^-24, FP32 rounding
   const float ub = 1.953125e-3f;            // 2^-9, BF16 rounding
   // operand error: plain (2ub + ub^2) |x||c|; split x = xh + xl + ex, c = ch + cl + ec with
-  // |xl| <= ub|x|, |ex| <= ub^2|x|: dropping xl.cl and the residues leaves <= 3.03 ub^2 |x||c|
-  const float op = planes > 1 ? 3.03f * ub * ub : 2.0f * ub + ub * ub;
+  // |xl| <= ub|x|, |ex| <= ub^2|x|: dropping xl.cl and the residues leaves <= 3.03 ub^2 |x||c|;
+  // x exact: only x.ec is dropped, <= ub^2 |x||c| (1.01 with margin)
+  const float op = mode == 1 ? 2.0f * ub + ub * ub : (mode == 2 ? 3.03f : 1.01f) * ub * ub;
   // FP32 accumulation in TMEM (from zero): at most one rounding per 16-product MMA step,
   // modelled with margin as (terms/16 + 2) 2^-21 relative to |start| + sum |products|. The
   // measured worst case on GB300 is >= 6x below this (tests/test_gpu_tensor_numerics.py
   // enforces >= 4x on the keys, start value included).
-  const int terms = planes > 1 ? 3 * d : d;
+  const int terms = (mode == 1 ? 1 : (mode == 2 ? 3 : 2)) * d;  // products per element
   const float gacc = (float)(terms / 16 + 2) * 4.76837158e-7f;
   const float pack = 3.81469727e-6f;        // 2^-18: 5 column bits in the mantissa
   const float cc = 0.5f * cm * cm;
@@ -228,7 +231,7 @@ template <int EPQ>
 __global__ void __launch_bounds__(threads_for(EPQ), 1)
 assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmXl,
                    const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmCl,
-                   AssignArgs p, int stages, int xbufs, int planes) {
+                   AssignArgs p, int stages, int xbufs, int mode) {
   constexpr int NUM_EPI_WARPS = 4 * EPQ;
   constexpr int EPI_PER_QUAD = EPQ;
   constexpr int COLS_PER_WARP = BN / EPQ;           // columns of a chunk per epilogue warp
@@ -294,8 +297,10 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   }
   // points: [buffer][plane][k-block] 16 KB boxes; C stage: [plane] 16 KB boxes of one
   // (chunk, k-block). plane 0 = BF16 value, plane 1 = BF16 residual (split tier).
-  const size_t xbuf_bytes = (size_t)planes * nkb * XKB_BYTES;
-  const uint32_t stage_bytes = (uint32_t)planes * CKB_BYTES;
+  const int xplanes = mode == 2 ? 2 : 1;  // BF16 planes of the points
+  const int cplanes = mode >= 2 ? 2 : 1;  // and of the centers
+  const size_t xbuf_bytes = (size_t)xplanes * nkb * XKB_BYTES;
+  const uint32_t stage_bytes = (uint32_t)cplanes * CKB_BYTES;
   uint8_t* cs = smem + (size_t)xbufs * xbuf_bytes;
 
   if (tid == 0) {
@@ -318,10 +323,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     fence_mbar_init();
     prefetch_tmap(&tmX);
     prefetch_tmap(&tmC);
-    if (planes > 1) {
-      prefetch_tmap(&tmXl);
-      prefetch_tmap(&tmCl);
-    }
+    if (xplanes > 1) prefetch_tmap(&tmXl);
+    if (cplanes > 1) prefetch_tmap(&tmCl);
   }
   if (warp == 1) {  // both CTAs: one collective allocation of the pair's TMEM
     asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -356,7 +359,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         const uint32_t xb = map_to_rank(xb_local, 0);
         uint8_t* xs = smem + (size_t)xi * xbuf_bytes;
         const int xrow = (int)(p.row0 + u * UNIT + rank * BM);
-        for (int pl = 0; pl < planes; ++pl)
+        for (int pl = 0; pl < xplanes; ++pl)
           for (int kb = 0; kb < nkb; ++kb)
             tma_load_2d_pair(smem_u32(xs + (size_t)(pl * nkb + kb) * XKB_BYTES), pl ? &tmXl : &tmX,
                              xb, kb * BK, xrow);
@@ -364,7 +367,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         // load (queued behind the center stages) is an L2 hit
         if (u + npairs < n_units) {
           const int nrow = (int)(p.row0 + (u + npairs) * UNIT + rank * BM);
-          for (int pl = 0; pl < planes; ++pl)
+          for (int pl = 0; pl < xplanes; ++pl)
             for (int kb = 0; kb < nkb; ++kb) tma_prefetch_2d(pl ? &tmXl : &tmX, kb * BK, nrow);
         }
         for (int c = 0; c < ui.nch && ok; ++c) {
@@ -380,7 +383,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             const uint32_t cb_local = smem_u32(&bars.c_full[stage]);
             if (rank == 0) mbar_arrive_expect_tx(cb_local, 2 * stage_bytes);
             const uint32_t cb = map_to_rank(cb_local, 0);
-            for (int pl = 0; pl < planes; ++pl)
+            for (int pl = 0; pl < cplanes; ++pl)
               tma_load_2d_pair(smem_u32(cs + (size_t)stage * stage_bytes + pl * CKB_BYTES),
                                pl ? &tmCl : &tmC, cb, kb * BK, crow);
           }
@@ -427,14 +430,15 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               const uint32_t acc = (kb | k16) ? 1u : 0u;  // the chunk's first product starts at 0
               const uint64_t ahi = sdesc_sw128(xhi + k16 * 32);
               const uint64_t bhi = sdesc_sw128(chi + k16 * 32);
-              if (planes == 1) {
+              if (mode == 1) {
                 umma_pair(dcol, ahi, bhi, acc);
               } else {
-                // x_hi.c_hi, x_hi.c_lo (x_hi read once into the A collector), x_lo.c_hi;
-                // x_lo.c_lo is below the bound
+                // x_hi.c_hi, x_hi.c_lo (x_hi read once into the A collector), then x_lo.c_hi
+                // unless every x is a BF16 number; x_lo.c_lo is below the bound
                 umma_pair_a_fill(dcol, ahi, bhi, acc);
                 umma_pair_a_lastuse(dcol, ahi, sdesc_sw128(chi + CKB_BYTES + k16 * 32));
-                umma_pair(dcol, sdesc_sw128(xhi + (size_t)nkb * XKB_BYTES + k16 * 32), bhi, 1u);
+                if (mode == 2)
+                  umma_pair(dcol, sdesc_sw128(xhi + (size_t)nkb * XKB_BYTES + k16 * 32), bhi, 1u);
               }
             }
             umma_commit_pair(smem_u32(&bars.c_empty[stage]));
@@ -609,7 +613,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             (bblk < 0 || none) ? ui.cbase : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
         p.labels[pt] = label;
         if (p.certify) {
-          const float eb = bound_acc(xn_pt, cm, p.d, planes);
+          const float eb = bound_acc(xn_pt, cm, p.d, mode);
           if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
             p.rerank_list[slot] = (int)pt;
@@ -704,17 +708,18 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
                                const void* Cl, long long ldcb, const AssignArgs& a,
                                cudaStream_t s) {
   if (a.n <= 0 || a.k <= 0 || a.d <= 0) return cudaSuccess;
-  const int planes = (Xl && Cl) ? 2 : 1;
+  const int planes = (Xl && Cl) ? 2 : 1;  // planes of the split tier's point buffer
+  const int mode = Cl ? (Xl ? 2 : 3) : 1;  // see bound_acc
   if (!bf16_tc_supported(a.d, planes) || (ldxb % 8) || (ldcb % 8) ||
       (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15) ||
       (reinterpret_cast<uintptr_t>(Xl) & 15) || (reinterpret_cast<uintptr_t>(Cl) & 15))
     return cudaErrorInvalidValue;
-  const int epq = epq_for(planes);
+  const int epq = epq_for(mode > 1 ? 2 : 1);
   VariantInfo& vi = g_variant[epq];
   if (epq == 2) KMGB_CUDA_TRY(prepare_variant<2>(vi));
   else KMGB_CUDA_TRY(prepare_variant<4>(vi));
-  const size_t xbytes = xbuf_bytes_for(a.d, planes);
-  const size_t stage_bytes = (size_t)planes * CKB_BYTES;
+  const size_t xbytes = xbuf_bytes_for(a.d, mode == 2 ? 2 : 1);
+  const size_t stage_bytes = (size_t)(mode > 1 ? 2 : 1) * CKB_BYTES;
   const size_t lim = vi.smem_budget;
   // double-buffer the unit's points when that still leaves a 3-stage ring (a single buffer
   // measured no slower on GB300: the next unit's points are prefetched into L2)
@@ -730,12 +735,12 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
                                   (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BNH));
   tmXl = tmX;
   tmCl = tmC;
-  if (planes > 1) {
+  if (mode == 2)
     KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmXl, Xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                                     (uint64_t)a.d, (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
+  if (mode > 1)
     KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmCl, Cl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                                     (uint64_t)a.d, (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BNH));
-  }
   const long long n_units = (a.n + UNIT - 1) / UNIT;
   const long long pairs = n_units < vi.max_pairs ? n_units : vi.max_pairs;
   if (pairs <= 0) return cudaSuccess;
@@ -753,10 +758,10 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   cfg.numAttrs = 1;
   if (epq == 2)
     KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2>, tmX, tmXl, tmC, tmCl, a, stages,
-                                     xbufs, planes));
+                                     xbufs, mode));
   else
     KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4>, tmX, tmXl, tmC, tmCl, a, stages,
-                                     xbufs, planes));
+                                     xbufs, mode));
   count_launches(1);
   return cudaSuccess;
 }

@@ -336,8 +336,19 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
             KMEANS_ERROR_INITIALIZE, "initial centers"))
     return f.code;
   if (f.set(launch_point_norms(X, ldx, rows, d, qn, xn, s), E, "norms")) return f.code;
-  if (tc && f.set(launch_to_bf16(X, ldx, rows, d, Xb, ldb, s, nullptr, Xl), E, "BF16 data"))
-    return f.code;
+  if (tc) {
+    // every x a BF16 number: the split tier drops the residual plane's product
+    int* inexact = nullptr;
+    int host_inexact = 1;
+    if (f.set(m.alloc(&inexact, 1), E, "BF16 data") ||
+        f.set(cudaMemsetAsync(inexact, 0, sizeof(int), s), E, "BF16 data") ||
+        f.set(launch_to_bf16(X, ldx, rows, d, Xb, ldb, s, nullptr, Xl, inexact), E, "BF16 data") ||
+        f.set(cudaMemcpyAsync(&host_inexact, inexact, sizeof(int), cudaMemcpyDeviceToHost, s), E,
+              "BF16 data") ||
+        f.set(cudaStreamSynchronize(s), E, "BF16 data"))
+      return f.code;
+    if (split && host_inexact == 0) Xl = nullptr;
+  }
 
   // problem tables
   GroupArgs g{};

@@ -193,6 +193,8 @@ struct kmgb_handle {
   unsigned long long* rr_stats = nullptr;
   int* err = nullptr;
   void* arena = nullptr;  // one device allocation holding every fixed buffer of the handle
+  int* xinexact = nullptr;  // set by the BF16 conversion when some x is not a BF16 number
+  bool x_exact = false;     // split tier: every x is a BF16 number -> two products, no x_lo
   // k-means++ work space (allocated on first use): D^2, block weight sums, max/pick, picks
   float* kpp_d2 = nullptr;
   unsigned long long* kpp_blk = nullptr;
@@ -377,6 +379,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     a.take(&h->stop, 1);
     a.take(&h->loopf, 2);
     a.take(&h->iters_done, 1);
+    a.take(&h->xinexact, 1);
     a.take(&w.hist, hist_elems);
     a.take(&w.scan_tmp, update_scan_tmp_elems(std::max<long long>(hist_elems, k + 1)));
     a.take(&w.label_off, k + 1);
@@ -457,9 +460,26 @@ int set_data(kmgb_handle* h, const float* X, bool on_device) {
            code);
   }
   KM_TRY(launch_point_norms(h->X, h->ldx, h->n, h->d, h->qn, h->xn, h->stream), code);
-  if (h->Xb)
-    KM_TRY(launch_to_bf16(h->X, h->ldx, h->n, h->d, h->Xb, h->ldb, h->stream, nullptr, h->Xl),
+  if (h->gexec) {  // a captured iteration bakes in the planes it reads: capture again
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  h->x_exact = false;
+  if (h->Xb) {
+    KM_TRY(cudaMemsetAsync(h->xinexact, 0, sizeof(int), h->stream), code);
+    KM_TRY(launch_to_bf16(h->X, h->ldx, h->n, h->d, h->Xb, h->ldb, h->stream, nullptr, h->Xl,
+                          h->xinexact),
            code);
+    if (h->Xl) {
+      // every x a BF16 number: the residual plane is zero and the split tier drops its product
+      int inexact = 1;
+      KM_TRY(cudaMemcpyAsync(&inexact, h->xinexact, sizeof(int), cudaMemcpyDeviceToHost,
+                             h->stream),
+             code);
+      KM_TRY(cudaStreamSynchronize(h->stream), code);
+      h->x_exact = inexact == 0;
+    }
+  }
   if (h->mini) {
     std::vector<int> perm;
     reference_perm((int)h->n, perm);
@@ -489,7 +509,7 @@ int step(kmgb_handle* h, int slot) {
   cudaStream_t s = h->stream;
   const float* Xa = h->X;
   const void* Xba = h->Xb;
-  const void* Xla = h->Xl;
+  const void* Xla = h->x_exact ? nullptr : h->Xl;
   const double* qna = h->qn;
   const float* xna = h->xn;
   if (h->mini) {
@@ -505,7 +525,7 @@ int step(kmgb_handle* h, int slot) {
              KMEANS_ERROR_CONSTRUCT_MINIBATCH);
     Xa = h->Xw;
     Xba = h->Xbw;
-    Xla = h->Xlw;
+    Xla = h->x_exact ? nullptr : h->Xlw;
     qna = h->qnw;
     xna = h->xnw;
   }
@@ -1278,7 +1298,8 @@ int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int
     if (cudaMemsetAsync(h->cmax, 0, sizeof(float), s) != cudaSuccess ||
         launch_prep_centers(h->C, h->ldx, k, d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s, nullptr,
                             h->cinit, h->Cl) != cudaSuccess ||
-        launch_assign_bf16(h->Xb, h->Xl, h->ldb, h->Cb, h->Cl, h->ldb, a, s) != cudaSuccess ||
+        launch_assign_bf16(h->Xb, split == 2 ? nullptr : h->Xl, h->ldb, h->Cb, h->Cl, h->ldb, a,
+                           s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
       rc = KMEANS_ERROR_CLOSEST_CENTERS;
   }

@@ -66,7 +66,8 @@ float assign_fp32_gamma(int d);
 
 // tcgen05 BF16 assignment. Xb: [n][ldb] BF16, Cb: [k][ldb] BF16, ldb a multiple of 8. With the
 // residual planes Xl / Cl (x - bf16(x), same layout; both nullable) the split tier computes
-// x_hi.c_hi + x_hi.c_lo + x_lo.c_hi.
+// x_hi.c_hi + x_hi.c_lo + x_lo.c_hi; with Cl but no Xl (every x a BF16 number) it computes
+// x.c_hi + x.c_lo, two products with the bound of an exact x.
 cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, const void* Cb,
                                const void* Cl, long long ldcb, const AssignArgs& a,
                                cudaStream_t s);
@@ -131,10 +132,11 @@ cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, flo
 cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,
                                float* xn, cudaStream_t s);
 // BF16 copy of the data set (zero padded to ldb columns).
-// Xl (nullable) receives the residual plane bf16(x - bf16(x)).
+// Xl (nullable) receives the residual plane bf16(x - bf16(x)); inexact (nullable, zeroed by the
+// caller) is set to 1 when some value is not a BF16 number.
 cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
                            long long ldb, cudaStream_t s, const int* stop = nullptr,
-                           void* Xl = nullptr);
+                           void* Xl = nullptr, int* inexact = nullptr);
 
 // Deterministic update: stable counting sort by label, FP64 piece sums, finalize.
 struct UpdateWork {

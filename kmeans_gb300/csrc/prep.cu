@@ -119,13 +119,16 @@ __global__ void point_norms_kernel(const float* __restrict__ X, long long ldx, l
 
 // One warp per row (grid-stride over rows): BF16 value plane and, when requested, the BF16
 // residual plane bf16(x - bf16(x)).
+// inexact (nullable): set to 1 when some value of X is not a BF16 number (v != bf16(v); NaN
+// included), i.e. when the residual plane carries information.
 __global__ void to_bf16_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
                                __nv_bfloat16* __restrict__ Xb, long long ldb, const int* stop,
-                               __nv_bfloat16* __restrict__ Xl) {
+                               __nv_bfloat16* __restrict__ Xl, int* inexact) {
   if (stopped(stop)) return;
   const int lane = threadIdx.x & 31;
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  bool off = false;
   for (long long r = w0; r < n; r += nw) {
     const float* x = X + (size_t)r * ldx;
     __nv_bfloat16* ob = Xb + (size_t)r * ldb;
@@ -134,9 +137,11 @@ __global__ void to_bf16_kernel(const float* __restrict__ X, long long ldx, long 
       const float v = c < d ? __ldg(x + c) : 0.0f;
       const __nv_bfloat16 hi = __float2bfloat16_rn(v);
       ob[c] = hi;
+      off |= !(v == __bfloat162float(hi));
       if (ol) ol[c] = __float2bfloat16_rn(v - __bfloat162float(hi));
     }
   }
+  if (inexact && __any_sync(0xffffffffu, off) && lane == 0) atomicExch(inexact, 1);
 }
 
 __global__ void gather_rows_kernel(const float* __restrict__ Xs, long long ldx,
@@ -195,10 +200,12 @@ cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d
 }
 
 cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
-                           long long ldb, cudaStream_t s, const int* stop, void* Xl) {
+                           long long ldb, cudaStream_t s, const int* stop, void* Xl,
+                           int* inexact) {
   if (n <= 0) return cudaSuccess;
   to_bf16_kernel<<<152 * 16, 256, 0, s>>>(X, ldx, n, d, reinterpret_cast<__nv_bfloat16*>(Xb),
-                                          ldb, stop, reinterpret_cast<__nv_bfloat16*>(Xl)); kmgb::count_launches(1);
+                                          ldb, stop, reinterpret_cast<__nv_bfloat16*>(Xl),
+                                          inexact); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

@@ -42,6 +42,18 @@ def test_odd_shapes(km, orc, torch_cuda, n, d, k, tier):
     check_same(res, orc.lloyd(X, init, 6))
 
 
+@pytest.mark.parametrize("n,d,k", [(20000, 128, 256), (3001, 17, 40), (50000, 256, 300)])
+def test_bf16_valued_data_two_product_mode(km, orc, torch_cuda, n, d, k):
+    # every x a BF16 number: the split tier drops the x_lo product (its residual plane is zero)
+    # and certifies with the exact-x bound; labels and centers stay those of the oracle
+    X, _, _ = mixture_numpy(n, d, k, seed=n + d)
+    X = torch_cuda.from_numpy(X).to(torch_cuda.bfloat16).float().numpy()
+    init = X[sample_init(n, k, seed=4)]
+    for tier in (1, 2):
+        res = km.lloyd(X, k, init=init, max_iters=5, assign_tier=tier)
+        check_same(res, orc.lloyd(X, init, 5))
+
+
 @pytest.mark.parametrize("tier", TIERS)
 def test_near_ties_are_resolved_exactly(km, orc, torch_cuda, tier):
     # points placed on (or within a few ulps of) the bisector of two centers

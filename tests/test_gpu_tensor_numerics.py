@@ -31,15 +31,22 @@ def cases():
     yield "d256", X4, C4.astype(np.float32)
 
 
-@pytest.mark.parametrize("use_split", [False, True])
+@pytest.mark.parametrize("use_split", [0, 1, 2])
 def test_tc_accumulation_error_model(km, torch_cuda, use_split):
     f = lambda a: a.astype(np.float64)
     for name, X, C in cases():
         d = X.shape[1]
+        if use_split == 2:  # the two-product mode takes BF16-valued points
+            X = bf16(X).astype(np.float32)
         acc = km.tc_accumulators(X, C, use_split).astype(np.float64)
         cn = (f(C) ** 2).sum(1).astype(np.float32)  # ||c||^2 rounded once to FP32
         start = -0.5 * f(cn)
-        if use_split:
+        if use_split == 2:
+            ch, cl = split(C)
+            prod = f(X) @ f(ch).T + f(X) @ f(cl).T
+            mag = np.abs(f(X)) @ np.abs(f(ch)).T + np.abs(f(X)) @ np.abs(f(cl)).T
+            terms = 2 * d
+        elif use_split:
             xh, xl = split(X)
             ch, cl = split(C)
             prod = f(xh) @ f(ch).T + f(xh) @ f(cl).T + f(xl) @ f(ch).T
