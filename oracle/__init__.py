@@ -64,7 +64,8 @@ def build_ref() -> bool:
        pre-Volta shuffles). Device code does not depend on the host architecture, so the cubin
        built here runs on the Arm GPU host.
     2. Wherever a CUDA toolkit is present, compile ref_kernels.cpp, the loader that plays the
-       reference's host side (the reference's own host code cannot be built for the GPU host).
+       reference's host side (the reference's own host driver needs a CMake-generated config.h
+       and cuBLAS, so it is not built here).
 
     Returns True when both the cubin and the loader exist.
     """

@@ -3,7 +3,8 @@
 // The reference's ClosestCenters.cu (main/cuda/ClosestCenters.cu) is compiled from its sources
 // into a cubin for sm_103a (oracle/__init__.py build_ref(), with oracle/ref_shfl_shim.h
 // force-included); its
-// host code needs an x86 build that cannot run on the Arm GPU host, so this loader takes the host
+// host driver (main/cpp/kmeans.cpp) needs a CMake-generated config.h and cuBLAS and is not built
+// here, so this loader takes the host
 // side's place: it loads the cubin with the CUDA driver API, finds the kernel instantiations the
 // reference's float entry uses (`_dev_ClosestCentersBegin<float, float4, DELTA, 4>`, DELTA =
 // 1..16, and `_dev_ClosestCentersEndNew<float>`), sets the reference's __constant__ shape
