@@ -17,8 +17,8 @@ region; `tensor_*` counts the tensor-core products the tier actually issues, thr
 in the split tier; `traffic` is the DRAM bytes of one launch from an ncu capture, scaled to N);
 `cpu_baseline` is the CPU restatement (oracle FP32 port, all host threads) on a sample.
 The reference arm (--impl reference) times that CPU path: the reference has no CPU
-implementation of its own and its host driver is not built here (it needs a CMake-generated
-config.h and cuBLAS). Its line also
+implementation of its own and its host code is not built (its sources are only in the x86
+development container; its driver also needs a CMake-generated config.h and cuBLAS). Its line also
 carries `reference_gpu`: the reference's own assignment kernels (compiled from its sources into
 oracle/_ref, launched as its ClosestCentersF does) timed on the same workload.
 """

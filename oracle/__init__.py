@@ -64,8 +64,8 @@ def build_ref() -> bool:
        pre-Volta shuffles). Device code does not depend on the host architecture, so the cubin
        built here runs on the Arm GPU host.
     2. Wherever a CUDA toolkit is present, compile ref_kernels.cpp, the loader that plays the
-       reference's host side (the reference's own host driver needs a CMake-generated config.h
-       and cuBLAS, so it is not built here).
+       reference's host side (host code built from the reference's sources, which exist only in
+       the x86 development container, could not run on the Arm GPU host).
 
     Returns True when both the cubin and the loader exist.
     """

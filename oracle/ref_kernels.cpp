@@ -2,10 +2,10 @@
 //
 // The reference's ClosestCenters.cu (main/cuda/ClosestCenters.cu) is compiled from its sources
 // into a cubin for sm_103a (oracle/__init__.py build_ref(), with oracle/ref_shfl_shim.h
-// force-included); its
-// host driver (main/cpp/kmeans.cpp) needs a CMake-generated config.h and cuBLAS and is not built
-// here, so this loader takes the host
-// side's place: it loads the cubin with the CUDA driver API, finds the kernel instantiations the
+// force-included). The reference's sources exist only in the development container, whose host
+// binaries are x86 and cannot run on the Arm GPU host (and its host driver, main/cpp/kmeans.cpp,
+// also needs a CMake-generated config.h and cuBLAS), so device code travels as a cubin and this
+// loader, built on the GPU host from this repository, takes the host side's place: it loads the cubin with the CUDA driver API, finds the kernel instantiations the
 // reference's float entry uses (`_dev_ClosestCentersBegin<float, float4, DELTA, 4>`, DELTA =
 // 1..16, and `_dev_ClosestCentersEndNew<float>`), sets the reference's __constant__ shape
 // variables and launches them with the reference's grid (ClosestCenters.cu:181-231, 312-315:
