@@ -41,6 +41,8 @@ def build(force: bool = False) -> str:
 
 _REF = os.path.join(_HERE, "_ref")
 _REF_CUBIN = os.path.join(_REF, "closest_centers.cubin")
+_REF_CC_CUBIN = os.path.join(_REF, "cluster_centers.cubin")
+_REF_CP_CUBIN = os.path.join(_REF, "compactness.cubin")
 _REF_SO = os.path.join(_REF, "libref_kernels.so")
 _REF_LOADER_SRC = os.path.join(_HERE, "ref_kernels.cpp")
 _REF_SHIM = os.path.join(_HERE, "ref_shfl_shim.h")
@@ -59,10 +61,10 @@ def _cuda_home() -> str:
 def build_ref() -> bool:
     """Recipe for oracle/_ref (git-ignored, test infrastructure).
 
-    1. Where the reference's sources are present, compile its main/cuda/ClosestCenters.cu, as it
-       lies, into a cubin for sm_103a with ref_shfl_shim.h force-included (the reference's
-       pre-Volta shuffles). Device code does not depend on the host architecture, so the cubin
-       built here runs on the Arm GPU host.
+    1. Where the reference's sources are present, compile its main/cuda/ClosestCenters.cu,
+       ClusterCenters.cu and Compactness.cu, as they lie, into cubins for sm_103a with
+       ref_shfl_shim.h force-included (the reference's pre-Volta shuffles). Device code does not
+       depend on the host architecture, so the cubins built here run on the Arm GPU host.
     2. Wherever a CUDA toolkit is present, compile ref_kernels.cpp, the loader that plays the
        reference's host side (host code built from the reference's sources, which exist only in
        the x86 development container, could not run on the Arm GPU host).
@@ -71,13 +73,15 @@ def build_ref() -> bool:
     """
     os.makedirs(_REF, exist_ok=True)
     cuda = _cuda_home()
-    src = os.path.join(_REFERENCE_CUDA_DIR, "ClosestCenters.cu")
-    if os.path.exists(src) and not os.path.exists(_REF_CUBIN):
-        nvcc = os.path.join(cuda, "bin", "nvcc")
-        subprocess.check_call([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
-                               "-w", "-include", _REF_SHIM, "-I", _REFERENCE_CUDA_DIR, src, "-o",
-                               _REF_CUBIN + ".tmp"])
-        os.replace(_REF_CUBIN + ".tmp", _REF_CUBIN)
+    nvcc = os.path.join(cuda, "bin", "nvcc")
+    for name, out in (("ClosestCenters.cu", _REF_CUBIN), ("ClusterCenters.cu", _REF_CC_CUBIN),
+                      ("Compactness.cu", _REF_CP_CUBIN)):
+        src = os.path.join(_REFERENCE_CUDA_DIR, name)
+        if os.path.exists(src) and not os.path.exists(out):
+            subprocess.check_call([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a",
+                                   "-O3", "-w", "-include", _REF_SHIM, "-I", _REFERENCE_CUDA_DIR,
+                                   src, "-o", out + ".tmp"])
+            os.replace(out + ".tmp", out)
     if os.path.isdir(os.path.join(cuda, "include")) and (
             not os.path.exists(_REF_SO)
             or os.path.getmtime(_REF_SO) < os.path.getmtime(_REF_LOADER_SRC)):
@@ -93,7 +97,9 @@ _ref_lib = None
 
 
 def ref_kernels():
-    """The reference's assignment kernels (cubin + loader), or None when oracle/_ref is absent."""
+    """The reference's assignment kernels (cubin + loader), or None when oracle/_ref is absent.
+    When its center and compactness cubins are present too, `has_update` is True and
+    refk_cluster_centers_f / refk_compactness_f are bound."""
     global _ref_lib
     with _lock:
         if _ref_lib is not None:
@@ -112,6 +118,19 @@ def ref_kernels():
         if found != 17:
             raise RuntimeError(f"reference cubin: found {found} of 17 kernels "
                                f"({L.refk_last_error().decode()})")
+        L.has_update = False
+        if os.path.exists(_REF_CC_CUBIN) and os.path.exists(_REF_CP_CUBIN):
+            L.refk_load_update.argtypes = [C.c_char_p, C.c_char_p]
+            L.refk_load_update.restype = C.c_int
+            L.refk_cluster_centers_f.argtypes = [C.c_int, C.c_int, C.c_int, P, P, P, P, P, P]
+            L.refk_cluster_centers_f.restype = C.c_int
+            L.refk_compactness_f.argtypes = [C.c_int, C.c_int, C.c_int, P, P, P, P]
+            L.refk_compactness_f.restype = C.c_int
+            got = L.refk_load_update(_REF_CC_CUBIN.encode(), _REF_CP_CUBIN.encode())
+            if got != 4:
+                raise RuntimeError(f"reference update cubins: found {got} of 4 kernels "
+                                   f"({L.refk_last_error().decode()})")
+            L.has_update = True
         _ref_lib = L
         return L
 

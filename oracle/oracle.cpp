@@ -8,10 +8,12 @@
 // pinned (1) to the reference's own known-answer procedure (test/python/distance.py.in:75-79,
 // arg-min of the norm expansion with numpy) and to independent restatements of its host-side
 // random streams through the committed fixtures in tests/golden/, and (2) to the reference's
-// own assignment kernels (main/cuda/ClosestCenters.cu built from its sources for the GPU and
-// launched with its grid; tests/test_gpu_reference_kernels.py): their labels equal the
-// oracle's on the test mixtures. The reference's host loop, update and SSE kernels are not run;
-// those rules follow its source line by line as cited below.
+// own kernels (main/cuda/ClosestCenters.cu, ClusterCenters.cu and Compactness.cu built from its
+// sources for the GPU and launched with its grids; tests/test_gpu_reference_kernels.py): their
+// labels equal the oracle's on the test mixtures, their centers are within the FP32 error bound
+// of the oracle's exact means (NaN for empty clusters in both) and their compactness within
+// the FP32 bound of the oracle's SSE. The reference's host loop is not run; its rules follow
+// its source line by line as cited below.
 //
 // Semantics restated here:
 //  * shuffle   : std::shuffle of row indices with std::default_random_engine(0)

@@ -1,4 +1,5 @@
-// Test infrastructure: runs the REFERENCE's own assignment kernels on the GPU.
+// Test infrastructure: runs the REFERENCE's own assignment, center and compactness kernels on
+// the GPU.
 //
 // The reference's ClosestCenters.cu (main/cuda/ClosestCenters.cu) is compiled from its sources
 // into a cubin for sm_103a (oracle/__init__.py build_ref(), with oracle/ref_shfl_shim.h
@@ -40,6 +41,10 @@ PFN_cuMemcpyHtoD_v3020 p_htod = nullptr;
 CUmodule g_mod = nullptr;
 CUfunction g_begin[17] = {};
 CUfunction g_end = nullptr;
+// ClusterCenters.cu / Compactness.cu: _dev_ClusterCentersBegin/End<float>,
+// _dev_Compactness/_dev_CompactnessEnd<float, 128>
+CUmodule g_mod_cc = nullptr, g_mod_cp = nullptr;
+CUfunction g_cc_begin = nullptr, g_cc_end = nullptr, g_cp = nullptr, g_cp_end = nullptr;
 char g_err[512] = "";
 
 template <typename F>
@@ -67,6 +72,50 @@ int set_const(const char* name, int value) {
     return -1;
   }
   return 0;
+}
+
+std::string demangled(CUfunction f) {
+  const char* mangled = nullptr;
+  if (p_name(&mangled, f) != CUDA_SUCCESS || !mangled) return std::string();
+  int st = 0;
+  char* dem = abi::__cxa_demangle(mangled, nullptr, nullptr, &st);
+  const std::string s = (st == 0 && dem) ? std::string(dem) : std::string(mangled);
+  std::free(dem);
+  return s;
+}
+
+// Loads a cubin and returns the functions whose demangled names start with the given prefixes.
+int load_named(const char* path, CUmodule* mod, const char* const* prefixes, CUfunction* out,
+               int count) {
+  if (p_load(mod, path) != CUDA_SUCCESS) {
+    std::snprintf(g_err, sizeof(g_err), "cuModuleLoad(%s) failed", path);
+    return -1;
+  }
+  unsigned int n = 0;
+  if (p_count(&n, *mod) != CUDA_SUCCESS || n == 0 || n > 4096) return -1;
+  CUfunction* fs = static_cast<CUfunction*>(std::calloc(n, sizeof(CUfunction)));
+  if (!fs || p_enum(fs, n, *mod) != CUDA_SUCCESS) {
+    std::free(fs);
+    return -1;
+  }
+  int found = 0;
+  for (unsigned int i = 0; i < n; ++i) {
+    const std::string name = demangled(fs[i]);
+    for (int j = 0; j < count; ++j)
+      if (!out[j] && name.compare(0, std::strlen(prefixes[j]), prefixes[j]) == 0) {
+        out[j] = fs[i];
+        ++found;
+      }
+  }
+  std::free(fs);
+  return found;
+}
+
+int num_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms;
 }
 
 }  // namespace
@@ -106,12 +155,7 @@ int refk_load(const char* cubin_path) {
   const std::string begin_prefix = "void _dev_ClosestCentersBegin<float, float4, ";
   const std::string end_prefix = "void _dev_ClosestCentersEndNew<float>(";
   for (unsigned int i = 0; i < n; ++i) {
-    const char* mangled = nullptr;
-    if (p_name(&mangled, fs[i]) != CUDA_SUCCESS || !mangled) continue;
-    int st = 0;
-    char* dem = abi::__cxa_demangle(mangled, nullptr, nullptr, &st);
-    const std::string s = (st == 0 && dem) ? std::string(dem) : std::string(mangled);
-    std::free(dem);
+    const std::string s = demangled(fs[i]);
     if (s.compare(0, begin_prefix.size(), begin_prefix) == 0) {
       int delta = 0, unroll = 0;
       if (std::sscanf(s.c_str() + begin_prefix.size(), "%d, %d>", &delta, &unroll) == 2 &&
@@ -176,6 +220,70 @@ int refk_closest_centers_f(int m0, int n, int d, const float* A, int k, const fl
     std::snprintf(g_err, sizeof(g_err), "launch of the reference's ClosestCentersEndNew failed");
     return -1;
   }
+  return 0;
+}
+
+// Loads the reference's ClusterCenters.cu and Compactness.cu cubins (after refk_load). Returns
+// the number of kernels found (4 expected) or -1.
+int refk_load_update(const char* cluster_cubin, const char* compact_cubin) {
+  if (!p_load) {
+    std::snprintf(g_err, sizeof(g_err), "refk_load first");
+    return -1;
+  }
+  const char* cc_names[2] = {"void _dev_ClusterCentersBegin<float>(",
+                             "void _dev_ClusterCentersEnd<float>("};
+  CUfunction cc[2] = {nullptr, nullptr};
+  const char* cp_names[2] = {"void _dev_Compactness<float, 128>(",
+                             "void _dev_CompactnessEnd<float, 128>("};
+  CUfunction cp[2] = {nullptr, nullptr};
+  const int a = load_named(cluster_cubin, &g_mod_cc, cc_names, cc, 2);
+  const int b = load_named(compact_cubin, &g_mod_cp, cp_names, cp, 2);
+  if (a < 0 || b < 0) return -1;
+  g_cc_begin = cc[0];
+  g_cc_end = cc[1];
+  g_cp = cp[0];
+  g_cp_end = cp[1];
+  return a + b;
+}
+
+// The reference's ClusterCentersF over one tile holding all m rows (lastTile; ClusterCenters.cu:
+// 101-133): 128-thread blocks, SMs*8 of them accumulate FP32 partial sums and counts per block
+// into centers_large (p x k x n) and counts_large (p x k), which the caller zeroes; then one
+// block per center adds the p partials and divides (0/0 = NaN for an empty cluster).
+int refk_cluster_centers_f(int m, int n, int k, const float* data, const int* labels,
+                           float* centers_large, int* counts_large, float* centers, int* counts) {
+  if (!g_cc_begin || !g_cc_end) {
+    std::snprintf(g_err, sizeof(g_err), "update cubins not loaded");
+    return -1;
+  }
+  int m0 = 0;
+  int p = num_sms() * 8;
+  void* a1[] = {&m0, &m, &n, &k, &data, &labels, &centers_large, &counts_large};
+  if (p_launch(g_cc_begin, (unsigned)p, 1, 1, 128, 1, 1, 0, nullptr, a1, nullptr) != CUDA_SUCCESS)
+    return -1;
+  void* a2[] = {&p, &n, &k, &centers_large, &counts_large, &centers, &counts};
+  const unsigned shm = (unsigned)(n * sizeof(float) + sizeof(int));
+  if (p_launch(g_cc_end, (unsigned)k, 1, 1, 128, 1, 1, shm, nullptr, a2, nullptr) != CUDA_SUCCESS)
+    return -1;
+  return 0;
+}
+
+// The reference's CompactnessF over one tile (Compactness.cu:70-96): SMs*8 blocks of 128
+// threads add sum_d (x_d - c_label,d)^2 of their rows into compactness[block] (FP32; the caller
+// zeroes p entries), then one block sums the p partials into compactness[0].
+int refk_compactness_f(int m, int n, int k, const float* data, const int* labels,
+                       const float* centers, float* compactness) {
+  if (!g_cp || !g_cp_end) {
+    std::snprintf(g_err, sizeof(g_err), "update cubins not loaded");
+    return -1;
+  }
+  int m0 = 0;
+  int p = num_sms() * 8;
+  void* a1[] = {&m0, &m, &n, &k, &data, &labels, &centers, &compactness};
+  if (p_launch(g_cp, (unsigned)p, 1, 1, 128, 1, 1, 0, nullptr, a1, nullptr) != CUDA_SUCCESS)
+    return -1;
+  void* a2[] = {&p, &compactness};
+  if (p_launch(g_cp_end, 1, 1, 1, 128, 1, 1, 0, nullptr, a2, nullptr) != CUDA_SUCCESS) return -1;
   return 0;
 }
 

@@ -126,3 +126,99 @@ def test_reference_kernels_time_on_the_4m_workload(ref, torch_cuda, km):
     tflops = 2.0 * n * k * d / (ms / 1000.0) / 1e12
     print(f"reference ClosestCentersF (FP32 SIMT, its own kernels) on 4M x 128, K=1024: "
           f"{ms:.2f} ms per assignment = {tflops:.1f} TFLOP/s")
+
+
+# --- the reference's center and compactness kernels (ClusterCenters.cu, Compactness.cu) ---------
+
+def ref_blocks(torch):
+    """getMaxConcurrentBlocks() of the reference (KmeansCudaKernels.h:138-149): SMs x 8."""
+    return torch.cuda.get_device_properties(0).multi_processor_count * 8
+
+
+def run_ref_update(ref, torch, X, labels, k, centers_for_sse):
+    if not getattr(ref, "has_update", False):
+        pytest.skip("the reference's ClusterCenters/Compactness cubins not built")
+    n, d = X.shape
+    p = ref_blocks(torch)
+    dev = torch.device("cuda")
+    Xd = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32)).to(dev)
+    Ld = torch.from_numpy(np.ascontiguousarray(labels, dtype=np.int32)).to(dev)
+    cl = torch.zeros(p * k * d, dtype=torch.float32, device=dev)
+    nl = torch.zeros(p * k, dtype=torch.int32, device=dev)
+    cen = torch.empty((k, d), dtype=torch.float32, device=dev)
+    cnt = torch.empty(k, dtype=torch.int32, device=dev)
+    rc = ref.refk_cluster_centers_f(n, d, k, Xd.data_ptr(), Ld.data_ptr(), cl.data_ptr(),
+                                    nl.data_ptr(), cen.data_ptr(), cnt.data_ptr())
+    assert rc == 0, ref.refk_last_error()
+    Cs = torch.from_numpy(np.ascontiguousarray(centers_for_sse, dtype=np.float32)).to(dev)
+    comp = torch.zeros(p, dtype=torch.float32, device=dev)
+    rc = ref.refk_compactness_f(n, d, k, Xd.data_ptr(), Ld.data_ptr(), Cs.data_ptr(),
+                                comp.data_ptr())
+    assert rc == 0, ref.refk_last_error()
+    torch.cuda.synchronize()
+    return cen.cpu().numpy(), cnt.cpu().numpy(), float(comp[0].item()), p
+
+
+def emulate_reference_centers(X, labels, k, p):
+    """The reference's FP32 summation order for the centers (ClusterCenters.cu:3-23, 47-87):
+    block b adds rows b, b+p, b+2p, ... into its own partial sums (one row per block per round);
+    one block per center then adds the p partials in block order and divides (0/0 = NaN)."""
+    n, d = X.shape
+    part = np.zeros((p, k, d), dtype=np.float32)
+    for r0 in range(0, n, p):
+        rows = np.arange(r0, min(n, r0 + p))
+        part[rows - r0, labels[rows]] += X[rows]
+    total = np.zeros((k, d), dtype=np.float32)
+    for b in range(p):
+        total += part[b]
+    counts = np.bincount(labels, minlength=k).astype(np.int32)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        centers = total / counts[:, None].astype(np.float32)
+    return centers, counts
+
+
+@pytest.mark.parametrize("n,d,k", [(20000, 32, 64), (12000, 130, 16), (9000, 7, 100)])
+def test_reference_center_and_compactness_kernels_agree_with_the_oracle(ref, torch_cuda, n, d,
+                                                                        k):
+    X, _, _ = mixture_numpy(n, d, k, seed=3 * n + d)
+    X = X.astype(np.float32)
+    init = X[sample_init(n, k, seed=5)].astype(np.float32)
+    init[[1, k - 2]] = 1e4  # two centers no point is closest to: empty clusters
+    labels = oracle.assign(X, init)
+    assert not np.isin(labels, [1, k - 2]).any()
+    newc, cnt_orc, sums = oracle.update(X, labels, k, old_centers=init)
+    cen_ref, cnt_ref, sse_ref, p = run_ref_update(ref, torch_cuda, X, labels, k, newc)
+
+    # the loader runs the reference's kernels in the reference's own summation order
+    cen_emu, cnt_emu = emulate_reference_centers(X, labels, k, p)
+    assert np.array_equal(cnt_ref, cnt_emu)
+    assert np.array_equal(cen_ref, cen_emu, equal_nan=True)
+
+    # counts are exact; empty clusters come out as 0/0 = NaN in the reference
+    assert np.array_equal(cnt_ref, cnt_orc.astype(np.int32))
+    empty = cnt_orc == 0
+    assert empty[[1, k - 2]].all()
+    assert np.isnan(cen_ref[empty]).all()
+
+    # against the oracle's exact sums: a sequential FP32 sum of c terms is within
+    # (c - 1) u sum|x| of the exact one, and the division adds u |mean| (u = 2^-24)
+    u = 2.0 ** -24
+    full = ~empty
+    c = cnt_orc[full].astype(np.float64)[:, None]
+    abs_sum = np.zeros((k, d))
+    np.add.at(abs_sum, labels, np.abs(X.astype(np.float64)))
+    exact = sums[full] / c
+    bound = 1.01 * ((c - 1) * u * abs_sum[full] / c + u * np.abs(exact)) + 1e-30
+    err = np.abs(cen_ref[full].astype(np.float64) - exact)
+    assert np.all(err <= bound), float((err / bound).max())
+    # the oracle's own centers are the exact means rounded once
+    assert np.array_equal(newc[full], exact.astype(np.float32))
+
+    # compactness: every term is positive, so the FP32 result is within (depth + 3) u of the
+    # FP64 sum, depth = rows per thread + the two 128-way trees + partials per thread
+    sse_orc = oracle.sse(X, labels, newc)
+    depth = math.ceil(n / p) * math.ceil(d / 128) + 7 + math.ceil(p / 128) + 7
+    assert abs(sse_ref - sse_orc) <= 1.01 * (depth + 3) * u * sse_orc, (sse_ref, sse_orc)
+    print(f"n={n} d={d} k={k}: centers bit-equal to the reference's FP32 order, max "
+          f"{float((err / bound).max()):.3f} of the bound from the oracle; SSE rel "
+          f"{abs(sse_ref - sse_orc) / sse_orc:.2e}")
