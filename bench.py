@@ -19,8 +19,9 @@ in the split tier; `traffic` is the DRAM bytes of one launch from an ncu capture
 The reference arm (--impl reference) times that CPU path: the reference has no CPU
 implementation of its own and its host code is not built (its sources are only in the x86
 development container; its driver also needs a CMake-generated config.h and cuBLAS). Its line also
-carries `reference_gpu`: the reference's own assignment kernels (compiled from its sources into
-oracle/_ref, launched as its ClosestCentersF does) timed on the same workload.
+carries `reference_gpu`: the reference's own GPU kernels (compiled from its sources into
+oracle/_ref, launched as its ClosestCentersF, ClusterCentersF and CompactnessF do) timed on the
+same workload, for one assignment pass and for one device-resident iteration.
 """
 from __future__ import annotations
 
@@ -120,11 +121,16 @@ def cpu_baseline(steps: int = 1):
                       f"{len(times)}", "seconds_per_sample_iter": t}
 
 
-def reference_gpu_assign(N=N, D=D, K=K, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0)):
-    """The reference's own assignment kernels (main/cuda/ClosestCenters.cu, compiled from its
-    sources into oracle/_ref and launched as its ClosestCentersF does) on an N x D, K workload
-    (default: the 4M x 128, K=1024 one): milliseconds per assignment pass, CUDA events on the
-    legacy default stream. None when oracle/_ref or a GPU is absent."""
+def reference_gpu_kernels(N=N, D=D, K=K, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0)):
+    """The reference's own GPU kernels (main/cuda/ClosestCenters.cu, ClusterCenters.cu and
+    Compactness.cu, compiled from its sources into oracle/_ref and launched as its
+    ClosestCentersF / ClusterCentersF / CompactnessF do) on an N x D, K workload (default: the
+    4M x 128, K=1024 one). Times, with CUDA events on the legacy default stream, (1) one
+    assignment pass and (2) one full-batch iteration as the reference's computeStandard runs it
+    on the GPU: its per-iteration reset (kmeans.cpp:1142-1170: clears of centers_large,
+    counts_large and the compactness partials; ||c||^2 of the centers), the assignment, the
+    center update and the compactness (kmeans.cpp:1019-1060), the new centers transposed back
+    for the next assignment. None when oracle/_ref or a GPU is absent."""
     try:
         import torch
         import oracle
@@ -154,19 +160,64 @@ def reference_gpu_assign(N=N, D=D, K=K, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3
             if ref.refk_closest_centers_f(*args) != 0:
                 return None
         torch.cuda.synchronize()
+        stream = torch.cuda.default_stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         reps = 5 if N * K * D > 1e10 else 50
-        e0.record(torch.cuda.default_stream())
+        e0.record(stream)
         for _ in range(reps):
             ref.refk_closest_centers_f(*args)
-        e1.record(torch.cuda.default_stream())
+        e1.record(stream)
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / reps
-        return {"kernels": "reference main/cuda/ClosestCenters.cu (ClosestCentersF), built from "
-                           "its sources for sm_103a", "assign_ms": ms,
-                "assign_tflops": 2.0 * N * K * D / (ms / 1000.0) / 1e12,
-                "note": "assignment pass only (FP32 labels); the reference's update and SSE "
-                        "kernels and host loop are not run"}
+        out = {"kernels": "reference main/cuda/ClosestCenters.cu (ClosestCentersF), built from "
+                          "its sources for sm_103a", "assign_ms": ms,
+               "assign_tflops": 2.0 * N * K * D / (ms / 1000.0) / 1e12}
+        if getattr(ref, "has_update", False):
+            p = torch.cuda.get_device_properties(0).multi_processor_count * 8
+            cl = torch.empty(p * K * D, dtype=torch.float32, device="cuda")
+            nl = torch.empty(p * K, dtype=torch.int32, device="cuda")
+            comp = torch.empty(p, dtype=torch.float32, device="cuda")
+            cen = torch.empty((K, D), dtype=torch.float32, device="cuda")
+            cnt = torch.empty(K, dtype=torch.int32, device="cuda")
+            Bv = B[: D * K].view(D, K)
+
+            def iteration():
+                cl.zero_()
+                nl.zero_()
+                comp.zero_()
+                torch.sum(Bv * Bv, 0, out=normB)
+                rc = ref.refk_closest_centers_f(*args)
+                rc |= ref.refk_cluster_centers_f(N, D, K, A.data_ptr(), labels.data_ptr(),
+                                                 cl.data_ptr(), nl.data_ptr(), cen.data_ptr(),
+                                                 cnt.data_ptr())
+                rc |= ref.refk_compactness_f(N, D, K, A.data_ptr(), labels.data_ptr(),
+                                             cen.data_ptr(), comp.data_ptr())
+                # an empty cluster (0/0 = NaN in the reference) keeps its old center here, so
+                # every center the next assignment sees is finite and every label in range
+                Bv.copy_(torch.where((cnt > 0)[:, None], cen, Bv.t()).t())
+                return rc
+
+            for _ in range(2):
+                if iteration() != 0:
+                    out["iteration_unavailable"] = ref.refk_last_error().decode()[:200]
+                    return out
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                iteration()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            it_ms = e0.elapsed_time(e1) / reps
+            out["kernels"] += ", ClusterCenters.cu, Compactness.cu"
+            out["iteration_ms"] = it_ms
+            out["iter_per_s"] = 1000.0 / it_ms
+            out["note"] = ("iteration = the reference's per-iteration clears + ||c||^2, "
+                           "ClosestCentersF, ClusterCentersF, CompactnessF and the centers' "
+                           "transpose (empty clusters keep their old center), device-resident; "
+                           "its host loop and convergence copy are not timed")
+        else:
+            out["note"] = "assignment pass only (center/compactness cubins not built)"
+        return out
     except Exception as e:  # noqa: BLE001 - an informational extra
         return {"unavailable": str(e)[:200]}
 
@@ -185,8 +236,8 @@ def reference_arm(args, rank: int):
             "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": cb["value"], "unit": "iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "reference_gpu": reference_gpu_assign(),
-            "reference_gpu_100kx32_K64": reference_gpu_assign(100_000, 32, 64, -10.0, 10.0,
+            "reference_gpu": reference_gpu_kernels(),
+            "reference_gpu_100kx32_K64": reference_gpu_kernels(100_000, 32, 64, -10.0, 10.0,
                                                                 (1.0, 1.0))}
     print(json.dumps(line), flush=True)
 
