@@ -10,8 +10,8 @@ points; synthetic, generated on the device). Prints one JSON line.
 
 `value` is Lloyd iterations/s with the data resident in HBM (CUDA events on the library's
 stream); `e2e` is the same metric through the public C-ABI one-shot call (kmgb_lloyd_f32) from
-pageable host memory, host<->device copies included, one call running the workload's 30
-iterations; `roofline` covers the assignment kernel
+pinned host memory (`pageable_value`: the same from pageable memory), host<->device copies
+included, one call running the workload's 30 iterations; `roofline` covers the assignment kernel
 (2*N*K*D FLOP per launch, per-launch time from CUDA events bracketing it inside the timed
 region; `tensor_*` counts the tensor-core products the tier actually issues, three per element
 in the split tier; `traffic` is the DRAM bytes of one launch from an ncu capture, scaled to N);
@@ -661,23 +661,35 @@ def main():
 
     e2e = None
     if not args.no_e2e and rank == 0:
-        Xh = X.cpu().numpy()
+        # the step's input in pinned host memory; the same rows in pageable memory as a second
+        # measurement
+        Xpin = torch.empty(X.shape, dtype=torch.float32, pin_memory=True)
+        Xpin.copy_(X)
+        Xh = Xpin.numpy()
+        Xpage = np.array(Xh, copy=True)
         del X
         torch.cuda.empty_cache()
-        # one untimed call first (module loading, allocator growth), like the device path's
-        # warm-up iterations; the timed call then includes all of its own host<->device copies
+
+        def timed_call(src):
+            t0 = time.perf_counter()
+            res = km.lloyd(src, K, init=init, max_iters=E2E_ITERS, assign_tier=tier_id)
+            return res, time.perf_counter() - t0
+
+        # one untimed call first (module loading, the library's memory pool), like the device
+        # path's warm-up iterations; the timed call then includes all of its own host<->device
+        # copies, its allocation and its release
         km.lloyd(Xh, K, init=init, max_iters=max(1, args.warmup), assign_tier=tier_id)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        res = km.lloyd(Xh, K, init=init, max_iters=E2E_ITERS, assign_tier=tier_id)
-        t1 = time.perf_counter()
-        e2e = {"value": E2E_ITERS / (t1 - t0), "unit": "iter/s",
+        res, sec = timed_call(Xh)
+        _, sec_page = timed_call(Xpage)
+        e2e = {"value": E2E_ITERS / sec, "unit": "iter/s",
                "h2d_bytes_per_step": (Xh.nbytes + init.nbytes) // E2E_ITERS,
                "d2h_bytes_per_step": (res.centers.nbytes + res.labels.nbytes + res.sse.nbytes)
                // E2E_ITERS, "iterations_per_call": E2E_ITERS,
-               "call": "kmgb_lloyd_f32 (host pageable X, init, centers/labels/SSE out); "
+               "call": "kmgb_lloyd_f32 (host pinned X, init, centers/labels/SSE out); "
                        "after one untimed call",
-               "seconds": t1 - t0}
+               "seconds": sec, "pageable_value": E2E_ITERS / sec_page}
+        del Xpin, Xh, Xpage
     cb = None
     if not args.no_cpu and rank == 0:
         cb = cpu_baseline(1)

@@ -298,6 +298,9 @@ KMGB_EXPORT int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const 
 /* Resident handle: data uploaded once, iterations run on the handle's own stream. */
 typedef struct kmgb_handle kmgb_handle;
 KMGB_EXPORT int kmgb_create(kmgb_handle** h, long long n, int d, int k, const kmgb_options* opt);
+/* kmgb_set_data copies the n x d rows of X (host or device memory) into the handle; a host
+ * buffer may be reused as soon as it returns, a device buffer once the handle's stream has
+ * passed the copy (kmgb_synchronize). */
 KMGB_EXPORT int kmgb_set_data(kmgb_handle* h, const float* X, int x_on_device);
 KMGB_EXPORT int kmgb_set_centers(kmgb_handle* h, const float* C, int c_on_device); /* NULL: reference init */
 /* k-means++ centers from the resident data (not for host-streamed handles); picks: k rows (host,
@@ -329,6 +332,12 @@ KMGB_EXPORT int kmgb_set_profiling(kmgb_handle* h, int on);
 KMGB_EXPORT int kmgb_get_phase_ms(kmgb_handle* h, double* ms, int* iters);
 /* Kernels launched by this library since the process started. */
 KMGB_EXPORT long long kmgb_launch_count(void);
+/* Handles take their device memory from a stream-ordered pool per device that keeps freed
+ * memory for the next handle (no reference counterpart: the reference allocates and frees with
+ * cudaMalloc/cudaFree in kmeans.cpp:577-683 and its destructor, kmeans.cpp:145-244). This call waits for the current
+ * device and returns every pool's unused memory to the device; 0 on success. Setting
+ * KMGB_POOL=0 in the environment makes every free return its memory at once. */
+KMGB_EXPORT int kmgb_release_cached_memory(void);
 
 /* Last error message of the calling thread (empty string if none). */
 KMGB_EXPORT const char* kmgb_last_error(void);

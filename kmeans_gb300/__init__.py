@@ -30,6 +30,7 @@ LIB_PATH = os.path.join(_HERE, "libkmeans_gb300.so")
 HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "kmeans_gb300.h")
 
 KMEANS_SUCCESS = 0
+KMEANS_ERROR_BUILDDATA = 1
 KMEANS_NONCONVERGENCE = 13
 ASSIGN_FP32 = 0
 ASSIGN_BF16 = 1
@@ -138,6 +139,7 @@ def lib():
             "kmgb_set_profiling": (i32, [P, i32]),
             "kmgb_get_phase_ms": (i32, [P, P, P]),
             "kmgb_launch_count": (i64, []),
+            "kmgb_release_cached_memory": (i32, []),
             "kmgb_sum_piece": (i32, []),
             "kmgb_reference_init": (i32, [P, i32, i32, i32, P, P, P]),
             "kmgb_tc_accumulators": (i32, [P, i64, i32, P, i32, i32, P]),
@@ -157,6 +159,13 @@ def lib():
 
 def launch_count() -> int:
     return int(lib().kmgb_launch_count())
+
+
+def release_cached_memory() -> None:
+    """Return the device memory that destroyed handles left in the library's pool (handles
+    reuse it otherwise; KMGB_POOL=0 returns it at every destroy)."""
+    if lib().kmgb_release_cached_memory() != 0:
+        raise KmeansError(KMEANS_ERROR_BUILDDATA, last_error())
 
 
 def last_error() -> str:

@@ -63,6 +63,15 @@ cudaError_t dalloc(T** p, size_t count) {
   return cudaMalloc(reinterpret_cast<void**>(p), sizeof(T) * count);
 }
 
+// a handle's buffer from the library's memory pool (devmem.cu), ordered on the handle's stream
+template <typename T>
+cudaError_t dalloc(T** p, size_t count, cudaStream_t s) {
+  void* v = nullptr;
+  const cudaError_t r = dev_alloc(&v, sizeof(T) * (count ? count : 1), s);
+  *p = static_cast<T*>(v);
+  return r;
+}
+
 bool is_device_ptr(const void* p) {
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -210,8 +219,6 @@ struct kmgb_handle {
   double* sse_dev = nullptr;
   int sse_cap = 0;
   std::vector<double> sse_host;
-  double* sse_pinned = nullptr;
-  double* loop_init = nullptr;  // pinned [2]
   int iterations = 0;
   int status = 0;
   double criterion = -1.0;
@@ -242,18 +249,22 @@ struct kmgb_handle {
 
   ~kmgb_handle() {
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
-    // the fixed buffers live in the arena; these are allocated on their own
-    void* ptrs[] = {arena, sse_dev, kpp_d2, kpp_blk, kpp_sc, kpp_picks};
-    for (void* p : ptrs)
-      if (p) cudaFree(p);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    // device memory goes back to the pool in the stream's order, after the work queued on it
+    // and on the copy stream
+    if (copy_stream) cudaStreamSynchronize(copy_stream);
+    if (stream) {
+      cudaStreamSynchronize(stream);
+      // the fixed buffers live in the arena; these are allocated on their own
+      void* ptrs[] = {arena, sse_dev, kpp_d2, kpp_blk, kpp_sc, kpp_picks};
+      for (void* p : ptrs) dev_free(p, stream);
+      cudaStreamSynchronize(stream);
+    }
     for (int b = 0; b < 2; ++b) {
       if (ev_copied[b]) cudaEventDestroy(ev_copied[b]);
       if (ev_free[b]) cudaEventDestroy(ev_free[b]);
     }
     if (copy_stream) cudaStreamDestroy(copy_stream);
-    if (sse_pinned) cudaFreeHost(sse_pinned);
-    if (loop_init) cudaFreeHost(loop_init);
-    if (gexec) cudaGraphExecDestroy(gexec);
     if (ev0) cudaEventDestroy(ev0);
     if (ev1) cudaEventDestroy(ev1);
     if (stream) cudaStreamDestroy(stream);
@@ -312,9 +323,10 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   KM_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), (delete h, code));
   KM_TRY(cudaEventCreate(&h->ev0), (delete h, code));
   KM_TRY(cudaEventCreate(&h->ev1), (delete h, code));
-  // Every fixed device buffer of the handle is carved from one allocation (one cudaMalloc and
-  // one cudaFree per handle: on GB300 about 0.2 + 2.4 ms for the 4M x 128 workload's 7 GB,
-  // against 3 + 5 ms as 25 separate buffers); the list runs twice, sizing then carving.
+  // Every fixed device buffer of the handle is carved from one allocation from the library's
+  // memory pool (25 separate cudaMalloc/cudaFree buffers cost 3 + 5 ms on GB300 for the
+  // 4M x 128 workload's 7 GB, one cudaMalloc/cudaFree 1 + 3.3 ms, a warm pool ~0); the list
+  // runs twice, sizing then carving.
   const long long na = h->n_act;
   const long long nl = h->streaming ? n : na;  // labels of every row when streaming
   if (bf16) {
@@ -392,7 +404,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   };
   Arena sizing;
   carve(sizing);
-  KM_TRY(cudaMalloc(&h->arena, sizing.off), (delete h, code));
+  KM_TRY(dev_alloc(&h->arena, sizing.off, h->stream), (delete h, code));
   Arena cut;
   cut.base = static_cast<char*>(h->arena);
   carve(cut);
@@ -416,9 +428,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   w.iters_done = h->iters_done;
   w.sse_indexed = h->streaming ? 0 : 1;  // host-streamed iterations write their own slot
   h->sse_cap = std::max(1, h->opt.max_iters);
-  KM_TRY(dalloc(&h->sse_dev, h->sse_cap), (delete h, code));
-  KM_TRY(cudaMallocHost(&h->sse_pinned, sizeof(double)), (delete h, code));
-  KM_TRY(cudaMallocHost(&h->loop_init, 2 * sizeof(double)), (delete h, code));
+  KM_TRY(dalloc(&h->sse_dev, h->sse_cap, h->stream), (delete h, code));
   *out = h;
   return 0;
 }
@@ -449,27 +459,63 @@ int set_data(kmgb_handle* h, const float* X, bool on_device) {
     return 0;
   }
   if (on_device) KM_TRY(order_after_default_stream(h), code);
-  const size_t row_bytes = sizeof(float) * h->d;
-  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  if (h->ldx == h->d) {
-    KM_TRY(cudaMemcpyAsync(h->X, X, row_bytes * h->n, kind, h->stream), code);
-  } else {
-    KM_TRY(cudaMemsetAsync(h->X, 0, sizeof(float) * h->ldx * h->n, h->stream), code);
-    KM_TRY(cudaMemcpy2DAsync(h->X, sizeof(float) * h->ldx, X, row_bytes, row_bytes, h->n, kind,
-                             h->stream),
-           code);
-  }
-  KM_TRY(launch_point_norms(h->X, h->ldx, h->n, h->d, h->qn, h->xn, h->stream), code);
   if (h->gexec) {  // a captured iteration bakes in the planes it reads: capture again
     cudaGraphExecDestroy(h->gexec);
     h->gexec = nullptr;
   }
   h->x_exact = false;
+  if (h->Xb) KM_TRY(cudaMemsetAsync(h->xinexact, 0, sizeof(int), h->stream), code);
+  const size_t row_bytes = sizeof(float) * h->d;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  // Rows [r0, r1) of X into the device copy, on stream cs.
+  auto copy_rows = [&](long long r0, long long r1, cudaStream_t cs) -> cudaError_t {
+    if (h->ldx == h->d)
+      return cudaMemcpyAsync(h->X + (size_t)r0 * h->ldx, X + (size_t)r0 * h->d,
+                             row_bytes * (r1 - r0), kind, cs);
+    return cudaMemcpy2DAsync(h->X + (size_t)r0 * h->ldx, sizeof(float) * h->ldx,
+                             X + (size_t)r0 * h->d, row_bytes, row_bytes, r1 - r0, kind, cs);
+  };
+  // Norms and BF16 planes of rows [r0, r1), on the handle's stream.
+  auto prepare_rows = [&](long long r0, long long r1) -> cudaError_t {
+    const size_t xo = (size_t)r0 * h->ldx, bo = (size_t)r0 * h->ldb * 2;
+    cudaError_t r = launch_point_norms(h->X + xo, h->ldx, r1 - r0, h->d, h->qn + r0, h->xn + r0,
+                                       h->stream);
+    if (r != cudaSuccess || !h->Xb) return r;
+    return launch_to_bf16(h->X + xo, h->ldx, r1 - r0, h->d, static_cast<char*>(h->Xb) + bo,
+                          h->ldb, h->stream, nullptr,
+                          h->Xl ? static_cast<char*>(h->Xl) + bo : nullptr, h->xinexact);
+  };
+  if (h->ldx != h->d)  // the copies write d of ldx columns: the padding stays zero
+    KM_TRY(cudaMemsetAsync(h->X, 0, sizeof(float) * h->ldx * h->n, h->stream), code);
+  const long long kUploadChunks = 8;
+  if (!on_device && h->n >= kUploadChunks * 4096) {
+    // Host data crosses the link at ~210 GB/s on GB300 whatever the number of streams; the
+    // upload goes in chunks on a second stream and the handle's stream prepares each chunk
+    // once it has landed, so only the last chunk's preparation follows the copy.
+    if (!h->copy_stream)
+      KM_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), code);
+    if (!h->ev_copied[0])
+      KM_TRY(cudaEventCreateWithFlags(&h->ev_copied[0], cudaEventDisableTiming), code);
+    cudaEvent_t ev = h->ev_copied[0];
+    // the copies overwrite X only after the handle's earlier work (and the padding memset)
+    KM_TRY(cudaEventRecord(ev, h->stream), code);
+    KM_TRY(cudaStreamWaitEvent(h->copy_stream, ev, 0), code);
+    const long long rows = (h->n + kUploadChunks - 1) / kUploadChunks;
+    for (long long r0 = 0; r0 < h->n; r0 += rows) {
+      const long long r1 = std::min(h->n, r0 + rows);
+      KM_TRY(copy_rows(r0, r1, h->copy_stream), code);
+      KM_TRY(cudaEventRecord(ev, h->copy_stream), code);
+      KM_TRY(cudaStreamWaitEvent(h->stream, ev, 0), code);
+      KM_TRY(prepare_rows(r0, r1), code);
+    }
+    // the caller may reuse its host buffer once this returns
+    KM_TRY(cudaStreamSynchronize(h->copy_stream), code);
+  } else {
+    KM_TRY(copy_rows(0, h->n, h->stream), code);
+    KM_TRY(prepare_rows(0, h->n), code);
+    if (!on_device) KM_TRY(cudaStreamSynchronize(h->stream), code);
+  }
   if (h->Xb) {
-    KM_TRY(cudaMemsetAsync(h->xinexact, 0, sizeof(int), h->stream), code);
-    KM_TRY(launch_to_bf16(h->X, h->ldx, h->n, h->d, h->Xb, h->ldb, h->stream, nullptr, h->Xl,
-                          h->xinexact),
-           code);
     if (h->Xl) {
       // every x a BF16 number: the residual plane is zero and the split tier drops its product
       int inexact = 1;
@@ -821,8 +867,8 @@ int run(kmgb_handle* h, int iters, double criterion) {
   iters = std::max(iters, 0);
   if (iters > h->sse_cap) {
     double* nd = nullptr;
-    KM_TRY(dalloc(&nd, iters), KMEANS_ERROR_COMPUTE);
-    cudaFree(h->sse_dev);
+    KM_TRY(dalloc(&nd, iters, h->stream), KMEANS_ERROR_COMPUTE);
+    dev_free(h->sse_dev, h->stream);
     h->sse_dev = nd;
     h->sse_cap = iters;
   }
@@ -831,12 +877,10 @@ int run(kmgb_handle* h, int iters, double criterion) {
   h->uw.criterion = criterion;
   h->criterion = criterion;
   // loop state (kmeans.cpp:40-41): SSE_old = 0, relErr = 1, not stopped
-  KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);  // pinned init buffer reuse
-  h->loop_init[0] = 0.0;
-  h->loop_init[1] = 1.0;
+  static const double kLoopInit[2] = {0.0, 1.0};  // a constant source: nothing to keep alive
   KM_TRY(cudaMemsetAsync(h->stop, 0, sizeof(int), h->stream), KMEANS_ERROR_COMPUTE);
   KM_TRY(cudaMemsetAsync(h->iters_done, 0, sizeof(int), h->stream), KMEANS_ERROR_COMPUTE);
-  KM_TRY(cudaMemcpyAsync(h->loopf, h->loop_init, 2 * sizeof(double), cudaMemcpyHostToDevice,
+  KM_TRY(cudaMemcpyAsync(h->loopf, kLoopInit, 2 * sizeof(double), cudaMemcpyHostToDevice,
                          h->stream),
          KMEANS_ERROR_COMPUTE);
   KM_TRY(cudaEventRecord(h->ev0, h->stream), KMEANS_ERROR_COMPUTE);
@@ -943,10 +987,10 @@ int init_kmeanspp(kmgb_handle* h, unsigned long long seed, int* picks_out) {
     return code;
   }
   if (!h->kpp_d2) {
-    KM_TRY(dalloc(&h->kpp_d2, (size_t)kmeanspp_d2_elems(h->n)), code);
-    KM_TRY(dalloc(&h->kpp_blk, (size_t)kmeanspp_blocks(h->n)), code);
-    KM_TRY(dalloc(&h->kpp_sc, 3), code);
-    KM_TRY(dalloc(&h->kpp_picks, (size_t)h->k), code);
+    KM_TRY(dalloc(&h->kpp_d2, (size_t)kmeanspp_d2_elems(h->n), h->stream), code);
+    KM_TRY(dalloc(&h->kpp_blk, (size_t)kmeanspp_blocks(h->n), h->stream), code);
+    KM_TRY(dalloc(&h->kpp_sc, 3, h->stream), code);
+    KM_TRY(dalloc(&h->kpp_picks, (size_t)h->k, h->stream), code);
   }
   KM_TRY(cudaMemsetAsync(h->C, 0, sizeof(float) * h->ldx * h->k, h->stream), code);
   KM_TRY(launch_kmeanspp(h->X, h->ldx, h->n, h->d, h->k, seed, h->C, h->ldx, h->kpp_picks,

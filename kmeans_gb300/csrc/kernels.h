@@ -256,4 +256,10 @@ bool reference_picks(int m, int k, std::vector<int>& picks);
 // Message returned by kmgb_last_error() on the calling thread.
 void set_last_error(const char* msg);
 
+// Device memory from the library's stream-ordered pool of the current device (devmem.cu):
+// dev_alloc returns memory usable from every stream; dev_free gives it back in the order of s.
+cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s);
+void dev_free(void* p, cudaStream_t s);
+cudaError_t dev_release_cached();
+
 }  // namespace kmgb

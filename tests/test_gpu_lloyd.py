@@ -284,3 +284,41 @@ def test_host_streamed_tiles_reject_device_data_and_mini_batch(km, torch_cuda):
         km.lloyd(torch_cuda.from_numpy(X).cuda(), 8, init=init, max_iters=2, stream_tile_rows=1000)
     with pytest.raises(km.KmeansError):
         km.lloyd(X, 8, init=init, max_iters=2, stream_tile_rows=1000, mini_batch_fraction=0.5)
+
+
+def test_memory_pool_reuses_and_releases_handle_memory(km, torch_cuda):
+    """A destroyed handle's device memory stays in the library's pool, the next handle of the
+    same size takes it again without growing the pool, and release_cached_memory gives it back.
+    The second run's results equal the first's (reused memory carries nothing over)."""
+    torch = torch_cuda
+    n, d, k = 1_000_000, 128, 256
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    X = torch.randn(n, d, device="cuda", generator=gen)
+    init = X[:k].cpu().numpy()
+    torch.cuda.synchronize()
+    km.release_cached_memory()
+    free0 = torch.cuda.mem_get_info()[0]
+
+    def one_run():
+        h = km.Handle(n, d, k, assign_tier=km.ASSIGN_BF16X3)
+        h.set_data(X, True)
+        h.set_centers(init)
+        h.run(2)
+        out = (h.centers(), h.labels(), h.sse(2))
+        h.close()
+        torch.cuda.synchronize()
+        return out
+
+    a = one_run()
+    free1 = torch.cuda.mem_get_info()[0]
+    b = one_run()
+    free2 = torch.cuda.mem_get_info()[0]
+    mib = 1 << 20
+    # X alone is 512 MB in the handle; its BF16 planes another 512 MB
+    assert free0 - free1 > 1000 * mib, (free0, free1)
+    assert abs(free1 - free2) < 64 * mib, (free1, free2)
+    km.release_cached_memory()
+    free3 = torch.cuda.mem_get_info()[0]
+    assert abs(free3 - free0) < 64 * mib, (free0, free3)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert np.array_equal(a[2], b[2])
