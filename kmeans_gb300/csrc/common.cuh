@@ -119,6 +119,24 @@ __device__ __forceinline__ unsigned lanemask_lt() {
   return m;
 }
 
+// Bits of a label below k (0 for k <= 1).
+__device__ __forceinline__ int label_bits(int k) { return k <= 1 ? 0 : 32 - __clz(k - 1); }
+
+// The lanes of the warp holding the same label as this lane (labels in [0, 2^nbits), or -1 for
+// "none": the -1 lanes form one group of their own). One ballot per label bit: with mostly
+// distinct labels in a warp (K ~ 1000 centers) this is much cheaper than __match_any_sync.
+// Every lane of the warp calls it with the same nbits.
+__device__ __forceinline__ unsigned warp_peers(int l, int nbits) {
+  const unsigned valid = __ballot_sync(0xffffffffu, l >= 0);
+  unsigned m = l >= 0 ? valid : ~valid;
+  for (int b = 0; b < nbits; ++b) {
+    const bool bit = (l >> b) & 1;
+    const unsigned set = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? set : ~set;
+  }
+  return m;
+}
+
 }  // namespace kmgb
 
 // Host-side: 2-D row-major tensor map (inner dim = columns) with 128-byte swizzle.

@@ -12,6 +12,7 @@
 // mode 1 (expansion):  value = nb_j - 2 x.c_j with the caller's norms nb (per-kernel ABI,
 //                      KmeansCudaKernels.h:238-244); absolute bound from ||x|| and max ||c||.
 #include <cfloat>
+#include <cstdint>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -552,26 +553,47 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
 }
 
-// ||x - c||^2 as a float-float (hi, lo), summed over the warp (every lane ends with the total).
-// Lane l takes dimensions l, l+32, ... For each: u = x - c is split exactly into uh + ul
+constexpr int kGroupLanes = 8;  // lanes per candidate in the fast path: 4 candidates at a time
+static_assert(kMaxCand <= 32, "one lane per recorded candidate");
+
+// One term of ||x - c||^2 into the float-float (hi, lo): u = x - c is split exactly into uh + ul
 // (two_sum), uh^2 = p + e exactly (FMA), and the remaining 2*uh*ul + ul^2 + e is added with one
 // rounding; hi collects the p's by two_sum, lo the rest.
-__device__ __forceinline__ void ff_dist(const float* __restrict__ x, const float* __restrict__ c,
-                                        int d, int lane, float& hi, float& lo) {
+__device__ __forceinline__ void ff_term(float xv, float cv, float& hi, float& lo) {
+  float uh, ul;
+  two_sum(xv, -cv, uh, ul);
+  const float p = __fmul_rn(uh, uh);
+  const float e = __fmaf_rn(uh, uh, -p);
+  const float r = __fmaf_rn(ul, ul, __fmaf_rn(__fadd_rn(uh, uh), ul, e));
+  float s, err;
+  two_sum(hi, p, s, err);
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(err, r));
+}
+
+// ||x - c||^2 over the first d dimensions as a float-float (hi, lo), summed over each group of
+// 8 consecutive lanes (every lane of a group ends with its group's total; all 32 lanes call it,
+// a group with nothing to do passes d = 0). Lane r of a group takes dimensions 4r..4r+3,
+// 4r+32.. with 16-byte loads (VEC: d, both row strides and both bases multiples of 4 floats),
+// else r, r+8, ...: at most m = 4 ceil(d/32) terms per lane, then three reduction levels.
+template <bool VEC>
+__device__ __forceinline__ void ff_dist8(const float* __restrict__ x, const float* __restrict__ c,
+                                         int d, int r, float& hi, float& lo) {
   hi = 0.0f;
   lo = 0.0f;
-  for (int t = lane; t < d; t += 32) {
-    float uh, ul;
-    two_sum(__ldg(x + t), -__ldg(c + t), uh, ul);
-    const float p = __fmul_rn(uh, uh);
-    const float e = __fmaf_rn(uh, uh, -p);
-    const float r = __fmaf_rn(ul, ul, __fmaf_rn(__fadd_rn(uh, uh), ul, e));
-    float s, err;
-    two_sum(hi, p, s, err);
-    hi = s;
-    lo = __fadd_rn(lo, __fadd_rn(err, r));
+  if (VEC) {
+    for (int t = 4 * r; t < d; t += 4 * kGroupLanes) {
+      const float4 xv = __ldg(reinterpret_cast<const float4*>(x + t));
+      const float4 cv = __ldg(reinterpret_cast<const float4*>(c + t));
+      ff_term(xv.x, cv.x, hi, lo);
+      ff_term(xv.y, cv.y, hi, lo);
+      ff_term(xv.z, cv.z, hi, lo);
+      ff_term(xv.w, cv.w, hi, lo);
+    }
+  } else {
+    for (int t = r; t < d; t += kGroupLanes) ff_term(__ldg(x + t), __ldg(c + t), hi, lo);
   }
-  for (int o = 16; o > 0; o >>= 1) {
+  for (int o = kGroupLanes / 2; o > 0; o >>= 1) {
     const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
     const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
     float s, err;
@@ -581,19 +603,62 @@ __device__ __forceinline__ void ff_dist(const float* __restrict__ x, const float
   }
 }
 
+// ||x - c||^2 over the first d dimensions in FP32, summed over each group of 8 consecutive lanes
+// (all 32 lanes call it; a group with nothing to do passes d = 0). Every step is one explicitly
+// rounded operation: u = x - c, then s = u*u + s by FMA. VEC: four independent chains per lane
+// (the float4 components, at most ceil(d/32) terms each) merged in two levels, then three
+// butterfly levels; scalar: one chain of at most ceil(d/8) terms, then three levels.
+template <bool VEC>
+__device__ __forceinline__ float f32_dist8(const float* __restrict__ x, const float* __restrict__ c,
+                                           int d, int r) {
+  float s;
+  if (VEC) {
+    float a0 = 0.0f, a1 = 0.0f, a2 = 0.0f, a3 = 0.0f;
+    for (int t = 4 * r; t < d; t += 4 * kGroupLanes) {
+      const float4 xv = __ldg(reinterpret_cast<const float4*>(x + t));
+      const float4 cv = __ldg(reinterpret_cast<const float4*>(c + t));
+      const float u0 = __fsub_rn(xv.x, cv.x), u1 = __fsub_rn(xv.y, cv.y);
+      const float u2 = __fsub_rn(xv.z, cv.z), u3 = __fsub_rn(xv.w, cv.w);
+      a0 = __fmaf_rn(u0, u0, a0);
+      a1 = __fmaf_rn(u1, u1, a1);
+      a2 = __fmaf_rn(u2, u2, a2);
+      a3 = __fmaf_rn(u3, u3, a3);
+    }
+    s = __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
+  } else {
+    s = 0.0f;
+    for (int t = r; t < d; t += kGroupLanes) {
+      const float u = __fsub_rn(__ldg(x + t), __ldg(c + t));
+      s = __fmaf_rn(u, u, s);
+    }
+  }
+  for (int o = kGroupLanes / 2; o > 0; o >>= 1)
+    s = __fadd_rn(s, __shfl_xor_sync(0xffffffffu, s, o));
+  return s;
+}
+
 // Resolves every flagged point from its recorded candidates. The candidate set holds every center
 // whose FP64 distance can be the minimum; the label is the oracle's: smallest FP64 distance
 // (sequential fma over the dimensions), lowest index on ties.
 //
-// Fast path (FP32 pipe, whole warp per candidate): the float-float distance v of each candidate
-// is within rel*v + abs of the exact distance, and the oracle's FP64 value is within
-// (d+2)*2^-52 relative of it. Per lane (m = ceil(d/32) terms) the lo accumulator's roundings are
-// bounded by (m+1)^2 * 2^-47 relative, the 2*uh*ul + ul^2 + e terms by 2^-46, the five reduction
-// levels by 5 * (m+6) * 2^-47; rel takes 8x that sum. abs covers products that reach the
-// subnormal range. If the best candidate beats the runner-up by more than both tolerances, it is
-// the oracle's arg-min. Otherwise (near ties, duplicate centers, non-finite values) the point's
-// candidates are evaluated exactly as the oracle does, one lane per candidate, in FP64.
-// Points with more candidates than recorded (or none) go to `over` for the full re-rank.
+// First tier (FP32, 8 lanes per candidate, 4 candidates at a time): every term of the FP32 value
+// is non-negative and passes through at most m + 7 roundings of 2^-24 (the subtraction twice, as
+// u^2, then at most m = ceil(d/8) FMAs, two merges and three butterfly levels), so it is within
+// rel32 = (m + 8) 2^-24 (x1.1) of the exact distance, plus abs32 for results in the subnormal
+// range; with the oracle's own (d+2) 2^-52, a best candidate ahead of the runner-up by more than
+// both is the oracle's arg-min. Flagged points are mostly ahead by far more than that.
+//
+// Second tier (FP32 pipe, 8 lanes per candidate, 4 candidates at a time): the float-float distance
+// v of each candidate is within rel*v + abs of the exact distance, and the oracle's FP64 value is
+// within (d+2)*2^-52 relative of it. Per lane (m = 4 ceil(d/32) terms) the lo accumulator's
+// roundings are bounded by (m+1)^2 * 2^-47 relative, the 2*uh*ul + ul^2 + e terms by 2^-46, the
+// three reduction levels by 3 * (m+6) * 2^-47; rel takes 8x that sum. abs covers products that
+// reach the subnormal range. If the best candidate beats the runner-up by more than both
+// tolerances, it is the oracle's arg-min. Otherwise (near ties, duplicate centers, non-finite
+// values) the point's candidates are evaluated exactly as the oracle does, one lane per
+// candidate, in FP64. Points with more candidates than recorded (or none) go to `over` for the
+// full re-rank.
+template <bool VEC>
 __global__ void resolve_candidates_kernel(const int* __restrict__ list, const int* __restrict__ count,
                                           long long max_list, const int* __restrict__ cand,
                                           const int* __restrict__ cand_cnt,
@@ -605,45 +670,93 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
   if (stopped(stop)) return;
   const long long cnt = min((long long)*(volatile const int*)count, max_list);
   const int lane = threadIdx.x & 31;
+  const int grp = lane / kGroupLanes, sub = lane % kGroupLanes;
+  constexpr int kGroups = 32 / kGroupLanes;
   const long long w0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  const double m = (double)((d + 31) / 32);
-  const double rel = 8.0 * ((m + 1.0) * (m + 1.0) + 2.0 + 5.0 * (m + 6.0)) * 0x1p-47 +
+  const double m = 4.0 * (double)((d + 31) / 32);
+  const double rel = 8.0 * ((m + 1.0) * (m + 1.0) + 2.0 + 3.0 * (m + 6.0)) * 0x1p-47 +
                      (double)(d + 2) * 0x1p-52;
   const double abs_tol = (double)(d + 32) * 0x1p-118;
+  const double m32 = (double)((d + kGroupLanes - 1) / kGroupLanes);
+  const double rel32 = 1.1 * (m32 + 8.0) * 0x1p-24 + (double)(d + 2) * 0x1p-52;
+  const double abs32 = (double)(d + 32) * (m32 + 8.0) * 0x1p-149;
   for (long long slot = w0; slot < cnt; slot += nw) {
     const int pt = list[slot];
     const int nc = cand_cnt[slot];
-    if (nc <= 0) {
+    if (nc <= 0 || nc > kMaxCand) {
       if (lane == 0) over[atomicAdd(over_count, 1)] = pt;
       continue;
     }
     const float* x = X + (size_t)pt * ldx;
-    // fast path: certifies only a strict separation, so the list order (column slice by column
-    // slice) does not matter
+    // lane q holds candidate q and whether it is usable
+    const int myj = lane < nc ? cand[slot * kMaxCand + lane] : -1;
+    const int myok = (myj >= 0 && cn[myj] < INFINITY) ? 1 : 0;
+    // both fast tiers certify only a strict separation, so the list order (column slice by
+    // column slice) does not matter
     double v1 = INFINITY, v2 = INFINITY;
     int i1 = -1;
     bool finite = true;
-    for (int q = 0; q < nc; ++q) {
-      const int j = cand[slot * kMaxCand + q];
-      if (!(cn[j] < INFINITY)) continue;  // unusable center
-      float hi, lo;
-      ff_dist(x, C + (size_t)j * ldc, d, lane, hi, lo);
-      const double v = (double)hi + (double)lo;
-      if (!(v < 1.0e300)) finite = false;  // overflow, inf or NaN on the FP32 pipe
-      if (v < v1) {
-        v2 = v1;
-        v1 = v;
-        i1 = j;
-      } else if (v < v2) {
-        v2 = v;
+    for (int q0 = 0; q0 < nc; q0 += kGroups) {
+      const int q = q0 + grp;  // <= 31: q0 is a multiple of 4 below nc <= kMaxCand = 32
+      const int j = __shfl_sync(0xffffffffu, myj, q);
+      const int ok = __shfl_sync(0xffffffffu, myok, q) && q < nc;
+      const float v = f32_dist8<VEC>(x, ok ? C + (size_t)j * ldc : x, ok ? d : 0, sub);
+      for (int g = 0; g < kGroups; ++g) {
+        const double vg = (double)__shfl_sync(0xffffffffu, v, g * kGroupLanes);
+        const int jg = __shfl_sync(0xffffffffu, j, g * kGroupLanes);
+        if (!__shfl_sync(0xffffffffu, ok, g * kGroupLanes)) continue;
+        if (!(vg < 3.0e38)) finite = false;  // overflow, inf or NaN
+        if (vg < v1) {
+          v2 = v1;
+          v1 = vg;
+          i1 = jg;
+        } else if (vg < v2) {
+          v2 = vg;
+        }
       }
     }
     if (i1 < 0) {  // no usable candidate
       if (lane == 0) over[atomicAdd(over_count, 1)] = pt;
       continue;
     }
-    if (finite && (v2 - v1 > (v1 + v2) * rel + 2.0 * abs_tol)) {
+    // one usable candidate (v2 infinite, its value finite) is the arg-min itself
+    if (finite && (v2 == INFINITY || v2 - v1 > (v1 + v2) * rel32 + 2.0 * abs32)) {
+      if (lane == 0) labels[pt] = i1;
+      continue;
+    }
+    v1 = INFINITY;
+    v2 = INFINITY;
+    i1 = -1;
+    finite = true;
+    for (int q0 = 0; q0 < nc; q0 += kGroups) {
+      const int q = q0 + grp;  // <= 31: q0 is a multiple of 4 below nc <= kMaxCand = 32
+      const int j = __shfl_sync(0xffffffffu, myj, q);
+      const int ok = __shfl_sync(0xffffffffu, myok, q) && q < nc;
+      float hi, lo;
+      ff_dist8<VEC>(x, ok ? C + (size_t)j * ldc : x, ok ? d : 0, sub, hi, lo);
+      const double v = (double)hi + (double)lo;
+      for (int g = 0; g < kGroups; ++g) {
+        const double vg = __shfl_sync(0xffffffffu, v, g * kGroupLanes);
+        const int jg = __shfl_sync(0xffffffffu, j, g * kGroupLanes);
+        if (!__shfl_sync(0xffffffffu, ok, g * kGroupLanes)) continue;
+        if (!(vg < 1.0e300)) finite = false;  // overflow, inf or NaN on the FP32 pipe
+        if (vg < v1) {
+          v2 = v1;
+          v1 = vg;
+          i1 = jg;
+        } else if (vg < v2) {
+          v2 = vg;
+        }
+      }
+    }
+    if (i1 < 0) {  // no usable candidate
+      if (lane == 0) over[atomicAdd(over_count, 1)] = pt;
+      continue;
+    }
+    // one usable candidate (v2 infinite, every value finite) is the arg-min itself; the
+    // comparison below would read inf > inf
+    if (finite && (v2 == INFINITY || v2 - v1 > (v1 + v2) * rel + 2.0 * abs_tol)) {
       if (lane == 0) labels[pt] = i1;
       continue;
     }
@@ -699,8 +812,16 @@ cudaError_t launch_resolve_candidates(const int* list, const int* count, long lo
                                       long long ldx, const float* C, long long ldc, const float* cn,
                                       int d, int* labels, int* over, int* over_count,
                                       const int* stop, cudaStream_t s) {
-  resolve_candidates_kernel<<<152 * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt, X, ldx,
-                                                    C, ldc, cn, d, labels, over, over_count, stop);
+  const bool vec = d % 4 == 0 && ldx % 4 == 0 && ldc % 4 == 0 &&
+                   reinterpret_cast<uintptr_t>(X) % 16 == 0 && reinterpret_cast<uintptr_t>(C) % 16 == 0;
+  if (vec)
+    resolve_candidates_kernel<true><<<152 * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
+                                                            X, ldx, C, ldc, cn, d, labels, over,
+                                                            over_count, stop);
+  else
+    resolve_candidates_kernel<false><<<152 * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
+                                                             X, ldx, C, ldc, cn, d, labels, over,
+                                                             over_count, stop);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -97,26 +97,53 @@ __global__ void scan_seg_kernel(int* __restrict__ data, long long n, const int* 
   }
 }
 
+// hist[l * ntiles + tile] = members of label l in the tile. SMEM: the tile counts in shared
+// memory (k ints) and writes each nonzero count once; otherwise global atomics per warp group.
+template <bool SMEM>
 __global__ void hist_kernel(const int* __restrict__ labels, long long n, int k, int tile_pts,
                             int ntiles, int* __restrict__ hist, int* err, const int* stop) {
   if (stopped(stop)) return;
+  extern __shared__ int cnt_s[];
   const int tile = blockIdx.x;
   const long long i0 = (long long)tile * tile_pts;
   const long long i1 = min(n, i0 + tile_pts);
   const int lane = threadIdx.x & 31;
-  for (long long b = i0; b < i1; b += blockDim.x) {
-    const long long i = b + threadIdx.x;
-    int l = -1;
-    if (i < i1) {
-      l = labels[i];
-      if (l < 0 || l >= k) {
+  if (SMEM) {
+    for (int j = threadIdx.x; j < k; j += blockDim.x) cnt_s[j] = 0;
+    __syncthreads();
+  }
+  const int nbits = label_bits(k);
+  constexpr int U = 8;  // labels loaded ahead per thread: one memory round trip per U steps
+  for (long long b = i0; b < i1; b += (long long)blockDim.x * U) {
+    int lv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long i = b + (long long)u * blockDim.x + threadIdx.x;
+      lv[u] = i < i1 ? __ldg(labels + i) : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      int l = lv[u];
+      const long long i = b + (long long)u * blockDim.x + threadIdx.x;
+      if (i < i1 && (l < 0 || l >= k)) {
         set_error(err, KMGB_DEV_BAD_LABEL);
         l = -1;
       }
+      if (SMEM) {
+        if (l >= 0) atomicAdd(&cnt_s[l], 1);
+      } else {
+        const unsigned peers = warp_peers(l, nbits);
+        if (l >= 0 && lane == __ffs(peers) - 1)
+          atomicAdd(&hist[(size_t)l * ntiles + tile], __popc(peers));
+      }
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, l);
-    const int leader = __ffs(peers) - 1;
-    if (l >= 0 && lane == leader) atomicAdd(&hist[(size_t)l * ntiles + tile], __popc(peers));
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+      const int c = cnt_s[j];
+      if (c) hist[(size_t)j * ntiles + tile] = c;
+    }
   }
 }
 
@@ -155,26 +182,85 @@ __global__ void scatter_kernel(const int* __restrict__ labels, long long n, int 
   volatile int* vpos = pos;
   const long long i0 = (long long)tile * tile_pts;
   const long long i1 = min(n, i0 + tile_pts);
-  for (long long b = i0; b < i1; b += 32) {
-    const long long i = b + lane;
-    int l = -1;
-    if (i < i1) {
-      l = labels[i];
-      if (l < 0 || l >= k) l = -1;
+  const int nbits = label_bits(k);
+  constexpr int U = 8;  // labels loaded ahead: one memory round trip per U steps of 32 points
+  for (long long b = i0; b < i1; b += 32 * U) {
+    int lv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long i = b + 32 * u + lane;
+      lv[u] = i < i1 ? __ldg(labels + i) : -1;
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, l);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const long long i = b + 32 * u + lane;
+      int l = lv[u];
+      if (l < 0 || l >= k) l = -1;
+      const unsigned peers = warp_peers(l, nbits);
+      const int leader = __ffs(peers) - 1;
+      const int rank = __popc(peers & lanemask_lt());
+      int base = 0;
+      if (l >= 0 && lane == leader)
+        base = SMEM ? cnt_s[l] : vpos[(size_t)l * ntiles + tile];
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (l >= 0) sorted[base + rank] = (int)i;
+      if (l >= 0 && lane == leader) {
+        const int nv = base + __popc(peers);
+        if (SMEM) cnt_s[l] = nv;
+        else vpos[(size_t)l * ntiles + tile] = nv;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Stable scatter of one tile by kScatterWarps warps: warp w takes the w-th slice of the tile's
+// rows, counts its labels in shared memory, an exclusive scan over the warps (label by label,
+// from the tile's start positions) gives every warp its own first positions, and the warps then
+// place their rows in parallel. Same positions as one warp walking the tile in order.
+constexpr int kScatterWarps = 8;
+
+__global__ void scatter_multi_kernel(const int* __restrict__ labels, long long n, int k,
+                                     int tile_pts, int ntiles, const int* __restrict__ pos,
+                                     int* __restrict__ sorted, const int* stop) {
+  if (stopped(stop)) return;
+  extern __shared__ int wcnt[];  // [kScatterWarps][k]
+  const int tile = blockIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long i0 = (long long)tile * tile_pts;
+  const long long i1 = min(n, i0 + tile_pts);
+  const long long span = ((i1 - i0 + kScatterWarps - 1) / kScatterWarps + 31) / 32 * 32;
+  const long long s0 = min(i1, i0 + w * span), s1 = min(i1, s0 + span);
+  int* mine = wcnt + (size_t)w * k;
+  for (int j = threadIdx.x; j < kScatterWarps * k; j += blockDim.x) wcnt[j] = 0;
+  __syncthreads();
+  for (long long i = s0 + lane; i < s1; i += 32) {
+    const int l = __ldg(labels + i);
+    if (l >= 0 && l < k) atomicAdd(&mine[l], 1);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    int run = pos[(size_t)j * ntiles + tile];
+    for (int v = 0; v < kScatterWarps; ++v) {
+      const int c = wcnt[(size_t)v * k + j];
+      wcnt[(size_t)v * k + j] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  const int nbits = label_bits(k);
+  for (long long b = s0; b < s1; b += 32) {
+    const long long i = b + lane;
+    int l = i < s1 ? __ldg(labels + i) : -1;
+    if (l < 0 || l >= k) l = -1;
+    const unsigned peers = warp_peers(l, nbits);
     const int leader = __ffs(peers) - 1;
     const int rank = __popc(peers & lanemask_lt());
     int base = 0;
-    if (l >= 0 && lane == leader)
-      base = SMEM ? cnt_s[l] : vpos[(size_t)l * ntiles + tile];
+    if (l >= 0 && lane == leader) base = mine[l];
     base = __shfl_sync(0xffffffffu, base, leader);
     if (l >= 0) sorted[base + rank] = (int)i;
-    if (l >= 0 && lane == leader) {
-      const int nv = base + __popc(peers);
-      if (SMEM) cnt_s[l] = nv;
-      else vpos[(size_t)l * ntiles + tile] = nv;
-    }
+    if (l >= 0 && lane == leader) mine[l] = base + __popc(peers);
     __syncwarp();
   }
 }
@@ -482,10 +568,12 @@ cudaError_t excl_scan(int* data, long long n, int* tmp, cudaStream_t s, const in
 
 }  // namespace
 
-// Tile size of the label histogram: keeps K x T below ~16M entries (one scan of <= 64 MB).
+// Tile size of the label histogram: at least 4096 points (the histogram, its scan and the
+// scatter's strided counter loads scale with K x T), and K x T below ~16M entries (one scan of
+// <= 64 MB).
 void plan_update_tiles(long long n, int k, int* tile_pts, int* ntiles) {
   const long long per = (n * (long long)k + (16LL << 20) - 1) / (16LL << 20);
-  long long tp = per < 1024 ? 1024 : (per + 31) / 32 * 32;
+  long long tp = per < 4096 ? 4096 : (per + 31) / 32 * 32;
   if (tp > (1LL << 30)) tp = 1LL << 30;
   *tile_pts = (int)tp;
   *ntiles = (int)((n + tp - 1) / tp);
@@ -501,15 +589,39 @@ static cudaError_t sort_by_label(const int* labels, const UpdateWork& w, cudaStr
   const int k = w.k;
   const long long hist_elems = (long long)k * w.ntiles;
   KMGB_CUDA_TRY(cudaMemsetAsync(w.hist, 0, sizeof(int) * hist_elems, s));
-  hist_kernel<<<w.ntiles, 256, 0, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist, w.err, w.stop); kmgb::count_launches(1);
+  const size_t smem = sizeof(int) * (size_t)k;
+  if (smem <= 96 * 1024) {
+    static int hist_attr_k = -1;
+    if (smem > 48 * 1024 && hist_attr_k < k) {
+      KMGB_CUDA_TRY(cudaFuncSetAttribute(hist_kernel<true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+      hist_attr_k = k;
+    }
+    hist_kernel<true><<<w.ntiles, 256, smem, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist, w.err,
+                                                  w.stop);
+  } else {
+    hist_kernel<false><<<w.ntiles, 256, 0, s>>>(labels, n, k, w.tile_pts, w.ntiles, w.hist, w.err,
+                                                w.stop);
+  }
+  kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   KMGB_CUDA_TRY(excl_scan(w.hist, hist_elems, w.scan_tmp, s, w.stop));
   label_offsets_kernel<<<(k + 1 + 255) / 256, 256, 0, s>>>(w.hist, n, k, w.ntiles, w.label_off,
                                                           w.piece_cnt, w.counts, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
   KMGB_CUDA_TRY(excl_scan(w.piece_cnt, k + 1, w.scan_tmp, s, w.stop));
-  const size_t smem = sizeof(int) * (size_t)k;
-  if (smem <= 96 * 1024) {
+  const size_t msmem = sizeof(int) * (size_t)k * kScatterWarps;
+  if (msmem <= 96 * 1024) {
+    static int multi_attr_k = -1;
+    if (msmem > 48 * 1024 && multi_attr_k < k) {
+      KMGB_CUDA_TRY(cudaFuncSetAttribute(scatter_multi_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
+      multi_attr_k = k;
+    }
+    scatter_multi_kernel<<<w.ntiles, 32 * kScatterWarps, msmem, s>>>(
+        labels, n, k, w.tile_pts, w.ntiles, w.hist, w.sorted, w.stop);
+    kmgb::count_launches(1);
+  } else if (smem <= 96 * 1024) {
     static int attr_k = -1;
     if (smem > 48 * 1024 && attr_k < k) {
       KMGB_CUDA_TRY(cudaFuncSetAttribute(scatter_kernel<true>,
@@ -746,6 +858,7 @@ __global__ void hist_batched_kernel(const int* __restrict__ labels, BatchUpdate 
   const int cb = b.c_off[prob], kp = b.k[prob], nt = b.ntiles[prob];
   int* h = hist + b.hoff[prob];
   const int lane = threadIdx.x & 31;
+  const int nbits = label_bits(kp);
   for (long long base = i0; base < i1; base += blockDim.x) {
     const long long i = base + threadIdx.x;
     int l = -1;
@@ -756,7 +869,7 @@ __global__ void hist_batched_kernel(const int* __restrict__ labels, BatchUpdate 
         l = -1;
       }
     }
-    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    const unsigned peers = warp_peers(l, nbits);
     const int leader = __ffs(peers) - 1;
     if (l >= 0 && lane == leader) atomicAdd(&h[(size_t)l * nt + tl], __popc(peers));
   }
@@ -802,6 +915,7 @@ __global__ void scatter_batched_kernel(const int* __restrict__ labels, BatchUpda
     for (int j = lane; j < kp; j += 32) cnt_s[j] = vpos[(size_t)j * nt + tl];
     __syncwarp();
   }
+  const int nbits = label_bits(kp);
   int lnext = (i0 + lane < i1) ? labels[i0 + lane] : 0;
   for (long long base = i0; base < i1; base += 32) {
     const long long i = base + lane;
@@ -811,7 +925,7 @@ __global__ void scatter_batched_kernel(const int* __restrict__ labels, BatchUpda
       if (l < 0 || l >= kp) l = -1;
     }
     if (base + 32 + lane < i1) lnext = labels[base + 32 + lane];  // next batch in flight
-    const unsigned peers = __match_any_sync(0xffffffffu, l);
+    const unsigned peers = warp_peers(l, nbits);
     const int leader = __ffs(peers) - 1;
     const int rank = __popc(peers & lanemask_lt());
     int bs = 0;
