@@ -96,6 +96,15 @@ typedef enum kmeansCudaErrorStatus {
   ERROR_COLNORMALIZE = 7
 } kmeansCudaErrorStatus;
 
+/* Replace MatMatMultF/D (KmeansCudaKernels.h:198-215, MatMatMult.cu:70-110): C = A B for
+ * row-major device matrices A (nRowsA x nColsA), B (nColsA x nColsB), C (nRowsA x nColsB), FP32
+ * / FP64 FMA accumulation over the columns of A in ascending order; asynchronous on the legacy
+ * default stream; ERROR_MATMATMULT for negative sizes or a failed launch. */
+KMGB_EXPORT kmeansCudaErrorStatus MatMatMultF(const int nRowsA, const int nColsA, const float* A,
+                                              const int nColsB, const float* B, float* C);
+KMGB_EXPORT kmeansCudaErrorStatus MatMatMultD(const int nRowsA, const int nColsA, const double* A,
+                                              const int nColsB, const double* B, double* C);
+
 /* Replaces ClosestCentersF (KmeansCudaKernels.h:238-244, ClosestCenters.cu:392-403).
  * A: nRowsA x nColsA row-major; B: nColsA x nColsB (centers are columns, K fastest);
  * CindicesFinal[m0 + i] = arg-min_j normColsOfB_squared[j] - 2 A_i.B_j, lowest j on ties,

@@ -5,7 +5,7 @@ Python mirror of the reference's interfaces (PaulMullowney/kmeans):
 * ``computeKmeansF`` / ``computeKmeansD`` -- the reference driver entry points
   (main/cpp/kmeans.hpp:102-132) with the same arguments, return codes and D x K result layout;
 * ``ClosestCentersF``, ``rowTransformMinimumF/D``, ``ClusterCentersF/D``, ``CompactnessF/D``,
-  ``rowNormalizeF/D``, ``colNormalizeF/D`` -- the per-kernel entry points
+  ``rowNormalizeF/D``, ``colNormalizeF/D``, ``MatMatMultF/D`` -- the per-kernel entry points
   (main/cuda/KmeansCudaKernels.h:198-474) on device pointers;
 * ``lloyd`` / ``Handle`` -- the extension: explicit initial centers, labels, per-iteration SSE,
   precision tier, resident data.
@@ -118,6 +118,8 @@ def lib():
             "ClusterCentersF_noalloc": (i32, [i32, i32, i32, i32, b, P, P, P, P, P, P]),
             "CompactnessF": (i32, [i32, i32, b, i32, i32, P, P, P, P]),
             "CompactnessD": (i32, [i32, i32, b, i32, i32, P, P, P, P]),
+            "MatMatMultF": (i32, [i32, i32, P, i32, P, P]),
+            "MatMatMultD": (i32, [i32, i32, P, i32, P, P]),
             "rowNormalizeF": (i32, [i32, i32, i32, P, P]),
             "rowNormalizeD": (i32, [i32, i32, i32, P, P]),
             "colNormalizeF": (i32, [i32, i32, P, P]),
@@ -319,6 +321,14 @@ def CompactnessF(m0, m, lastTile, n, k, data, indices, centers, compactness) -> 
 def CompactnessD(m0, m, lastTile, n, k, data, indices, centers, compactness) -> int:
     return int(lib().CompactnessD(m0, m, bool(lastTile), n, k, _ptr(data), _ptr(indices),
                                   _ptr(centers), _ptr(compactness)))
+
+
+def MatMatMultF(nRowsA, nColsA, A, nColsB, B, C) -> int:
+    return int(lib().MatMatMultF(nRowsA, nColsA, _ptr(A), nColsB, _ptr(B), _ptr(C)))
+
+
+def MatMatMultD(nRowsA, nColsA, A, nColsB, B, C) -> int:
+    return int(lib().MatMatMultD(nRowsA, nColsA, _ptr(A), nColsB, _ptr(B), _ptr(C)))
 
 
 def rowNormalizeF(m0, m, n, inp, out) -> int:

@@ -192,6 +192,76 @@ __global__ void col_norm_kernel(int m, int n, const T* __restrict__ in, T* __res
   }
 }
 
+// C = A B for row-major A (ra x ca), B (ca x cb) and C (ra x cb): 64 x 64 outputs per block of
+// 256 threads (4 x 4 per thread), k in steps of 16 through shared memory; each output is one FMA
+// chain over k in ascending order. Row tiles beyond the grid's y extent are taken in turn.
+template <typename T>
+__global__ void matmul_kernel(int ra, int ca, int cb, const T* __restrict__ A,
+                              const T* __restrict__ B, T* __restrict__ C) {
+  constexpr int TM = 64, TN = 64, TK = 16;
+  __shared__ T As[TK][TM + 1];
+  __shared__ T Bs[TK][TN];
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  const long long c0 = (long long)blockIdx.x * TN;
+  const long long row_tiles = ((long long)ra + TM - 1) / TM;
+  for (long long rt = blockIdx.y; rt < row_tiles; rt += gridDim.y) {
+    const long long r0 = rt * TM;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+    for (int k0 = 0; k0 < ca; k0 += TK) {
+      for (int e = threadIdx.x; e < TM * TK; e += blockDim.x) {
+        const int rr = e / TK, kk = e % TK;
+        const long long r = r0 + rr;
+        As[kk][rr] = (r < ra && k0 + kk < ca) ? A[r * ca + k0 + kk] : T(0);
+      }
+      for (int e = threadIdx.x; e < TK * TN; e += blockDim.x) {
+        const int kk = e / TN, cc = e % TN;
+        const long long c = c0 + cc;
+        Bs[kk][cc] = (k0 + kk < ca && c < cb) ? B[(long long)(k0 + kk) * cb + c] : T(0);
+      }
+      __syncthreads();
+      const int kn = min(TK, ca - k0);
+      for (int kk = 0; kk < kn; ++kk) {
+        T a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const long long r = r0 + ty + 16 * i;
+      if (r >= ra) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const long long c = c0 + tx + 16 * j;
+        if (c < cb) C[r * cb + c] = acc[i][j];
+      }
+    }
+  }
+}
+
+template <typename T>
+kmeansCudaErrorStatus mat_mat_mult(int ra, int ca, const T* A, int cb, const T* B, T* C) {
+  if (ra < 0 || ca < 0 || cb < 0) return ERROR_MATMATMULT;
+  if (ra == 0 || cb == 0) return NO_ERROR;
+  if (!C || (ca > 0 && (!A || !B))) return ERROR_MATMATMULT;
+  const long long col_tiles = ((long long)cb + 63) / 64, row_tiles = ((long long)ra + 63) / 64;
+  const dim3 grid((unsigned)col_tiles, (unsigned)(row_tiles < 65535 ? row_tiles : 65535));
+  matmul_kernel<T><<<grid, 256, 0, kDefault>>>(ra, ca, cb, A, B, C);
+  kmgb::count_launches(1);
+  return cudaGetLastError() ? ERROR_MATMATMULT : NO_ERROR;
+}
+
 template <typename T>
 kmeansCudaErrorStatus cluster_centers(int m0, int m, int n, int k, bool lastTile, const T* data,
                                       const int* indices, T* centers_large, int* counts_large,
@@ -418,6 +488,16 @@ kmeansCudaErrorStatus CompactnessD(const int m0, const int m, const bool lastTil
                                    const int k, const double* data, const int* indices,
                                    const double* centers, double* compactness_out) {
   return compactness<double>(m0, m, lastTile, n, k, data, indices, centers, compactness_out);
+}
+
+kmeansCudaErrorStatus MatMatMultF(const int nRowsA, const int nColsA, const float* A,
+                                  const int nColsB, const float* B, float* C) {
+  return mat_mat_mult<float>(nRowsA, nColsA, A, nColsB, B, C);
+}
+
+kmeansCudaErrorStatus MatMatMultD(const int nRowsA, const int nColsA, const double* A,
+                                  const int nColsB, const double* B, double* C) {
+  return mat_mat_mult<double>(nRowsA, nColsA, A, nColsB, B, C);
 }
 
 kmeansCudaErrorStatus rowNormalizeF(const int m0, const int m, const int n, const float* input,

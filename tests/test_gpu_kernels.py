@@ -179,3 +179,45 @@ def test_row_col_normalize(km, torch_cuda, dtype):
     rt = 1e-6 if dtype == np.float32 else 1e-13
     np.testing.assert_allclose(out.cpu().numpy()[4:], (A.astype(np.float64) ** 2).sum(1), rtol=rt)
     np.testing.assert_allclose(cout.cpu().numpy(), (A.astype(np.float64) ** 2).sum(0), rtol=rt)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("ra,ca,cb", [(1, 1, 1), (130, 77, 65), (1000, 128, 1024), (64, 0, 5),
+                                      (5, 300, 3)])
+def test_mat_mat_mult(km, torch_cuda, dtype, ra, ca, cb):
+    """MatMatMultF/D (MatMatMult.cu:70-110): C = A B, row-major. The reference's own test
+    (test/cpp/MatMultTests.cpp:85-107) compares against cuBLAS; here against FP64 (exact sums
+    for the FP64 entry, via math.fsum on a sample) within the FMA chain's bound."""
+    torch = torch_cuda
+    rng = np.random.default_rng(ra * 7 + ca * 3 + cb)
+    A = rng.standard_normal((ra, ca)).astype(dtype)
+    B = rng.standard_normal((ca, cb)).astype(dtype)
+    tdt = torch.float32 if dtype == np.float32 else torch.float64
+    C = torch.full((ra, cb), 7.0, dtype=tdt, device="cuda")
+    f = km.MatMatMultF if dtype == np.float32 else km.MatMatMultD
+    assert f(ra, ca, dev(torch, A) if ca else None, cb, dev(torch, B) if ca else None, C) == 0
+    torch.cuda.synchronize()
+    got = C.cpu().numpy().astype(np.float64)
+    if ca == 0:
+        assert (got == 0).all()
+        return
+    eps = 2.0 ** -24 if dtype == np.float32 else 2.0 ** -53
+    mag = np.abs(A.astype(np.float64)) @ np.abs(B.astype(np.float64))
+    bound = 1.01 * (ca + 1) * eps * mag
+    if dtype == np.float32:
+        exact = A.astype(np.float64) @ B.astype(np.float64)  # FP64 error << the FP32 bound
+        assert np.all(np.abs(got - exact) <= bound)
+    else:
+        import math
+        rr = rng.integers(0, ra, 40)
+        cc = rng.integers(0, cb, 40)
+        for r, c in zip(rr, cc):
+            exact = math.fsum(float(A[r, t]) * float(B[t, c]) for t in range(ca))
+            # the products themselves are exact only in the FP64 sum's own rounding: one more eps
+            assert abs(got[r, c] - exact) <= bound[r, c] + eps * mag[r, c]
+
+
+def test_mat_mat_mult_rejects_negative_sizes(km, torch_cuda):
+    out = torch_cuda.zeros(4, device="cuda")
+    assert km.MatMatMultF(-1, 2, None, 2, None, out) == 1  # ERROR_MATMATMULT
+    assert km.MatMatMultD(2, 2, None, -3, None, out) == 1
