@@ -64,7 +64,9 @@ KMGB_EXPORT const char* kmeansGetErrorString(kmeansErrorStatus err);
  * reference). initAlgorithm 1 (an extension) draws k-means++ centers with seeds 0 ..
  * numRetries-1 and keeps the run with the lowest final SSE; result then receives that run's
  * initial centers before its final ones. doFullSGEMM (0/1/2) and matrixFormat (0/1) are accepted and
- * all map to the same fused assignment. miniBatchFraction < 1 selects the reference's
+ * all map to the same fused assignment: the split BF16 tensor-core tier when n <= 256, the FP32
+ * tier above (the labels are the certified FP64 arg-min in both; the environment variable
+ * KMGB_ASSIGN=fp32|bf16|bf16x3 picks a tier). miniBatchFraction < 1 selects the reference's
  * sliding mini-batch windows. Returns KMEANS_NONCONVERGENCE (13) when the relative SSE change
  * is still above `criterion` after maxIters iterations (criterion < 0 always runs maxIters). */
 KMGB_EXPORT kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, const int k,

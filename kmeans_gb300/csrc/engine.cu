@@ -1437,8 +1437,15 @@ kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, co
   if (k > m) return KMEANS_ERROR_INITIALIZE;
   kmgb_options o;
   kmgb_default_options(&o);
-  const char* tier = std::getenv("KMGB_ASSIGN");
-  if (tier && std::strcmp(tier, "bf16") == 0 && bf16_tc_supported(n)) o.assign_tier = KMGB_ASSIGN_BF16;
+  // Every tier gives the certified FP64 arg-min; the split BF16 tier is the fastest where the
+  // dimension fits (D <= 256), FP32 otherwise. KMGB_ASSIGN=fp32|bf16|bf16x3 picks one.
+  o.assign_tier = bf16_tc_supported(n, 2) ? KMGB_ASSIGN_BF16X3 : KMGB_ASSIGN_FP32;
+  if (const char* tier = std::getenv("KMGB_ASSIGN")) {
+    if (std::strcmp(tier, "fp32") == 0) o.assign_tier = KMGB_ASSIGN_FP32;
+    else if (std::strcmp(tier, "bf16") == 0 && bf16_tc_supported(n)) o.assign_tier = KMGB_ASSIGN_BF16;
+    else if (std::strcmp(tier, "bf16x3") == 0 && bf16_tc_supported(n, 2))
+      o.assign_tier = KMGB_ASSIGN_BF16X3;
+  }
   o.max_iters = maxIters < 0 ? 0 : maxIters;
   o.criterion = criterion;
   o.mini_batch_fraction = miniBatchFraction;

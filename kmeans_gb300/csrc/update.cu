@@ -474,12 +474,17 @@ __global__ void finalize_kernel(const double* __restrict__ part, const double* _
     C[(size_t)j * ldc + c] = mu;
   }
   for (int o = 16; o > 0; o >>= 1) sse += __shfl_xor_sync(0xffffffffu, sse, o);
-  if (lane == 0 && sse_k) {
-    double q = 0.0;
-    if (g == 0 && partq && n > 0)
-      for (int pp = p0; pp < p1; ++pp) q += partq[pp];
-    sse_k[(size_t)j * groups + g] = (n > 0) ? sse + q : 0.0;
+  // the members' sum of ||x||^2, in piece order: the warp loads 32 pieces at a time, every
+  // lane adds them in order from shuffles
+  double q = 0.0;
+  if (g == 0 && partq && n > 0 && sse_k) {
+    for (int b = p0; b < p1; b += 32) {
+      const int cnt = min(32, p1 - b);
+      const double v = lane < cnt ? __ldg(partq + b + lane) : 0.0;
+      for (int i = 0; i < cnt; ++i) q += __shfl_sync(0xffffffffu, v, i);
+    }
   }
+  if (lane == 0 && sse_k) sse_k[(size_t)j * groups + g] = (n > 0) ? sse + q : 0.0;
 }
 
 // Clusters whose identity SSE (Q - 2 mu.S + n |mu|^2, summed over the groups) is within

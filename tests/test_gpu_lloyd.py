@@ -322,3 +322,58 @@ def test_memory_pool_reuses_and_releases_handle_memory(km, torch_cuda):
     assert abs(free3 - free0) < 64 * mib, (free0, free3)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert np.array_equal(a[2], b[2])
+
+
+# The reference's own test configurations: test/cpp/KmeansTests.cpp:52-60 (mat-sift, 898,790 x
+# 128, K=256, 50 iterations, rtol 1e-5, custom kernels, full batch), test/python/kmeansSIFT.py:2-3
+# (K=1024) and kmeansHOG.py:2-3 (mat-hog, 796,160 x 324, K=1024), each run with useCUBLAS 0 and 1.
+# The SIFT/HOG matrices are not shipped; seeded stand-ins with their shapes and value ranges
+# replace them: SIFT descriptors are integers in [0, 255] (so every x is a BF16 number and the
+# split tier runs its two-product mode), HOG features FP32 in [0, 1].
+REFERENCE_TEST_CONFIGS = [
+    ("sift", 898_790, 128, 256, 50),
+    ("sift", 898_790, 128, 1024, 50),
+    ("hog", 796_160, 324, 1024, 50),
+]
+
+
+def reference_test_data(kind, m, n):
+    if kind == "sift":
+        X, _, _ = mixture_numpy(m, n, 300, seed=11, mean_lo=0.0, mean_hi=120.0, std=(2.0, 25.0))
+        return np.clip(np.rint(X), 0, 255).astype(np.float32)
+    X, _, _ = mixture_numpy(m, n, 300, seed=12, mean_lo=0.0, mean_hi=0.5, std=(0.01, 0.1))
+    return np.clip(X, 0.0, 1.0).astype(np.float32)
+
+
+@pytest.mark.parametrize("kind,m,n,k,iters", REFERENCE_TEST_CONFIGS)
+def test_reference_test_configurations(km, orc, torch_cuda, kind, m, n, k, iters):
+    """computeKmeansF with the reference test's arguments returns the centers of the certified
+    loop; its last iteration is pinned to the oracle: labels from the centers one iteration
+    earlier on a row sample, the canonical update of all rows bit for bit, the SSE."""
+    X = reference_test_data(kind, m, n)
+    rtol = 1e-5
+    result = np.zeros(n * k, np.float32)
+    rc = km.computeKmeansF(X, m, n, k, rtol, iters, 1, 0, 0, 0, result, 1.0)
+    assert rc in (0, 13), km.kmeansGetErrorString(rc)
+    result_cublas = np.zeros_like(result)
+    assert km.computeKmeansF(X, m, n, k, rtol, iters, 1, 0, 1, 0, result_cublas, 1.0) == rc
+    assert np.array_equal(result_cublas, result, equal_nan=True)
+
+    # computeKmeansF runs the split BF16 tier where D <= 256, FP32 above; the labels (and so the
+    # centers) are the certified FP64 arg-min's in either
+    tier = km.ASSIGN_BF16X3 if n <= 256 else km.ASSIGN_FP32
+    full = km.lloyd(X, k, max_iters=iters, criterion=rtol, assign_tier=tier)
+    t = full.iterations
+    assert full.status == rc
+    assert np.array_equal(result.reshape(n, k), full.centers.T, equal_nan=True)  # D x K
+    assert t >= 2
+    prev = km.lloyd(X, k, max_iters=t - 1, criterion=rtol, assign_tier=tier)
+    assert prev.iterations == t - 1
+    rows = np.random.default_rng(5).choice(m, 16384, replace=False)
+    assert np.array_equal(orc.assign(X[rows], prev.centers), full.labels[rows])
+    newc, _, _ = orc.update(X, full.labels, k)
+    assert np.array_equal(newc, full.centers, equal_nan=True)
+    s = orc.sse(X, full.labels, full.centers)
+    assert abs(full.sse[-1] - s) <= 1e-10 * s
+    print(f"{kind} {m}x{n} K={k}: {t} iterations (rc {rc}), SSE {s:.6e}, "
+          f"re-ranked {full.reranked} points")
