@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <future>
 #include <random>
 #include <string>
 #include <vector>
@@ -446,7 +447,40 @@ cudaError_t order_after_default_stream(kmgb_handle* h) {
 }
 
 // Upload (or copy) the data set and compute its per-point norms and BF16 copy.
-int set_data(kmgb_handle* h, const float* X, bool on_device) {
+// The reference's shuffle permutation and initial picks (kmeans.cpp:554-557, 876-883). They do
+// not depend on the data, and std::shuffle over m indices is sequential (~20 ms at m = 4M), so
+// one-shot calls compute them on a host thread while the data set is uploaded.
+struct RefInit {
+  std::vector<int> perm, picks;
+  bool picks_ok = false;
+};
+
+std::shared_future<RefInit> start_reference_init(long long m, int k) {
+  auto task = [m, k] {
+    RefInit r;
+    r.picks_ok = reference_picks((int)m, k, r.picks);
+    reference_perm((int)m, r.perm);
+    return r;
+  };
+  try {
+    return std::async(std::launch::async, task).share();
+  } catch (...) {  // no thread to be had: run it when the result is asked for
+    return std::async(std::launch::deferred, task).share();
+  }
+}
+
+// The finished RefInit, or nullptr if its task threw (nothing may cross the C boundary).
+const RefInit* ref_result(std::shared_future<RefInit>& f) {
+  try {
+    return &f.get();
+  } catch (...) {
+    return nullptr;
+  }
+}
+
+// ref: the permutation for mini-batch windows from start_reference_init (else computed here).
+int set_data(kmgb_handle* h, const float* X, bool on_device,
+             std::shared_future<RefInit>* ref = nullptr) {
   const int code = KMEANS_ERROR_BUILDDATA;
   if (h->streaming) {
     if (on_device) {
@@ -527,12 +561,22 @@ int set_data(kmgb_handle* h, const float* X, bool on_device) {
     }
   }
   if (h->mini) {
-    std::vector<int> perm;
-    reference_perm((int)h->n, perm);
-    KM_TRY(cudaMemcpyAsync(h->perm, perm.data(), sizeof(int) * h->n, cudaMemcpyHostToDevice,
+    std::vector<int> own;
+    const std::vector<int>* perm = &own;
+    if (ref) {
+      const RefInit* r = ref_result(*ref);
+      if (!r) {
+        set_err("kmgb_set_data: the shuffle permutation could not be computed");
+        return code;
+      }
+      perm = &r->perm;
+    } else {
+      reference_perm((int)h->n, own);
+    }
+    KM_TRY(cudaMemcpyAsync(h->perm, perm->data(), sizeof(int) * h->n, cudaMemcpyHostToDevice,
                            h->stream),
            code);
-    KM_TRY(cudaStreamSynchronize(h->stream), code);  // perm is a stack buffer
+    KM_TRY(cudaStreamSynchronize(h->stream), code);  // perm is a host buffer
   }
   h->have_data = true;
   h->iter_base = 0;
@@ -946,16 +990,18 @@ int finish(kmgb_handle* h) {
   return 0;
 }
 
-int reference_init_host(kmgb_handle* h, const float* data_host, std::vector<float>& init_kxd) {
-  std::vector<int> perm, picks;
-  if (!reference_picks((int)h->n, h->k, picks)) {
-    set_err("reference initialisation needs 0 < k <= m");
+// Initial centers = shuffled rows picks[i] (kmeans.cpp:886-888), from start_reference_init.
+int reference_init_host(kmgb_handle* h, const float* data_host, std::shared_future<RefInit>& ref,
+                        std::vector<float>& init_kxd) {
+  const RefInit* r = ref_result(ref);
+  if (!r || !r->picks_ok) {
+    set_err(r ? "reference initialisation needs 0 < k <= m"
+              : "reference initialisation: the shuffle permutation could not be computed");
     return KMEANS_ERROR_INITIALIZE;
   }
-  reference_perm((int)h->n, perm);
   init_kxd.resize((size_t)h->k * h->d);
   for (int i = 0; i < h->k; ++i)
-    std::memcpy(&init_kxd[(size_t)i * h->d], data_host + (size_t)perm[picks[i]] * h->d,
+    std::memcpy(&init_kxd[(size_t)i * h->d], data_host + (size_t)r->perm[r->picks[i]] * h->d,
                 sizeof(float) * h->d);
   return 0;
 }
@@ -1378,7 +1424,10 @@ int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
   if (rc) return rc;
   const bool x_dev = is_device_ptr(X);
   const bool kpp = !init && o.init_algorithm == KMGB_INIT_KMEANSPP;
-  rc = set_data(h, X, x_dev);
+  const bool host_ref_init = !init && !kpp && !x_dev;
+  std::shared_future<RefInit> ref;
+  if (host_ref_init || (h->mini && !h->streaming)) ref = start_reference_init(n, k);
+  rc = set_data(h, X, x_dev, ref.valid() ? &ref : nullptr);
   if (!rc) {
     if (init) {
       rc = set_centers(h, init, is_device_ptr(init));
@@ -1386,7 +1435,7 @@ int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
       rc = run_kmeanspp_retries(h, o, nullptr);
     } else if (!x_dev) {
       std::vector<float> ini;
-      rc = reference_init_host(h, X, ini);
+      rc = reference_init_host(h, X, ref, ini);
       if (!rc) rc = set_centers(h, ini.data(), false);
     } else {
       rc = kmgb_set_centers(h, nullptr, 0);
@@ -1452,15 +1501,17 @@ kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, co
   kmgb_handle* h = nullptr;
   int rc = create_handle(&h, m, n, k, &o);
   if (rc) return (kmeansErrorStatus)rc;
-  rc = set_data(h, data, false);
-  std::vector<float> init((size_t)k * n);
   const bool kpp = initAlgorithm == KMGB_INIT_KMEANSPP;  // the reference ignores numRetries
+  std::shared_future<RefInit> ref;
+  if (!kpp || h->mini) ref = start_reference_init(m, k);
+  rc = set_data(h, data, false, ref.valid() ? &ref : nullptr);
+  std::vector<float> init((size_t)k * n);
   if (kpp) {
     o.num_retries = numRetries;
     o.seed = 0;
     if (!rc) rc = run_kmeanspp_retries(h, o, init.data());
   } else if (!rc) {
-    rc = reference_init_host(h, data, init);
+    rc = reference_init_host(h, data, ref, init);
     if (!rc) rc = set_centers(h, init.data(), false);
   }
   if (!rc) {
