@@ -432,6 +432,114 @@ __global__ void piece_sums_vec4_kernel(const float* __restrict__ X, long long ld
   }
 }
 
+// Small D (a multiple of 4, at most 64): L lanes per piece, each owning 4 consecutive
+// dimensions, 32/L pieces per warp. Each lane group walks its own piece's rows in order, so every
+// (piece, dimension) float-float sum is the same sequence of additions as in the
+// one-piece-per-warp kernel, and the whole warp computes each piece's sum of ||x||^2 with that
+// kernel's 32-lane tree; the results are identical, with 32/L times the rows in flight.
+template <int L>
+__global__ void piece_sums_small_kernel(const float* __restrict__ X, long long ldx,
+                                        const double* __restrict__ qn, const int* __restrict__ sorted,
+                                        const int* __restrict__ label_off,
+                                        const int* __restrict__ pstart, int k, int d,
+                                        double* __restrict__ part, double* __restrict__ partq,
+                                        const int* stop) {
+  if (stopped(stop)) return;
+  constexpr int G = 32 / L;
+  const int ptot = pstart[k];
+  const int lane = threadIdx.x & 31, grp = lane / L, sub = lane % L;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long p0 = gw * G; p0 < ptot; p0 += nw * G) {
+    const long long p = p0 + grp;
+    const bool live = p < ptot;
+    int b = 0, e = 0;
+    if (live) {
+      const int j = find_label(pstart, k, (int)p);
+      b = label_off[j] + ((int)p - pstart[j]) * kSumPiece;
+      e = min(b + kSumPiece, label_off[j + 1]);
+    }
+    if (qn) {  // the members' sum of ||x||^2, piece by piece, as the one-piece-per-warp kernel
+      for (int g = 0; g < G; ++g) {
+        const int bg = __shfl_sync(0xffffffffu, b, g * L);
+        const int eg = __shfl_sync(0xffffffffu, e, g * L);
+        if (p0 + g >= ptot) break;
+        double qs = 0.0;
+        for (int t0 = bg; t0 < eg; t0 += 32) {
+          const int nt = min(32, eg - t0);
+          double qv = lane < nt ? __ldg(qn + __ldg(sorted + t0 + lane)) : 0.0;
+          for (int o = 16; o > 0; o >>= 1) qv += __shfl_xor_sync(0xffffffffu, qv, o);
+          qs += qv;
+        }
+        if (lane == 0 && partq) partq[p0 + g] = qs;
+      }
+    } else if (partq && lane < G && p0 + lane < ptot) {
+      partq[p0 + lane] = 0.0;
+    }
+    const int c = 4 * sub;
+    const bool on = live && c < d;
+    const int n = e - b;
+    PieceAcc<float> a0, a1, a2, a3;
+    for (int t = 0; t < n; t += 8) {  // eight rows in flight per lane group
+      int idx[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) idx[r] = t + r < n ? __ldg(sorted + b + t + r) : -1;
+      float4 v[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+        v[r] = (on && idx[r] >= 0)
+                   ? __ldg(reinterpret_cast<const float4*>(X + (size_t)idx[r] * ldx + c))
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        if (t + r < n) {
+          a0.add(v[r].x);
+          a1.add(v[r].y);
+          a2.add(v[r].z);
+          a3.add(v[r].w);
+        }
+      }
+    }
+    if (on) {
+      double* o = part + (size_t)p * d + c;
+      o[0] = a0.value();
+      o[1] = a1.value();
+      o[2] = a2.value();
+      o[3] = a3.value();
+    }
+  }
+}
+
+// Canonical piece sums of FP32 rows: the small-D kernel where D <= 64, the float4 kernel for other
+// 16-byte-aligned rows, the scalar kernel otherwise.
+cudaError_t launch_piece_sums_f32(const float* X, long long ldx, const double* qn,
+                                  const int* sorted, const int* label_off, const int* pstart, int k,
+                                  int d, double* part, double* partq, const int* stop,
+                                  long long max_pieces, cudaStream_t s) {
+  const bool vec = ldx % 4 == 0 && d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  const int lanes = !vec || d > 64 ? 32 : (d <= 16 ? 4 : (d <= 32 ? 8 : 16));
+  long long warps = (max_pieces + 32 / lanes - 1) / (32 / lanes);
+  if (warps > 152LL * 64) warps = 152LL * 64;
+  const unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
+  if (vec && lanes == 4)
+    piece_sums_small_kernel<4><<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k, d,
+                                                      part, partq, stop);
+  else if (vec && lanes == 8)
+    piece_sums_small_kernel<8><<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k, d,
+                                                      part, partq, stop);
+  else if (vec && lanes == 16)
+    piece_sums_small_kernel<16><<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k,
+                                                       d, part, partq, stop);
+  else if (vec)
+    piece_sums_vec4_kernel<<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k, d,
+                                                  part, partq, stop);
+  else
+    piece_sums_kernel<float><<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k, d,
+                                                    part, partq, stop);
+  kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
 // One warp per (center j, group g of 32 dimensions): lane c of group g owns dimension
 // g*32 + c, adds the center's piece sums in piece order (the canonical order: centers are
 // unchanged by the split), divides in FP64 and rounds once. The group's SSE term
@@ -648,16 +756,8 @@ cudaError_t launch_update(const float* X, const double* qn, const int* labels, f
   const int k = w.k;
   if (w.n <= 0 || k <= 0) return cudaSuccess;
   KMGB_CUDA_TRY(sort_by_label(labels, w, s));
-  const long long max_pieces = w.max_pieces;
-  long long warps = max_pieces < 152LL * 64 ? max_pieces : 152LL * 64;
-  if (w.ldx % 4 == 0 && w.d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
-    piece_sums_vec4_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq, w.stop);
-  else
-    piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d, w.part, w.partq, w.stop);
-  kmgb::count_launches(1);
-  KMGB_CUDA_TRY(cudaGetLastError());
+  KMGB_CUDA_TRY(launch_piece_sums_f32(X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, k, w.d,
+                                     w.part, w.partq, w.stop, w.max_pieces, s));
   const long long fin_warps = (long long)k * ((w.d + 31) / 32);
   finalize_kernel<<<(unsigned)((fin_warps * 32 + 255) / 256), 256, 0, s>>>(
       w.part, qn ? w.partq : nullptr, w.label_off, w.piece_cnt, k, w.d, C, ldc, empty_policy,
@@ -804,15 +904,8 @@ cudaError_t launch_stream_accumulate(const float* X, long long ldx, const double
                                      int* accN, double* accQ, cudaStream_t s) {
   if (w.n <= 0 || w.k <= 0) return cudaSuccess;
   KMGB_CUDA_TRY(sort_by_label(labels, w, s));
-  long long warps = w.max_pieces < 152LL * 64 ? w.max_pieces : 152LL * 64;
-  if (w.ldx % 4 == 0 && w.d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
-    piece_sums_vec4_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, w.partq, w.stop);
-  else
-    piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-        X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, w.partq, w.stop);
-  kmgb::count_launches(1);
-  KMGB_CUDA_TRY(cudaGetLastError());
+  KMGB_CUDA_TRY(launch_piece_sums_f32(X, w.ldx, qn, w.sorted, w.label_off, w.piece_cnt, w.k, w.d,
+                                     w.part, w.partq, w.stop, w.max_pieces, s));
   accumulate_stream_kernel<<<(unsigned)(((long long)w.k * 32 + 255) / 256), 256, 0, s>>>(
       w.part, w.partq, w.label_off, w.piece_cnt, w.k, w.d, accS, accN, accQ, w.stop);
   kmgb::count_launches(1);
@@ -994,16 +1087,8 @@ cudaError_t launch_update_batched(const float* X, long long ldx, int d, const do
     scatter_batched_kernel<false><<<(unsigned)b.stiles, 32, 0, s>>>(labels, b, w.hist, w.sorted);
   count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
-  const long long max_pieces = w.max_pieces;
-  const long long warps = max_pieces < 152LL * 64 ? max_pieces : 152LL * 64;
-  if (ldx % 4 == 0 && d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0)
-    piece_sums_vec4_kernel<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-        X, ldx, qn, w.sorted, w.label_off, w.piece_cnt, b.K, d, w.part, w.partq, nullptr);
-  else
-    piece_sums_kernel<float><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
-        X, ldx, qn, w.sorted, w.label_off, w.piece_cnt, b.K, d, w.part, w.partq, nullptr);
-  count_launches(1);
-  KMGB_CUDA_TRY(cudaGetLastError());
+  KMGB_CUDA_TRY(launch_piece_sums_f32(X, ldx, qn, w.sorted, w.label_off, w.piece_cnt, b.K, d,
+                                     w.part, w.partq, nullptr, w.max_pieces, s));
   const int groups = (d + 31) / 32;
   const long long fin_warps = (long long)b.K * groups;
   finalize_kernel<<<(unsigned)((fin_warps * 32 + 255) / 256), 256, 0, s>>>(
