@@ -2,6 +2,8 @@
 FP64 oracle: labels bit-exact, centers bit-exact (canonical FP64 sums rounded once), SSE within
 1e-10 relative (the GPU evaluates each cluster's SSE as Q - 2 mu.S + n|mu|^2 in FP64, the
 oracle sums the direct form), iteration count and status equal."""
+import os
+
 import numpy as np
 import pytest
 
@@ -377,3 +379,30 @@ def test_reference_test_configurations(km, orc, torch_cuda, kind, m, n, k, iters
     assert abs(full.sse[-1] - s) <= 1e-10 * s
     print(f"{kind} {m}x{n} K={k}: {t} iterations (rc {rc}), SSE {s:.6e}, "
           f"re-ranked {full.reranked} points")
+
+
+def test_memory_pool_off_returns_memory_at_destroy(km, torch_cuda):
+    """KMGB_POOL=0 (read once per process, so in a child process): a destroyed handle's memory
+    goes back to the device without kmgb_release_cached_memory."""
+    import subprocess
+    import sys
+    code = (
+        "import torch, numpy as np, kmeans_gb300 as km\n"
+        "X = torch.randn(1_000_000, 128, device='cuda')\n"
+        "init = X[:256].cpu().numpy()\n"
+        "torch.cuda.synchronize()\n"
+        "f0 = torch.cuda.mem_get_info()[0]\n"
+        "h = km.Handle(1_000_000, 128, 256, assign_tier=km.ASSIGN_BF16X3)\n"
+        "h.set_data(X, True); h.set_centers(init); h.run(1)\n"
+        "f1 = torch.cuda.mem_get_info()[0]\n"
+        "h.close(); torch.cuda.synchronize()\n"
+        "f2 = torch.cuda.mem_get_info()[0]\n"
+        "assert f0 - f1 > 1000 * 2**20, (f0, f1)\n"
+        "assert abs(f2 - f0) < 64 * 2**20, (f0, f2)\n"
+        "print('pool off ok')\n")
+    env = dict(os.environ, KMGB_POOL="0")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env["PYTHONPATH"] = root + os.pathsep + env.get("PYTHONPATH", "")
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0 and "pool off ok" in r.stdout, r.stdout + r.stderr
