@@ -480,7 +480,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       // the point's norm bound is needed only after the last chunk: load it now so that its
       // HBM latency hides behind the unit's chunks
       const float xn_pt = (p.certify && !cand_mode && h == 0 && prow < n_rows)
-                              ? __ldg(p.xnorm + prow) : 0.0f;
+                              ? __ldg(p.xnorm + p.out0 + prow) : 0.0f;
       for (int c = 0; c < ui.nch; ++c, ++g) {
         const int b = (int)(g & 1);
         bool ok = mbar_wait(smem_u32(&bars.acc_full[b]), (uint32_t)((g >> 1) & 1), &abort_flag,
@@ -605,8 +605,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         b1 = fmaxf(b1, ob1[o]);
         b2 = nb2;
       }
-      const long long pt = prow;
-      if (pt < n_rows) {
+      const long long pt = p.out0 + prow;  // row of the data set
+      if (prow < n_rows) {
         const bool none = !(b1 > -1.0e38f);  // no usable center at all
         // no usable center at all: the first center of the point's problem
         const int label =

@@ -478,6 +478,45 @@ const RefInit* ref_result(std::shared_future<RefInit>& f) {
   }
 }
 
+// Host data go up in this many chunks (a second stream copies, the handle's stream prepares).
+constexpr long long kUploadChunks = 8;
+
+// Rows [r0, r1) of X (host or device, d floats per row) into the device copy, on stream cs.
+cudaError_t copy_rows(kmgb_handle* h, const float* X, long long r0, long long r1,
+                      cudaMemcpyKind kind, cudaStream_t cs) {
+  const size_t row_bytes = sizeof(float) * h->d;
+  if (h->ldx == h->d)
+    return cudaMemcpyAsync(h->X + (size_t)r0 * h->ldx, X + (size_t)r0 * h->d,
+                           row_bytes * (r1 - r0), kind, cs);
+  return cudaMemcpy2DAsync(h->X + (size_t)r0 * h->ldx, sizeof(float) * h->ldx,
+                           X + (size_t)r0 * h->d, row_bytes, row_bytes, r1 - r0, kind, cs);
+}
+
+// Norms and BF16 planes of rows [r0, r1), on the handle's stream.
+cudaError_t prepare_rows(kmgb_handle* h, long long r0, long long r1) {
+  const size_t xo = (size_t)r0 * h->ldx, bo = (size_t)r0 * h->ldb * 2;
+  cudaError_t r = launch_point_norms(h->X + xo, h->ldx, r1 - r0, h->d, h->qn + r0, h->xn + r0,
+                                     h->stream);
+  if (r != cudaSuccess || !h->Xb) return r;
+  return launch_to_bf16(h->X + xo, h->ldx, r1 - r0, h->d, static_cast<char*>(h->Xb) + bo,
+                        h->ldb, h->stream, nullptr,
+                        h->Xl ? static_cast<char*>(h->Xl) + bo : nullptr, h->xinexact);
+}
+
+// The copy stream and its event; the copies that follow overwrite X only after the work queued
+// on the handle's stream so far (earlier iterations, the padding memset).
+cudaError_t upload_start(kmgb_handle* h, cudaEvent_t* ev) {
+  cudaError_t r = cudaSuccess;
+  if (!h->copy_stream) r = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+  if (r == cudaSuccess && !h->ev_copied[0])
+    r = cudaEventCreateWithFlags(&h->ev_copied[0], cudaEventDisableTiming);
+  if (r != cudaSuccess) return r;
+  *ev = h->ev_copied[0];
+  r = cudaEventRecord(*ev, h->stream);
+  if (r == cudaSuccess) r = cudaStreamWaitEvent(h->copy_stream, *ev, 0);
+  return r;
+}
+
 // ref: the permutation for mini-batch windows from start_reference_init (else computed here).
 int set_data(kmgb_handle* h, const float* X, bool on_device,
              std::shared_future<RefInit>* ref = nullptr) {
@@ -499,54 +538,28 @@ int set_data(kmgb_handle* h, const float* X, bool on_device,
   }
   h->x_exact = false;
   if (h->Xb) KM_TRY(cudaMemsetAsync(h->xinexact, 0, sizeof(int), h->stream), code);
-  const size_t row_bytes = sizeof(float) * h->d;
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  // Rows [r0, r1) of X into the device copy, on stream cs.
-  auto copy_rows = [&](long long r0, long long r1, cudaStream_t cs) -> cudaError_t {
-    if (h->ldx == h->d)
-      return cudaMemcpyAsync(h->X + (size_t)r0 * h->ldx, X + (size_t)r0 * h->d,
-                             row_bytes * (r1 - r0), kind, cs);
-    return cudaMemcpy2DAsync(h->X + (size_t)r0 * h->ldx, sizeof(float) * h->ldx,
-                             X + (size_t)r0 * h->d, row_bytes, row_bytes, r1 - r0, kind, cs);
-  };
-  // Norms and BF16 planes of rows [r0, r1), on the handle's stream.
-  auto prepare_rows = [&](long long r0, long long r1) -> cudaError_t {
-    const size_t xo = (size_t)r0 * h->ldx, bo = (size_t)r0 * h->ldb * 2;
-    cudaError_t r = launch_point_norms(h->X + xo, h->ldx, r1 - r0, h->d, h->qn + r0, h->xn + r0,
-                                       h->stream);
-    if (r != cudaSuccess || !h->Xb) return r;
-    return launch_to_bf16(h->X + xo, h->ldx, r1 - r0, h->d, static_cast<char*>(h->Xb) + bo,
-                          h->ldb, h->stream, nullptr,
-                          h->Xl ? static_cast<char*>(h->Xl) + bo : nullptr, h->xinexact);
-  };
   if (h->ldx != h->d)  // the copies write d of ldx columns: the padding stays zero
     KM_TRY(cudaMemsetAsync(h->X, 0, sizeof(float) * h->ldx * h->n, h->stream), code);
-  const long long kUploadChunks = 8;
   if (!on_device && h->n >= kUploadChunks * 4096) {
-    // Host data crosses the link at ~210 GB/s on GB300 whatever the number of streams; the
+    // Host data cross the link at ~210 GB/s on GB300 whatever the number of streams; the
     // upload goes in chunks on a second stream and the handle's stream prepares each chunk
     // once it has landed, so only the last chunk's preparation follows the copy.
-    if (!h->copy_stream)
-      KM_TRY(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking), code);
-    if (!h->ev_copied[0])
-      KM_TRY(cudaEventCreateWithFlags(&h->ev_copied[0], cudaEventDisableTiming), code);
-    cudaEvent_t ev = h->ev_copied[0];
-    // the copies overwrite X only after the handle's earlier work (and the padding memset)
-    KM_TRY(cudaEventRecord(ev, h->stream), code);
-    KM_TRY(cudaStreamWaitEvent(h->copy_stream, ev, 0), code);
+    cudaEvent_t ev = nullptr;
+    KM_TRY(upload_start(h, &ev), code);
     const long long rows = (h->n + kUploadChunks - 1) / kUploadChunks;
     for (long long r0 = 0; r0 < h->n; r0 += rows) {
       const long long r1 = std::min(h->n, r0 + rows);
-      KM_TRY(copy_rows(r0, r1, h->copy_stream), code);
+      KM_TRY(copy_rows(h, X, r0, r1, kind, h->copy_stream), code);
       KM_TRY(cudaEventRecord(ev, h->copy_stream), code);
       KM_TRY(cudaStreamWaitEvent(h->stream, ev, 0), code);
-      KM_TRY(prepare_rows(r0, r1), code);
+      KM_TRY(prepare_rows(h, r0, r1), code);
     }
     // the caller may reuse its host buffer once this returns
     KM_TRY(cudaStreamSynchronize(h->copy_stream), code);
   } else {
-    KM_TRY(copy_rows(0, h->n, h->stream), code);
-    KM_TRY(prepare_rows(0, h->n), code);
+    KM_TRY(copy_rows(h, X, 0, h->n, kind, h->stream), code);
+    KM_TRY(prepare_rows(h, 0, h->n), code);
     if (!on_device) KM_TRY(cudaStreamSynchronize(h->stream), code);
   }
   if (h->Xb) {
@@ -594,8 +607,12 @@ long long window_start(long long m, long long m_mb, int it) {
   return s;
 }
 
-// One Lloyd iteration on the handle's stream; SSE lands in sse_dev[slot].
-int step(kmgb_handle* h, int slot) {
+// One Lloyd iteration on the handle's stream; SSE lands in sse_dev[slot]. upload (tensor tiers,
+// full batch): the host data set arrives during this iteration -- chunk by chunk, each copied on
+// the copy stream, then prepared and assigned on the handle's stream while the next one crosses
+// the link. Whether every x is a BF16 number is known only afterwards, so this iteration uses
+// the three-product bound, which holds for any x.
+int step(kmgb_handle* h, int slot, const float* upload = nullptr) {
   cudaStream_t s = h->stream;
   const float* Xa = h->X;
   const void* Xba = h->Xb;
@@ -644,7 +661,33 @@ int step(kmgb_handle* h, int slot) {
   a.stop = h->stop;
   a.cinit = h->cinit;
   const bool tc = h->opt.assign_tier != KMGB_ASSIGN_FP32;
-  if (tc) {
+  if (tc && upload) {
+    a.gamma = assign_bf16_gamma(h->d);
+    a.thr_out = h->opt.certify ? h->thr_full : nullptr;
+    if (h->Xb) KM_TRY(cudaMemsetAsync(h->xinexact, 0, sizeof(int), s), KMEANS_ERROR_COPY_TILE);
+    if (h->ldx != h->d)  // the copies write d of ldx columns: the padding stays zero
+      KM_TRY(cudaMemsetAsync(h->X, 0, sizeof(float) * h->ldx * h->n, s), KMEANS_ERROR_COPY_TILE);
+    cudaEvent_t ev = nullptr;
+    KM_TRY(upload_start(h, &ev), KMEANS_ERROR_COPY_TILE);
+    const long long rows = (h->n + kUploadChunks - 1) / kUploadChunks;
+    const size_t plane = (size_t)h->ldb * 2;  // bytes per BF16 row
+    for (long long r0 = 0; r0 < h->n; r0 += rows) {
+      const long long r1 = std::min(h->n, r0 + rows);
+      KM_TRY(copy_rows(h, upload, r0, r1, cudaMemcpyHostToDevice, h->copy_stream),
+             KMEANS_ERROR_COPY_TILE);
+      KM_TRY(cudaEventRecord(ev, h->copy_stream), KMEANS_ERROR_COPY_TILE);
+      KM_TRY(cudaStreamWaitEvent(s, ev, 0), KMEANS_ERROR_COPY_TILE);
+      KM_TRY(prepare_rows(h, r0, r1), KMEANS_ERROR_COPY_TILE);
+      AssignArgs ac = a;
+      ac.n = r1 - r0;
+      ac.out0 = r0;
+      KM_TRY(launch_assign_bf16(static_cast<const char*>(h->Xb) + (size_t)r0 * plane,
+                                h->Xl ? static_cast<const char*>(h->Xl) + (size_t)r0 * plane
+                                      : nullptr,
+                                h->ldb, h->Cb, h->Cl, h->ldb, ac, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+    }
+  } else if (tc) {
     a.gamma = assign_bf16_gamma(h->d);
     a.thr_out = h->opt.certify ? h->thr_full : nullptr;
     KM_TRY(launch_assign_bf16(Xba, Xla, h->ldb, h->Cb, h->Cl, h->ldb, a, s),
@@ -903,7 +946,8 @@ bool graphs_enabled() {
   return !(v && std::strcmp(v, "0") == 0);
 }
 
-int run(kmgb_handle* h, int iters, double criterion) {
+// upload: see step(); the first iteration brings the host data set along (one-shot calls).
+int run(kmgb_handle* h, int iters, double criterion, const float* upload = nullptr) {
   if (!h->have_data || !h->have_centers) {
     set_err("kmgb_run: data and centers must be set first");
     return KMEANS_ERROR_COMPUTE;
@@ -928,14 +972,28 @@ int run(kmgb_handle* h, int iters, double criterion) {
                          h->stream),
          KMEANS_ERROR_COMPUTE);
   KM_TRY(cudaEventRecord(h->ev0, h->stream), KMEANS_ERROR_COMPUTE);
+  int first = 0;
+  if (upload && iters > 0) {
+    int rc = step(h, 0, upload);
+    if (rc) return rc;
+    first = 1;
+    if (h->Xl) {  // every x a BF16 number: the later iterations drop the x_lo product
+      int inexact = 1;
+      KM_TRY(cudaMemcpyAsync(&inexact, h->xinexact, sizeof(int), cudaMemcpyDeviceToHost,
+                             h->stream),
+             KMEANS_ERROR_COMPUTE);
+      KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_COMPUTE);
+      h->x_exact = inexact == 0;
+    }
+  }
   // Every iteration is enqueued; the SSE reduction evaluates the stop rule on the device and
   // the kernels of later iterations return at once after it fires.
   int graph_rc = -1;
-  if (!h->streaming && !h->mini && !h->prof && iters > 0 && graphs_enabled()) {
-    graph_rc = run_graph(h, iters);
+  if (!h->streaming && !h->mini && !h->prof && iters - first > 0 && graphs_enabled()) {
+    graph_rc = run_graph(h, iters - first);
     if (graph_rc > 0) return graph_rc;
   }
-  for (int it = 0; it < iters && graph_rc != 0; ++it) {
+  for (int it = first; it < iters && graph_rc != 0; ++it) {
     if (h->streaming) {
       // a streamed iteration copies the whole data set: look at the stop flag between
       // iterations so that a converged run issues no further copies
@@ -988,6 +1046,26 @@ int finish(kmgb_handle* h) {
            KMEANS_ERROR_COMPACTNESS);
   }
   return 0;
+}
+
+// One-shot calls with their initial centers given: host data, a tensor tier, full batches and
+// at least one iteration -- the data set can travel with the first iteration (step's upload
+// mode) instead of ahead of it; the first iteration's assignment then hides under the upload.
+bool upload_with_first_step(const kmgb_handle* h, int iters) {
+  return h->opt.assign_tier != KMGB_ASSIGN_FP32 && !h->mini && !h->streaming && iters > 0 &&
+         h->n >= kUploadChunks * 4096 && h->Xb;
+}
+
+// The data set will arrive with the first iteration: the handle's data state as set_data leaves
+// it, without the copy.
+void expect_data_with_first_step(kmgb_handle* h) {
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  h->x_exact = false;
+  h->have_data = true;
+  h->iter_base = 0;
 }
 
 // Initial centers = shuffled rows picks[i] (kmeans.cpp:886-888), from start_reference_init.
@@ -1427,7 +1505,11 @@ int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
   const bool host_ref_init = !init && !kpp && !x_dev;
   std::shared_future<RefInit> ref;
   if (host_ref_init || (h->mini && !h->streaming)) ref = start_reference_init(n, k);
-  rc = set_data(h, X, x_dev, ref.valid() ? &ref : nullptr);
+  // with the initial centers given, the data set can travel with the first iteration (with the
+  // reference initialisation the upload overlaps the host's shuffle instead)
+  const bool fused = !x_dev && init && upload_with_first_step(h, o.max_iters);
+  if (fused) expect_data_with_first_step(h);
+  else rc = set_data(h, X, x_dev, ref.valid() ? &ref : nullptr);
   if (!rc) {
     if (init) {
       rc = set_centers(h, init, is_device_ptr(init));
@@ -1441,7 +1523,7 @@ int kmgb_lloyd_f32(const float* X, long long n, int d, int k, const float* init,
       rc = kmgb_set_centers(h, nullptr, 0);
     }
   }
-  if (!rc && !kpp) rc = run(h, o.max_iters, o.criterion);
+  if (!rc && !kpp) rc = run(h, o.max_iters, o.criterion, fused ? X : nullptr);
   if (!rc && !kpp) rc = finish(h);
   if (!rc && centers) rc = get_centers(h, centers, is_device_ptr(centers));
   if (!rc && labels) rc = get_labels(h, labels, is_device_ptr(labels));

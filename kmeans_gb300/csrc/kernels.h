@@ -21,6 +21,8 @@ struct AssignArgs {
   // BF16 tiers only:
   const int* n_dev;       // nullable: rows actually present = min(*n_dev, n) (device count)
   long long row0;         // first row of this batch (rows row0 .. row0 + present - 1)
+  long long out0;         // full pass: the launch's rows are rows out0.. of the data set (labels,
+                          // norms, floors and flagged-list entries are indexed by those)
   float* thr_out;         // nullable: for every flagged point, best key - 2E (candidate floor)
   const float* thr_in;    // candidate mode: per-row floor; keys >= floor are recorded in cand
   int* cand;              // candidate mode: [n][kMaxCand] center indices

@@ -406,3 +406,23 @@ def test_memory_pool_off_returns_memory_at_destroy(km, torch_cuda):
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
                        timeout=300)
     assert r.returncode == 0 and "pool off ok" in r.stdout, r.stdout + r.stderr
+
+
+@pytest.mark.parametrize("tier", [1, 2])
+@pytest.mark.parametrize("bf16_values", [False, True])
+def test_upload_with_first_iteration_matches_resident(km, orc, torch_cuda, tier, bf16_values):
+    """A one-shot call on host data sends the data set along with the first iteration (chunks
+    assigned as they land, three-product bound until every x is known to be a BF16 number); the
+    run from device data uploads first. Labels, centers, SSE and status are the same, and equal
+    the oracle's."""
+    X, _, _ = mixture_numpy(70_001, 40, 48, seed=21, mean_lo=-8, mean_hi=8)
+    if bf16_values:
+        X = torch_cuda.from_numpy(X).to(torch_cuda.bfloat16).float().numpy()
+    init = X[sample_init(len(X), 48, seed=22)]
+    host = km.lloyd(X, 48, init=init, max_iters=7, assign_tier=tier)
+    dev = km.lloyd(torch_cuda.from_numpy(X).cuda(), 48, init=init, max_iters=7, assign_tier=tier)
+    assert host.status == dev.status and host.iterations == dev.iterations == 7
+    assert np.array_equal(host.labels, dev.labels)
+    assert np.array_equal(host.centers, dev.centers, equal_nan=True)
+    assert np.array_equal(host.sse, dev.sse)
+    check_same(host, orc.lloyd(X, init, 7))
