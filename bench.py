@@ -471,6 +471,53 @@ def large_k_workload(args, n=16_000_000, d=256, k=65_536):
     print(json.dumps(out), flush=True)
 
 
+def fp64_workload(args, n=4_000_000, d=128, k=1024, iters=5):
+    """The FP64 entry, computeKmeansD, on the 4M x 128, K=1024 mixture in FP64 (host data,
+    reference initialisation, criterion < 0): the tensor path (split BF16 tier on FP32 roundings,
+    exact FP64 scan of the uncertified points) against the exact FP64 scan of every point
+    (KMGB_ASSIGN=fp32). Per-iteration times come from calls of `iters` and of one iteration (the
+    difference removes the call's fixed cost: upload, initialisation, result). Both give the
+    FP64 arg-min labels, so one iteration of each must return the same centers bit for bit."""
+    import torch
+    import kmeans_gb300 as km
+    from kmeans_gb300.synthetic import mixture_torch
+    km.build()
+    X, _, _ = mixture_torch(n, d, k, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+    Xh = X.double().cpu().numpy()
+    del X
+    torch.cuda.empty_cache()
+
+    def call(its, scan):
+        if scan:
+            os.environ["KMGB_ASSIGN"] = "fp32"
+        try:
+            result = np.zeros(d * k, np.float64)
+            t0 = time.perf_counter()
+            rc = km.computeKmeansD(Xh, n, d, k, -1.0, its, 1, 0, 0, 0, result, 1.0)
+            return rc, time.perf_counter() - t0, result
+        finally:
+            os.environ.pop("KMGB_ASSIGN", None)
+
+    call(1, False)  # warm
+    rc_n, t_n, _ = call(iters, False)
+    rc_1, t_1, r_1 = call(1, False)
+    rc_s, t_s, r_s = call(1, True)
+    per_iter = (t_n - t_1) / (iters - 1)
+    fixed = t_1 - per_iter
+    out = {"metric": f"computeKmeansD, N={n}, D={d}, K={k} (s per iteration)", "unit": "s",
+           "higher_is_better": False, "data": "synthetic (FP64)",
+           "config": {"workload": "fp64_4Mx128_K1024", "n": n, "d": d, "k": k},
+           "value": per_iter,
+           "tensor": {"status": rc_n, "iterations": iters, "call_s": t_n,
+                      "one_iteration_call_s": t_1, "s_per_iteration": per_iter,
+                      "fixed_s": fixed},
+           "fp64_scan": {"status": rc_s, "one_iteration_call_s": t_s,
+                         "s_per_iteration": t_s - fixed},
+           "same_centers_after_one_iteration": bool(np.array_equal(r_1, r_s, equal_nan=True)),
+           "speedup": (t_s - fixed) / per_iter if per_iter > 0 else None}
+    print(json.dumps(out), flush=True)
+
+
 def streamed_workload(args, n=200_000_000, d=96, k=4096, iters=10, tile=4_000_000):
     """Host-resident data set: 200M x 96 (76.8 GB of host memory), K=4096 isotropic Gaussians
     (sigma 1.5, means U[-15,15]^96, equal weights), initial centers a seeded sample of points;
@@ -551,7 +598,7 @@ def main():
     ap.add_argument("--only-init", action="store_true",
                     help="time only the k-means++ initialisation (profiling captures)")
     ap.add_argument("--workload", default="lloyd",
-                    choices=["lloyd", "batched", "large_k", "streamed"],
+                    choices=["lloyd", "batched", "large_k", "streamed", "fp64"],
                     help="batched: the many-problems workload through kmgb_lloyd_batched_f32; "
                          "large_k: 16M x 256, K=65536 split BF16 vs FP32; streamed: 200M x 96, "
                          "K=4096 host data, streamed tiles vs resident (own JSON lines; not the "
@@ -574,6 +621,9 @@ def main():
         return large_k_workload(args)
     if args.workload == "streamed":
         return streamed_workload(args)
+    if args.workload == "fp64":
+        fp64_workload(args)
+        return
 
     import torch
     import kmeans_gb300 as km

@@ -613,7 +613,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             (bblk < 0 || none) ? ui.cbase : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
         p.labels[pt] = label;
         if (p.certify) {
-          const float eb = bound_acc(xn_pt, cm, p.d, mode);
+          const float eb = bound_acc(xn_pt, cm, p.d, mode) +
+                           1.02f * p.pert * (xn_pt * cm * 1.01f + 0.5f * cm * cm);
           if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
             p.rerank_list[slot] = (int)pt;

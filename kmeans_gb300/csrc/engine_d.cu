@@ -9,6 +9,8 @@
 // fast one; every kernel is plain SIMT.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <random>
 #include <string>
@@ -33,12 +35,18 @@ __global__ void transpose_d_kernel(const double* __restrict__ C, int k, int d, d
 }
 
 // One warp per point, lanes over centers (coalesced reads of CT); exact FP64 direct distance.
+// list (nullable): only the points list[0 .. *count) (the tensor pass's uncertified points).
 __global__ void assign_d_kernel(const double* __restrict__ X, long long n, int d,
-                                const double* __restrict__ CT, int k, int* __restrict__ labels) {
+                                const double* __restrict__ CT, int k, int* __restrict__ labels,
+                                const int* __restrict__ list = nullptr,
+                                const int* __restrict__ count = nullptr) {
   extern __shared__ double xs_all[];
   const int warps = blockDim.x >> 5, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double* xs = xs_all + (size_t)w * d;
-  for (long long i = (long long)blockIdx.x * warps + w; i < n; i += (long long)gridDim.x * warps) {
+  const long long todo = list ? (long long)*count : n;
+  for (long long slot = (long long)blockIdx.x * warps + w; slot < todo;
+       slot += (long long)gridDim.x * warps) {
+    const long long i = list ? (long long)list[slot] : slot;
     for (int t = lane; t < d; t += 32) xs[t] = X[(size_t)i * d + t];
     __syncwarp();
     double best = INFINITY;
@@ -63,6 +71,17 @@ __global__ void assign_d_kernel(const double* __restrict__ X, long long n, int d
     }
     if (lane == 0) labels[i] = bi < 0 ? 0 : bi;
     __syncwarp();
+  }
+}
+
+// out[r][c] = (float)in[r][c] (round to nearest) for c < d, 0 for d <= c < ldo.
+__global__ void d2f_kernel(const double* __restrict__ in, long long rows, int d,
+                           float* __restrict__ out, long long ldo) {
+  const long long total = rows * ldo;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long r = e / ldo, c = e - r * ldo;
+    out[e] = c < d ? __double2float_rn(in[(size_t)r * d + c]) : 0.0f;
   }
 }
 
@@ -229,6 +248,43 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
   KD_TRY(B.alloc(&w.sorted, m_mb), E);
   KD_TRY(B.alloc(&w.part, (size_t)w.max_pieces * n), E);
 
+  // Tensor path (full batches, D within the split tier's limit): X and the centers are rounded
+  // to FP32, the split BF16 tier assigns every point under its bound widened by that rounding
+  // (|key(x,c) - key(fl(x),fl(c))| <= 2^-23 (|x||c| + |c|^2/2), taken twice), and the points it
+  // cannot certify get the exact FP64 scan. KMGB_ASSIGN=fp32 keeps the FP64 scan for every point.
+  const char* tier_env = std::getenv("KMGB_ASSIGN");
+  const bool tc = !mini && bf16_tc_supported(n, 2) &&
+                  !(tier_env && std::strcmp(tier_env, "fp32") == 0);
+  const long long ldx = (n + 3) / 4 * 4, ldb = (n + 7) / 8 * 8;
+  float *Xf = nullptr, *xn = nullptr, *Cf = nullptr, *Cop = nullptr, *cn = nullptr,
+        *cmax = nullptr, *cinit = nullptr;
+  double* qn = nullptr;
+  uint16_t *Xb = nullptr, *Xl = nullptr, *Cb = nullptr, *Cl = nullptr;
+  int *rr_list = nullptr, *rr_count = nullptr, *derr = nullptr;
+  if (tc) {
+    const kmeansErrorStatus EA = KMEANS_ERROR_CLOSEST_CENTERS;
+    KD_TRY(B.alloc(&Xf, (size_t)m * ldx), E);
+    KD_TRY(B.alloc(&xn, m), E);
+    KD_TRY(B.alloc(&qn, m), E);
+    KD_TRY(B.alloc(&Xb, (size_t)m * ldb), E);
+    KD_TRY(B.alloc(&Xl, (size_t)m * ldb), E);
+    KD_TRY(B.alloc(&Cf, (size_t)k * ldx), E);
+    KD_TRY(B.alloc(&Cop, (size_t)k * ldx), E);
+    KD_TRY(B.alloc(&Cb, (size_t)k * ldb), E);
+    KD_TRY(B.alloc(&Cl, (size_t)k * ldb), E);
+    KD_TRY(B.alloc(&cn, k), E);
+    KD_TRY(B.alloc(&cmax, 1), E);
+    KD_TRY(B.alloc(&cinit, (size_t)((k + kCenterPad - 1) / kCenterPad * kCenterPad)), E);
+    KD_TRY(B.alloc(&rr_list, m), E);
+    KD_TRY(B.alloc(&rr_count, 3), E);
+    KD_TRY(B.alloc(&derr, 1), E);
+    KD_TRY(cudaMemsetAsync(derr, 0, sizeof(int), s), E);
+    d2f_kernel<<<152 * 8, 256, 0, s>>>(X, m, n, Xf, ldx); kmgb::count_launches(1);
+    KD_TRY(cudaGetLastError(), E);
+    KD_TRY(launch_point_norms(Xf, ldx, m, n, qn, xn, s), E);
+    KD_TRY(launch_to_bf16(Xf, ldx, m, n, Xb, ldb, s, nullptr, Xl, nullptr), EA);
+  }
+
   const int threads = 256;
   const size_t smem = sizeof(double) * n * (threads / 32);
   if (smem > 200 * 1024) return KMEANS_ERROR_CLOSEST_CENTERS;
@@ -246,7 +302,34 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
       Xa = Xw;
     }
     transpose_d_kernel<<<152 * 4, 256, 0, s>>>(Cd, k, n, CT); kmgb::count_launches(1);
-    assign_d_kernel<<<152 * 8, threads, smem, s>>>(Xa, m_mb, n, CT, k, lab); kmgb::count_launches(1);
+    if (tc) {
+      const kmeansErrorStatus EA = KMEANS_ERROR_CLOSEST_CENTERS;
+      d2f_kernel<<<152 * 4, 256, 0, s>>>(Cd, k, n, Cf, ldx); kmgb::count_launches(1);
+      KD_TRY(cudaMemsetAsync(cmax, 0, sizeof(float), s), EA);
+      KD_TRY(cudaMemsetAsync(rr_count, 0, 3 * sizeof(int), s), EA);
+      KD_TRY(launch_prep_centers(Cf, ldx, k, n, Cop, Cb, ldb, cn, cmax, s, nullptr, cinit, Cl), EA);
+      AssignArgs a{};
+      a.cn = cn;
+      a.xnorm = xn;
+      a.cmax = cmax;
+      a.cinit = cinit;
+      a.labels = lab;
+      a.rerank_list = rr_list;
+      a.rerank_count = rr_count;
+      a.err = derr;
+      a.n = m;
+      a.k = k;
+      a.d = n;
+      a.certify = 1;
+      a.gamma = assign_bf16_gamma(n);
+      a.pert = 0x1p-22f;
+      KD_TRY(launch_assign_bf16(Xb, Xl, ldb, Cb, Cl, ldb, a, s), EA);
+      assign_d_kernel<<<152 * 8, threads, smem, s>>>(X, m, n, CT, k, lab, rr_list, rr_count);
+      kmgb::count_launches(1);
+    } else {
+      assign_d_kernel<<<152 * 8, threads, smem, s>>>(Xa, m_mb, n, CT, k, lab);
+      kmgb::count_launches(1);
+    }
     KD_TRY(cudaGetLastError(), KMEANS_ERROR_CLOSEST_CENTERS);
     KD_TRY(cudaMemsetAsync(acc, 0, sizeof(double) * (size_t)k * n, s), KMEANS_ERROR_RESET);
     KD_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * k, s), KMEANS_ERROR_RESET);
@@ -269,6 +352,14 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
   }
   KD_TRY(cudaMemcpy(C.data(), Cd, sizeof(double) * C.size(), cudaMemcpyDeviceToHost),
          KMEANS_ERROR_GET_CENTERS);
+  if (tc) {  // a bounded wait of the tensor pass gave up: its labels cannot be trusted
+    int e = 0;
+    KD_TRY(cudaMemcpy(&e, derr, sizeof(int), cudaMemcpyDeviceToHost), KMEANS_ERROR_CLOSEST_CENTERS);
+    if (e) {
+      set_last_error("computeKmeansD: a bounded wait in the tensor-core assignment gave up");
+      return KMEANS_ERROR_CLOSEST_CENTERS;
+    }
+  }
   for (int i = 0; i < k; ++i)
     for (int j = 0; j < n; ++j) result[(size_t)j * k + i] = C[(size_t)i * n + j];
   return (rel <= criterion) ? KMEANS_SUCCESS : KMEANS_NONCONVERGENCE;

@@ -36,6 +36,8 @@ struct AssignArgs {
   int d;
   int certify;            // 0: write arg-min labels only
   float gamma;
+  float pert;             // FP64 data rounded to FP32 for the tensor pass: every key's bound
+                          // grows by 1.02 pert (||x|| cmax 1.01 + cmax^2 / 2); 0 for FP32 data
   const int* stop;        // device stop flag of the run (nullable)
   // BF16 tiers, grouped problems (batched Lloyd; null otherwise): unit u (rows 256u .. 256u+255)
   // belongs to problem u_prob[u], whose centers are rows g_coff[p] .. g_coff[p] + g_k[p] - 1 (a

@@ -426,3 +426,47 @@ def test_upload_with_first_iteration_matches_resident(km, orc, torch_cuda, tier,
     assert np.array_equal(host.centers, dev.centers, equal_nan=True)
     assert np.array_equal(host.sse, dev.sse)
     check_same(host, orc.lloyd(X, init, 7))
+
+
+def test_compute_kmeans_d_tensor_path(km, orc, torch_cuda):
+    """computeKmeansD with D <= 256 runs the split BF16 tier on FP32 roundings of the FP64 data
+    and centers, with the bound widened by that rounding, and the exact FP64 scan for the points
+    it cannot certify: the result equals the FP64 oracle's. The data carry FP64 precision (an
+    FP32 rounding of x loses information)."""
+    X, _, _ = mixture_numpy(150_001, 64, 96, seed=31, mean_lo=-5, mean_hi=5)
+    rng = np.random.default_rng(32)
+    X = X.astype(np.float64) + rng.uniform(-1e-6, 1e-6, X.shape)
+    m, n, k = X.shape[0], X.shape[1], 96
+    result = np.zeros(n * k, np.float64)
+    assert km.computeKmeansD(X, m, n, k, -1.0, 5, 1, 0, 0, 0, result, 1.0) == 13
+    perm = orc.shuffle_perm(m)
+    init = X[perm[orc.init_picks(m, k)]]
+    st, c, lab, sse, it = orc.lloyd_d(X, init, 5)
+    assert np.array_equal(result.reshape(n, k), c.T, equal_nan=True)
+
+
+def test_compute_kmeans_d_fp64_near_ties(km, orc, torch_cuda):
+    """Near-ties only FP64 resolves, and exact FP64 duplicates, planted where the reference
+    initialisation picks its centers: centers 11 and 12 differ by ~1e-11 (identical after FP32
+    rounding), center 7 duplicates center 3, and 200 points sit within 1e-13 of the bisector of
+    11 and 12. The tensor pass cannot certify them; the FP64 scan decides (lowest index on
+    exact ties), as the oracle does."""
+    rng = np.random.default_rng(33)
+    m, d, k = 40_600, 16, 40
+    X, _, _ = mixture_numpy(m, d, k, seed=34, mean_lo=-4, mean_hi=4)
+    X = X.astype(np.float64)
+    rows = orc.shuffle_perm(m)[orc.init_picks(m, k)]  # data rows that become the centers
+    X[rows[12]] = X[rows[11]] + 1e-11 * rng.standard_normal(d)
+    X[rows[7]] = X[rows[3]]
+    free = np.setdiff1d(np.arange(m), rows)
+    mid = 0.5 * (X[rows[11]] + X[rows[12]])
+    X[free[:200]] = mid + 1e-13 * rng.standard_normal((200, d))
+    X[free[200:400]] = X[rows[3]] + 1e-3 * rng.standard_normal((200, d))
+    # the planted structure is what the oracle's first iteration sees
+    _, _, lab1, _, _ = orc.lloyd_d(X, X[rows], 1)
+    assert set(lab1[free[:200]].tolist()) == {11, 12}
+    assert (lab1[free[200:400]] == 3).all()
+    res = np.zeros(d * k, np.float64)
+    assert km.computeKmeansD(X, m, d, k, -1.0, 3, 1, 0, 0, 0, res, 1.0) == 13
+    _, c, _, _, _ = orc.lloyd_d(X, X[rows], 3)
+    assert np.array_equal(res.reshape(d, k), c.T, equal_nan=True)
