@@ -75,7 +75,12 @@ KMGB_EXPORT kmeansErrorStatus computeKmeansF(const float* data, const int m, con
                                  const int doFullSGEMM, const int matrixFormat, float* result,
                                  const float miniBatchFraction);
 
-/* Replaces computeKmeansD (main/cpp/kmeans.hpp:127-132, main/cpp/kmeans.cpp:1364-1409). */
+/* Replaces computeKmeansD (main/cpp/kmeans.hpp:127-132, main/cpp/kmeans.cpp:1364-1409), with
+ * computeKmeansF's arguments and layouts on FP64 data. Labels are the FP64 arg-min of the
+ * direct distance (lowest index on ties); centers are canonical FP64 sums over the counts. Full
+ * batches with n <= 256 assign on the tensor cores (the split BF16 tier on FP32 roundings of the
+ * data and centers, its bound widened by that rounding, the uncertified points rescanned in
+ * FP64); mini-batch windows, wider data and KMGB_ASSIGN=fp32 use the FP64 scan for every point. */
 KMGB_EXPORT kmeansErrorStatus computeKmeansD(const double* data, const int m, const int n, const int k,
                                  const double criterion, const int maxIters,
                                  const int numRetries, const int initAlgorithm,
