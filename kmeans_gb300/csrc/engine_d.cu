@@ -12,6 +12,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <future>
 #include <random>
 #include <string>
 #include <vector>
@@ -157,37 +158,25 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
   const bool mini = fraction < 1.0;
   const long long m_mb = mini ? (long long)(int)((float)fraction * (float)m) : m;
   if (m_mb <= 0) return KMEANS_ERROR_TILING;
-  // reference initialisation on the host (kmeans.cpp:554-564, 876-888)
-  std::vector<int> perm(m);
-  for (int i = 0; i < m; ++i) perm[i] = i;
-  {
-    unsigned seed = 0;
-    std::shuffle(perm.begin(), perm.end(), std::default_random_engine(seed));
+  // reference initialisation on the host (kmeans.cpp:554-564, 876-888): the shuffle is
+  // sequential and independent of the data, so it runs on a host thread while the data set is
+  // allocated and uploaded
+  struct RefInit {
+    std::vector<int> perm, picks;
+    bool ok = true;
+  };
+  auto ref_task = [m, k, kpp_seed] {
+    RefInit r;
+    reference_perm(m, r.perm);
+    if (kpp_seed < 0) r.ok = reference_picks(m, k, r.picks);
+    return r;
+  };
+  std::future<RefInit> ref;
+  try {
+    ref = std::async(std::launch::async, ref_task);
+  } catch (...) {  // no thread to be had: run it when the result is asked for
+    ref = std::async(std::launch::deferred, ref_task);
   }
-  std::vector<int> picks;
-  if (kpp_seed < 0) {
-    struct random_data rd;
-    std::memset(&rd, 0, sizeof(rd));
-    std::vector<char> state(128, 0);
-    if (initstate_r(42u, state.data(), state.size(), &rd) != 0) return KMEANS_ERROR_INITIALIZE;
-    for (int i = 0; i < k; ++i) {
-      int32_t r = 0;
-      random_r(&rd, &r);
-      int index = r % m;
-      while (std::binary_search(picks.begin(), picks.end(), index)) {
-        random_r(&rd, &r);
-        index = r % m;
-      }
-      picks.push_back(index);
-    }
-  }
-  std::vector<double> C((size_t)k * n);
-  if (kpp_seed < 0)
-    for (int i = 0; i < k; ++i)
-      for (int j = 0; j < n; ++j) {
-        C[(size_t)i * n + j] = data[(size_t)perm[picks[i]] * n + j];
-        result[(size_t)j * k + i] = C[(size_t)i * n + j];
-      }
 
   DevBufs B;
   double *X = nullptr, *Xw = nullptr, *Cd = nullptr, *CT = nullptr, *acc = nullptr, *part = nullptr,
@@ -197,6 +186,23 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
   const kmeansErrorStatus E = KMEANS_ERROR_BUILDDATA;
   KD_TRY(B.alloc(&X, (size_t)m * n), E);
   KD_TRY(cudaMemcpy(X, data, sizeof(double) * (size_t)m * n, cudaMemcpyHostToDevice), E);
+
+  RefInit r;
+  try {
+    r = ref.get();
+  } catch (...) {
+    return KMEANS_ERROR_INITIALIZE;
+  }
+  if (!r.ok) return KMEANS_ERROR_INITIALIZE;
+  const std::vector<int>& perm = r.perm;
+  const std::vector<int>& picks = r.picks;
+  std::vector<double> C((size_t)k * n);
+  if (kpp_seed < 0)
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < n; ++j) {
+        C[(size_t)i * n + j] = data[(size_t)perm[picks[i]] * n + j];
+        result[(size_t)j * k + i] = C[(size_t)i * n + j];
+      }
   if (mini) {
     KD_TRY(B.alloc(&Xw, (size_t)m_mb * n), E);
     KD_TRY(B.alloc(&permd, m), E);
