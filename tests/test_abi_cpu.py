@@ -31,7 +31,8 @@ def test_reference_entry_points_present(km):
     names = ["computeKmeansF", "computeKmeansD", "kmeansGetErrorString", "ClosestCentersF",
              "ClosestCentersD", "rowTransformMinimumF", "rowTransformMinimumD",
              "ClusterCentersF", "ClusterCentersD", "CompactnessF", "CompactnessD",
-             "rowNormalizeF", "rowNormalizeD", "colNormalizeF", "colNormalizeD"]
+             "rowNormalizeF", "rowNormalizeD", "colNormalizeF", "colNormalizeD",
+             "MatMatMultF", "MatMatMultD"]
     decl = declared_symbols(km)
     for n in names:
         assert n in decl
@@ -51,6 +52,12 @@ def test_default_options(km):
     o = km.default_options()
     assert (o.assign_tier, o.certify, o.empty_policy, o.max_iters) == (0, 1, 0, 20)
     assert o.criterion < 0 and o.mini_batch_fraction == 1.0
+
+
+def test_mat_mat_mult_rejects_negative_sizes_without_gpu(km):
+    # ERROR_MATMATMULT (1) before any device call
+    assert km.MatMatMultF(-1, 2, None, 2, None, None) == 1
+    assert km.MatMatMultD(2, -2, None, 2, None, None) == 1
 
 
 def test_invalid_arguments_rejected_without_gpu(km):
