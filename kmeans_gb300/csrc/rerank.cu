@@ -1,6 +1,12 @@
 // Exact re-rank of the points whose approximate top-2 margin did not certify the arg-min.
 //
-// One warp per flagged point, lanes over centers. Pass 1 evaluates every usable center in
+// Stages in this file: the candidate path of the tensor tiers (gather_flagged_kernel copies the
+// flagged rows for the candidate pass; resolve_candidates_kernel settles each point from its
+// recorded candidates in FP32, then float-float, then exact FP64), the tiled FP32 stage and the
+// tiled exact FP64 stage for everything else, the per-point kernel described next (both modes),
+// and the grouped kernel of batched problems.
+//
+// Per-point kernel: one warp per flagged point, lanes over centers. Pass 1 evaluates every usable center in
 // FP32 together with a rigorous interval [lo_j, hi_j] around the exact value and takes
 // best_hi = min_j hi_j. Pass 2 re-evaluates the centers with lo_j <= best_hi (the only ones
 // that can be the FP64 arg-min) in FP64 exactly as the oracle does and keeps the smallest,

@@ -3,14 +3,18 @@
 // Replaces the reference's privatised accumulation (main/cuda/ClusterCenters.cu:3-23, one
 // G x K x D partial buffer), its per-center reduce and divide (ClusterCenters.cu:47-87), and the
 // compactness reduction (main/cuda/Compactness.cu:3-59). Instead of G*K*D partials:
-//   1. hist     per-tile label histogram (tile = `tile_pts` consecutive points), K x T int32,
-//               warp-aggregated integer atomics;
+//   1. hist     per-tile label histogram (tile = `tile_pts` >= 4096 consecutive points),
+//               K x T int32, counted in shared memory (global atomics per peer group when K
+//               does not fit);
 //   2. scan     exclusive scan of the K-major histogram = start of every (label, tile) run;
-//   3. scatter  one warp per tile walks its points in order and writes each point id to
-//               start + rank, so the sort by label is stable (ascending point id per label);
-//   4. pieces   every label's run is cut into pieces of kSumPiece points; one warp per piece
-//               sums its rows in point order (FP32 data: error-free float-float sum turned into
-//               FP64 once per piece; FP64 data: FP64) and the rows' FP64 ||x||^2;
+//   3. scatter  eight warps share a tile: each counts its slice, a scan across the warps gives
+//               each its first positions, and each walks its points in order writing every
+//               point id to start + rank (rank among equal labels of a 32-point step, from
+//               ballot peer groups), so the sort by label is stable (ascending point id);
+//   4. pieces   every label's run is cut into pieces of kSumPiece points; one lane group per
+//               piece (a warp, or 32/L pieces per warp when D <= 64) sums its rows in point
+//               order (FP32 data: error-free float-float sum turned into FP64 once per piece;
+//               FP64 data: FP64) and the warp the rows' FP64 ||x||^2;
 //   5. finalize one warp per center adds its pieces in order, divides by the count in FP64,
 //               rounds once to FP32 (empty cluster: NaN as in ClusterCenters.cu:81, or keep the
 //               previous center), and evaluates the cluster's SSE against the new center with
