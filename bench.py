@@ -100,6 +100,18 @@ class Clocks:
                 "samples": len(rows)}
 
 
+def replica_rate(ms: float, steps: int, world: int, dist=None, device: str = "cuda"):
+    """N independent replicas (one per GPU, each running `steps` iterations of its own copy of
+    the workload): the slowest rank's timed region sets the whole job's time (max over ranks),
+    and the job's rate counts every rank's iterations. Returns (max ms, iter/s)."""
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * steps / (ms / 1000.0)
+
+
 def cpu_baseline(steps: int = 1):
     """Oracle FP32 port (CPU restatement, OpenMP, all host threads) on a bounded sample: one
     Lloyd iteration over CPU_SAMPLE_ROWS rows of the workload, scaled to the full N."""
@@ -679,11 +691,7 @@ def main():
     launches = km.launch_count() - launches0
     phase, piters = h.phase_ms()
     st = h.stats()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * args.steps / (ms / 1000.0)
+    ms, value = replica_rate(ms, args.steps, world, dist)
 
     flop = 2.0 * n * K * D
     assign_ms = phase[1] / max(piters, 1)
