@@ -73,7 +73,11 @@ KMGB_EXPORT kmeansErrorStatus computeKmeansF(const float* data, const int m, con
                                  const float criterion, const int maxIters,
                                  const int numRetries, const int initAlgorithm,
                                  const int doFullSGEMM, const int matrixFormat, float* result,
+#if defined(__cplusplus)
+                                 const float miniBatchFraction = 1.0f); /* as kmeans.hpp:107 */
+#else
                                  const float miniBatchFraction);
+#endif
 
 /* Replaces computeKmeansD (main/cpp/kmeans.hpp:127-132, main/cpp/kmeans.cpp:1364-1409), with
  * computeKmeansF's arguments and layouts on FP64 data. Labels are the FP64 arg-min of the
@@ -85,7 +89,11 @@ KMGB_EXPORT kmeansErrorStatus computeKmeansD(const double* data, const int m, co
                                  const double criterion, const int maxIters,
                                  const int numRetries, const int initAlgorithm,
                                  const int doFullSGEMM, const int matrixFormat, double* result,
+#if defined(__cplusplus)
+                                 const double miniBatchFraction = 1.0); /* as kmeans.hpp:132 */
+#else
                                  const double miniBatchFraction);
+#endif
 
 /* ---------------------------------------------------------------------------------------
  * 2. Reference per-kernel API (device pointers, asynchronous on the default stream)
@@ -354,6 +362,23 @@ KMGB_EXPORT long long kmgb_launch_count(void);
  * device and returns every pool's unused memory to the device; 0 on success. Setting
  * KMGB_POOL=0 in the environment makes every free return its memory at once. */
 KMGB_EXPORT int kmgb_release_cached_memory(void);
+
+/* Test hooks for failure paths (no reference counterpart; the reference reports failures only
+ * through its error enums, kmeans.hpp:44-59). kmgb_debug_fail_nth makes the nth later event of a
+ * kind fail once, as the CUDA call would have failed: kind 1 = a device allocation from the
+ * library's pool, 2 = a host<->device copy of a data set, centers or results, 3 = the launch of a
+ * Lloyd-phase kernel (assignment, re-rank, update, center preparation, norms, BF16 conversion);
+ * nth <= 0 disarms it. The call that meets the failure returns the kmeansErrorStatus of its phase
+ * and releases what it allocated. Process-wide, not thread-safe with concurrent calls. */
+KMGB_EXPORT void kmgb_debug_fail_nth(int kind, long long nth);
+/* Test hook: FP32-tier assignment launches of handles run after this call issue no TMA load for
+ * pipeline step `stage` and later (stage > 0; 0 disarms), and every wait of that kernel gives up
+ * after wait_cycles SM cycles (0: the default, about 2 s). The wait for the withheld step runs
+ * out, the kernel records KMGB_DEV_TIMEOUT_FULL in the handle's device error word and returns
+ * (no copy is left in flight), and the run reports KMEANS_ERROR_CLOSEST_CENTERS. */
+KMGB_EXPORT void kmgb_debug_withhold_stage(long long stage, unsigned long long wait_cycles);
+/* Bytes of the current device's library pool handed out and not yet given back (-1 on error). */
+KMGB_EXPORT long long kmgb_debug_pool_used_bytes(void);
 
 /* Last error message of the calling thread (empty string if none). */
 KMGB_EXPORT const char* kmgb_last_error(void);

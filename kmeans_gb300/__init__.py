@@ -31,6 +31,13 @@ HEADER_PATH = os.path.join(os.path.dirname(_HERE), "include", "kmeans_gb300.h")
 
 KMEANS_SUCCESS = 0
 KMEANS_ERROR_BUILDDATA = 1
+KMEANS_ERROR_INITIALIZE = 2
+KMEANS_ERROR_CLOSEST_CENTERS = 3
+KMEANS_ERROR_CLUSTER_CENTERS = 4
+KMEANS_ERROR_COMPACTNESS = 5
+KMEANS_ERROR_RESET = 7
+KMEANS_ERROR_COMPUTE = 8
+KMEANS_ERROR_GET_CENTERS = 9
 KMEANS_NONCONVERGENCE = 13
 ASSIGN_FP32 = 0
 ASSIGN_BF16 = 1
@@ -150,6 +157,9 @@ def lib():
             "kmgb_kmeanspp_f64": (i32, [P, i64, i32, i32, C.c_ulonglong, P, P]),
             "kmgb_init_kmeanspp": (i32, [P, C.c_ulonglong, P]),
             "kmgb_lloyd_batched_f32": (i32, [P, i32, P, P]),
+            "kmgb_debug_fail_nth": (None, [i32, i64]),
+            "kmgb_debug_withhold_stage": (None, [i64, C.c_ulonglong]),
+            "kmgb_debug_pool_used_bytes": (i64, []),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -168,6 +178,26 @@ def release_cached_memory() -> None:
     reuse it otherwise; KMGB_POOL=0 returns it at every destroy)."""
     if lib().kmgb_release_cached_memory() != 0:
         raise KmeansError(KMEANS_ERROR_BUILDDATA, last_error())
+
+
+FAULT_ALLOC, FAULT_COPY, FAULT_LAUNCH = 1, 2, 3
+
+
+def debug_fail_nth(kind: int, nth: int) -> None:
+    """Test hook: the nth later event of `kind` (FAULT_ALLOC / FAULT_COPY / FAULT_LAUNCH) fails
+    once, as the CUDA call would have failed; nth <= 0 disarms it."""
+    lib().kmgb_debug_fail_nth(int(kind), int(nth))
+
+
+def debug_withhold_stage(stage: int, wait_cycles: int = 0) -> None:
+    """Test hook: FP32-tier assignment launches withhold their TMA loads from pipeline step
+    `stage` on (0 disarms) and bound every wait by `wait_cycles` SM cycles."""
+    lib().kmgb_debug_withhold_stage(int(stage), int(wait_cycles))
+
+
+def debug_pool_used_bytes() -> int:
+    """Bytes of the current device's library pool handed out and not yet given back."""
+    return int(lib().kmgb_debug_pool_used_bytes())
 
 
 def last_error() -> str:

@@ -708,6 +708,7 @@ float assign_bf16_gamma(int d) {
 cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, const void* Cb,
                                const void* Cl, long long ldcb, const AssignArgs& a,
                                cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (a.n <= 0 || a.k <= 0 || a.d <= 0) return cudaSuccess;
   const int planes = (Xl && Cl) ? 2 : 1;  // planes of the split tier's point buffer
   const int mode = Cl ? (Xl ? 2 : 3) : 1;  // see bound_acc

@@ -61,7 +61,11 @@ assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
 
   // Thread 0 doubles as the TMA producer: it fills the ring, then refills each stage as soon
   // as all 8 warps have released it.
+  // test hook: steps from p.test_withhold on are never loaded, so the wait for the first of them
+  // runs out (every step before it has been loaded and consumed: no copy is left in flight)
+  const unsigned long long wait_lim = p.test_wait_cycles ? p.test_wait_cycles : KMGB_WAIT_CYCLES;
   auto issue = [&](int step) {
+    if (p.test_withhold > 0 && step >= p.test_withhold) return;
     const int stage = step % STAGES;
     const int chunk = step / nkb, kb = step % nkb;
     const uint32_t dst = smem_u32(smem + stage * STAGE_BYTES);
@@ -111,7 +115,7 @@ assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       const int stage = s % STAGES;
       const uint32_t parity = (s / STAGES) & 1;
       bool ok = mbar_wait(smem_u32(&full_bar[stage]), parity, &abort_flag, p.err,
-                          KMGB_DEV_TIMEOUT_FULL);
+                          KMGB_DEV_TIMEOUT_FULL, wait_lim);
       ok = __all_sync(0xffffffffu, ok);
       if (!ok) {
         alive = false;
@@ -143,7 +147,7 @@ assign_fp32_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         bool ok2 = true;
         if (tid == 0 && s + STAGES < total) {
           ok2 = mbar_wait(smem_u32(&empty_bar[stage]), parity, &abort_flag, p.err,
-                          KMGB_DEV_TIMEOUT_EMPTY);
+                          KMGB_DEV_TIMEOUT_EMPTY, wait_lim);
           if (ok2) issue(s + STAGES);
         }
         if (!__all_sync(0xffffffffu, ok2)) {
@@ -423,6 +427,7 @@ float assign_fp32_gamma(int d) {
 cudaError_t launch_assign_fp32(const float* X, long long ldx, const float* Cop, long long ldc,
                                const AssignArgs& a, cudaStream_t s, const GroupArgs* grp,
                                long long tiles) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (a.n <= 0 || a.k <= 0 || a.d <= 0) return cudaSuccess;
   if ((ldx % 4) || (ldc % 4) || (reinterpret_cast<uintptr_t>(X) & 15) ||
       (reinterpret_cast<uintptr_t>(Cop) & 15))

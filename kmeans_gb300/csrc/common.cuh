@@ -71,14 +71,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Bounded wait. `abort_flag` is a CTA-shared word: once set, waits return false at once.
+// `limit`: SM cycles before giving up (KMGB_WAIT_CYCLES unless a test shortens it).
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
-                                          int* err, int code) {
+                                          int* err, int code,
+                                          unsigned long long limit = KMGB_WAIT_CYCLES) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   while (true) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort_flag) return false;
-    if ((unsigned long long)(clock64() - t0) > KMGB_WAIT_CYCLES) {
+    if ((unsigned long long)(clock64() - t0) > limit) {
       *abort_flag = 1;
       set_error(err, code);
       return false;

@@ -9,6 +9,7 @@
 // once); KMGB_POOL=0 trims after every free, which gives back cudaMalloc/cudaFree behaviour.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
@@ -62,8 +63,42 @@ cudaError_t pool_of_current_device(cudaMemPool_t* out) {
 
 }  // namespace
 
+// Test hooks: a countdown per event kind; the event that brings it to zero fails once.
+std::atomic<long long> g_fail_countdown[4];
+std::atomic<long long> g_test_withhold{0};
+std::atomic<unsigned long long> g_test_wait{0};
+
+bool inject_fault(int kind) {
+  if (kind < 1 || kind > 3) return false;
+  long long v = g_fail_countdown[kind].load(std::memory_order_relaxed);
+  while (v > 0) {
+    if (g_fail_countdown[kind].compare_exchange_weak(v, v - 1, std::memory_order_relaxed))
+      return v == 1;
+  }
+  return false;
+}
+
+void test_wait_hook(long long* withhold, unsigned long long* wait_cycles) {
+  *withhold = g_test_withhold.load(std::memory_order_relaxed);
+  *wait_cycles = g_test_wait.load(std::memory_order_relaxed);
+}
+
+int num_sms() {
+  static std::atomic<int> cached[kMaxDevices];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return 148;
+  int v = cached[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      v = 148;  // any positive count only sizes grids; every kernel strides over its work
+    cached[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
+
 cudaError_t dev_alloc(void** p, size_t bytes, cudaStream_t s) {
   *p = nullptr;
+  if (inject_fault(kFaultAlloc)) return cudaErrorMemoryAllocation;
   if (bytes == 0) bytes = 1;
   cudaMemPool_t pool = nullptr;
   cudaError_t r = pool_of_current_device(&pool);
@@ -108,6 +143,24 @@ cudaError_t dev_release_cached() {
 }  // namespace kmgb
 
 extern "C" {
+
+void kmgb_debug_fail_nth(int kind, long long nth) {
+  if (kind < 1 || kind > 3) return;
+  kmgb::g_fail_countdown[kind].store(nth > 0 ? nth : 0, std::memory_order_relaxed);
+}
+
+void kmgb_debug_withhold_stage(long long stage, unsigned long long wait_cycles) {
+  kmgb::g_test_withhold.store(stage > 0 ? stage : 0, std::memory_order_relaxed);
+  kmgb::g_test_wait.store(stage > 0 ? wait_cycles : 0, std::memory_order_relaxed);
+}
+
+long long kmgb_debug_pool_used_bytes(void) {
+  cudaMemPool_t pool = nullptr;
+  if (kmgb::pool_of_current_device(&pool) != cudaSuccess) return -1;
+  uint64_t used = 0;
+  if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess) return -1;
+  return (long long)used;
+}
 
 int kmgb_release_cached_memory(void) {
   const cudaError_t r = kmgb::dev_release_cached();

@@ -484,6 +484,7 @@ constexpr long long kUploadChunks = 8;
 // Rows [r0, r1) of X (host or device, d floats per row) into the device copy, on stream cs.
 cudaError_t copy_rows(kmgb_handle* h, const float* X, long long r0, long long r1,
                       cudaMemcpyKind kind, cudaStream_t cs) {
+  if (inject_fault(kFaultCopy)) return cudaErrorInvalidValue;
   const size_t row_bytes = sizeof(float) * h->d;
   if (h->ldx == h->d)
     return cudaMemcpyAsync(h->X + (size_t)r0 * h->ldx, X + (size_t)r0 * h->d,
@@ -660,6 +661,7 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr) {
   a.certify = h->opt.certify;
   a.stop = h->stop;
   a.cinit = h->cinit;
+  test_wait_hook(&a.test_withhold, &a.test_wait_cycles);  // zero unless a test asks
   const bool tc = h->opt.assign_tier != KMGB_ASSIGN_FP32;
   if (tc && upload) {
     a.gamma = assign_bf16_gamma(h->d);
@@ -1041,6 +1043,8 @@ int finish(kmgb_handle* h) {
   if (h->iterations > 0 && cudaEventElapsedTime(&ms, h->ev0, h->ev1) == cudaSuccess)
     h->ms_total = ms;
   if (h->iterations > 0) {
+    KM_TRY(inject_fault(kFaultCopy) ? cudaErrorInvalidValue : cudaSuccess,
+           KMEANS_ERROR_COMPACTNESS);
     KM_TRY(cudaMemcpy(h->sse_host.data(), h->sse_dev, sizeof(double) * h->iterations,
                       cudaMemcpyDeviceToHost),
            KMEANS_ERROR_COMPACTNESS);
@@ -1090,6 +1094,7 @@ int set_centers(kmgb_handle* h, const float* C, bool on_device) {
   const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
   KM_TRY(cudaMemsetAsync(h->C, 0, sizeof(float) * h->ldx * h->k, h->stream),
          KMEANS_ERROR_INITIALIZE);
+  KM_TRY(inject_fault(kFaultCopy) ? cudaErrorInvalidValue : cudaSuccess, KMEANS_ERROR_INITIALIZE);
   KM_TRY(cudaMemcpy2DAsync(h->C, sizeof(float) * h->ldx, C, row_bytes, row_bytes, h->k, kind,
                            h->stream),
          KMEANS_ERROR_INITIALIZE);
@@ -1138,6 +1143,7 @@ int init_kmeanspp(kmgb_handle* h, unsigned long long seed, int* picks_out) {
 
 int get_centers(kmgb_handle* h, float* out, bool on_device) {
   const size_t row_bytes = sizeof(float) * h->d;
+  KM_TRY(inject_fault(kFaultCopy) ? cudaErrorInvalidValue : cudaSuccess, KMEANS_ERROR_GET_CENTERS);
   KM_TRY(cudaMemcpy2DAsync(out, row_bytes, h->C, sizeof(float) * h->ldx, row_bytes, h->k,
                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                            h->stream),
@@ -1149,6 +1155,7 @@ int get_centers(kmgb_handle* h, float* out, bool on_device) {
 // Labels of the last assignment in source-row order.
 int get_labels(kmgb_handle* h, int* out, bool on_device) {
   KM_TRY(cudaStreamSynchronize(h->stream), KMEANS_ERROR_GET_CENTERS);
+  KM_TRY(inject_fault(kFaultCopy) ? cudaErrorInvalidValue : cudaSuccess, KMEANS_ERROR_GET_CENTERS);
   if (!h->mini) {
     KM_TRY(cudaMemcpy(out, h->labels, sizeof(int) * h->n,
                       on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost),

@@ -213,7 +213,7 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
   KD_TRY(B.alloc(&acc, (size_t)k * n), E);
   KD_TRY(B.alloc(&cnt, k), E);
   KD_TRY(B.alloc(&lab, m_mb), E);
-  const int sse_blocks = 152 * 4;
+  const int sse_blocks = kmgb::num_sms() * 4;
   KD_TRY(B.alloc(&part, sse_blocks), E);
   KD_TRY(B.alloc(&sse, 1), E);
   if (kpp_seed < 0) {
@@ -285,7 +285,7 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
     KD_TRY(B.alloc(&rr_count, 3), E);
     KD_TRY(B.alloc(&derr, 1), E);
     KD_TRY(cudaMemsetAsync(derr, 0, sizeof(int), s), E);
-    d2f_kernel<<<152 * 8, 256, 0, s>>>(X, m, n, Xf, ldx); kmgb::count_launches(1);
+    d2f_kernel<<<kmgb::num_sms() * 8, 256, 0, s>>>(X, m, n, Xf, ldx); kmgb::count_launches(1);
     KD_TRY(cudaGetLastError(), E);
     KD_TRY(launch_point_norms(Xf, ldx, m, n, qn, xn, s), E);
     KD_TRY(launch_to_bf16(Xf, ldx, m, n, Xb, ldb, s, nullptr, Xl, nullptr), EA);
@@ -304,13 +304,13 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
   while (it < maxIters && rel > criterion) {
     const double* Xa = X;
     if (mini) {
-      gather_d_kernel<<<152 * 8, 256, 0, s>>>(X, n, permd, m, start, m_mb, Xw); kmgb::count_launches(1);
+      gather_d_kernel<<<kmgb::num_sms() * 8, 256, 0, s>>>(X, n, permd, m, start, m_mb, Xw); kmgb::count_launches(1);
       Xa = Xw;
     }
-    transpose_d_kernel<<<152 * 4, 256, 0, s>>>(Cd, k, n, CT); kmgb::count_launches(1);
+    transpose_d_kernel<<<kmgb::num_sms() * 4, 256, 0, s>>>(Cd, k, n, CT); kmgb::count_launches(1);
     if (tc) {
       const kmeansErrorStatus EA = KMEANS_ERROR_CLOSEST_CENTERS;
-      d2f_kernel<<<152 * 4, 256, 0, s>>>(Cd, k, n, Cf, ldx); kmgb::count_launches(1);
+      d2f_kernel<<<kmgb::num_sms() * 4, 256, 0, s>>>(Cd, k, n, Cf, ldx); kmgb::count_launches(1);
       KD_TRY(cudaMemsetAsync(cmax, 0, sizeof(float), s), EA);
       KD_TRY(cudaMemsetAsync(rr_count, 0, 3 * sizeof(int), s), EA);
       KD_TRY(launch_prep_centers(Cf, ldx, k, n, Cop, Cb, ldb, cn, cmax, s, nullptr, cinit, Cl), EA);
@@ -330,10 +330,10 @@ kmeansErrorStatus run_d(const double* data, int m, int n, int k, double criterio
       a.gamma = assign_bf16_gamma(n);
       a.pert = 0x1p-22f;
       KD_TRY(launch_assign_bf16(Xb, Xl, ldb, Cb, Cl, ldb, a, s), EA);
-      assign_d_kernel<<<152 * 8, threads, smem, s>>>(X, m, n, CT, k, lab, rr_list, rr_count);
+      assign_d_kernel<<<kmgb::num_sms() * 8, threads, smem, s>>>(X, m, n, CT, k, lab, rr_list, rr_count);
       kmgb::count_launches(1);
     } else {
-      assign_d_kernel<<<152 * 8, threads, smem, s>>>(Xa, m_mb, n, CT, k, lab);
+      assign_d_kernel<<<kmgb::num_sms() * 8, threads, smem, s>>>(Xa, m_mb, n, CT, k, lab);
       kmgb::count_launches(1);
     }
     KD_TRY(cudaGetLastError(), KMEANS_ERROR_CLOSEST_CENTERS);

@@ -48,6 +48,11 @@ struct AssignArgs {
   const int* g_k;
   const long long* g_rend;
   const int* g_done;
+  // test hook of the FP32 tier (kmgb_debug_withhold_stage): the producer issues no TMA load for
+  // pipeline steps >= test_withhold (0: every step), and every wait gives up after
+  // test_wait_cycles SM cycles (0: KMGB_WAIT_CYCLES)
+  long long test_withhold;
+  unsigned long long test_wait_cycles;
 };
 
 // Many problems of one dimension in one launch (batched Lloyd): problem p owns rows
@@ -259,6 +264,20 @@ bool reference_picks(int m, int k, std::vector<int>& picks);
 
 // Message returned by kmgb_last_error() on the calling thread.
 void set_last_error(const char* msg);
+
+// Streaming multiprocessors of the current device (cached per device); sizes grids.
+int num_sms();
+
+// Test hooks (devmem.cu; kmgb_debug_fail_nth, kmgb_debug_withhold_stage): inject_fault(kind)
+// is true for the one event of that kind that a test asked to fail; the library then returns
+// the CUDA error that event would have produced instead of performing it.
+constexpr int kFaultAlloc = 1;   // device allocation from the pool
+constexpr int kFaultCopy = 2;    // host<->device copy of a data set, centers or results
+constexpr int kFaultLaunch = 3;  // launch of a Lloyd-phase kernel
+bool inject_fault(int kind);
+// FP32-tier assignment launches: withhold the TMA loads of pipeline steps >= *withhold (0: off)
+// and bound every wait by *wait_cycles SM cycles (0: the default limit).
+void test_wait_hook(long long* withhold, unsigned long long* wait_cycles);
 
 // Device memory from the library's stream-ordered pool of the current device (devmem.cu):
 // dev_alloc returns memory usable from every stream; dev_free gives it back in the order of s.

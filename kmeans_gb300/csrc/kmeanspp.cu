@@ -457,7 +457,7 @@ cudaError_t kmeanspp_impl(const T* X, long long ldx, long long n, int d, int k,
                                                pick, picks);
     count_launches(3);
   }
-  kpp_gather_kernel<T><<<152 * 4, 256, 0, s>>>(X, ldx, d, picks, k, C, ldc);
+  kpp_gather_kernel<T><<<kmgb::num_sms() * 4, 256, 0, s>>>(X, ldx, d, picks, k, C, ldc);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -179,6 +179,7 @@ __global__ void gather_vec_kernel(const double* __restrict__ qs, const float* __
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop, void* Cb,
                                 long long ldcb, float* cn, float* cmax, cudaStream_t s,
                                 const int* stop, float* cinit, void* Cl) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (k <= 0) return cudaSuccess;
   const int threads = 256;
   const int kpad = (k + kCenterPad - 1) / kCenterPad * kCenterPad;
@@ -192,6 +193,7 @@ cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, flo
 
 cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,
                                float* xn, cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (n <= 0) return cudaSuccess;
   const int threads = 256;
   const long long blocks = (n * 32 + threads - 1) / threads;
@@ -202,8 +204,9 @@ cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d
 cudaError_t launch_to_bf16(const float* X, long long ldx, long long n, int d, void* Xb,
                            long long ldb, cudaStream_t s, const int* stop, void* Xl,
                            int* inexact) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (n <= 0) return cudaSuccess;
-  to_bf16_kernel<<<152 * 16, 256, 0, s>>>(X, ldx, n, d, reinterpret_cast<__nv_bfloat16*>(Xb),
+  to_bf16_kernel<<<kmgb::num_sms() * 16, 256, 0, s>>>(X, ldx, n, d, reinterpret_cast<__nv_bfloat16*>(Xb),
                                           ldb, stop, reinterpret_cast<__nv_bfloat16*>(Xl),
                                           inexact); kmgb::count_launches(1);
   return cudaGetLastError();
@@ -224,7 +227,7 @@ cudaError_t launch_gather_vec(const double* qsrc, const float* xsrc, const int* 
                               long long start, long long m_mb, double* qdst, float* xdst,
                               cudaStream_t s, const int* stop) {
   if (m_mb <= 0) return cudaSuccess;
-  gather_vec_kernel<<<152 * 4, 256, 0, s>>>(qsrc, xsrc, perm, m, start, m_mb, qdst, xdst, stop); kmgb::count_launches(1);
+  gather_vec_kernel<<<kmgb::num_sms() * 4, 256, 0, s>>>(qsrc, xsrc, perm, m, start, m_mb, qdst, xdst, stop); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

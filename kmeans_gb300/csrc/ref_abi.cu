@@ -304,7 +304,7 @@ kmeansCudaErrorStatus compactness(int m0, int m, bool lastTile, int n, int k, co
   if (m < 0 || n <= 0 || !out) return ERROR_COMPACTNESS;
   double* acc = (sizeof(T) == 4) ? reinterpret_cast<double*>(out + 2) : reinterpret_cast<double*>(out + 1);
   if (reinterpret_cast<uintptr_t>(acc) & 7) return ERROR_COMPACTNESS;
-  const int blocks = 152 * 4;
+  const int blocks = kmgb::num_sms() * 4;
   double* part = nullptr;
   cudaError_t e = tmp_alloc(&part, blocks);
   if (!e) {
@@ -355,12 +355,12 @@ kmeansCudaErrorStatus ClosestCentersF(const int m0, const int nRowsA, const int 
   if (!e) e = cudaMemsetAsync(err, 0, sizeof(int), kDefault);
   const float* Xa = A;
   if (!e && !direct) {
-    copy_pad_kernel<<<152 * 8, 256, 0, kDefault>>>(A, nRowsA, d, Ap, ld); kmgb::count_launches(1);
+    copy_pad_kernel<<<kmgb::num_sms() * 8, 256, 0, kDefault>>>(A, nRowsA, d, Ap, ld); kmgb::count_launches(1);
     e = cudaGetLastError();
     Xa = Ap;
   }
   if (!e) {
-    transpose_centers_kernel<float><<<152 * 4, 256, 0, kDefault>>>(B, d, k, Bt, ld); kmgb::count_launches(1);
+    transpose_centers_kernel<float><<<kmgb::num_sms() * 4, 256, 0, kDefault>>>(B, d, k, Bt, ld); kmgb::count_launches(1);
     e = cudaGetLastError();
   }
   if (!e) e = launch_point_norms(Xa, ld, nRowsA, d, nullptr, xn, kDefault);
@@ -435,7 +435,7 @@ kmeansCudaErrorStatus ClosestCentersD(const int m0, const int nRowsA, const int 
       cudaFuncSetAttribute(closest_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)smem) != cudaSuccess)
     return ERROR_CLOSESTCENTERS;
-  closest_fp64_kernel<<<152 * 8, threads, smem, kDefault>>>(m0, nRowsA, nColsA, A, nColsB, B,
+  closest_fp64_kernel<<<kmgb::num_sms() * 8, threads, smem, kDefault>>>(m0, nRowsA, nColsA, A, nColsB, B,
                                                             normColsOfB_squared, CindicesFinal); kmgb::count_launches(1);
   return cudaGetLastError() ? ERROR_CLOSESTCENTERS : NO_ERROR;
 }
@@ -446,7 +446,7 @@ kmeansCudaErrorStatus rowTransformMinimumF(const int m0, const int m, const int 
                                            int* output) {
   if (m < 0 || n <= 0) return ERROR_ROWTRANSFORMMINIMUM;
   if (m == 0) return NO_ERROR;
-  row_transform_min_kernel<float><<<152 * 8, 256, 0, kDefault>>>(
+  row_transform_min_kernel<float><<<kmgb::num_sms() * 8, 256, 0, kDefault>>>(
       m0, m, n, normRowsOfA_squared, normColsOfB_squared, input, output); kmgb::count_launches(1);
   return cudaGetLastError() ? ERROR_ROWTRANSFORMMINIMUM : NO_ERROR;
 }
@@ -457,7 +457,7 @@ kmeansCudaErrorStatus rowTransformMinimumD(const int m0, const int m, const int 
                                            const double* input, int* output) {
   if (m < 0 || n <= 0) return ERROR_ROWTRANSFORMMINIMUM;
   if (m == 0) return NO_ERROR;
-  row_transform_min_kernel<double><<<152 * 8, 256, 0, kDefault>>>(
+  row_transform_min_kernel<double><<<kmgb::num_sms() * 8, 256, 0, kDefault>>>(
       m0, m, n, normRowsOfA_squared, normColsOfB_squared, input, output); kmgb::count_launches(1);
   return cudaGetLastError() ? ERROR_ROWTRANSFORMMINIMUM : NO_ERROR;
 }
@@ -504,7 +504,7 @@ kmeansCudaErrorStatus rowNormalizeF(const int m0, const int m, const int n, cons
                                     float* output) {
   if (m < 0 || n <= 0) return ERROR_ROWNORMALIZE;
   if (m == 0) return NO_ERROR;
-  row_norm_kernel<float><<<152 * 8, 256, 0, kDefault>>>(m0, m, n, input, output); kmgb::count_launches(1);
+  row_norm_kernel<float><<<kmgb::num_sms() * 8, 256, 0, kDefault>>>(m0, m, n, input, output); kmgb::count_launches(1);
   return cudaGetLastError() ? ERROR_ROWNORMALIZE : NO_ERROR;
 }
 
@@ -512,7 +512,7 @@ kmeansCudaErrorStatus rowNormalizeD(const int m0, const int m, const int n, cons
                                     double* output) {
   if (m < 0 || n <= 0) return ERROR_ROWNORMALIZE;
   if (m == 0) return NO_ERROR;
-  row_norm_kernel<double><<<152 * 8, 256, 0, kDefault>>>(m0, m, n, input, output); kmgb::count_launches(1);
+  row_norm_kernel<double><<<kmgb::num_sms() * 8, 256, 0, kDefault>>>(m0, m, n, input, output); kmgb::count_launches(1);
   return cudaGetLastError() ? ERROR_ROWNORMALIZE : NO_ERROR;
 }
 

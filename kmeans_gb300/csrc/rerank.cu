@@ -804,8 +804,9 @@ cudaError_t launch_gather_flagged(const int* list, const int* count, long long c
                                   const void* Xb, const void* Xl, long long ldb, const float* thr,
                                   void* XbC, void* XlC, float* thrC, int* over, int* over_count,
                                   const int* stop, cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if ((ldb * 2) % 16) return cudaErrorInvalidValue;
-  gather_flagged_kernel<<<152 * 8, 256, 0, s>>>(
+  gather_flagged_kernel<<<kmgb::num_sms() * 8, 256, 0, s>>>(
       list, count, cap, reinterpret_cast<const uint4*>(Xb), reinterpret_cast<const uint4*>(Xl),
       ldb * 2 / 16, thr, reinterpret_cast<uint4*>(XbC), reinterpret_cast<uint4*>(XlC), thrC, over,
       over_count, stop);
@@ -818,14 +819,15 @@ cudaError_t launch_resolve_candidates(const int* list, const int* count, long lo
                                       long long ldx, const float* C, long long ldc, const float* cn,
                                       int d, int* labels, int* over, int* over_count,
                                       const int* stop, cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   const bool vec = d % 4 == 0 && ldx % 4 == 0 && ldc % 4 == 0 &&
                    reinterpret_cast<uintptr_t>(X) % 16 == 0 && reinterpret_cast<uintptr_t>(C) % 16 == 0;
   if (vec)
-    resolve_candidates_kernel<true><<<152 * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
+    resolve_candidates_kernel<true><<<kmgb::num_sms() * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
                                                             X, ldx, C, ldc, cn, d, labels, over,
                                                             over_count, stop);
   else
-    resolve_candidates_kernel<false><<<152 * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
+    resolve_candidates_kernel<false><<<kmgb::num_sms() * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
                                                              X, ldx, C, ldc, cn, d, labels, over,
                                                              over_count, stop);
   count_launches(1);
@@ -840,6 +842,7 @@ cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long lo
 }
 
 cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (a.n <= 0 || a.k <= 0) return cudaSuccess;
   const int dq = (a.d + 3) / 4;
   const size_t smem = sizeof(float4) * (size_t)(TP + TC) * (dq + 1) + sizeof(float) * TC;
@@ -847,13 +850,14 @@ cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStrea
   if (smem > 48 * 1024)
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_exact_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  rerank_exact_kernel<<<152 * 2, 256, smem, s>>>(a, hi2);
+  rerank_exact_kernel<<<kmgb::num_sms() * 2, 256, smem, s>>>(a, hi2);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, float* hi2,
                                 cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (a.n <= 0 || a.k <= 0) return cudaSuccess;
   const int dq = (a.d + 3) / 4;
   const size_t smem = sizeof(float4) * (size_t)(TP + TC) * (dq + 1) + sizeof(float) * TC;
@@ -861,7 +865,7 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, fl
   if (smem > 48 * 1024)
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_tiled_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  rerank_tiled_kernel<<<152 * 2, 256, smem, s>>>(a, list2, count2, hi2);
+  rerank_tiled_kernel<<<kmgb::num_sms() * 2, 256, smem, s>>>(a, list2, count2, hi2);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -873,7 +877,7 @@ cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaS
   if (smem > 48 * 1024)
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_grouped_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  rerank_grouped_kernel<<<152 * 4, RG_WARPS * 32, smem, s>>>(a, g);
+  rerank_grouped_kernel<<<kmgb::num_sms() * 4, RG_WARPS * 32, smem, s>>>(a, g);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -888,7 +892,7 @@ cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s) {
                                        (int)smem));
   }
   // Persistent grid: the flagged count lives on the device, so no host round trip is needed.
-  rerank_kernel<<<152 * 4, threads, smem, s>>>(a); kmgb::count_launches(1);
+  rerank_kernel<<<kmgb::num_sms() * 4, threads, smem, s>>>(a); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

@@ -12,13 +12,18 @@
 // that loads the library holds it until the process exits. In host code the array's name is a
 // host-side stand-in, not a device address, so its device address is looked up once per device
 // with cudaGetSymbolAddress (with that device current) and cached. The first call on a device
-// performs that lookup; make that first call before any stream capture.
+// performs that lookup; make that first call before any stream capture. The cached address
+// belongs to the device's primary context: after cudaDeviceReset (or anything else that destroys
+// that context) the module is loaded again and the array may sit elsewhere, so a reset drops the
+// cache (the lookup is keyed on the context that is current when the call is made).
 //
 // All calls share the one array and it keeps the last call's contents; everything that must start
 // at zero (the histogram) is cleared by the call itself. Calls that overlap on the GPU (different
 // streams or threads, or ClusterCentersF_noalloc calls queued from several host threads) race on
 // the array and must be serialised by the caller. Sizes whose working memory exceeds the array
 // are rejected with ERROR_CLUSTERCENTERS and a message from kmgb_last_error().
+#include <cudaTypedefs.h>
+
 #include <mutex>
 
 #include "../../include/kmeans_gb300.h"
@@ -34,19 +39,41 @@ namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_scratch_ptr[kMaxDevices] = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};  // context the cached address belongs to
 
-// Device address of the scratch array on the current device (looked up once per device).
+// The current driver context (through the runtime's driver entry point: no -lcuda link).
+CUcontext current_context() {
+  static PFN_cuCtxGetCurrent_v4000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+  });
+  CUcontext ctx = nullptr;
+  if (!fn || fn(&ctx) != CUDA_SUCCESS) return nullptr;
+  return ctx;
+}
+
+// Device address of the scratch array on the current device, looked up once per device and
+// context: a new primary context (after a device reset) gets a fresh lookup.
 cudaError_t scratch_address(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  // null until the runtime has made the device's primary context current
+  const CUcontext ctx = current_context();
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!ctx || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);  // also initialises the context
     if (e != cudaSuccess) return e;
     g_scratch_ptr[dev] = p;
+    g_scratch_ctx[dev] = current_context();
   }
   *out = g_scratch_ptr[dev];
   return cudaSuccess;
@@ -83,27 +110,31 @@ extern "C" kmeansCudaErrorStatus ClusterCentersF_noalloc(const int m0, const int
   const size_t o_sorted = o_pcnt + align256(sizeof(int) * (size_t)(k + 1));
   const size_t o_part = o_sorted + align256(sizeof(int) * (size_t)(m > 0 ? m : 1));
   const size_t total = o_part + align256(sizeof(double) * (size_t)w.max_pieces * n);
-  if (total > KMGB_NOALLOC_SCRATCH_BYTES) {
-    set_last_error("ClusterCentersF_noalloc: this m, n, k needs more working memory than the "
-                   "8 MiB static scratch array holds");
-    return ERROR_CLUSTERCENTERS;
-  }
-  void* base = nullptr;
-  if (scratch_address(&base) != cudaSuccess) {
-    set_last_error("ClusterCentersF_noalloc: cudaGetSymbolAddress of the scratch array failed");
-    return ERROR_CLUSTERCENTERS;
-  }
-  unsigned char* s = static_cast<unsigned char*>(base);
-  w.hist = reinterpret_cast<int*>(s + o_hist);
-  w.scan_tmp = reinterpret_cast<int*>(s + o_scan);
-  w.label_off = reinterpret_cast<int*>(s + o_off);
-  w.piece_cnt = reinterpret_cast<int*>(s + o_pcnt);
-  w.sorted = reinterpret_cast<int*>(s + o_sorted);
-  w.part = reinterpret_cast<double*>(s + o_part);
   const cudaStream_t stream = 0;  // the reference's per-kernel entries run on the default stream
   cudaError_t e = cudaSuccess;
-  if (m > 0)  // clears the histogram itself before counting
+  // only a call with rows uses the working memory: a finalize-only call (m == 0, lastTile) is
+  // accepted at any size, as ClusterCentersF accepts it
+  if (m > 0) {
+    if (total > KMGB_NOALLOC_SCRATCH_BYTES) {
+      set_last_error("ClusterCentersF_noalloc: this m, n, k needs more working memory than the "
+                     "8 MiB static scratch array holds");
+      return ERROR_CLUSTERCENTERS;
+    }
+    void* base = nullptr;
+    if (scratch_address(&base) != cudaSuccess) {
+      set_last_error("ClusterCentersF_noalloc: cudaGetSymbolAddress of the scratch array failed");
+      return ERROR_CLUSTERCENTERS;
+    }
+    unsigned char* s = static_cast<unsigned char*>(base);
+    w.hist = reinterpret_cast<int*>(s + o_hist);
+    w.scan_tmp = reinterpret_cast<int*>(s + o_scan);
+    w.label_off = reinterpret_cast<int*>(s + o_off);
+    w.piece_cnt = reinterpret_cast<int*>(s + o_pcnt);
+    w.sorted = reinterpret_cast<int*>(s + o_sorted);
+    w.part = reinterpret_cast<double*>(s + o_part);
+    // clears the histogram itself before counting
     e = launch_tile_accumulate<float>(data, n, indices + m0, w, acc, counts_large, stream);
+  }
   if (e == cudaSuccess && lastTile)
     e = launch_finalize_acc<float>(acc, counts_large, k, n, centers, counts, stream);
   return e == cudaSuccess ? NO_ERROR : ERROR_CLUSTERCENTERS;

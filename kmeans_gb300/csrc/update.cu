@@ -523,7 +523,7 @@ cudaError_t launch_piece_sums_f32(const float* X, long long ldx, const double* q
   const bool vec = ldx % 4 == 0 && d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
   const int lanes = !vec || d > 64 ? 32 : (d <= 16 ? 4 : (d <= 32 ? 8 : 16));
   long long warps = (max_pieces + 32 / lanes - 1) / (32 / lanes);
-  if (warps > 152LL * 64) warps = 152LL * 64;
+  if (warps > kmgb::num_sms() * 64LL) warps = kmgb::num_sms() * 64LL;
   const unsigned blocks = (unsigned)((warps * 32 + 255) / 256);
   if (vec && lanes == 4)
     piece_sums_small_kernel<4><<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k, d,
@@ -757,6 +757,7 @@ static cudaError_t sort_by_label(const int* labels, const UpdateWork& w, cudaStr
 cudaError_t launch_update(const float* X, const double* qn, const int* labels, float* C,
                           long long ldc, int empty_policy, const UpdateWork& w, double* sse_out,
                           cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   const int k = w.k;
   if (w.n <= 0 || k <= 0) return cudaSuccess;
   KMGB_CUDA_TRY(sort_by_label(labels, w, s));
@@ -887,7 +888,7 @@ cudaError_t launch_tile_accumulate(const T* X, long long ldx, const int* labels,
                                    double* acc, int* acc_counts, cudaStream_t s) {
   if (w.n <= 0 || w.k <= 0) return cudaSuccess;
   KMGB_CUDA_TRY(sort_by_label(labels, w, s));
-  long long warps = w.max_pieces < 152LL * 64 ? w.max_pieces : 152LL * 64;
+  long long warps = w.max_pieces < kmgb::num_sms() * 64LL ? w.max_pieces : kmgb::num_sms() * 64LL;
   piece_sums_kernel<T><<<(unsigned)((warps * 32 + 255) / 256), 256, 0, s>>>(
       X, ldx, nullptr, w.sorted, w.label_off, w.piece_cnt, w.k, w.d, w.part, nullptr, w.stop); kmgb::count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
@@ -899,7 +900,7 @@ cudaError_t launch_tile_accumulate(const T* X, long long ldx, const int* labels,
 template <typename T>
 cudaError_t launch_finalize_acc(const double* acc, const int* acc_counts, int k, int d, T* centers,
                                 int* counts, cudaStream_t s) {
-  finalize_acc_kernel<T><<<152 * 4, 256, 0, s>>>(acc, acc_counts, k, d, centers, counts); kmgb::count_launches(1);
+  finalize_acc_kernel<T><<<kmgb::num_sms() * 4, 256, 0, s>>>(acc, acc_counts, k, d, centers, counts); kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

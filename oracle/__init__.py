@@ -46,9 +46,15 @@ _REF_CP_CUBIN = os.path.join(_REF, "compactness.cubin")
 _REF_SO = os.path.join(_REF, "libref_kernels.so")
 _REF_LOADER_SRC = os.path.join(_HERE, "ref_kernels.cpp")
 _REF_SHIM = os.path.join(_HERE, "ref_shfl_shim.h")
-# The reference's CUDA sources; present only in the development container, never on the GPU host
-# (which uses the prebuilt cubin from oracle/_ref).
-_REFERENCE_CUDA_DIR = "/root/reference/main/cuda"
+
+
+def _reference_cuda_dir() -> str:
+    """main/cuda of the reference checkout: $KMGB_REFERENCE_DIR when set, else a checkout named
+    `reference` beside this repository. Present only where the reference's sources are (the
+    development machine), never on the GPU host, which uses the prebuilt cubins in oracle/_ref."""
+    root = os.environ.get("KMGB_REFERENCE_DIR") or os.path.join(
+        os.path.dirname(os.path.dirname(_HERE)), "reference")
+    return os.path.join(root, "main", "cuda")
 
 
 def _cuda_home() -> str:
@@ -72,14 +78,15 @@ def build_ref() -> bool:
     Returns True when both the cubin and the loader exist.
     """
     os.makedirs(_REF, exist_ok=True)
+    ref_dir = _reference_cuda_dir()
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     for name, out in (("ClosestCenters.cu", _REF_CUBIN), ("ClusterCenters.cu", _REF_CC_CUBIN),
                       ("Compactness.cu", _REF_CP_CUBIN)):
-        src = os.path.join(_REFERENCE_CUDA_DIR, name)
+        src = os.path.join(ref_dir, name)
         if os.path.exists(src) and not os.path.exists(out):
             subprocess.check_call([nvcc, "-cubin", "-gencode", "arch=compute_103a,code=sm_103a",
-                                   "-O3", "-w", "-include", _REF_SHIM, "-I", _REFERENCE_CUDA_DIR,
+                                   "-O3", "-w", "-include", _REF_SHIM, "-I", ref_dir,
                                    src, "-o", out + ".tmp"])
             os.replace(out + ".tmp", out)
     if os.path.isdir(os.path.join(cuda, "include")) and (

@@ -87,3 +87,33 @@ def test_reference_init_matches_oracle_and_fixtures(km, orc):
             continue
         _, _, p = km.reference_init(Z, k)
         assert p.tolist() == v, key
+
+
+def test_header_compiles_as_c_and_cpp_with_reference_default(km, tmp_path):
+    """A C++ caller of the reference passes 11 arguments to computeKmeansF/D (miniBatchFraction
+    defaults to 1.0 in kmeans.hpp:102-132); the header keeps that default for C++ and stays valid
+    C."""
+    inc = os.path.dirname(km.HEADER_PATH)
+    cpp = tmp_path / "caller.cpp"
+    cpp.write_text('#include "kmeans_gb300.h"\n'
+                   "int f(const float* d, float* r, const double* dd, double* rd) {\n"
+                   "  return computeKmeansF(d, 4, 2, 2, -1.0f, 1, 1, 0, 0, 0, r) +\n"
+                   "         computeKmeansD(dd, 4, 2, 2, -1.0, 1, 1, 0, 0, 0, rd);\n}\n")
+    c = tmp_path / "caller.c"
+    c.write_text('#include "kmeans_gb300.h"\n'
+                 "int f(const float* d, float* r) {\n"
+                 "  return computeKmeansF(d, 4, 2, 2, -1.0f, 1, 1, 0, 0, 0, r, 1.0f);\n}\n")
+    subprocess.run(["g++", "-std=c++17", "-c", "-I", inc, str(cpp), "-o", str(tmp_path / "a.o")],
+                   check=True)
+    subprocess.run(["gcc", "-std=c99", "-c", "-I", inc, str(c), "-o", str(tmp_path / "b.o")],
+                   check=True)
+
+
+def test_debug_hooks_exported_and_inert_without_gpu(km):
+    lib = km.lib()
+    # arming and disarming touches no device
+    km.debug_fail_nth(km.FAULT_LAUNCH, 3)
+    km.debug_fail_nth(km.FAULT_LAUNCH, 0)
+    km.debug_withhold_stage(0, 0)
+    for s in ("kmgb_debug_fail_nth", "kmgb_debug_withhold_stage", "kmgb_debug_pool_used_bytes"):
+        assert getattr(lib, s) is not None

@@ -56,3 +56,27 @@ def test_noalloc_rejects_sizes_beyond_its_array(km, torch_cuda):
     rc = km.ClusterCentersF_noalloc(0, m, d, k, True, X, lab, big, cnt_big, cen, cnt)
     assert rc == 4  # ERROR_CLUSTERCENTERS
     assert "8 MiB" in km.last_error()
+
+
+def test_noalloc_finalize_only_call_at_any_size(km, torch_cuda):
+    """A finalize-only call (no rows, lastTile) uses no working memory: it is accepted whatever
+    k and n, as ClusterCentersF accepts it, and gives the same means from the same totals."""
+    torch = torch_cuda
+    rng = np.random.default_rng(3)
+    k, d = 4096, 300  # (k + 1) * d * 8 bytes of sums alone exceed the 8 MiB array
+    sums = torch.from_numpy(rng.standard_normal(k * d) * 50).cuda()  # FP64 running sums
+    counts = torch.from_numpy(rng.integers(0, 9, size=k).astype(np.int32)).cuda()
+    outs = []
+    for fn in (km.ClusterCentersF, km.ClusterCentersF_noalloc):
+        big = sums.clone().view(torch.float32)
+        cnt_big = counts.clone()
+        cen = torch.zeros((k, d), dtype=torch.float32, device="cuda")
+        cnt = torch.zeros(k, dtype=torch.int32, device="cuda")
+        dummy = torch.zeros(1, dtype=torch.float32, device="cuda")
+        lab = torch.zeros(1, dtype=torch.int32, device="cuda")
+        rc = fn(0, 0, d, k, True, dummy, lab, big, cnt_big, cen, cnt)
+        assert rc == 0, km.last_error()
+        torch.cuda.synchronize()
+        outs.append((cen.cpu().numpy(), cnt.cpu().numpy()))
+    assert np.array_equal(outs[0][0], outs[1][0], equal_nan=True)
+    assert np.array_equal(outs[0][1], outs[1][1])
