@@ -241,7 +241,14 @@ typedef struct kmgb_options {
   int num_retries;           /* k-means++: runs seeded seed, seed+1, ...; the run with the lowest
                                 final SSE is returned (< 1 counts as 1) */
   unsigned long long seed;   /* k-means++ seed */
-  int reserved[4];
+  int router;                /* 1: learned router (needs a BF16 tier, full batches, resident
+                                data): after the first iteration an MLP routes every point to one
+                                group of centers, the point is scanned against that group only and
+                                certified (see kmgb_get_router_stats); uncertified points take the
+                                full scan, so labels are unchanged */
+  int router_groups;         /* G, groups of centers (0: 256) */
+  int router_retrain;        /* retrain every this many iterations (0: 5) */
+  int router_hidden;         /* hidden units of the MLP, 256 or 512 (0: 512) */
 } kmgb_options;
 
 typedef struct kmgb_stats {
@@ -253,8 +260,29 @@ typedef struct kmgb_stats {
                                       (FP32 then FP64) instead of their recorded candidates */
   long long empty_clusters;        /* empty clusters seen after the last update */
   double ms_total;                 /* wall time of the iterations (CUDA events) */
-  long long reserved[8];
+  long long reserved[8];           /* with the router: [0] points routed to a group scan, [1]
+                                      of those certified, [2] points that took the full scan,
+                                      [3] trainings, [4] training wall time (us), [5] routed
+                                      points whose in-group margin took the candidate pass */
 } kmgb_stats;
+
+/* The learned router's record (kmgb_get_router_stats); counters sum over the iterations run. */
+typedef struct kmgb_router_stats {
+  long long trainings;        /* trainings run (the groups are formed at the first) */
+  double train_ms;            /* wall time of the trainings, grouping included */
+  double group_ms;            /* of which forming the groups of centers */
+  double last_loss;           /* mean cross-entropy of the last training batch */
+  double last_accuracy;       /* share of that batch routed to its label's group */
+  int groups_nonempty;        /* groups holding at least one center */
+  int components;             /* components of linked centers packed into the groups */
+  unsigned long long routed;  /* points routed to a group scan */
+  unsigned long long flagged; /* of those, points whose in-group margin took the candidate pass */
+  unsigned long long certified; /* points whose group winner was certified as the arg-min */
+  unsigned long long fallback;  /* points that took the full scan instead */
+  long long routed_iterations;  /* iterations that ran the routed scan */
+  long long device_bytes;       /* device memory of the router (fallback buffers excluded) */
+  long long reserved[4];
+} kmgb_router_stats;
 
 /* The reference's initial centers, computed on the host: k x d row-major copies of data rows
  * perm[picks[i]], perm from std::shuffle(default_random_engine(0)) and picks from srand(42) /
@@ -337,6 +365,18 @@ KMGB_EXPORT int kmgb_get_centers(kmgb_handle* h, float* C, int c_on_device);
 KMGB_EXPORT int kmgb_get_labels(kmgb_handle* h, int* labels, int on_device);
 KMGB_EXPORT int kmgb_get_sse(kmgb_handle* h, double* sse, int max_count); /* returns the count written */
 KMGB_EXPORT int kmgb_get_stats(kmgb_handle* h, kmgb_stats* stats);
+/* The router's record (all zero when the handle runs without it). No reference counterpart:
+ * the reference scans every center for every point (ClosestCenters.cu:46-83). */
+KMGB_EXPORT int kmgb_get_router_stats(kmgb_handle* h, kmgb_router_stats* stats);
+/* The router's network alone, for checking it: trains the MLP X (rows x d, host) -> groups with
+ * labels y (host, in [0, groups)) from the flat parameters `params` (host, in/out: W1 hidden x d,
+ * b1, W2 groups x hidden, b2, row-major) with Adam (lr, betas 0.9 / 0.999, eps 1e-8) on
+ * consecutive batches of `batch` rows, `steps` steps. steps == 0: one forward and backward pass
+ * over the first batch, its gradients in grads_out (host, nullable) and the parameters unchanged.
+ * loss (nullable): the mean cross-entropy of the last batch before its update. */
+KMGB_EXPORT int kmgb_router_mlp_train(const float* X, int rows, int d, const int* y, int hidden,
+                                      int groups, float* params, int batch, int steps, float lr,
+                                      double* loss, float* grads_out);
 KMGB_EXPORT void* kmgb_stream(kmgb_handle* h); /* cudaStream_t of the handle */
 KMGB_EXPORT int kmgb_destroy(kmgb_handle* h);
 

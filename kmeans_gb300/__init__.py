@@ -76,7 +76,8 @@ class kmgb_options(C.Structure):
                 ("max_iters", C.c_int), ("criterion", C.c_double),
                 ("mini_batch_fraction", C.c_float), ("stream_tile_rows", C.c_int),
                 ("init_algorithm", C.c_int), ("num_retries", C.c_int),
-                ("seed", C.c_ulonglong), ("reserved", C.c_int * 4)]
+                ("seed", C.c_ulonglong), ("router", C.c_int), ("router_groups", C.c_int),
+                ("router_retrain", C.c_int), ("router_hidden", C.c_int)]
 
 
 class kmgb_problem(C.Structure):
@@ -84,6 +85,19 @@ class kmgb_problem(C.Structure):
                 ("init", C.c_void_p), ("centers", C.c_void_p), ("labels", C.c_void_p),
                 ("sse", C.c_void_p), ("iterations", C.c_int), ("status", C.c_int),
                 ("reserved", C.c_longlong * 4)]
+
+
+class kmgb_router_stats(C.Structure):
+    _fields_ = [("trainings", C.c_longlong), ("train_ms", C.c_double), ("group_ms", C.c_double),
+                ("last_loss", C.c_double), ("last_accuracy", C.c_double),
+                ("groups_nonempty", C.c_int), ("components", C.c_int),
+                ("routed", C.c_ulonglong), ("flagged", C.c_ulonglong),
+                ("certified", C.c_ulonglong), ("fallback", C.c_ulonglong),
+                ("routed_iterations", C.c_longlong), ("device_bytes", C.c_longlong),
+                ("reserved", C.c_longlong * 4)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
 class kmgb_stats(C.Structure):
@@ -157,6 +171,8 @@ def lib():
             "kmgb_kmeanspp_f64": (i32, [P, i64, i32, i32, C.c_ulonglong, P, P]),
             "kmgb_init_kmeanspp": (i32, [P, C.c_ulonglong, P]),
             "kmgb_lloyd_batched_f32": (i32, [P, i32, P, P]),
+            "kmgb_get_router_stats": (i32, [P, P]),
+            "kmgb_router_mlp_train": (i32, [P, i32, i32, P, i32, i32, P, i32, i32, f32, P, P]),
             "kmgb_debug_fail_nth": (None, [i32, i64]),
             "kmgb_debug_withhold_stage": (None, [i64, C.c_ulonglong]),
             "kmgb_debug_pool_used_bytes": (i64, []),
@@ -193,6 +209,24 @@ def debug_withhold_stage(stage: int, wait_cycles: int = 0) -> None:
     """Test hook: FP32-tier assignment launches withhold their TMA loads from pipeline step
     `stage` on (0 disarms) and bound every wait by `wait_cycles` SM cycles."""
     lib().kmgb_debug_withhold_stage(int(stage), int(wait_cycles))
+
+
+def router_mlp_train(X: np.ndarray, y: np.ndarray, params: np.ndarray, hidden: int, groups: int,
+                     batch: int, steps: int, lr: float = 1e-3):
+    """The router's network alone (kmgb_router_mlp_train): steps == 0 returns (loss, gradients)
+    of one forward/backward pass over the first batch; otherwise trains `params` in place with
+    Adam and returns (loss of the last batch, None)."""
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.int32)
+    assert params.dtype == np.float32 and params.flags.c_contiguous
+    rows, d = X.shape
+    loss = C.c_double()
+    grads = np.empty_like(params) if steps == 0 else None
+    rc = lib().kmgb_router_mlp_train(_ptr(X), rows, d, _ptr(y), hidden, groups, _ptr(params),
+                                     batch, steps, lr, C.byref(loss), _ptr(grads))
+    if rc:
+        raise KmeansError(rc, last_error())
+    return loss.value, grads
 
 
 def debug_pool_used_bytes() -> int:
@@ -398,7 +432,8 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
           assign_tier: int = ASSIGN_FP32, certify: bool = True, empty_policy: int = EMPTY_NAN,
           mini_batch_fraction: float = 1.0, stream_tile_rows: int = 0,
           init_algorithm: int = INIT_REFERENCE, num_retries: int = 1,
-          seed: int = 0) -> LloydResult:
+          seed: int = 0, router: bool = False, router_groups: int = 0,
+          router_retrain: int = 0) -> LloydResult:
     """One-shot Lloyd run through kmgb_lloyd_f32. X: numpy (host) or torch (device) n x d
     float32; init: k x d float32, or None for init_algorithm (the reference initialisation, or
     k-means++ with num_retries seeded runs keeping the lowest final SSE). stream_tile_rows > 0
@@ -412,7 +447,8 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
                           empty_policy=empty_policy, max_iters=max_iters, criterion=criterion,
                           mini_batch_fraction=mini_batch_fraction,
                           stream_tile_rows=stream_tile_rows, init_algorithm=init_algorithm,
-                          num_retries=num_retries, seed=seed)
+                          num_retries=num_retries, seed=seed, router=int(router),
+                          router_groups=router_groups, router_retrain=router_retrain)
     cen = np.empty((k, d), dtype=np.float32)
     lab = np.empty(n, dtype=np.int32)
     sse = np.zeros(max(max_iters, 1), dtype=np.float64)
@@ -519,6 +555,11 @@ class Handle:
     def stats(self) -> kmgb_stats:
         st = kmgb_stats()
         self._chk(lib().kmgb_get_stats(self._h, C.byref(st)))
+        return st
+
+    def router_stats(self) -> kmgb_router_stats:
+        st = kmgb_router_stats()
+        self._chk(lib().kmgb_get_router_stats(self._h, C.byref(st)))
         return st
 
     def set_profiling(self, on: bool = True):

@@ -50,7 +50,7 @@ constexpr int threads_for(int epq) { return 64 + 4 * epq * 32; }
 constexpr uint32_t XKB_BYTES = BM * BK * 2;   // 16 KB: one k-block of one plane of the points
 constexpr uint32_t CKB_BYTES = BNH * BK * 2;  // 16 KB: one k-block of one plane of the centers
 constexpr int MAX_STAGES = 8;
-constexpr int MAX_D = 256;
+constexpr int MAX_D = 512;  // one plane; the shared-memory check limits two planes to 320
 constexpr uint32_t TMEM_COLS = 512;           // two 256-column accumulator buffers
 constexpr size_t SMEM_CAP = 227 * 1024;       // upper bound; the device's opt-in limit is queried
 constexpr float kUnusable = -3.0e38f;         // start value of padding / unusable centers
@@ -265,6 +265,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const long long n_units = (n_rows + UNIT - 1) / UNIT;
   const bool cand_mode = p.thr_in != nullptr;
   const bool grouped = p.u_prob != nullptr;
+  const bool store_mode = p.store_out != nullptr;
   // A unit's chunks: how many, the first center, the rows that exist, and a rotation -- each pair
   // visits the chunks in its own rotated order so that at any moment the pairs stream different
   // chunks of C from L2. Every role of both CTAs derives the same sequence (false: skipped unit).
@@ -517,6 +518,32 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               cur[4 * j4 + 3] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 3]), hv.w));
             }
           }
+          if (store_mode) {
+            // router hidden layer: BF16 of the key (bias included), ReLU when asked; 64 bytes
+            // per thread per 32-column block, as four 16-byte stores
+            if (prow < n_rows) {
+              uint4* dst = reinterpret_cast<uint4*>(
+                  static_cast<__nv_bfloat16*>(p.store_out) +
+                  (size_t)(p.out0 + prow) * (size_t)p.store_ld + col0 + cb * 32);
+#pragma unroll
+              for (int q4 = 0; q4 < 4; ++q4) {
+                uint32_t w[4];
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                  float lo = __uint_as_float(cur[q4 * 8 + 2 * t]);
+                  float hi = __uint_as_float(cur[q4 * 8 + 2 * t + 1]);
+                  if (p.store_relu) {
+                    lo = fmaxf(lo, 0.0f);
+                    hi = fmaxf(hi, 0.0f);
+                  }
+                  const __nv_bfloat162 b2v = __floats2bfloat162_rn(lo, hi);
+                  w[t] = *reinterpret_cast<const uint32_t*>(&b2v);
+                }
+                dst[q4] = make_uint4(w[0], w[1], w[2], w[3]);
+              }
+            }
+            continue;
+          }
           if (p.dump) {  // diagnostic: keys of this point before the column bits are packed
             if (prow < n_rows) {
               float* dst = p.dump + (size_t)prow * (size_t)((p.k + kCenterPad - 1) / kCenterPad * kCenterPad) + col0 + cb * 32;
@@ -553,6 +580,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         }
       }
       if (!alive) break;
+      if (store_mode) continue;  // every key was stored; no arg-max to merge
       // ---- merge the column slices of each point: warps (q, 1..) -> warp (q, 0) ----
       const uint32_t mfull = smem_u32(&bars.merge_full[q]);
       const uint32_t mempty = smem_u32(&bars.merge_empty[q]);
@@ -712,6 +740,8 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   if (a.n <= 0 || a.k <= 0 || a.d <= 0) return cudaSuccess;
   const int planes = (Xl && Cl) ? 2 : 1;  // planes of the split tier's point buffer
   const int mode = Cl ? (Xl ? 2 : 3) : 1;  // see bound_acc
+  if (a.store_out && ((a.store_ld % 8) || (reinterpret_cast<uintptr_t>(a.store_out) & 15)))
+    return cudaErrorInvalidValue;
   if (!bf16_tc_supported(a.d, planes) || (ldxb % 8) || (ldcb % 8) ||
       (reinterpret_cast<uintptr_t>(Xb) & 15) || (reinterpret_cast<uintptr_t>(Cb) & 15) ||
       (reinterpret_cast<uintptr_t>(Xl) & 15) || (reinterpret_cast<uintptr_t>(Cl) & 15))

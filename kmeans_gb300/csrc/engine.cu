@@ -27,6 +27,7 @@
 #include "../../include/kmeans_gb300.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "router.h"
 
 using namespace kmgb;
 
@@ -205,6 +206,18 @@ struct kmgb_handle {
   void* arena = nullptr;  // one device allocation holding every fixed buffer of the handle
   int* xinexact = nullptr;  // set by the BF16 conversion when some x is not a BF16 number
   bool x_exact = false;     // split tier: every x is a BF16 number -> two products, no x_lo
+  // learned router (opt.router): created at its first training; points it cannot certify go
+  // through the full scan as a compact data set (fb_*: allocated with the router)
+  Router* router = nullptr;
+  int router_groups = 0, router_retrain = 0, router_hidden = 0;
+  void* fb_arena = nullptr;
+  int* fb_list = nullptr;
+  int* fb_count = nullptr;
+  int* labF = nullptr;
+  float* XF = nullptr;
+  float* xnF = nullptr;
+  void* XbF = nullptr;
+  void* XlF = nullptr;
   // k-means++ work space (allocated on first use): D^2, block weight sums, max/pick, picks
   float* kpp_d2 = nullptr;
   unsigned long long* kpp_blk = nullptr;
@@ -257,8 +270,9 @@ struct kmgb_handle {
     if (stream) {
       cudaStreamSynchronize(stream);
       // the fixed buffers live in the arena; these are allocated on their own
-      void* ptrs[] = {arena, sse_dev, kpp_d2, kpp_blk, kpp_sc, kpp_picks};
+      void* ptrs[] = {arena, sse_dev, kpp_d2, kpp_blk, kpp_sc, kpp_picks, fb_arena};
       for (void* p : ptrs) dev_free(p, stream);
+      router_destroy(router, stream);
       cudaStreamSynchronize(stream);
     }
     for (int b = 0; b < 2; ++b) {
@@ -314,6 +328,24 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     delete h;
     set_err("kmgb_create: host-streamed tiles run full-batch Lloyd (mini_batch_fraction 1)");
     return KMEANS_ERROR_TILING;
+  }
+  if (h->opt.router) {
+    if (h->opt.assign_tier == KMGB_ASSIGN_FP32 || h->mini || h->streaming || !h->opt.certify) {
+      delete h;
+      set_err("kmgb_create: the router needs a BF16 tensor-core tier, full batches of resident "
+              "data and certified labels");
+      return KMEANS_ERROR_BUILDDATA;
+    }
+    h->router_groups = h->opt.router_groups > 0 ? h->opt.router_groups : 256;
+    h->router_retrain = h->opt.router_retrain > 0 ? h->opt.router_retrain : 5;
+    h->router_hidden = h->opt.router_hidden > 0 ? h->opt.router_hidden : 512;
+    if (h->router_groups < 2 || h->router_groups > 1024 || h->router_hidden % 256 != 0 ||
+        h->router_hidden > 512 || n < 256) {
+      delete h;
+      set_err("kmgb_create: router groups must be in [2, 1024], hidden units 256 or 512, and "
+              "the data set at least 256 rows");
+      return KMEANS_ERROR_BUILDDATA;
+    }
   }
   h->tile_rows = h->streaming ? h->opt.stream_tile_rows : n;
   h->n_act = h->mini ? h->m_mb : h->tile_rows;
@@ -608,6 +640,173 @@ long long window_start(long long m, long long m_mb, int it) {
   return s;
 }
 
+// Exact settlement of the points the assignment flagged (list h->rr_list, count h->rr_count):
+// tensor tiers first record and resolve each point's candidates, then every point still open
+// takes the FP32 rescan and the exact FP64 stage. Xa / Xba / Xla / labels: the rows the
+// assignment ran on (na rows at most).
+int rerank_flagged(kmgb_handle* h, const AssignArgs& a, const float* Xa, const void* Xba,
+                   const void* Xla, int* labels, long long na, bool tc) {
+  cudaStream_t s = h->stream;
+  RerankArgs r{};
+  r.X = Xa;
+  r.ldx = h->ldx;
+  r.C = h->Cop;
+  r.ldc = h->ldx;
+  r.cn = h->cn;
+  r.list = h->rr_list;
+  r.count = h->rr_count;
+  r.labels = labels;
+  r.stats = h->rr_stats;
+  r.n = na;
+  r.k = h->k;
+  r.d = h->d;
+  r.mode = 0;
+  r.max_list = na;
+  r.stop = h->stop;
+  if (tc) {
+    // BF16 tiers: a second tensor-core pass over the flagged rows records every center whose
+    // key reaches the point's floor (best - 2E); those few candidates are resolved in FP64.
+    // Points with more than kMaxCand candidates take the full rescan below.
+    KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, Xba, Xla, h->ldb,
+                                 h->thr_full, h->XbC, Xla ? h->XlC : nullptr, h->thr_c,
+                                 h->rr_over, h->rr_count + 1, h->stop, s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
+    AssignArgs c2 = a;
+    c2.n = h->cand_cap;
+    c2.labels = nullptr;
+    c2.certify = 0;
+    c2.thr_out = nullptr;
+    c2.n_dev = h->rr_count;
+    c2.row0 = 0;
+    c2.thr_in = h->thr_c;
+    c2.cand = h->cand;
+    c2.cand_cnt = h->cand_cnt;
+    KM_TRY(launch_assign_bf16(h->XbC, Xla ? h->XlC : nullptr, h->ldb, h->Cb, h->Cl, h->ldb, c2,
+                              s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
+    KM_TRY(launch_resolve_candidates(h->rr_list, h->rr_count, h->cand_cap, h->cand, h->cand_cnt, Xa,
+                                     h->ldx, h->Cop, h->ldx, h->cn, h->d, labels, h->rr_over,
+                                     h->rr_count + 1, h->stop, s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
+    r.list = h->rr_over;
+    r.count = h->rr_count + 1;
+  }
+  // FP32 stage over the points still open, exact FP64 stage over what FP32 cannot separate
+  KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 2, h->rr_hi2, s),
+         KMEANS_ERROR_CLOSEST_CENTERS);
+  r.list = h->rr_list2;
+  r.count = h->rr_count + 2;
+  r.stats = nullptr;
+  KM_TRY(launch_rerank_exact(r, h->rr_hi2, s), KMEANS_ERROR_CLOSEST_CENTERS);
+  KM_TRY(launch_count_stats(h->rr_count, tc ? 1 : 0, h->rr_stats, h->stop, s),
+         KMEANS_ERROR_CLOSEST_CENTERS);
+  return 0;
+}
+
+// ---------------------------------- learned router ----------------------------------
+RouterIO router_io(kmgb_handle* h) {
+  RouterIO io{};
+  io.n = h->n;
+  io.d = h->d;
+  io.k = h->k;
+  io.ldx = h->ldx;
+  io.ldb = h->ldb;
+  io.X = h->X;
+  io.Xb = h->Xb;
+  io.Xl = h->x_exact ? nullptr : h->Xl;
+  io.xn = h->xn;
+  io.C = h->C;
+  io.Cop = h->Cop;
+  io.Cb = h->Cb;
+  io.Cl = h->Cl;
+  io.cn = h->cn;
+  io.cinit = h->cinit;
+  io.cmax = h->cmax;
+  io.labels = h->labels;
+  io.err = h->err;
+  io.stop = h->stop;
+  return io;
+}
+
+// Compact buffers of the points the router sends to the full scan (up to every row).
+cudaError_t alloc_fallback(kmgb_handle* h) {
+  auto carve = [&](Arena& a) {
+    a.take(&h->fb_list, h->n);
+    a.take(&h->fb_count, 1);
+    a.take(&h->labF, h->n);
+    a.take(&h->XF, (size_t)h->n * h->ldx);
+    a.take(&h->xnF, h->n);
+    a.take_bytes(&h->XbF, (size_t)h->n * h->ldb * 2);
+    if (h->Xl) a.take_bytes(&h->XlF, (size_t)h->n * h->ldb * 2);
+  };
+  Arena sizing;
+  carve(sizing);
+  cudaError_t e = dev_alloc(&h->fb_arena, sizing.off, h->stream);
+  if (e != cudaSuccess) return e;
+  Arena cut;
+  cut.base = static_cast<char*>(h->fb_arena);
+  carve(cut);
+  return cudaSuccess;
+}
+
+// After iteration `slot` of the run: (re)train the router every router_retrain iterations of the
+// handle (after the first, the sixth, ...), on this iteration's labels and the updated centers.
+int router_maybe_train(kmgb_handle* h, int slot) {
+  if (!h->opt.router || (h->run_base + slot) % h->router_retrain != 0) return 0;
+  cudaStream_t s = h->stream;
+  // the centers' operand copies, norms and planes for the updated centers
+  KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
+  KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
+                             nullptr, h->cinit, h->Cl),
+         KMEANS_ERROR_RESET);
+  const RouterIO io = router_io(h);
+  if (!h->router) {
+    cudaError_t e = router_create(&h->router, io, h->router_groups, h->router_hidden,
+                                  h->Cl != nullptr, s);
+    if (e == cudaSuccess && !h->fb_arena) e = alloc_fallback(h);
+    if (e != cudaSuccess) {
+      set_err("router: device memory", e);
+      return KMEANS_ERROR_COMPUTE;
+    }
+  }
+  const cudaError_t e = router_train(h->router, io, s);
+  if (e != cudaSuccess) {
+    set_err("router training", e);
+    return KMEANS_ERROR_COMPUTE;
+  }
+  return 0;
+}
+
+// Routed assignment: every point scans its routed group; the points the certificate does not
+// settle are gathered into a compact data set and take the full scan (assignment over all
+// centers, then the same exact settlement as every other point).
+int router_step(kmgb_handle* h, AssignArgs a) {
+  cudaStream_t s = h->stream;
+  const RouterIO io = router_io(h);
+  KM_TRY(cudaMemsetAsync(h->fb_count, 0, sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS);
+  KM_TRY(router_assign(h->router, io, h->fb_list, h->fb_count, s), KMEANS_ERROR_CLOSEST_CENTERS);
+  KM_TRY(h->pmark(2), KMEANS_ERROR_CLOSEST_CENTERS);
+  void* XlF = io.Xl ? h->XlF : nullptr;
+  KM_TRY(router_gather_fallback(h->fb_list, h->fb_count, h->n, h->X, h->ldx, h->xn, h->Xb, io.Xl,
+                                h->ldb, h->XF, h->xnF, h->XbF, XlF, h->stop, s),
+         KMEANS_ERROR_CLOSEST_CENTERS);
+  a.gamma = assign_bf16_gamma(h->d);
+  a.n = h->n;
+  a.n_dev = h->fb_count;
+  a.row0 = 0;
+  a.out0 = 0;
+  a.xnorm = h->xnF;
+  a.labels = h->labF;
+  a.thr_out = h->thr_full;
+  KM_TRY(launch_assign_bf16(h->XbF, XlF, h->ldb, h->Cb, h->Cl, h->ldb, a, s),
+         KMEANS_ERROR_CLOSEST_CENTERS);
+  const int rc = rerank_flagged(h, a, h->XF, h->XbF, XlF, h->labF, h->n, true);
+  if (rc) return rc;
+  KM_TRY(router_scatter_labels(h->fb_list, h->fb_count, h->n, h->labF, h->labels, h->stop, s),
+         KMEANS_ERROR_CLOSEST_CENTERS);
+  return 0;
+}
+
 // One Lloyd iteration on the handle's stream; SSE lands in sse_dev[slot]. upload (tensor tiers,
 // full batch): the host data set arrives during this iteration -- chunk by chunk, each copied on
 // the copy stream, then prepared and assigned on the handle's stream while the next one crosses
@@ -663,7 +862,11 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr) {
   a.cinit = h->cinit;
   test_wait_hook(&a.test_withhold, &a.test_wait_cycles);  // zero unless a test asks
   const bool tc = h->opt.assign_tier != KMGB_ASSIGN_FP32;
-  if (tc && upload) {
+  const bool routed = h->router && router_trained(h->router) && !upload && !h->mini;
+  if (routed) {
+    const int rc = router_step(h, a);
+    if (rc) return rc;
+  } else if (tc && upload) {
     a.gamma = assign_bf16_gamma(h->d);
     a.thr_out = h->opt.certify ? h->thr_full : nullptr;
     if (h->Xb) KM_TRY(cudaMemsetAsync(h->xinexact, 0, sizeof(int), s), KMEANS_ERROR_COPY_TILE);
@@ -698,61 +901,12 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr) {
     a.gamma = assign_fp32_gamma(h->d);
     KM_TRY(launch_assign_fp32(Xa, h->ldx, h->Cop, h->ldx, a, s), KMEANS_ERROR_CLOSEST_CENTERS);
   }
-  KM_TRY(h->pmark(2), KMEANS_ERROR_CLOSEST_CENTERS);
-  if (h->opt.certify) {
-    RerankArgs r{};
-    r.X = Xa;
-    r.ldx = h->ldx;
-    r.C = h->Cop;
-    r.ldc = h->ldx;
-    r.cn = h->cn;
-    r.list = h->rr_list;
-    r.count = h->rr_count;
-    r.labels = h->labels;
-    r.stats = h->rr_stats;
-    r.n = na;
-    r.k = h->k;
-    r.d = h->d;
-    r.mode = 0;
-    r.max_list = na;
-    r.stop = h->stop;
-    if (tc) {
-      // BF16 tiers: a second tensor-core pass over the flagged rows records every center whose
-      // key reaches the point's floor (best - 2E); those few candidates are resolved in FP64.
-      // Points with more than kMaxCand candidates take the full rescan below.
-      KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, Xba, Xla, h->ldb,
-                                   h->thr_full, h->XbC, Xla ? h->XlC : nullptr, h->thr_c,
-                                   h->rr_over, h->rr_count + 1, h->stop, s),
-             KMEANS_ERROR_CLOSEST_CENTERS);
-      AssignArgs c2 = a;
-      c2.n = h->cand_cap;
-      c2.labels = nullptr;
-      c2.certify = 0;
-      c2.thr_out = nullptr;
-      c2.n_dev = h->rr_count;
-      c2.row0 = 0;
-      c2.thr_in = h->thr_c;
-      c2.cand = h->cand;
-      c2.cand_cnt = h->cand_cnt;
-      KM_TRY(launch_assign_bf16(h->XbC, Xla ? h->XlC : nullptr, h->ldb, h->Cb, h->Cl, h->ldb, c2,
-                                s),
-             KMEANS_ERROR_CLOSEST_CENTERS);
-      KM_TRY(launch_resolve_candidates(h->rr_list, h->rr_count, h->cand_cap, h->cand, h->cand_cnt, Xa,
-                                       h->ldx, h->Cop, h->ldx, h->cn, h->d, h->labels, h->rr_over,
-                                       h->rr_count + 1, h->stop, s),
-             KMEANS_ERROR_CLOSEST_CENTERS);
-      r.list = h->rr_over;
-      r.count = h->rr_count + 1;
+  if (!routed) {
+    KM_TRY(h->pmark(2), KMEANS_ERROR_CLOSEST_CENTERS);
+    if (h->opt.certify) {
+      const int rc = rerank_flagged(h, a, Xa, Xba, Xla, h->labels, na, tc);
+      if (rc) return rc;
     }
-    // FP32 stage over the points still open, exact FP64 stage over what FP32 cannot separate
-    KM_TRY(launch_rerank_tiled(r, h->rr_list2, h->rr_count + 2, h->rr_hi2, s),
-           KMEANS_ERROR_CLOSEST_CENTERS);
-    r.list = h->rr_list2;
-    r.count = h->rr_count + 2;
-    r.stats = nullptr;
-    KM_TRY(launch_rerank_exact(r, h->rr_hi2, s), KMEANS_ERROR_CLOSEST_CENTERS);
-    KM_TRY(launch_count_stats(h->rr_count, tc ? 1 : 0, h->rr_stats, h->stop, s),
-           KMEANS_ERROR_CLOSEST_CENTERS);
   }
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
   // cluster centers + compactness (kmeans.cpp:1018-1104)
@@ -762,7 +916,7 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr) {
          KMEANS_ERROR_CLUSTER_CENTERS);
   KM_TRY(h->pmark(4), KMEANS_ERROR_CLUSTER_CENTERS);
   if (h->prof) ++h->pused;
-  return 0;
+  return router_maybe_train(h, slot);
 }
 
 // One Lloyd iteration over host-streamed tiles: the centers are prepared once, then every tile
@@ -991,7 +1145,8 @@ int run(kmgb_handle* h, int iters, double criterion, const float* upload = nullp
   // Every iteration is enqueued; the SSE reduction evaluates the stop rule on the device and
   // the kernels of later iterations return at once after it fires.
   int graph_rc = -1;
-  if (!h->streaming && !h->mini && !h->prof && iters - first > 0 && graphs_enabled()) {
+  if (!h->streaming && !h->mini && !h->prof && !h->opt.router && iters - first > 0 &&
+      graphs_enabled()) {
     graph_rc = run_graph(h, iters - first);
     if (graph_rc > 0) return graph_rc;
   }
@@ -1406,6 +1561,38 @@ int kmgb_get_stats(kmgb_handle* h, kmgb_stats* st) {
   long long e = 0;
   for (long long c : cnt) e += (c == 0);
   st->empty_clusters = e;
+  if (h->router) {  // reserved[0..5]: the router's counters (kmgb_stats in the header)
+    RouterStats rs;
+    KM_TRY(router_stats(h->router, &rs, h->stream), KMEANS_ERROR_COMPUTE);
+    st->reserved[0] = (long long)rs.routed;
+    st->reserved[1] = (long long)rs.certified;
+    st->reserved[2] = (long long)rs.fallback;
+    st->reserved[3] = rs.trainings;
+    st->reserved[4] = (long long)(rs.train_ms * 1000.0);
+    st->reserved[5] = (long long)rs.flagged;
+  }
+  return 0;
+}
+
+int kmgb_get_router_stats(kmgb_handle* h, kmgb_router_stats* out) {
+  if (!h || !out) return KMEANS_ERROR_COMPUTE;
+  std::memset(out, 0, sizeof(*out));
+  if (!h->router) return 0;
+  RouterStats rs;
+  KM_TRY(router_stats(h->router, &rs, h->stream), KMEANS_ERROR_COMPUTE);
+  out->trainings = rs.trainings;
+  out->train_ms = rs.train_ms;
+  out->group_ms = rs.group_ms;
+  out->last_loss = rs.last_loss;
+  out->last_accuracy = rs.last_accuracy;
+  out->groups_nonempty = rs.groups_nonempty;
+  out->components = rs.components;
+  out->routed = rs.routed;
+  out->flagged = rs.flagged;
+  out->certified = rs.certified;
+  out->fallback = rs.fallback;
+  out->routed_iterations = rs.routed_iterations;
+  out->device_bytes = (long long)router_device_bytes(h->router);
   return 0;
 }
 

@@ -48,6 +48,12 @@ struct AssignArgs {
   const int* g_k;
   const long long* g_rend;
   const int* g_done;
+  // BF16 tiers, store mode (the router's hidden layer; null otherwise): instead of the arg-max,
+  // every key (accumulator + cinit[j]) is written as BF16 to store_out[row * store_ld + j],
+  // clamped at zero when store_relu is set; labels and the certificate are not produced
+  void* store_out;
+  long long store_ld;
+  int store_relu;
   // test hook of the FP32 tier (kmgb_debug_withhold_stage): the producer issues no TMA load for
   // pipeline steps >= test_withhold (0: every step), and every wait gives up after
   // test_wait_cycles SM cycles (0: KMGB_WAIT_CYCLES)
@@ -81,6 +87,8 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
                                const void* Cl, long long ldcb, const AssignArgs& a,
                                cudaStream_t s);
 float assign_bf16_gamma(int d);
+// D up to 512 with one BF16 plane of the points (plain tier, split tier with BF16-valued points,
+// store mode), up to 320 with two (split tier): the unit's points stay in shared memory.
 bool bf16_tc_supported(int d, int planes = 1);
 
 // Exact re-rank of flagged points. mode 0 (Lloyd): FP64 arg-min of sum_d (x_d - c_d)^2.
@@ -112,7 +120,8 @@ cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaS
 cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s);
 // Candidate re-rank of the BF16 tiers: compact copy of up to `cap` flagged rows (the rest go to
 // `over`), then FP64 resolution of their recorded candidates (overflowing points are appended
-// to `over`).
+// to `over`). With row_map (the router's routed scan), list entries are routed rows whose
+// candidates are stored per routed row and whose FP32 row is X[row_map[entry]].
 cudaError_t launch_gather_flagged(const int* list, const int* count, long long cap,
                                   const void* Xb, const void* Xl, long long ldb, const float* thr,
                                   void* XbC, void* XlC, float* thrC, int* over, int* over_count,
@@ -121,7 +130,8 @@ cudaError_t launch_resolve_candidates(const int* list, const int* count, long lo
                                       const int* cand, const int* cand_cnt, const float* X,
                                       long long ldx, const float* C, long long ldc, const float* cn,
                                       int d, int* labels, int* over, int* over_count,
-                                      const int* stop, cudaStream_t s);
+                                      const int* stop, cudaStream_t s,
+                                      const int* row_map = nullptr);
 // stats[0] += counts[0] (points flagged by the assignment), stats[1] += counts[full_idx]
 // (points that needed a full rescan of the centers).
 cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long long* stats,

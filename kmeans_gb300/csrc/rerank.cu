@@ -672,7 +672,8 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
                                           const float* __restrict__ C, long long ldc,
                                           const float* __restrict__ cn, int d,
                                           int* __restrict__ labels, int* __restrict__ over,
-                                          int* __restrict__ over_count, const int* stop) {
+                                          int* __restrict__ over_count, const int* stop,
+                                          const int* __restrict__ row_map) {
   if (stopped(stop)) return;
   const long long cnt = min((long long)*(volatile const int*)count, max_list);
   const int lane = threadIdx.x & 31;
@@ -689,14 +690,17 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
   const double abs32 = (double)(d + 32) * (m32 + 8.0) * 0x1p-149;
   for (long long slot = w0; slot < cnt; slot += nw) {
     const int pt = list[slot];
-    const int nc = cand_cnt[slot];
+    // with row_map (routed scan) the candidates are kept per routed row pt, and the point's FP32
+    // row is row_map[pt]; otherwise per list slot, and the row is pt
+    const long long ci = row_map ? (long long)pt : slot;
+    const int nc = cand_cnt[ci];
     if (nc <= 0 || nc > kMaxCand) {
       if (lane == 0) over[atomicAdd(over_count, 1)] = pt;
       continue;
     }
-    const float* x = X + (size_t)pt * ldx;
+    const float* x = X + (size_t)(row_map ? row_map[pt] : pt) * ldx;
     // lane q holds candidate q and whether it is usable
-    const int myj = lane < nc ? cand[slot * kMaxCand + lane] : -1;
+    const int myj = lane < nc ? cand[ci * kMaxCand + lane] : -1;
     const int myok = (myj >= 0 && cn[myj] < INFINITY) ? 1 : 0;
     // both fast tiers certify only a strict separation, so the list order (column slice by
     // column slice) does not matter
@@ -771,7 +775,7 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
     double best = INFINITY;
     int bidx = -1;
     for (int q = lane; q < nc; q += 32) {
-      const int j = cand[slot * kMaxCand + q];
+      const int j = cand[ci * kMaxCand + q];
       if (cn[j] < INFINITY) {
         const float* c = C + (size_t)j * ldc;
         double s = 0.0;
@@ -818,18 +822,18 @@ cudaError_t launch_resolve_candidates(const int* list, const int* count, long lo
                                       const int* cand, const int* cand_cnt, const float* X,
                                       long long ldx, const float* C, long long ldc, const float* cn,
                                       int d, int* labels, int* over, int* over_count,
-                                      const int* stop, cudaStream_t s) {
+                                      const int* stop, cudaStream_t s, const int* row_map) {
   if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   const bool vec = d % 4 == 0 && ldx % 4 == 0 && ldc % 4 == 0 &&
                    reinterpret_cast<uintptr_t>(X) % 16 == 0 && reinterpret_cast<uintptr_t>(C) % 16 == 0;
   if (vec)
     resolve_candidates_kernel<true><<<kmgb::num_sms() * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
                                                             X, ldx, C, ldc, cn, d, labels, over,
-                                                            over_count, stop);
+                                                            over_count, stop, row_map);
   else
     resolve_candidates_kernel<false><<<kmgb::num_sms() * 8, 256, 0, s>>>(list, count, max_list, cand, cand_cnt,
                                                              X, ldx, C, ldc, cn, d, labels, over,
-                                                             over_count, stop);
+                                                             over_count, stop, row_map);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -66,6 +66,23 @@ def mixture_torch(n: int, d: int, k: int, seed: int = 0, mean_lo: float = -10.0,
     return X, comp, means
 
 
+def zipf_blobs_numpy(n: int, d: int, k: int, seed: int = 0, s: float = 1.1, sigma: float = 1.0,
+                     mean_std: float = 5.0, bf16: bool = True):
+    """The c4 shape at any size: k isotropic Gaussians (sigma) with Zipf(s) sizes around means
+    drawn from N(0, mean_std^2 I); values rounded to BF16 numbers when bf16 is set."""
+    rng = np.random.default_rng(seed)
+    w = 1.0 / np.arange(1, k + 1) ** s
+    comp = rng.choice(k, size=n, p=w / w.sum()).astype(np.int32)
+    means = (rng.standard_normal((k, d)) * mean_std).astype(np.float32)
+    X = rng.standard_normal((n, d), dtype=np.float32) * np.float32(sigma)
+    X += means[comp]
+    if bf16:  # round to nearest even BF16 through the bit pattern
+        b = X.view(np.uint32)
+        b += np.uint32(0x7FFF) + ((b >> 16) & np.uint32(1))
+        b &= np.uint32(0xFFFF0000)
+    return X, comp, means
+
+
 def sample_init(n: int, k: int, seed: int = 1) -> np.ndarray:
     """k distinct row indices chosen uniformly by seed (initial centers = those rows)."""
     rng = np.random.default_rng(seed)
