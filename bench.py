@@ -412,18 +412,14 @@ def batched_workload(args):
     print(json.dumps(line), flush=True)
 
 
-def large_k_workload(args, n=16_000_000, d=256, k=65_536):
-    """Large-K workload: 16M points, D=256, K=65,536 clusters with Zipf(1.1) sizes, unit-variance
-    Gaussians around means drawn from N(0, 25 I), values rounded to BF16 (BF16 points);
-    initial centers a seeded sample of points. Times split-BF16 iterations against one plain
-    FP32 iteration from the same centers and checks that both give the same labels (both are
-    the FP64 arg-min)."""
+def large_k_data(n, d, k, seed=77):
+    """16M x 256, K=65,536 clusters with Zipf(1.1) sizes, unit-variance Gaussians around means
+    drawn from N(0, 25 I), values rounded to BF16 (BF16 points), on the device; initial centers a
+    seeded sample of points."""
     import torch
-    import kmeans_gb300 as km
     from kmeans_gb300.synthetic import sample_init
-    km.build()
     g = torch.Generator(device="cuda")
-    g.manual_seed(77)
+    g.manual_seed(seed)
     w = 1.0 / torch.arange(1, k + 1, device="cuda", dtype=torch.float64) ** 1.1
     lab = torch.multinomial((w / w.sum()).float(), n, replacement=True, generator=g)
     means = torch.randn((k, d), device="cuda", generator=g) * 5.0
@@ -434,52 +430,110 @@ def large_k_workload(args, n=16_000_000, d=256, k=65_536):
                     ).to(torch.bfloat16).float()
     del lab, means
     init = X[torch.from_numpy(sample_init(n, k, seed=5)).cuda()].cpu().numpy()
+    return X, init
+
+
+def timed_run(km, torch, X, init, tier, iters, **opts):
+    """`iters` iterations of a fresh handle from `init` (one untimed warm-up iteration first),
+    CUDA events on the handle's stream around the run. Returns (ms per iteration, phases,
+    labels, centers, SSE history, stats, router stats)."""
+    n, d = X.shape
+    k = init.shape[0]
+    h = km.Handle(n, d, k, assign_tier=tier, max_iters=iters + 1, **opts)
+    h.set_data(X, True)
+    h.set_centers(init, False)
+    if not opts.get("router"):
+        h.run(1)  # warm-up (module loading, graph capture)
+        h.synchronize()
+        h.set_centers(init, False)
+    stream = torch.cuda.ExternalStream(h.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h.set_profiling(True)
+    e0.record(stream)
+    h.run(iters)
+    e1.record(stream)
+    h.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    phase, pit = h.phase_ms()
+    out = (ms, {nm: p / max(pit, 1) for nm, p in zip(["prep", "assign", "rerank", "update"], phase)},
+           h.labels(), h.centers(), h.sse(iters), h.stats(), h.router_stats())
+    h.close()
+    return out
+
+
+def large_k_workload(args, n=16_000_000, d=256, k=65_536):
+    """Large-K workload (16M x 256, K=65,536, Zipf cluster sizes, BF16 points): the learned
+    router (split BF16 tier, MLP 256->512->256 groups, retrained every 5 iterations) for the
+    configuration's 25 iterations, against (a) the split BF16 tier without the router for the
+    same 25 iterations from the same centers -- labels, centers and SSE must be identical, both
+    being the FP64 arg-min -- and (b) one iteration of the plain FP32 tier (the denominator of the
+    >= 5x target; its labels equal the split tier's first iteration)."""
+    import torch
+    import kmeans_gb300 as km
+    km.build()
+    iters = args.iters
+    X, init = large_k_data(n, d, k)
     flop = 2.0 * n * k * d
     out = {"metric": f"Lloyd iteration, N={n}, D={d}, K={k} (ms)", "unit": "ms",
            "higher_is_better": False, "data": "synthetic (Zipf 1.1 cluster sizes, BF16 points)",
-           "config": {"workload": "lloyd_16Mx256_K65536", "n": n, "d": d, "k": k}}
-    labels = {}
-    for tier, iters in (("bf16x3", 3), ("fp32", 1)):
-        if tier not in args.tiers.split(","):
-            continue
-        tid = km.ASSIGN_BF16X3 if tier == "bf16x3" else km.ASSIGN_FP32
-        h = km.Handle(n, d, k, assign_tier=tid, max_iters=iters + 1)
+           "config": {"workload": "lloyd_16Mx256_K65536", "n": n, "d": d, "k": k,
+                      "iterations": iters}}
+    tiers = args.tiers.split(",")
+    res = {}
+    if "router" in tiers:
+        ms, ph, lab, cen, sse, st, rs = timed_run(km, torch, X, init, km.ASSIGN_BF16X3, iters,
+                                                  router=1, router_groups=256, router_retrain=5)
+        res["router"] = (lab, cen, sse)
+        routed_pts = n * rs.routed_iterations
+        out["router"] = {"ms_per_iteration": ms, "phase_ms_per_iter": ph, "iterations": iters,
+                         "iter_per_s": 1000.0 / ms,
+                         "certified_share": rs.certified / max(1, routed_pts),
+                         "fallback_share": rs.fallback / max(1, routed_pts),
+                         "in_group_near_tie_share": rs.flagged / max(1, rs.routed),
+                         "retrain_every": 5, "groups": 256, "hidden": 512,
+                         "train_ms_total": rs.train_ms, "group_ms": rs.group_ms,
+                         "trainings": rs.trainings, "last_train_accuracy": rs.last_accuracy,
+                         "components": rs.components, "groups_nonempty": rs.groups_nonempty,
+                         "max_group_centers": rs.max_group,
+                         "max_component_centers": rs.max_component,
+                         "group_scan_share_of_full": rs.scan_chunks / max(1, rs.routed)
+                         / ((k + 255) // 256),
+                         "routed_iterations": rs.routed_iterations,
+                         "stage_ms_per_routed_iter": {
+                             k_: v / max(1, rs.routed_iterations)
+                             for k_, v in zip(km.kmgb_router_stats.STAGES, list(rs.stage_ms))},
+                         "reranked_points": st.reranked}
+    if "bf16x3" in tiers:
+        ms, ph, lab, cen, sse, st, _ = timed_run(km, torch, X, init, km.ASSIGN_BF16X3, iters)
+        res["bf16x3"] = (lab, cen, sse)
+        out["bf16x3"] = {"ms_per_iteration": ms, "phase_ms_per_iter": ph, "iterations": iters,
+                         "assign_tflops": flop / (ph["assign"] / 1000.0) / 1e12,
+                         "reranked_points": st.reranked, "full_rescan_points": st.reranked_fp64}
+    if "fp32" in tiers:
+        ms, ph, lab, _, _, _, _ = timed_run(km, torch, X, init, km.ASSIGN_FP32, 1)
+        out["fp32"] = {"ms_per_iteration": ms, "phase_ms_per_iter": ph, "iterations": 1,
+                       "assign_tflops": flop / (ph["assign"] / 1000.0) / 1e12}
+        h = km.Handle(n, d, k, assign_tier=km.ASSIGN_BF16X3, max_iters=1)
         h.set_data(X, True)
         h.set_centers(init, False)
-        if tier == "bf16x3":
-            h.run(1)  # warm-up
-            h.synchronize()
-            h.set_centers(init, False)
-        stream = torch.cuda.ExternalStream(h.stream)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        h.set_profiling(True)
-        e0.record(stream)
-        h.run(iters)
-        e1.record(stream)
+        h.run(1)
         h.synchronize()
-        ms = e0.elapsed_time(e1) / iters
-        phase, pit = h.phase_ms()
-        st = h.stats()
-        out[tier] = {"ms_per_iteration": ms, "assign_ms": phase[1] / max(pit, 1),
-                     "assign_tflops": flop / (phase[1] / max(pit, 1) / 1000.0) / 1e12,
-                     "phase_ms_per_iter": {nm: p / max(pit, 1) for nm, p in
-                                           zip(["prep", "assign", "rerank", "update"], phase)},
-                     "iterations": iters, "reranked_points": st.reranked,
-                     "full_rescan_points": st.reranked_fp64}
-        if tier == "fp32":
-            labels[tier] = h.labels()
-        else:
-            # labels after the first iteration from the same initial centers
-            h.set_centers(init, False)
-            h.run(1)
-            h.synchronize()
-            labels[tier] = h.labels()
+        out["fp32"]["labels_equal_split_first_iteration"] = bool(np.array_equal(h.labels(), lab))
         h.close()
-    if "bf16x3" in out:
-        out["value"] = out["bf16x3"]["ms_per_iteration"]
-    if "bf16x3" in out and "fp32" in out:
-        out["speedup_vs_fp32"] = out["fp32"]["ms_per_iteration"] / out["bf16x3"]["ms_per_iteration"]
-        out["labels_identical"] = bool(np.array_equal(labels["fp32"], labels["bf16x3"]))
+    if "router" in res and "bf16x3" in res:
+        a, b = res["router"], res["bf16x3"]
+        out["router_vs_split"] = {
+            "labels_identical": bool(np.array_equal(a[0], b[0])),
+            "centers_identical": bool(np.array_equal(a[1], b[1], equal_nan=True)),
+            "sse_identical": bool(np.array_equal(a[2], b[2])),
+            "speedup": out["bf16x3"]["ms_per_iteration"] / out["router"]["ms_per_iteration"]}
+    main_tier = "router" if "router" in out else "bf16x3"
+    if main_tier in out:
+        out["value"] = out[main_tier]["ms_per_iteration"]
+        out["tier"] = main_tier
+    if "fp32" in out and main_tier in out:
+        out["speedup_vs_plain_fp32"] = (out["fp32"]["ms_per_iteration"]
+                                        / out[main_tier]["ms_per_iteration"])
     print(json.dumps(out), flush=True)
 
 
@@ -617,7 +671,9 @@ def main():
                          "headline)")
     ap.add_argument("--problems", type=int, default=10_000,
                     help="problems of the batched workload")
-    ap.add_argument("--tiers", default="bf16x3,fp32", help="tiers of the large_k workload")
+    ap.add_argument("--tiers", default="router,bf16x3,fp32",
+                    help="tiers of the large_k workload (router = split BF16 + learned router)")
+    ap.add_argument("--iters", type=int, default=25, help="iterations of the large_k workload")
     ap.add_argument("--bf16-data", action="store_true",
                     help="the workload's points stored as BF16 values (the configuration's BF16 "
                          "storage variant)")

@@ -275,12 +275,20 @@ typedef struct kmgb_router_stats {
   double last_accuracy;       /* share of that batch routed to its label's group */
   int groups_nonempty;        /* groups holding at least one center */
   int components;             /* components of linked centers packed into the groups */
+  int max_group;              /* centers of the largest group */
+  int max_component;          /* centers of the largest component */
+  unsigned long long scan_chunks; /* sum over routed points of their group's 256-center chunks
+                                     (a full scan is ceil(k / 256) per point) */
   unsigned long long routed;  /* points routed to a group scan */
   unsigned long long flagged; /* of those, points whose in-group margin took the candidate pass */
   unsigned long long certified; /* points whose group winner was certified as the arg-min */
   unsigned long long fallback;  /* points that took the full scan instead */
   long long routed_iterations;  /* iterations that ran the routed scan */
   long long device_bytes;       /* device memory of the router (fallback buffers excluded) */
+  double stage_ms[7];           /* with profiling on (kmgb_set_profiling): CUDA-event ms of the
+                                   routed assignment's stages summed over the routed iterations:
+                                   center separation, centers in group order, network inference,
+                                   sort by group, group scan, in-group near ties, certificate */
   long long reserved[4];
 } kmgb_router_stats;
 

@@ -91,13 +91,20 @@ class kmgb_router_stats(C.Structure):
     _fields_ = [("trainings", C.c_longlong), ("train_ms", C.c_double), ("group_ms", C.c_double),
                 ("last_loss", C.c_double), ("last_accuracy", C.c_double),
                 ("groups_nonempty", C.c_int), ("components", C.c_int),
+                ("max_group", C.c_int), ("max_component", C.c_int),
+                ("scan_chunks", C.c_ulonglong),
                 ("routed", C.c_ulonglong), ("flagged", C.c_ulonglong),
                 ("certified", C.c_ulonglong), ("fallback", C.c_ulonglong),
                 ("routed_iterations", C.c_longlong), ("device_bytes", C.c_longlong),
-                ("reserved", C.c_longlong * 4)]
+                ("stage_ms", C.c_double * 7), ("reserved", C.c_longlong * 4)]
+
+    STAGES = ("separation", "permute_centers", "inference", "sort", "group_scan",
+              "near_ties", "certificate")
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("reserved", "stage_ms")}
+        d["stage_ms"] = dict(zip(self.STAGES, list(self.stage_ms)))
+        return d
 
 
 class kmgb_stats(C.Structure):

@@ -768,6 +768,7 @@ int router_maybe_train(kmgb_handle* h, int slot) {
       set_err("router: device memory", e);
       return KMEANS_ERROR_COMPUTE;
     }
+    router_set_profiling(h->router, h->prof);
   }
   const cudaError_t e = router_train(h->router, io, s);
   if (e != cudaSuccess) {
@@ -1587,12 +1588,16 @@ int kmgb_get_router_stats(kmgb_handle* h, kmgb_router_stats* out) {
   out->last_accuracy = rs.last_accuracy;
   out->groups_nonempty = rs.groups_nonempty;
   out->components = rs.components;
+  out->max_group = rs.max_group;
+  out->max_component = rs.max_component;
+  out->scan_chunks = rs.scan_chunks;
   out->routed = rs.routed;
   out->flagged = rs.flagged;
   out->certified = rs.certified;
   out->fallback = rs.fallback;
   out->routed_iterations = rs.routed_iterations;
   out->device_bytes = (long long)router_device_bytes(h->router);
+  for (int t = 0; t < 7; ++t) out->stage_ms[t] = rs.stage_ms[t];
   return 0;
 }
 
@@ -1602,6 +1607,7 @@ int kmgb_set_profiling(kmgb_handle* h, int on) {
   if (!h) return KMEANS_ERROR_COMPUTE;
   h->prof = on != 0;
   h->pused = 0;
+  router_set_profiling(h->router, h->prof);
   return 0;
 }
 

@@ -5,8 +5,10 @@
 // Zipf-sized Gaussian clusters) most of that scan is wasted. Here:
 //   1. Groups. On the first training the usable centers are linked into components: c and c'
 //      are linked when d(c, c') <= min(max(t_c, t_c'), cap), t_c = 2.4 x the median distance of
-//      c's members (from a sample of points), cap = 3.6 x the median of those medians over the
-//      centers (a union-find over all center pairs, centers_pair_kernel). Components are
+//      c's members (from a sample of points), cap = 2.5 x the median of those medians over the
+//      centers (a union-find over all center pairs, centers_pair_kernel). (With 3.6 x, chains
+//      of centers lying between clusters merged half of the 65,536 centers of the Zipf-sized
+//      16M x 256 workload into one component.) Components are
 //      bin-packed, largest first into the lightest, into G groups; the groups stay fixed.
 //   2. Network. An MLP (router_mlp.cu) learns, from a sample of (point, group of its label)
 //      pairs, to predict the group; it is retrained every `retrain` iterations on the labels of
@@ -29,6 +31,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <random>
@@ -288,22 +291,25 @@ __global__ void route_count_kernel(const int* __restrict__ route, long long n, i
 
 // One block: group row offsets (each group's rows padded to 256), the unit table of the pair
 // kernel (unit u -> group, or G for units past the last group), and the routed-point counter.
-__global__ void route_tables_kernel(const int* __restrict__ gcnt, int G, long long max_units,
+__global__ void route_tables_kernel(const int* __restrict__ gcnt, const int* __restrict__ gk,
+                                    int G, long long max_units,
                                     long long* __restrict__ row_off, long long* __restrict__ rend,
                                     int* __restrict__ gdone, int* __restrict__ fill,
-                                    int* __restrict__ uprob, unsigned long long* stats,
-                                    const int* stop) {
+                                    int* __restrict__ uprob, unsigned long long* rows_stat,
+                                    unsigned long long* chunks_stat, const int* stop) {
   if (stopped(stop)) return;
   __shared__ long long off[1025];
   if (threadIdx.x == 0) {
-    long long o = 0, routed = 0;
+    long long o = 0, routed = 0, chunks = 0;
     for (int g = 0; g < G; ++g) {
       off[g] = o;
       o += rup(gcnt[g], kUnitRows);
       routed += gcnt[g];
+      chunks += (long long)gcnt[g] * ((gk[g] + kUnitRows - 1) / kUnitRows);
     }
     off[G] = o;
-    stats[0] += (unsigned long long)routed;
+    *rows_stat += (unsigned long long)routed;
+    *chunks_stat += (unsigned long long)chunks;
   }
   __syncthreads();
   for (int g = threadIdx.x; g <= G; g += blockDim.x) {
@@ -377,6 +383,86 @@ route_scatter_kernel(const int* __restrict__ route, long long n, int G, const in
       }
     }
     __syncthreads();
+  }
+}
+
+// Near ties of the group scan, compacted: the flagged routed rows counted per group
+// (shared-memory histogram), ...
+__global__ void flag_count_kernel(const int* __restrict__ flag, const int* __restrict__ count,
+                                  long long cap, const int* __restrict__ uprob, int G,
+                                  int* __restrict__ gcnt, const int* stop) {
+  if (stopped(stop)) return;
+  extern __shared__ int hist[];
+  for (int g = threadIdx.x; g < G; g += blockDim.x) hist[g] = 0;
+  __syncthreads();
+  const long long c = min((long long)*count, cap);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < c;
+       i += (long long)gridDim.x * blockDim.x)
+    atomicAdd(hist + uprob[flag[i] / kUnitRows], 1);
+  __syncthreads();
+  for (int g = threadIdx.x; g < G; g += blockDim.x)
+    if (hist[g]) atomicAdd(gcnt + g, hist[g]);
+}
+
+// ... then copied, one warp per flagged row, into rows of their group in a second layout (row
+// q of group g in [row_off2[g], rend2[g]); one atomic per group and warp reserves the rows), with
+// their floors, routed rows and data rows; list2[i] = the compact row of flagged entry i.
+__global__ void flag_scatter_kernel(const int* __restrict__ flag, const int* __restrict__ count,
+                                    long long cap, const int* __restrict__ uprob,
+                                    const long long* __restrict__ row_off2, int* __restrict__ fill2,
+                                    const uint4* __restrict__ XbR, const uint4* __restrict__ XlR,
+                                    long long vb, const float* __restrict__ thrR,
+                                    const int* __restrict__ rowmap, uint4* __restrict__ Xb2,
+                                    uint4* __restrict__ Xl2, float* __restrict__ thr2,
+                                    int* __restrict__ xrow2, int* __restrict__ rmap2,
+                                    int* __restrict__ list2, const int* stop) {
+  if (stopped(stop)) return;
+  const long long c = min((long long)*count, cap);
+  const int lane = threadIdx.x & 31;
+  for (long long base = ((long long)blockIdx.x * blockDim.x + threadIdx.x) & ~31LL; base < c;
+       base += (long long)gridDim.x * blockDim.x) {
+    const long long i = base + lane;
+    const bool live = i < c;
+    const int r = live ? flag[i] : 0;
+    const int g = live ? uprob[r / kUnitRows] : -1;
+    // lanes of the same group reserve their rows with one atomic (the lowest lane)
+    const unsigned peers = __match_any_sync(0xffffffffu, g);
+    const int leader = __ffs(peers) - 1;
+    const int rank = __popc(peers & lanemask_lt());
+    int q0 = 0;
+    if (live && lane == leader) q0 = atomicAdd(fill2 + g, __popc(peers));
+    q0 = __shfl_sync(0xffffffffu, q0, leader);
+    const long long q = live ? row_off2[g] + q0 + rank : -1;
+    if (live) {
+      thr2[q] = thrR[r];
+      xrow2[q] = rowmap[r];
+      rmap2[q] = r;
+      list2[i] = (int)q;
+    }
+    // the rows, one warp per row
+    for (int t = 0; t < 32; ++t) {
+      const long long qt = __shfl_sync(0xffffffffu, q, t);
+      const int rt = __shfl_sync(0xffffffffu, r, t);
+      if (qt < 0) continue;
+      for (long long v = lane; v < vb; v += 32) {
+        Xb2[qt * vb + v] = XbR[(size_t)rt * vb + v];
+        if (Xl2) Xl2[qt * vb + v] = XlR[(size_t)rt * vb + v];
+      }
+    }
+  }
+}
+
+// The compact rows' labels back to their routed rows.
+__global__ void flag_copy_back_kernel(const int* __restrict__ list2, const int* __restrict__ count,
+                                      long long cap, const int* __restrict__ rmap2,
+                                      const int* __restrict__ lab2, int* __restrict__ labR,
+                                      const int* stop) {
+  if (stopped(stop)) return;
+  const long long c = min((long long)*count, cap);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < c;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int q = list2[i];
+    labR[rmap2[q]] = lab2[q];
   }
 }
 
@@ -557,6 +643,13 @@ __global__ void scatter_fallback_kernel(const int* __restrict__ fb_list,
     labels[fb_list[r]] = labF[r];
 }
 
+// Linking cap as a multiple of the median member distance (KMGB_ROUTER_CAP overrides it).
+float cap_factor() {
+  const char* v = std::getenv("KMGB_ROUTER_CAP");
+  const float f = v ? (float)std::atof(v) : 0.0f;
+  return f > 0.0f ? f : 2.5f;
+}
+
 cudaError_t sync_err(cudaStream_t s) {
   cudaError_t e = cudaStreamSynchronize(s);
   return e != cudaSuccess ? e : cudaGetLastError();
@@ -584,12 +677,18 @@ struct Router {
   void *CbP = nullptr, *ClP = nullptr;
   float *CopP = nullptr, *cinitP = nullptr, *cnP = nullptr;
   // routing
-  int *route = nullptr, *rowmap = nullptr, *labR = nullptr, *flagR = nullptr, *overR = nullptr;
+  int *route = nullptr, *rowmap = nullptr, *labR = nullptr, *flagR = nullptr;
   int *candR = nullptr, *ccntR = nullptr, *uprob = nullptr, *gcnt = nullptr, *fill = nullptr;
   int *gdone = nullptr, *rcount = nullptr;
   long long *row_off = nullptr, *rend = nullptr;
   void *XbR = nullptr, *XlR = nullptr;
   float *xnR = nullptr, *thrR = nullptr;
+  // the routed rows with near ties, compacted by group for the candidate pass
+  void *Xb2 = nullptr, *Xl2 = nullptr;
+  float* thr2 = nullptr;
+  int *xrow2 = nullptr, *rmap2 = nullptr, *list2 = nullptr, *lab2 = nullptr, *over2 = nullptr;
+  int *uprob2 = nullptr, *gcnt2 = nullptr, *fill2 = nullptr, *gdone2 = nullptr;
+  long long *row_off2 = nullptr, *rend2 = nullptr;
   unsigned long long* dstats = nullptr;
   // network
   MlpShape sh{};
@@ -607,6 +706,20 @@ struct Router {
   float *cin1 = nullptr, *cin2 = nullptr;
   int G_pad = 0;
   RouterStats st;
+  // stage events (profiling): 8 per routed iteration, read out by router_stats
+  bool prof = false;
+  std::vector<cudaEvent_t> ev;
+  size_t ev_used = 0, ev_read = 0;
+  cudaError_t mark(cudaStream_t s) {
+    if (!prof) return cudaSuccess;
+    if (ev_used == ev.size()) {
+      cudaEvent_t e;
+      cudaError_t r = cudaEventCreate(&e);
+      if (r != cudaSuccess) return r;
+      ev.push_back(e);
+    }
+    return cudaEventRecord(ev[ev_used++], s);
+  }
 
   void carve(Carve& c) {
     c.take(&group, k);
@@ -626,7 +739,6 @@ struct Router {
     c.take(&rowmap, rows_cap);
     c.take(&labR, rows_cap);
     c.take(&flagR, rows_cap);
-    c.take(&overR, rows_cap);
     c.take(&candR, (size_t)rows_cap * kMaxCand);
     c.take(&ccntR, rows_cap);
     c.take(&uprob, max_units);
@@ -639,7 +751,20 @@ struct Router {
     c.take_bytes(&XbR, (size_t)rows_cap * ldb * 2);
     c.take(&xnR, rows_cap);
     c.take(&thrR, rows_cap);
-    c.take(&dstats, 4);
+    c.take(&dstats, 8);
+    c.take_bytes(&Xb2, (size_t)rows_cap * ldb * 2);
+    c.take(&thr2, rows_cap);
+    c.take(&xrow2, rows_cap);
+    c.take(&rmap2, rows_cap);
+    c.take(&list2, rows_cap);
+    c.take(&lab2, rows_cap);
+    c.take(&over2, rows_cap);
+    c.take(&uprob2, max_units);
+    c.take(&gcnt2, G + 1);
+    c.take(&fill2, G + 1);
+    c.take(&gdone2, G + 1);
+    c.take(&row_off2, G + 1);
+    c.take(&rend2, G + 1);
     c.take(&P, np);
     c.take(&Gr, np);
     c.take(&Am, np);
@@ -696,7 +821,7 @@ cudaError_t router_create(Router** out, const RouterIO& io, int groups, int hidd
   Carve cut;
   cut.base = static_cast<char*>(r->arena);
   r->carve(cut);
-  e = cudaMemsetAsync(r->dstats, 0, 4 * sizeof(unsigned long long), s);
+  e = cudaMemsetAsync(r->dstats, 0, 8 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) {
     router_destroy(r, s);
     return e;
@@ -707,12 +832,17 @@ cudaError_t router_create(Router** out, const RouterIO& io, int groups, int hidd
 
 void router_destroy(Router* r, cudaStream_t s) {
   if (!r) return;
+  for (cudaEvent_t e : r->ev) cudaEventDestroy(e);
   if (r->XlR) dev_free(r->XlR, s);
+  if (r->Xl2) dev_free(r->Xl2, s);
   dev_free(r->arena, s);
   delete r;
 }
 
 bool router_trained(const Router* r) { return r && r->trained; }
+void router_set_profiling(Router* r, bool on) {
+  if (r) r->prof = on;
+}
 size_t router_device_bytes(const Router* r) { return r ? r->arena_bytes : 0; }
 
 // Components of the usable centers and their packing into groups (first training only).
@@ -744,7 +874,7 @@ static cudaError_t form_groups(Router* r, const RouterIO& io, cudaStream_t s) {
   if (!meds.empty()) {
     auto mid = meds.begin() + meds.size() / 2;
     std::nth_element(meds.begin(), mid, meds.end());
-    cap = 3.6f * *mid;
+    cap = cap_factor() * *mid;
   }
   KMGB_CUDA_TRY(cudaMemcpyAsync(r->thr, thr.data(), sizeof(float) * k, cudaMemcpyHostToDevice, s));
   uf_init_kernel<<<num_sms() * 4, 256, 0, s>>>(r->par, k);
@@ -793,6 +923,8 @@ static cudaError_t form_groups(Router* r, const RouterIO& io, cudaStream_t s) {
   for (int c = 0; c < k; ++c)  // ascending center index inside a group: lowest index on ties
     if (r->group_h[c] >= 0) cperm[pos[r->group_h[c]]++] = c;
   r->st.components = (int)roots.size();
+  r->st.max_group = *std::max_element(gkh.begin(), gkh.begin() + G);
+  r->st.max_component = roots.empty() ? 0 : size[roots[0]];
   r->st.groups_nonempty = (int)std::count_if(gkh.begin(), gkh.begin() + G, [](int v) { return v > 0; });
   KMGB_CUDA_TRY(cudaMemcpyAsync(r->group, r->group_h.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s));
   KMGB_CUDA_TRY(cudaMemcpyAsync(r->cperm, cperm.data(), sizeof(int) * r->KPmax, cudaMemcpyHostToDevice, s));
@@ -831,6 +963,8 @@ static cudaError_t refresh_separation(Router* r, const RouterIO& io, cudaStream_
 }
 
 cudaError_t router_train(Router* r, const RouterIO& io, cudaStream_t s) {
+  // the iterations queued before the training are not part of its time
+  KMGB_CUDA_TRY(sync_err(s));
   const auto t0 = std::chrono::steady_clock::now();
   if (!r->grouped) {
     KMGB_CUDA_TRY(form_groups(r, io, s));
@@ -898,8 +1032,14 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
                           cudaStream_t s) {
   const int G = r->G, k = r->k;
   const long long vb = r->ldb * 2 / 16, vx = r->ldx / 4;
+  if (r->prof && r->ev_used - r->ev_read > 4096) {  // read out what has accumulated
+    RouterStats tmp;
+    KMGB_CUDA_TRY(router_stats(r, &tmp, s));
+  }
+  KMGB_CUDA_TRY(r->mark(s));
   // the separation bound for the current centers
   KMGB_CUDA_TRY(refresh_separation(r, io, s));
+  KMGB_CUDA_TRY(r->mark(s));
   // centers in group order
   permute_centers_kernel<<<num_sms() * 8, 256, 0, s>>>(
       r->cperm, r->KP, static_cast<const uint4*>(io.Cb), static_cast<const uint4*>(io.Cl), vb,
@@ -907,6 +1047,7 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
       io.Cl ? static_cast<uint4*>(r->ClP) : nullptr, reinterpret_cast<float4*>(r->CopP), r->cinitP,
       r->cnP, io.stop);
   count_launches(1);
+  KMGB_CUDA_TRY(r->mark(s));
   // inference: hidden layer (store mode), then the group (arg-max mode), in row chunks
   for (long long r0 = 0; r0 < r->n; r0 += kChunkRows) {
     const long long rows = std::min<long long>(kChunkRows, r->n - r0);
@@ -933,13 +1074,15 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
     b.stop = io.stop;
     KMGB_CUDA_TRY(launch_assign_bf16(r->Hbuf, nullptr, r->hidden, r->W2b, nullptr, r->hidden, b, s));
   }
+  KMGB_CUDA_TRY(r->mark(s));
   // sort the points by group
   KMGB_CUDA_TRY(cudaMemsetAsync(r->gcnt, 0, sizeof(int) * (G + 1), s));
   route_count_kernel<<<num_sms() * 4, 1024, sizeof(int) * G, s>>>(r->route, r->n, G, r->gk,
                                                                    r->gcnt, fb_list, fb_count,
                                                                    io.stop);
-  route_tables_kernel<<<1, 1024, 0, s>>>(r->gcnt, G, r->max_units, r->row_off, r->rend, r->gdone,
-                                         r->fill, r->uprob, r->dstats, io.stop);
+  route_tables_kernel<<<1, 1024, 0, s>>>(r->gcnt, r->gk, G, r->max_units, r->row_off, r->rend,
+                                         r->gdone, r->fill, r->uprob, r->dstats, r->dstats + 4,
+                                         io.stop);
   count_launches(2);
   if (io.Xl && !r->XlR) KMGB_CUDA_TRY(dev_alloc(&r->XlR, (size_t)r->rows_cap * r->ldb * 2, s));
   route_scatter_kernel<<<num_sms() * 2, 256, sizeof(int) * (2 * G + kScatterPts), s>>>(
@@ -947,6 +1090,7 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
       static_cast<const uint4*>(io.Xl), vb, io.xn, r->rowmap, static_cast<uint4*>(r->XbR),
       io.Xl ? static_cast<uint4*>(r->XlR) : nullptr, r->xnR, io.stop);
   count_launches(1);
+  KMGB_CUDA_TRY(r->mark(s));
   // scan of each point's group, certified within the group
   KMGB_CUDA_TRY(cudaMemsetAsync(r->rcount, 0, sizeof(int) * 4, s));
   int no_floor_bits;
@@ -980,26 +1124,52 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
   KMGB_CUDA_TRY(launch_assign_bf16(r->XbR, XlR, r->ldb, r->CbP, ClP, r->ldb, a, s));
   add_count_kernel<<<1, 32, 0, s>>>(r->rcount, r->dstats + 1, io.stop);
   count_launches(1);
-  // near ties inside the group: every center whose key reaches the point's floor
+  KMGB_CUDA_TRY(r->mark(s));
+  // near ties inside the group: the flagged rows, compacted by group, take a second scan of
+  // their group that records every center whose key reaches the point's floor; those
+  // candidates are resolved exactly
+  KMGB_CUDA_TRY(cudaMemsetAsync(r->gcnt2, 0, sizeof(int) * (G + 1), s));
+  flag_count_kernel<<<num_sms() * 2, 1024, sizeof(int) * G, s>>>(r->flagR, r->rcount, r->rows_cap,
+                                                                  r->uprob, G, r->gcnt2, io.stop);
+  route_tables_kernel<<<1, 1024, 0, s>>>(r->gcnt2, r->gk, G, r->max_units, r->row_off2,
+                                         r->rend2, r->gdone2, r->fill2, r->uprob2, r->dstats + 6,
+                                         r->dstats + 7, io.stop);
+  if (XlR && !r->Xl2) KMGB_CUDA_TRY(dev_alloc(&r->Xl2, (size_t)r->rows_cap * r->ldb * 2, s));
+  flag_scatter_kernel<<<num_sms() * 4, 256, 0, s>>>(
+      r->flagR, r->rcount, r->rows_cap, r->uprob, r->row_off2, r->fill2,
+      static_cast<const uint4*>(r->XbR), static_cast<const uint4*>(XlR), vb, r->thrR, r->rowmap,
+      static_cast<uint4*>(r->Xb2), XlR ? static_cast<uint4*>(r->Xl2) : nullptr, r->thr2, r->xrow2,
+      r->rmap2, r->list2, io.stop);
+  count_launches(3);
   AssignArgs c2 = a;
   c2.labels = nullptr;
   c2.certify = 0;
   c2.thr_out = nullptr;
-  c2.thr_in = r->thrR;
+  c2.xnorm = nullptr;
+  c2.thr_in = r->thr2;
   c2.cand = r->candR;
   c2.cand_cnt = r->ccntR;
-  KMGB_CUDA_TRY(launch_assign_bf16(r->XbR, XlR, r->ldb, r->CbP, ClP, r->ldb, c2, s));
-  KMGB_CUDA_TRY(launch_resolve_candidates(r->flagR, r->rcount, r->rows_cap, r->candR, r->ccntR,
-                                          io.X, r->ldx, r->CopP, r->ldx, r->cnP, r->d, r->labR,
-                                          r->overR, r->rcount + 1, io.stop, s, r->rowmap));
-  mark_over_kernel<<<num_sms() * 2, 256, 0, s>>>(r->overR, r->rcount + 1, r->rows_cap, r->labR,
+  c2.u_prob = r->uprob2;
+  c2.g_rend = r->rend2;
+  c2.g_done = r->gdone2;
+  KMGB_CUDA_TRY(launch_assign_bf16(r->Xb2, XlR ? r->Xl2 : nullptr, r->ldb, r->CbP, ClP, r->ldb,
+                                   c2, s));
+  KMGB_CUDA_TRY(launch_resolve_candidates(r->list2, r->rcount, r->rows_cap, r->candR, r->ccntR,
+                                          io.X, r->ldx, r->CopP, r->ldx, r->cnP, r->d, r->lab2,
+                                          r->over2, r->rcount + 1, io.stop, s, r->xrow2));
+  mark_over_kernel<<<num_sms() * 2, 256, 0, s>>>(r->over2, r->rcount + 1, r->rows_cap, r->lab2,
                                                  io.stop);
+  flag_copy_back_kernel<<<num_sms() * 2, 256, 0, s>>>(r->list2, r->rcount, r->rows_cap, r->rmap2,
+                                                      r->lab2, r->labR, io.stop);
+  count_launches(2);
+  KMGB_CUDA_TRY(r->mark(s));
   // certificate against every center outside the group
   router_finish_kernel<<<num_sms() * 8, 256, 0, s>>>(
       r->rows_cap, G, r->uprob, r->rend, r->rowmap, r->labR, r->KP, r->cperm, r->cnP, io.X,
       r->ldx, io.C, r->d, r->m0, io.labels, fb_list, fb_count, r->dstats, io.stop);
   add_count_kernel<<<1, 32, 0, s>>>(fb_count, r->dstats + 3, io.stop);
   count_launches(3);
+  KMGB_CUDA_TRY(r->mark(s));
   r->st.routed_iterations += 1;
   return cudaGetLastError();
 }
@@ -1027,9 +1197,19 @@ cudaError_t router_scatter_labels(const int* fb_list, const int* fb_count, long 
 }
 
 cudaError_t router_stats(Router* r, RouterStats* out, cudaStream_t s) {
-  unsigned long long v[4] = {0, 0, 0, 0};
+  unsigned long long v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   KMGB_CUDA_TRY(cudaMemcpyAsync(v, r->dstats, sizeof(v), cudaMemcpyDeviceToHost, s));
   KMGB_CUDA_TRY(cudaStreamSynchronize(s));
+  // stage times of the routed iterations recorded since the last read (8 events each)
+  for (; r->ev_read + 8 <= r->ev_used; r->ev_read += 8)
+    for (int t = 0; t < 7; ++t) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, r->ev[r->ev_read + t], r->ev[r->ev_read + t + 1]) ==
+          cudaSuccess)
+        r->st.stage_ms[t] += ms;
+    }
+  if (r->ev_read == r->ev_used) r->ev_read = r->ev_used = 0;  // reuse the events
+  r->st.scan_chunks = v[4];
   r->st.routed = v[0];
   r->st.flagged = v[1];
   r->st.certified = v[2];

@@ -65,11 +65,19 @@ struct RouterStats {
   double last_accuracy = 0.0;  // share of the training sample routed to its label's group
   int groups_nonempty = 0;
   int components = 0;
+  int max_group = 0;       // centers of the largest group
+  int max_component = 0;   // centers of the largest component
+  unsigned long long scan_chunks = 0;  // sum over routed points of their group's 256-center chunks
   // device-side counters summed over routed iterations: points routed to a group scan, points
   // whose in-group margin needed the candidate pass, points certified by the group rule, points
   // sent to the full scan
   unsigned long long routed = 0, flagged = 0, certified = 0, fallback = 0;
   long long routed_iterations = 0;
+  // with profiling on (router_set_profiling), CUDA-event milliseconds of the routed assignment's
+  // stages summed over the routed iterations: [0] center separation, [1] centers in group order,
+  // [2] network inference, [3] sort by group, [4] group scan, [5] in-group near ties (candidate
+  // pass and resolve), [6] certificate
+  double stage_ms[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 // groups: G; hidden: H; split: the tier has the BF16 residual planes of the centers.
@@ -99,5 +107,7 @@ cudaError_t router_scatter_labels(const int* fb_list, const int* fb_count, long 
 // Host copy of the statistics (reads the device counters; synchronises s).
 cudaError_t router_stats(Router* r, RouterStats* out, cudaStream_t s);
 size_t router_device_bytes(const Router* r);
+// Stage timing of the routed assignment (CUDA events on its stream).
+void router_set_profiling(Router* r, bool on);
 
 }  // namespace kmgb
