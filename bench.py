@@ -51,7 +51,6 @@ TENSOR_PRODUCTS = {"bf16x3": 3, "bf16": 1}
 # the workload's run is 30 Lloyd iterations: the end-to-end leg makes that one public call
 E2E_ITERS = 30
 METRIC = "Lloyd iter/s (N=4M, D=128, K=1024), labels = FP64 arg-min"
-CPU_SAMPLE_ROWS = 65_536
 
 
 def peaks():
@@ -112,25 +111,52 @@ def replica_rate(ms: float, steps: int, world: int, dist=None, device: str = "cu
     return ms, world * steps / (ms / 1000.0)
 
 
-def cpu_baseline(steps: int = 1):
-    """Oracle FP32 port (CPU restatement, OpenMP, all host threads) on a bounded sample: one
-    Lloyd iteration over CPU_SAMPLE_ROWS rows of the workload, scaled to the full N."""
+def host_info():
+    """Host cores and CPU model of the machine the CPU baseline runs on."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:  # noqa: BLE001 - informational
+        pass
+    return {"nproc": os.cpu_count(), "cpu_model": model}
+
+
+def workload_host(n=N):
+    """The GPU arm's data set and initial centers (same generator, seed and picks), on the host."""
+    import torch
+    from kmeans_gb300.synthetic import mixture_torch, sample_init
+    X, _, _ = mixture_torch(n, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+    Xh = X.cpu().numpy()
+    del X
+    torch.cuda.empty_cache()
+    return Xh, Xh[sample_init(n, K, seed=99)].copy()
+
+
+def cpu_baseline(X, init, steps: int, warmup: int = 1):
+    """The oracle's FP32 port of the reference loop (CPU restatement, OpenMP, all host threads)
+    over ALL rows of the workload: `warmup` untimed iterations, then `steps` timed iterations,
+    each continuing from the previous one's centers (one full Lloyd iteration per step)."""
     import oracle
-    from kmeans_gb300.synthetic import mixture_numpy, sample_init
-    X, _, _ = mixture_numpy(CPU_SAMPLE_ROWS, D, K, seed=5, mean_lo=-20, mean_hi=20, std=(0.3, 3.0))
-    init = X[sample_init(CPU_SAMPLE_ROWS, K, seed=6)]
-    oracle.port_lloyd(X[:4096], init, 1)  # warm the thread pool
+    C = np.ascontiguousarray(init, dtype=np.float32)
+    for _ in range(max(0, warmup)):
+        C, _, _ = oracle.port_lloyd(X, C, 1)
     times = []
     for _ in range(max(1, steps)):
         t0 = time.perf_counter()
-        oracle.port_lloyd(X, init, 1)
+        C, _, _ = oracle.port_lloyd(X, C, 1)
         times.append(time.perf_counter() - t0)
-    t = float(np.median(times))
-    return {"value": (CPU_SAMPLE_ROWS / N) / t, "unit": "iter/s", "cores": oracle.num_threads(),
+    t = float(np.sum(times))
+    info = host_info()
+    return {"value": len(times) / t, "unit": "iter/s", "cores": oracle.num_threads(),
             "kind": "port",
-            "sample": f"1 Lloyd iteration over {CPU_SAMPLE_ROWS} of the {N} rows (D={D}, K={K}), "
-                      f"FP32 port of the reference loop, time scaled linearly to N; median of "
-                      f"{len(times)}", "seconds_per_sample_iter": t}
+            "sample": f"{len(times)} full Lloyd iterations over all {len(X)} rows (D={D}, "
+                      f"K={K}) of the GPU arm's data and initial centers, FP32 port of the "
+                      f"reference loop, {warmup} untimed first",
+            "seconds_per_iteration": t / len(times), **info}
 
 
 def reference_gpu_kernels(N=N, D=D, K=K, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0)):
@@ -234,23 +260,55 @@ def reference_gpu_kernels(N=N, D=D, K=K, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 
         return {"unavailable": str(e)[:200]}
 
 
+def reference_loop_parity():
+    """Whole runs of this library (FP32 and split BF16 tiers) in lockstep with the reference's own
+    kernels run in its loop order from the same initial centers (oracle/ref_loop.py): the
+    100,000 x 32, K=64 configuration for its 20 iterations and the 4M x 128 distribution at
+    200,000 rows for 10. Reports how many iterations agree exactly, the center / SSE differences
+    while they do, and the first differing iteration's rows with their FP64 margins."""
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        import kmeans_gb300 as km
+        from kmeans_gb300.synthetic import mixture_numpy, sample_init
+        from oracle.ref_loop import trajectory_parity
+        km.build()
+        out = {}
+        for name, (n, d, k, iters, lo, hi, std) in {
+                "100000x32_K64": (100_000, 32, 64, 20, -10.0, 10.0, (1.0, 1.0)),
+                "200000x128_K1024": (200_000, 128, 1024, 10, -20.0, 20.0, (0.3, 3.0))}.items():
+            X, _, _ = mixture_numpy(n, d, k, seed=31, mean_lo=lo, mean_hi=hi, std=std)
+            init = X[sample_init(n, k, seed=32)].copy()
+            for tier, tn in ((km.ASSIGN_FP32, "fp32"), (km.ASSIGN_BF16X3, "bf16x3")):
+                r = trajectory_parity(km, X, init, iters, tier)
+                if r is None:
+                    return {"unavailable": "oracle/_ref (the reference's kernels) not built"}
+                out[f"{name}_{tn}"] = r
+        return out
+    except Exception as e:  # noqa: BLE001 - an informational extra
+        return {"unavailable": str(e)[:200]}
+
+
 def reference_arm(args, rank: int):
     if rank != 0:
         return
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_baseline(1)
-    cb = cpu_baseline(max(1, min(args.steps, 3)))
+    X, init = workload_host()
+    cb = cpu_baseline(X, init, steps=args.steps, warmup=min(args.warmup, 2))
+    del X
     line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": "iter/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 / cb["value"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "lloyd_4Mx128_K1024", "n": N, "d": D, "k": K},
-            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                                "nproc", "cpu_model")},
             "e2e": {"value": cb["value"], "unit": "iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "reference_gpu": reference_gpu_kernels(),
             "reference_gpu_100kx32_K64": reference_gpu_kernels(100_000, 32, 64, -10.0, 10.0,
-                                                                (1.0, 1.0))}
+                                                                (1.0, 1.0)),
+            "reference_loop_parity": reference_loop_parity()}
     print(json.dumps(line), flush=True)
 
 
@@ -433,7 +491,7 @@ def large_k_data(n, d, k, seed=77):
     return X, init
 
 
-def timed_run(km, torch, X, init, tier, iters, **opts):
+def timed_run(km, torch, X, init, tier, iters, warm=True, **opts):
     """`iters` iterations of a fresh handle from `init` (one untimed warm-up iteration first),
     CUDA events on the handle's stream around the run. Returns (ms per iteration, phases,
     labels, centers, SSE history, stats, router stats)."""
@@ -442,7 +500,7 @@ def timed_run(km, torch, X, init, tier, iters, **opts):
     h = km.Handle(n, d, k, assign_tier=tier, max_iters=iters + 1, **opts)
     h.set_data(X, True)
     h.set_centers(init, False)
-    if not opts.get("router"):
+    if warm and not opts.get("router"):
         h.run(1)  # warm-up (module loading, graph capture)
         h.synchronize()
         h.set_centers(init, False)
@@ -510,7 +568,7 @@ def large_k_workload(args, n=16_000_000, d=256, k=65_536):
                          "assign_tflops": flop / (ph["assign"] / 1000.0) / 1e12,
                          "reranked_points": st.reranked, "full_rescan_points": st.reranked_fp64}
     if "fp32" in tiers:
-        ms, ph, lab, _, _, _, _ = timed_run(km, torch, X, init, km.ASSIGN_FP32, 1)
+        ms, ph, lab, _, _, _, _ = timed_run(km, torch, X, init, km.ASSIGN_FP32, 1, warm=False)
         out["fp32"] = {"ms_per_iteration": ms, "phase_ms_per_iter": ph, "iterations": 1,
                        "assign_tflops": flop / (ph["assign"] / 1000.0) / 1e12}
         h = km.Handle(n, d, k, assign_tier=km.ASSIGN_BF16X3, max_iters=1)
@@ -535,6 +593,38 @@ def large_k_workload(args, n=16_000_000, d=256, k=65_536):
         out["speedup_vs_plain_fp32"] = (out["fp32"]["ms_per_iteration"]
                                         / out[main_tier]["ms_per_iteration"])
     print(json.dumps(out), flush=True)
+
+
+def large_k_summary(km, torch, n=16_000_000, d=256, k=65_536, iters=25):
+    """The large-K configuration (16M x 256, K=65,536, Zipf sizes, BF16 points, 25 iterations)
+    outside the headline's timed region: the learned router's run, the same iterations of the
+    split BF16 tier without it (labels, centers and SSE must be identical), and one plain FP32
+    iteration (the denominator of the >= 5x target)."""
+    X, init = large_k_data(n, d, k)
+    rt = timed_run(km, torch, X, init, km.ASSIGN_BF16X3, iters, router=1, router_groups=256,
+                   router_retrain=5)
+    st = timed_run(km, torch, X, init, km.ASSIGN_BF16X3, iters)
+    ft = timed_run(km, torch, X, init, km.ASSIGN_FP32, 1, warm=False)
+    rs = rt[6]
+    del X
+    torch.cuda.empty_cache()
+    routed_pts = n * max(1, rs.routed_iterations)
+    return {"workload": "lloyd_16Mx256_K65536", "iterations": iters,
+            "router_ms_per_iteration": rt[0], "split_bf16_ms_per_iteration": st[0],
+            "plain_fp32_ms_per_iteration": ft[0],
+            "speedup_vs_plain_fp32": ft[0] / rt[0], "speedup_vs_split_bf16": st[0] / rt[0],
+            "labels_identical": bool(np.array_equal(rt[2], st[2])),
+            "centers_identical": bool(np.array_equal(rt[3], st[3], equal_nan=True)),
+            "sse_identical": bool(np.array_equal(rt[4], st[4])),
+            "certified_share": rs.certified / routed_pts,
+            "fallback_share": rs.fallback / routed_pts, "trainings": rs.trainings,
+            "train_ms_total": rs.train_ms, "last_train_accuracy": rs.last_accuracy,
+            "router_stage_ms_per_routed_iter": {
+                k_: v / max(1, rs.routed_iterations)
+                for k_, v in zip(km.kmgb_router_stats.STAGES, list(rs.stage_ms))},
+            "router_phase_ms_per_iter": rt[1], "split_phase_ms_per_iter": st[1],
+            "timing": "CUDA events on each handle's stream around the whole run (trainings "
+                      "included); plain FP32: one iteration"}
 
 
 def fp64_workload(args, n=4_000_000, d=128, k=1024, iters=5):
@@ -654,6 +744,8 @@ def main():
                     help="assignment tier: bf16x3 (split BF16 tensor cores, default), bf16, fp32")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-large-k", action="store_true",
+                    help="skip the large-K (16M x 256, K=65,536) router summary")
     ap.add_argument("--n", type=int, default=N, help="rows (default: the 4M workload); smaller "
                     "values are for profiling captures only")
     ap.add_argument("--k", type=int, default=NUM_CENTERS, help="centers (default 1024); other values are "
@@ -815,11 +907,22 @@ def main():
                                     "status": rc_ref,
                                     "call": "computeKmeansF (host pinned data, reference shuffle "
                                             "and initialisation, D x K result)"}}
-        del Xpin, Xh, Xpage
+        del Xpin, Xh
     cb = None
     if not args.no_cpu and rank == 0:
-        cb = cpu_baseline(1)
-        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        # the same rows and initial centers, on the host: 3 timed full iterations
+        Xc = Xpage if e2e is not None else X.cpu().numpy()
+        cb = cpu_baseline(Xc, init, steps=3, warmup=1)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "nproc",
+                                 "cpu_model")}
+        del Xc
+    if e2e is not None:
+        del Xpage
+    h.close()
+    large_k = None
+    if not args.no_large_k and rank == 0 and n == N:
+        torch.cuda.empty_cache()
+        large_k = large_k_summary(km, torch)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
@@ -843,9 +946,8 @@ def main():
                 "plain_fp32": checks["plain_fp32"] if checks else None,
                 "speedup_vs_plain_fp32": (value / checks["plain_fp32"]["iter_per_s"]
                                           if checks else None),
-                "gpu_launches": launches, "clocks": cl}
+                "gpu_launches": launches, "clocks": cl, "large_k": large_k}
         print(json.dumps(line), flush=True)
-    h.close()
     if dist:
         dist.destroy_process_group()
 
