@@ -100,9 +100,9 @@ class Clocks:
 
 
 def replica_rate(ms: float, steps: int, world: int, dist=None, device: str = "cuda"):
-    """N independent replicas (one per GPU, each running `steps` iterations of its own copy of
-    the workload): the slowest rank's timed region sets the whole job's time (max over ranks),
-    and the job's rate counts every rank's iterations. Returns (max ms, iter/s)."""
+    """N ranks, each processing its own 4M-row shard for `steps` iterations: the slowest rank's
+    timed region sets the whole job's time (max over ranks), and the job's rate counts every
+    rank's iterations over its rows. Returns (max ms, iter/s)."""
     if dist is not None and world > 1:
         import torch
         t = torch.tensor([ms], dtype=torch.float64, device=device)
@@ -733,6 +733,50 @@ def streamed_workload(args, n=200_000_000, d=96, k=4096, iters=10, tile=4_000_00
     print(json.dumps(out), flush=True)
 
 
+def sharded_arm(args, rank: int, world: int, local: int, dist):
+    """N > 1: the workload's rows on every rank (the job's data set is N x 4M rows, weak scaling),
+    one sharded Lloyd run (kmeans_gb300/shard.py): each iteration every rank assigns its rows,
+    the ranks all-gather their FP64 per-cluster sums over NCCL and add them in rank order, and
+    every rank updates the same centers. Timed with CUDA events between barriers, max over ranks."""
+    import torch
+    import kmeans_gb300 as km
+    from kmeans_gb300.shard import LibraryShard, lloyd_sharded_device
+    from kmeans_gb300.synthetic import mixture_torch, sample_init
+    tier = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3}[args.tier]
+    X, _, _ = mixture_torch(N, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
+    init = X[torch.from_numpy(sample_init(N, K, seed=99)).cuda()].cpu().numpy()
+    sh = LibraryShard(X, K, init, tier)
+    lloyd_sharded_device(sh, K, D, args.warmup, dist=dist)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    l0 = km.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    res = lloyd_sharded_device(sh, K, D, args.steps, dist=dist)
+    e1.record()
+    torch.cuda.synchronize()
+    dist.barrier()
+    cl = clocks.stop()
+    launches = km.launch_count() - l0
+    ms, value = replica_rate(e0.elapsed_time(e1), args.steps, world, dist)
+    sh.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if args.tier == "fp32" else "bf16", "data": "synthetic",
+                "config": {"workload": "lloyd_4Mx128_K1024", "n": N, "d": D, "k": K,
+                           "tier": args.tier, "certified_labels": True,
+                           "parallelism": f"sharded rows over {world} GPUs (N x 4M rows), one "
+                                          f"all-gather of FP64 per-cluster sums per iteration",
+                           "l2": "inputs larger than L2 (X: 2.05 GB FP32 per rank)"},
+                "exchanged_bytes_per_iteration": res.exchanged_bytes_per_iteration,
+                "sse_last": float(res.sse[-1]), "gpu_launches": launches, "clocks": cl,
+                "e2e": None, "roofline": None, "cpu_baseline": None}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -795,6 +839,10 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+        km.build()
+        sharded_arm(args, rank, world, local, dist)
+        dist.destroy_process_group()
+        return
     km.build()
     lib = km.lib()
     tier = args.tier
@@ -935,7 +983,7 @@ def main():
                            "tier": tier, "certified_labels": True,
                            "storage": "bf16 values" if args.bf16_data else "fp32",
                            "l2": "inputs larger than L2 (X: 2.05 GB FP32 per pass)",
-                           "parallelism": "replicas" if world > 1 else "single"},
+                           "parallelism": "single"},
                 "assign_tflops": achieved,
                 "phase_ms_per_iter": {n: p / max(piters, 1) for n, p in
                                       zip(["prep", "assign", "rerank", "update"], phase)},

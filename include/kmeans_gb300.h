@@ -388,6 +388,22 @@ KMGB_EXPORT int kmgb_router_mlp_train(const float* X, int rows, int d, const int
 KMGB_EXPORT void* kmgb_stream(kmgb_handle* h); /* cudaStream_t of the handle */
 KMGB_EXPORT int kmgb_destroy(kmgb_handle* h);
 
+/* Sharded Lloyd (points partitioned by rows over ranks or GPUs; no reference counterpart: the
+ * reference runs on one GPU, and its update and compactness, kmeans.cpp:1018-1104, are what the
+ * ranks exchange). Each rank holds its rows in a full-batch handle with the same centers.
+ * kmgb_shard_partials assigns the handle's rows to its current centers (labels as kmgb_run's:
+ * the FP64 arg-min) and writes the canonical FP64 sums of those rows per cluster: S (k x d,
+ * row-major), counts (k), Q (k, sums of ||x||^2). The caller adds every rank's S, counts and Q
+ * in rank order (0 + S_0 + S_1 + ..., in FP64) and gives the totals to kmgb_shard_update on every
+ * rank: the new centers (the handle's, with its empty-cluster policy) and the iteration's SSE
+ * against them (sse: host). The result equals a single handle whose rows are streamed in tiles
+ * equal to the shards (opt.stream_tile_rows). Pointers are host memory (on_device 0) or device
+ * memory (on_device 1). */
+KMGB_EXPORT int kmgb_shard_partials(kmgb_handle* h, double* S, int* counts, double* Q,
+                                    int on_device);
+KMGB_EXPORT int kmgb_shard_update(kmgb_handle* h, const double* S, const int* counts,
+                                  const double* Q, double* sse, int on_device);
+
 /* Diagnostic: raw tcgen05 accumulators x.c_j - ||c_j||^2/2 for every point and center, as the
  * BF16 (split = 0), split BF16 (split = 1) or split BF16 with BF16-valued X (split = 2: the two
  * products x.c_hi + x.c_lo; X must hold BF16 numbers) assignment kernel computes them. X: n x d, C: k x d,

@@ -179,6 +179,8 @@ def lib():
             "kmgb_init_kmeanspp": (i32, [P, C.c_ulonglong, P]),
             "kmgb_lloyd_batched_f32": (i32, [P, i32, P, P]),
             "kmgb_get_router_stats": (i32, [P, P]),
+            "kmgb_shard_partials": (i32, [P, P, P, P, i32]),
+            "kmgb_shard_update": (i32, [P, P, P, P, P, i32]),
             "kmgb_router_mlp_train": (i32, [P, i32, i32, P, i32, i32, P, i32, i32, f32, P, P]),
             "kmgb_debug_fail_nth": (None, [i32, i64]),
             "kmgb_debug_withhold_stage": (None, [i64, C.c_ulonglong]),
@@ -563,6 +565,27 @@ class Handle:
         st = kmgb_stats()
         self._chk(lib().kmgb_get_stats(self._h, C.byref(st)))
         return st
+
+    def shard_partials(self, S=None, counts=None, Q=None):
+        """Assign the handle's rows to its centers; canonical FP64 sums per cluster. With torch
+        device tensors given (S k*d float64, counts k int32, Q k float64) they are filled on the
+        device; otherwise host numpy arrays are returned."""
+        on_dev = S is not None and not isinstance(S, np.ndarray)
+        if S is None:
+            S = np.empty(self.k * self.d, np.float64)
+            counts = np.empty(self.k, np.int32)
+            Q = np.empty(self.k, np.float64)
+        self._chk(lib().kmgb_shard_partials(self._h, _ptr(S), _ptr(counts), _ptr(Q),
+                                            int(on_dev)))
+        return S, counts, Q
+
+    def shard_update(self, S, counts, Q) -> float:
+        """New centers from the summed partials of all shards; returns the iteration's SSE."""
+        on_dev = not isinstance(S, np.ndarray)
+        sse = C.c_double()
+        self._chk(lib().kmgb_shard_update(self._h, _ptr(S), _ptr(counts), _ptr(Q),
+                                          C.byref(sse), int(on_dev)))
+        return sse.value
 
     def router_stats(self) -> kmgb_router_stats:
         st = kmgb_router_stats()

@@ -211,6 +211,9 @@ struct kmgb_handle {
   Router* router = nullptr;
   int router_groups = 0, router_retrain = 0, router_hidden = 0;
   void* fb_arena = nullptr;
+  // sharded Lloyd (kmgb_shard_*): FP64 accumulators of a resident handle (streaming handles have
+  // them in their arena)
+  void* shard_arena = nullptr;
   int* fb_list = nullptr;
   int* fb_count = nullptr;
   int* labF = nullptr;
@@ -270,7 +273,7 @@ struct kmgb_handle {
     if (stream) {
       cudaStreamSynchronize(stream);
       // the fixed buffers live in the arena; these are allocated on their own
-      void* ptrs[] = {arena, sse_dev, kpp_d2, kpp_blk, kpp_sc, kpp_picks, fb_arena};
+      void* ptrs[] = {arena, sse_dev, kpp_d2, kpp_blk, kpp_sc, kpp_picks, fb_arena, shard_arena};
       for (void* p : ptrs) dev_free(p, stream);
       router_destroy(router, stream);
       cudaStreamSynchronize(stream);
@@ -813,7 +816,8 @@ int router_step(kmgb_handle* h, AssignArgs a) {
 // the copy stream, then prepared and assigned on the handle's stream while the next one crosses
 // the link. Whether every x is a BF16 number is known only afterwards, so this iteration uses
 // the three-product bound, which holds for any x.
-int step(kmgb_handle* h, int slot, const float* upload = nullptr) {
+// assign_only (sharded Lloyd): labels of the handle's rows for its current centers, no update.
+int step(kmgb_handle* h, int slot, const float* upload = nullptr, bool assign_only = false) {
   cudaStream_t s = h->stream;
   const float* Xa = h->X;
   const void* Xba = h->Xb;
@@ -910,6 +914,7 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr) {
     }
   }
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
+  if (assign_only) return 0;
   // cluster centers + compactness (kmeans.cpp:1018-1104)
   // the SSE lands in sse_dev[iteration of the run] (device-side index)
   KM_TRY(launch_update(Xa, qna, h->labels, h->C, h->ldx, h->opt.empty_policy, h->uw,
@@ -1573,6 +1578,98 @@ int kmgb_get_stats(kmgb_handle* h, kmgb_stats* st) {
     st->reserved[5] = (long long)rs.flagged;
   }
   return 0;
+}
+
+// Sharded Lloyd: the handle holds one rank's rows; the ranks exchange the canonical FP64 sums.
+static int shard_prepare(kmgb_handle* h) {
+  if (!h) return KMEANS_ERROR_COMPUTE;
+  if (h->streaming || h->mini || !h->have_data || !h->have_centers) {
+    set_err("sharded Lloyd needs a full-batch handle with resident data and centers");
+    return KMEANS_ERROR_COMPUTE;
+  }
+  if (!h->accS) {
+    auto carve = [&](Arena& a) {
+      a.take(&h->accS, (size_t)h->k * h->d);
+      a.take(&h->accQ, h->k);
+      a.take(&h->accN, h->k);
+    };
+    Arena sizing;
+    carve(sizing);
+    KM_TRY(dev_alloc(&h->shard_arena, sizing.off, h->stream), KMEANS_ERROR_COMPUTE);
+    Arena cut;
+    cut.base = static_cast<char*>(h->shard_arena);
+    carve(cut);
+  }
+  return 0;
+}
+
+static int shard_check_error_word(kmgb_handle* h) {
+  int e = 0;
+  KM_TRY(cudaMemcpy(&e, h->err, sizeof(int), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPUTE);
+  if (e) {
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), "device error word %d (see kmgb_dev_error)", e);
+    set_err(buf);
+    return e == KMGB_DEV_BAD_LABEL ? KMEANS_ERROR_CLUSTER_CENTERS : KMEANS_ERROR_CLOSEST_CENTERS;
+  }
+  return 0;
+}
+
+int kmgb_shard_partials(kmgb_handle* h, double* S, int* counts, double* Q, int on_device) {
+  int rc = shard_prepare(h);
+  if (rc) return rc;
+  if (!S || !counts || !Q) return KMEANS_ERROR_COMPUTE;
+  cudaStream_t s = h->stream;
+  // the device stop flag only serves kmgb_run's own loop: the caller decides here
+  KM_TRY(cudaMemsetAsync(h->stop, 0, sizeof(int), s), KMEANS_ERROR_COMPUTE);
+  rc = step(h, 0, nullptr, true);
+  if (rc) return rc;
+  KM_TRY(cudaMemsetAsync(h->accS, 0, sizeof(double) * (size_t)h->k * h->d, s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  KM_TRY(cudaMemsetAsync(h->accQ, 0, sizeof(double) * h->k, s), KMEANS_ERROR_CLUSTER_CENTERS);
+  KM_TRY(cudaMemsetAsync(h->accN, 0, sizeof(int) * h->k, s), KMEANS_ERROR_CLUSTER_CENTERS);
+  KM_TRY(launch_stream_accumulate(h->X, h->ldx, h->qn, h->labels, h->uw, h->accS, h->accN, h->accQ,
+                                  s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  KM_TRY(inject_fault(kFaultCopy) ? cudaErrorInvalidValue : cudaSuccess, KMEANS_ERROR_COMPUTE);
+  KM_TRY(cudaMemcpyAsync(S, h->accS, sizeof(double) * (size_t)h->k * h->d, kind, s),
+         KMEANS_ERROR_COMPUTE);
+  KM_TRY(cudaMemcpyAsync(counts, h->accN, sizeof(int) * h->k, kind, s), KMEANS_ERROR_COMPUTE);
+  KM_TRY(cudaMemcpyAsync(Q, h->accQ, sizeof(double) * h->k, kind, s), KMEANS_ERROR_COMPUTE);
+  KM_TRY(cudaStreamSynchronize(s), KMEANS_ERROR_COMPUTE);
+  return shard_check_error_word(h);
+}
+
+int kmgb_shard_update(kmgb_handle* h, const double* S, const int* counts, const double* Q,
+                      double* sse, int on_device) {
+  int rc = shard_prepare(h);
+  if (rc) return rc;
+  if (!S || !counts || !Q) return KMEANS_ERROR_COMPUTE;
+  cudaStream_t s = h->stream;
+  const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  KM_TRY(cudaMemcpyAsync(h->accS, S, sizeof(double) * (size_t)h->k * h->d, kind, s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  KM_TRY(cudaMemcpyAsync(h->accN, counts, sizeof(int) * h->k, kind, s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  KM_TRY(cudaMemcpyAsync(h->accQ, Q, sizeof(double) * h->k, kind, s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  UpdateWork w = h->uw;  // the SSE goes to sse_dev[0]; no device loop state
+  w.stop = nullptr;
+  w.sse_prev = nullptr;
+  w.rel_out = nullptr;
+  w.iters_done = nullptr;
+  w.sse_indexed = 0;
+  KM_TRY(launch_stream_finalize(h->accS, h->accN, h->accQ, h->C, h->ldx, h->opt.empty_policy, w,
+                                h->sse_dev, s),
+         KMEANS_ERROR_CLUSTER_CENTERS);
+  double v = 0.0;
+  KM_TRY(cudaMemcpyAsync(&v, h->sse_dev, sizeof(double), cudaMemcpyDeviceToHost, s),
+         KMEANS_ERROR_COMPACTNESS);
+  KM_TRY(cudaStreamSynchronize(s), KMEANS_ERROR_COMPACTNESS);
+  if (sse) *sse = v;
+  h->iter_base += 1;
+  return shard_check_error_word(h);
 }
 
 int kmgb_get_router_stats(kmgb_handle* h, kmgb_router_stats* out) {
