@@ -210,8 +210,12 @@ KMGB_EXPORT kmeansCudaErrorStatus colNormalizeD(const int m, const int n, const 
 
 enum kmgb_assign_tier {
   KMGB_ASSIGN_FP32 = 0,  /* plain FP32 fused kernel (TMA + FFMA) */
-  KMGB_ASSIGN_BF16 = 1,  /* tcgen05 BF16 tensor cores, FP32 accumulate in TMEM (D <= 256) */
-  KMGB_ASSIGN_BF16X3 = 2 /* tcgen05 split BF16: x.c = xh.ch + xh.cl + xl.ch (D <= 256) */
+  KMGB_ASSIGN_BF16 = 1,  /* tcgen05 BF16 tensor cores, FP32 accumulate in TMEM (D <= 512) */
+  KMGB_ASSIGN_BF16X3 = 2, /* tcgen05 split BF16: x.c = xh.ch + xh.cl + xl.ch (D <= 320) */
+  KMGB_ASSIGN_FP8 = 3     /* tcgen05 FP8 E4M3 (kind::f8f6f4), every point row with its own
+                             power-of-two scale, the centers with one; full batches of resident
+                             data, D <= 512; labels certified against the E4M3 bound and settled
+                             exactly like the BF16 tiers' */
 };
 
 enum kmgb_empty_policy {
@@ -405,8 +409,9 @@ KMGB_EXPORT int kmgb_shard_update(kmgb_handle* h, const double* S, const int* co
                                   const double* Q, double* sse, int on_device);
 
 /* Diagnostic: raw tcgen05 accumulators x.c_j - ||c_j||^2/2 for every point and center, as the
- * BF16 (split = 0), split BF16 (split = 1) or split BF16 with BF16-valued X (split = 2: the two
- * products x.c_hi + x.c_lo; X must hold BF16 numbers) assignment kernel computes them. X: n x d, C: k x d,
+ * BF16 (split = 0), split BF16 (split = 1), split BF16 with BF16-valued X (split = 2: the two
+ * products x.c_hi + x.c_lo; X must hold BF16 numbers) or FP8 (split = 3: sx sc (x8.c8))
+ * assignment kernel computes them. X: n x d, C: k x d,
  * host row-major FP32; out: host n x k. For validating the accumulation-error model on a
  * device; allocates device memory, small problems only. */
 KMGB_EXPORT int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int k,

@@ -42,6 +42,7 @@ KMEANS_NONCONVERGENCE = 13
 ASSIGN_FP32 = 0
 ASSIGN_BF16 = 1
 ASSIGN_BF16X3 = 2
+ASSIGN_FP8 = 3
 EMPTY_NAN = 0
 EMPTY_KEEP = 1
 INIT_REFERENCE = 0

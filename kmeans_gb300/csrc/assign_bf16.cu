@@ -62,6 +62,11 @@ static_assert(kCenterPad % BN == 0, "start values are padded to whole chunks");
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(UNIT >> 4) << 24);
 
+// kind::f8f6f4: D=F32, A=B=E4M3 (format 0), both K-major; K = 32 elements (32 bytes) per MMA, so
+// the shared-memory layout and the per-MMA byte advance are those of the BF16 path.
+constexpr uint32_t IDESC8 = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(UNIT >> 4) << 24);
+constexpr int BK8 = 128;  // E4M3 elements per k-block (one 128-byte swizzle row)
+
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
   d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
@@ -126,6 +131,29 @@ __device__ __forceinline__ float bound_acc(float xn, float cm, int d, int mode) 
   return e * 1.02f + 1e-30f;
 }
 
+// The FP8 tier's bound (accumulator units) of |key - (x.c - ||c||^2/2)|. x = sx x8 + ex with
+// |ex_i| <= u8 |x_i| + ax (u8 = 2^-4: E4M3 keeps 3 mantissa bits; ax = sx 2^-10: half the spacing
+// of the subnormals), likewise c with sc: dropping ex.c + x.ec + ex.ec leaves at most
+// (2 u8 + u8^2)|x||c| + (1 + u8) sqrt(d) (ax |c| + ac |x|) + d ax ac. The products of E4M3 numbers
+// are exact in FP32; their accumulation in TMEM takes the BF16 path's model with the magnitude
+// sum|products| <= 1.2 |x||c| + that slack, and acc * (sx sc) is exact (powers of two) before
+// the FMA with the start value rounds once.
+__device__ __forceinline__ float bound_fp8(float xn, float cm, int d, float sx, float sc) {
+  const float u = 5.9604645e-8f;
+  const float u8 = 0.0625f;
+  const float ax = sx * 9.765625e-4f, ac = sc * 9.765625e-4f;  // 2^-10
+  const float rd = sqrtf((float)d);
+  const float xc = xn * cm * 1.01f;
+  const float slack = (1.0f + u8) * rd * (ax * cm + ac * xn) + (float)d * ax * ac;
+  const float op = (2.0f * u8 + u8 * u8) * xc + slack;
+  const float gacc = (float)(d / 16 + 2) * 4.76837158e-7f;
+  const float pack = 3.81469727e-6f;
+  const float cc = 0.5f * cm * cm;
+  const float s64 = (float)(d + 2) * 1.2e-16f * (xn + cm) * (xn + cm);
+  const float e = 0.5f * u * cm * cm + op + (gacc + pack + u) * (cc + 1.2f * xc + slack) + s64;
+  return e * 1.02f + 1e-30f;
+}
+
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -178,6 +206,17 @@ __device__ __forceinline__ void umma_pair(uint32_t tmem_d, uint64_t adesc, uint6
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
       "l"(adesc), "l"(bdesc), "r"(IDESC), "r"(accumulate)
+      : "memory");
+}
+
+// Pair MMA on E4M3 operands (the FP8 tier).
+__device__ __forceinline__ void umma_pair8(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
+                                           uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(IDESC8), "r"(accumulate)
       : "memory");
 }
 
@@ -253,7 +292,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   }
   const bool stop_now = stopped(p.stop);  // uniform: every CTA of the grid sees the same flag
   if (stop_now) return;
-  const int nkb = (p.d + BK - 1) / BK;
+  const int bk = mode == 4 ? BK8 : BK;  // elements per k-block (128 bytes per row either way)
+  const int nkb = (p.d + bk - 1) / bk;
   const int nchunks = (p.k + BN - 1) / BN;
   const long long pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
   // rows of this launch: [row0, row0 + n_rows); a device count bounds them in candidate mode
@@ -298,8 +338,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   }
   // points: [buffer][plane][k-block] 16 KB boxes; C stage: [plane] 16 KB boxes of one
   // (chunk, k-block). plane 0 = BF16 value, plane 1 = BF16 residual (split tier).
-  const int xplanes = mode == 2 ? 2 : 1;  // BF16 planes of the points
-  const int cplanes = mode >= 2 ? 2 : 1;  // and of the centers
+  const int xplanes = mode == 2 ? 2 : 1;                // BF16 planes of the points
+  const int cplanes = (mode == 2 || mode == 3) ? 2 : 1;  // and of the centers
   const size_t xbuf_bytes = (size_t)xplanes * nkb * XKB_BYTES;
   const uint32_t stage_bytes = (uint32_t)cplanes * CKB_BYTES;
   uint8_t* cs = smem + (size_t)xbufs * xbuf_bytes;
@@ -363,13 +403,13 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         for (int pl = 0; pl < xplanes; ++pl)
           for (int kb = 0; kb < nkb; ++kb)
             tma_load_2d_pair(smem_u32(xs + (size_t)(pl * nkb + kb) * XKB_BYTES), pl ? &tmXl : &tmX,
-                             xb, kb * BK, xrow);
+                             xb, kb * bk, xrow);
         // the next unit's points come from HBM: start them towards L2 now, so that their TMA
         // load (queued behind the center stages) is an L2 hit
         if (u + npairs < n_units) {
           const int nrow = (int)(p.row0 + (u + npairs) * UNIT + rank * BM);
           for (int pl = 0; pl < xplanes; ++pl)
-            for (int kb = 0; kb < nkb; ++kb) tma_prefetch_2d(pl ? &tmXl : &tmX, kb * BK, nrow);
+            for (int kb = 0; kb < nkb; ++kb) tma_prefetch_2d(pl ? &tmXl : &tmX, kb * bk, nrow);
         }
         for (int c = 0; c < ui.nch && ok; ++c) {
           const int crow = ui.cbase + chunk_of(ui, c) * BN + (int)rank * BNH;
@@ -386,7 +426,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             const uint32_t cb = map_to_rank(cb_local, 0);
             for (int pl = 0; pl < cplanes; ++pl)
               tma_load_2d_pair(smem_u32(cs + (size_t)stage * stage_bytes + pl * CKB_BYTES),
-                               pl ? &tmCl : &tmC, cb, kb * BK, crow);
+                               pl ? &tmCl : &tmC, cb, kb * bk, crow);
           }
         }
       }
@@ -433,6 +473,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               const uint64_t bhi = sdesc_sw128(chi + k16 * 32);
               if (mode == 1) {
                 umma_pair(dcol, ahi, bhi, acc);
+              } else if (mode == 4) {
+                umma_pair8(dcol, ahi, bhi, acc);
               } else {
                 // x_hi.c_hi, x_hi.c_lo (x_hi read once into the A collector), then x_lo.c_hi
                 // unless every x is a BF16 number; x_lo.c_lo is below the bound
@@ -482,6 +524,11 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       // HBM latency hides behind the unit's chunks
       const float xn_pt = (p.certify && !cand_mode && h == 0 && prow < n_rows)
                               ? __ldg(p.xnorm + p.out0 + prow) : 0.0f;
+      // FP8 tier: the row's scale and the accumulator multiplier sx * sc (a power of two)
+      const float sx_pt = (mode == 4 && prow < n_rows)
+                              ? __ldg(p.xscale + (cand_mode ? p.row0 : p.out0) + prow) : 0.0f;
+      const float sc_all = mode == 4 ? __ldg(p.cscale) : 0.0f;
+      const float mrow = sx_pt * sc_all;
       for (int c = 0; c < ui.nch; ++c, ++g) {
         const int b = (int)(g & 1);
         bool ok = mbar_wait(smem_u32(&bars.acc_full[b]), (uint32_t)((g >> 1) & 1), &abort_flag,
@@ -509,13 +556,24 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           // padding and unusable centers carry a huge negative start value
           {
             const float4* hs = reinterpret_cast<const float4*>(p.cinit + (size_t)col0 + cb * 32);
+            if (mode == 4) {
 #pragma unroll
-            for (int j4 = 0; j4 < 8; ++j4) {
-              const float4 hv = __ldg(hs + j4);
-              cur[4 * j4 + 0] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 0]), hv.x));
-              cur[4 * j4 + 1] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 1]), hv.y));
-              cur[4 * j4 + 2] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 2]), hv.z));
-              cur[4 * j4 + 3] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 3]), hv.w));
+              for (int j4 = 0; j4 < 8; ++j4) {
+                const float4 hv = __ldg(hs + j4);
+                cur[4 * j4 + 0] = __float_as_uint(__fmaf_rn(__uint_as_float(cur[4 * j4 + 0]), mrow, hv.x));
+                cur[4 * j4 + 1] = __float_as_uint(__fmaf_rn(__uint_as_float(cur[4 * j4 + 1]), mrow, hv.y));
+                cur[4 * j4 + 2] = __float_as_uint(__fmaf_rn(__uint_as_float(cur[4 * j4 + 2]), mrow, hv.z));
+                cur[4 * j4 + 3] = __float_as_uint(__fmaf_rn(__uint_as_float(cur[4 * j4 + 3]), mrow, hv.w));
+              }
+            } else {
+#pragma unroll
+              for (int j4 = 0; j4 < 8; ++j4) {
+                const float4 hv = __ldg(hs + j4);
+                cur[4 * j4 + 0] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 0]), hv.x));
+                cur[4 * j4 + 1] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 1]), hv.y));
+                cur[4 * j4 + 2] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 2]), hv.z));
+                cur[4 * j4 + 3] = __float_as_uint(__fadd_rn(__uint_as_float(cur[4 * j4 + 3]), hv.w));
+              }
             }
           }
           if (store_mode) {
@@ -641,7 +699,8 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             (bblk < 0 || none) ? ui.cbase : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
         p.labels[pt] = label;
         if (p.certify) {
-          const float eb = bound_acc(xn_pt, cm, p.d, mode) +
+          const float eb = (mode == 4 ? bound_fp8(xn_pt, cm, p.d, sx_pt, sc_all)
+                                      : bound_acc(xn_pt, cm, p.d, mode)) +
                            1.02f * p.pert * (xn_pt * cm * 1.01f + 0.5f * cm * cm);
           if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
@@ -733,11 +792,61 @@ float assign_bf16_gamma(int d) {
   return (float)(2.0 * 1.953125e-3 + (d + 32) * 4.76837158e-7);
 }
 
+bool fp8_tc_supported(int d) {
+  return d > 0 && d <= MAX_D &&
+         (size_t)((d + BK8 - 1) / BK8) * XKB_BYTES + 2 * (size_t)CKB_BYTES +
+                 static_smem_for(4) <= SMEM_CAP;
+}
+
+// The FP8 tier (mode 4): E4M3 rows of ld8x / ld8c bytes; one product per k-step.
+static cudaError_t launch_assign_fp8(const void* X8, long long ld8x, const void* C8,
+                                     long long ld8c, const AssignArgs& a, cudaStream_t s) {
+  if (!fp8_tc_supported(a.d) || (ld8x % 16) || (ld8c % 16) || !a.xscale || !a.cscale ||
+      (reinterpret_cast<uintptr_t>(X8) & 15) || (reinterpret_cast<uintptr_t>(C8) & 15) ||
+      a.store_out || a.u_prob)
+    return cudaErrorInvalidValue;
+  VariantInfo& vi = g_variant[4];
+  KMGB_CUDA_TRY(prepare_variant<4>(vi));
+  const size_t xbytes = (size_t)((a.d + BK8 - 1) / BK8) * XKB_BYTES;
+  const size_t stage_bytes = CKB_BYTES;
+  const size_t lim = vi.smem_budget;
+  const int xbufs = (2 * xbytes + 3 * stage_bytes <= lim) ? 2 : 1;
+  if (lim < xbufs * xbytes + 2 * stage_bytes) return cudaErrorInvalidValue;
+  int stages = (int)((lim - xbufs * xbytes) / stage_bytes);
+  if (stages > MAX_STAGES) stages = MAX_STAGES;
+  const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes;
+  CUtensorMap tmX, tmC;
+  KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmX, X8, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, (uint64_t)a.d,
+                                  (uint64_t)a.n, (uint64_t)ld8x, BK8, BM));
+  KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmC, C8, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, (uint64_t)a.d,
+                                  (uint64_t)a.k, (uint64_t)ld8c, BK8, BNH));
+  const long long n_units = (a.n + UNIT - 1) / UNIT;
+  const long long pairs = n_units < vi.max_pairs ? n_units : vi.max_pairs;
+  if (pairs <= 0) return cudaSuccess;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(2 * pairs));
+  cfg.blockDim = dim3(threads_for(4));
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = 2;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4>, tmX, tmX, tmC, tmC, a, stages,
+                                   xbufs, 4));
+  count_launches(1);
+  return cudaSuccess;
+}
+
 cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, const void* Cb,
                                const void* Cl, long long ldcb, const AssignArgs& a,
                                cudaStream_t s) {
   if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (a.n <= 0 || a.k <= 0 || a.d <= 0) return cudaSuccess;
+  if (a.fp8) return launch_assign_fp8(Xb, ldxb, Cb, ldcb, a, s);
   const int planes = (Xl && Cl) ? 2 : 1;  // planes of the split tier's point buffer
   const int mode = Cl ? (Xl ? 2 : 3) : 1;  // see bound_acc
   if (a.store_out && ((a.store_ld % 8) || (reinterpret_cast<uintptr_t>(a.store_out) & 15)))

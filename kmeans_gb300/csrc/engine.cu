@@ -165,6 +165,14 @@ struct kmgb_handle {
   float* X = nullptr;
   void* Xb = nullptr;
   void* Xl = nullptr;   // split tier residual plane
+  // FP8 tier: E4M3 rows (ld8 bytes, a multiple of 16), per-row power-of-two scales; the centers'
+  // E4M3 copy with one scale; compact scales of the candidate pass
+  long long ld8 = 0;
+  void* X8 = nullptr;
+  float* sx = nullptr;
+  void* C8 = nullptr;
+  float* cscale = nullptr;
+  float* sxC = nullptr;
   double* qn = nullptr;
   float* xn = nullptr;
   bool have_data = false;
@@ -305,7 +313,8 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   if (opt) h->opt = *opt;
   else kmgb_default_options(&h->opt);
   const int planes = h->opt.assign_tier == KMGB_ASSIGN_BF16X3 ? 2 : 1;
-  if (h->opt.assign_tier != KMGB_ASSIGN_FP32 && !bf16_tc_supported(d, planes)) {
+  if ((h->opt.assign_tier == KMGB_ASSIGN_BF16 || h->opt.assign_tier == KMGB_ASSIGN_BF16X3) &&
+      !bf16_tc_supported(d, planes)) {
     delete h;
     set_err("kmgb_create: the BF16 tensor-core tier does not support this dimension");
     return KMEANS_ERROR_BUILDDATA;
@@ -332,8 +341,15 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     set_err("kmgb_create: host-streamed tiles run full-batch Lloyd (mini_batch_fraction 1)");
     return KMEANS_ERROR_TILING;
   }
+  if (h->opt.assign_tier == KMGB_ASSIGN_FP8 &&
+      (h->mini || h->streaming || h->opt.router || !fp8_tc_supported(d))) {
+    delete h;
+    set_err("kmgb_create: the FP8 tier runs full batches of resident data with D <= 512");
+    return KMEANS_ERROR_BUILDDATA;
+  }
   if (h->opt.router) {
-    if (h->opt.assign_tier == KMGB_ASSIGN_FP32 || h->mini || h->streaming || !h->opt.certify) {
+    if (h->opt.assign_tier == KMGB_ASSIGN_FP32 || h->opt.assign_tier == KMGB_ASSIGN_FP8 ||
+        h->mini || h->streaming || !h->opt.certify) {
       delete h;
       set_err("kmgb_create: the router needs a BF16 tensor-core tier, full batches of resident "
               "data and certified labels");
@@ -353,8 +369,11 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   h->tile_rows = h->streaming ? h->opt.stream_tile_rows : n;
   h->n_act = h->mini ? h->m_mb : h->tile_rows;
   const long long nx = h->tile_rows;  // rows of a device data buffer
-  const bool bf16 = h->opt.assign_tier != KMGB_ASSIGN_FP32;
+  const bool tcore = h->opt.assign_tier != KMGB_ASSIGN_FP32;  // a tensor-core tier
+  const bool fp8 = h->opt.assign_tier == KMGB_ASSIGN_FP8;
+  const bool bf16 = tcore && !fp8;
   const bool split = h->opt.assign_tier == KMGB_ASSIGN_BF16X3;
+  h->ld8 = round_up(d, 16);
   const int code = KMEANS_ERROR_BUILDDATA;
   KM_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), (delete h, code));
   KM_TRY(cudaEventCreate(&h->ev0), (delete h, code));
@@ -365,7 +384,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   // runs twice, sizing then carving.
   const long long na = h->n_act;
   const long long nl = h->streaming ? n : na;  // labels of every row when streaming
-  if (bf16) {
+  if (tcore) {
     // flagged points are ~1-2% of the rows for the split tier and ~1/3 for plain BF16; the
     // compact copies hold half of the rows, at least 1024 and at most 8M; any excess takes the
     // full rescan. (With many near-equal centers -- K=65,536 drawn from Zipf-sized clusters --
@@ -386,6 +405,10 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     a.take(&h->xn, nx);
     if (bf16) a.take_bytes(&h->Xb, (size_t)nx * h->ldb * 2);
     if (split) a.take_bytes(&h->Xl, (size_t)nx * h->ldb * 2);
+    if (fp8) {
+      a.take_bytes(&h->X8, (size_t)nx * h->ld8);
+      a.take(&h->sx, nx);
+    }
     if (h->streaming) {
       a.take(&h->X2, (size_t)nx * h->ldx);
       a.take(&h->accS, (size_t)k * d);
@@ -404,20 +427,26 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     a.take(&h->Cop, (size_t)k * h->ldx);
     if (bf16) a.take_bytes(&h->Cb, (size_t)k * h->ldb * 2);
     if (split) a.take_bytes(&h->Cl, (size_t)k * h->ldb * 2);
+    if (fp8) {
+      a.take_bytes(&h->C8, (size_t)k * h->ld8);
+      a.take(&h->cscale, 1);
+    }
     a.take(&h->cn, k);
     a.take(&h->cmax, 1);
-    if (bf16) a.take(&h->cinit, (size_t)round_up(k, kCenterPad));
+    if (tcore) a.take(&h->cinit, (size_t)round_up(k, kCenterPad));
     a.take(&h->labels, nl);
     a.take(&h->rr_list, na);
     a.take(&h->rr_count, 3);
     a.take(&h->rr_list2, na);
     a.take(&h->rr_hi2, na);
-    if (bf16) {
+    if (tcore) {
       const long long cc = h->cand_cap;
       a.take(&h->rr_over, na);
       a.take(&h->thr_full, na);
       a.take(&h->thr_c, cc);
+      // compact rows: BF16 (ldb * 2 bytes) or E4M3 (ld8 <= ldb * 2 bytes)
       a.take_bytes(&h->XbC, (size_t)cc * h->ldb * 2);
+      if (fp8) a.take(&h->sxC, cc);
       if (split) a.take_bytes(&h->XlC, (size_t)cc * h->ldb * 2);
       a.take(&h->cand, (size_t)cc * kMaxCand);
       a.take(&h->cand_cnt, cc);
@@ -533,6 +562,10 @@ cudaError_t prepare_rows(kmgb_handle* h, long long r0, long long r1) {
   const size_t xo = (size_t)r0 * h->ldx, bo = (size_t)r0 * h->ldb * 2;
   cudaError_t r = launch_point_norms(h->X + xo, h->ldx, r1 - r0, h->d, h->qn + r0, h->xn + r0,
                                      h->stream);
+  if (r == cudaSuccess && h->X8)
+    return launch_to_fp8(h->X + xo, h->ldx, r1 - r0, h->d,
+                         static_cast<char*>(h->X8) + (size_t)r0 * h->ld8, h->ld8, h->sx + r0,
+                         h->stream);
   if (r != cudaSuccess || !h->Xb) return r;
   return launch_to_bf16(h->X + xo, h->ldx, r1 - r0, h->d, static_cast<char*>(h->Xb) + bo,
                         h->ldb, h->stream, nullptr,
@@ -667,14 +700,17 @@ int rerank_flagged(kmgb_handle* h, const AssignArgs& a, const float* Xa, const v
   r.max_list = na;
   r.stop = h->stop;
   if (tc) {
-    // BF16 tiers: a second tensor-core pass over the flagged rows records every center whose
+    // tensor tiers: a second tensor-core pass over the flagged rows records every center whose
     // key reaches the point's floor (best - 2E); those few candidates are resolved in FP64.
     // Points with more than kMaxCand candidates take the full rescan below.
-    KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, Xba, Xla, h->ldb,
-                                 h->thr_full, h->XbC, Xla ? h->XlC : nullptr, h->thr_c,
-                                 h->rr_over, h->rr_count + 1, h->stop, s),
+    const bool f8 = a.fp8 != 0;
+    KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, Xba, Xla,
+                                 f8 ? h->ld8 : h->ldb * 2, h->thr_full, h->XbC,
+                                 Xla ? h->XlC : nullptr, h->thr_c, h->rr_over, h->rr_count + 1,
+                                 h->stop, s, f8 ? h->sx : nullptr, f8 ? h->sxC : nullptr),
            KMEANS_ERROR_CLOSEST_CENTERS);
     AssignArgs c2 = a;
+    if (f8) c2.xscale = h->sxC;
     c2.n = h->cand_cap;
     c2.labels = nullptr;
     c2.certify = 0;
@@ -684,9 +720,13 @@ int rerank_flagged(kmgb_handle* h, const AssignArgs& a, const float* Xa, const v
     c2.thr_in = h->thr_c;
     c2.cand = h->cand;
     c2.cand_cnt = h->cand_cnt;
-    KM_TRY(launch_assign_bf16(h->XbC, Xla ? h->XlC : nullptr, h->ldb, h->Cb, h->Cl, h->ldb, c2,
-                              s),
-           KMEANS_ERROR_CLOSEST_CENTERS);
+    if (f8)
+      KM_TRY(launch_assign_bf16(h->XbC, nullptr, h->ld8, h->C8, nullptr, h->ld8, c2, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
+    else
+      KM_TRY(launch_assign_bf16(h->XbC, Xla ? h->XlC : nullptr, h->ldb, h->Cb, h->Cl, h->ldb,
+                                c2, s),
+             KMEANS_ERROR_CLOSEST_CENTERS);
     KM_TRY(launch_resolve_candidates(h->rr_list, h->rr_count, h->cand_cap, h->cand, h->cand_cnt, Xa,
                                      h->ldx, h->Cop, h->ldx, h->cn, h->d, labels, h->rr_over,
                                      h->rr_count + 1, h->stop, s),
@@ -849,6 +889,10 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr, bool assign_on
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
                              h->stop, h->cinit, h->Cl),
          KMEANS_ERROR_RESET);
+  if (h->C8)
+    KM_TRY(launch_centers_fp8(h->Cop, h->ldx, h->k, h->d, h->cmax, h->C8, h->ld8, h->cscale, s,
+                              h->stop),
+           KMEANS_ERROR_RESET);
   KM_TRY(h->pmark(1), KMEANS_ERROR_RESET);
   // closest centers (kmeans.cpp:910-1014)
   AssignArgs a{};
@@ -897,6 +941,16 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr, bool assign_on
                                 h->ldb, h->Cb, h->Cl, h->ldb, ac, s),
              KMEANS_ERROR_CLOSEST_CENTERS);
     }
+  } else if (tc && h->X8) {
+    // FP8 tier: E4M3 rows and centers with their power-of-two scales
+    a.thr_out = h->opt.certify ? h->thr_full : nullptr;
+    a.fp8 = 1;
+    a.xscale = h->sx;
+    a.cscale = h->cscale;
+    Xba = h->X8;
+    Xla = nullptr;
+    KM_TRY(launch_assign_bf16(h->X8, nullptr, h->ld8, h->C8, nullptr, h->ld8, a, s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
   } else if (tc) {
     a.gamma = assign_bf16_gamma(h->d);
     a.thr_out = h->opt.certify ? h->thr_full : nullptr;
@@ -1007,7 +1061,7 @@ int step_stream(kmgb_handle* h, int slot) {
       r.max_list = h->n_act;
       r.stop = h->stop;
       if (tc) {
-        KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, h->Xb, h->Xl, h->ldb,
+        KM_TRY(launch_gather_flagged(h->rr_list, h->rr_count, h->cand_cap, h->Xb, h->Xl, h->ldb * 2,
                                      h->thr_full, h->XbC, h->Xl ? h->XlC : nullptr, h->thr_c,
                                      h->rr_over, h->rr_count + 1, h->stop, s),
                KMEANS_ERROR_CLOSEST_CENTERS);
@@ -1731,7 +1785,7 @@ int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int
   if (!X || !C || !out || n <= 0 || d <= 0 || k <= 0) return KMEANS_ERROR_BUILDDATA;
   kmgb_options o;
   kmgb_default_options(&o);
-  o.assign_tier = split ? KMGB_ASSIGN_BF16X3 : KMGB_ASSIGN_BF16;
+  o.assign_tier = split == 3 ? KMGB_ASSIGN_FP8 : (split ? KMGB_ASSIGN_BF16X3 : KMGB_ASSIGN_BF16);
   o.certify = 0;
   o.max_iters = 1;
   kmgb_handle* h = nullptr;
@@ -1760,13 +1814,23 @@ int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int
     a.certify = 0;
     a.cinit = h->cinit;
     a.dump = dump;
-    if (cudaMemsetAsync(h->cmax, 0, sizeof(float), s) != cudaSuccess ||
-        launch_prep_centers(h->C, h->ldx, k, d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s, nullptr,
-                            h->cinit, h->Cl) != cudaSuccess ||
-        launch_assign_bf16(h->Xb, split == 2 ? nullptr : h->Xl, h->ldb, h->Cb, h->Cl, h->ldb, a,
-                           s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      rc = KMEANS_ERROR_CLOSEST_CENTERS;
+    cudaError_t e = cudaMemsetAsync(h->cmax, 0, sizeof(float), s);
+    if (e == cudaSuccess)
+      e = launch_prep_centers(h->C, h->ldx, k, d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
+                              nullptr, h->cinit, h->Cl);
+    if (e == cudaSuccess && split == 3) {
+      e = launch_centers_fp8(h->Cop, h->ldx, k, d, h->cmax, h->C8, h->ld8, h->cscale, s);
+      a.fp8 = 1;
+      a.xscale = h->sx;
+      a.cscale = h->cscale;
+      if (e == cudaSuccess)
+        e = launch_assign_bf16(h->X8, nullptr, h->ld8, h->C8, nullptr, h->ld8, a, s);
+    } else if (e == cudaSuccess) {
+      e = launch_assign_bf16(h->Xb, split == 2 ? nullptr : h->Xl, h->ldb, h->Cb, h->Cl, h->ldb, a,
+                             s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = KMEANS_ERROR_CLOSEST_CENTERS;
   }
   if (!rc) {
     host.resize((size_t)n * kpad);
@@ -1871,6 +1935,7 @@ kmeansErrorStatus computeKmeansF(const float* data, const int m, const int n, co
   if (const char* tier = std::getenv("KMGB_ASSIGN")) {
     if (std::strcmp(tier, "fp32") == 0) o.assign_tier = KMGB_ASSIGN_FP32;
     else if (std::strcmp(tier, "bf16") == 0 && bf16_tc_supported(n)) o.assign_tier = KMGB_ASSIGN_BF16;
+    else if (std::strcmp(tier, "fp8") == 0 && fp8_tc_supported(n)) o.assign_tier = KMGB_ASSIGN_FP8;
     else if (std::strcmp(tier, "bf16x3") == 0 && bf16_tc_supported(n, 2))
       o.assign_tier = KMGB_ASSIGN_BF16X3;
   }

@@ -54,6 +54,12 @@ struct AssignArgs {
   void* store_out;
   long long store_ld;
   int store_relu;
+  // FP8 tier (fp8 = 1): X and C are E4M3 copies, rows of ld bytes (launch_assign_bf16's ldxb /
+  // ldcb count bytes); key = acc * (xscale[row] * *cscale) + cinit[j]; xscale is indexed like
+  // thr_in in the candidate pass (row0 + row) and like xnorm otherwise (out0 + row)
+  int fp8;
+  const float* xscale;
+  const float* cscale;
   // test hook of the FP32 tier (kmgb_debug_withhold_stage): the producer issues no TMA load for
   // pipeline steps >= test_withhold (0: every step), and every wait gives up after
   // test_wait_cycles SM cycles (0: KMGB_WAIT_CYCLES)
@@ -90,6 +96,8 @@ float assign_bf16_gamma(int d);
 // D up to 512 with one BF16 plane of the points (plain tier, split tier with BF16-valued points,
 // store mode), up to 320 with two (split tier): the unit's points stay in shared memory.
 bool bf16_tc_supported(int d, int planes = 1);
+// The FP8 tier (AssignArgs.fp8 through launch_assign_bf16): D up to 512.
+bool fp8_tc_supported(int d);
 
 // Exact re-rank of flagged points. mode 0 (Lloyd): FP64 arg-min of sum_d (x_d - c_d)^2.
 // mode 1 (expansion, caller norms): FP64 arg-min of nb_j - 2 x.c_j with the given nb.
@@ -122,10 +130,13 @@ cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStrea
 // `over`), then FP64 resolution of their recorded candidates (overflowing points are appended
 // to `over`). With row_map (the router's routed scan), list entries are routed rows whose
 // candidates are stored per routed row and whose FP32 row is X[row_map[entry]].
+// row_bytes: bytes per row of Xb / Xl (a multiple of 16); xs / xsC (nullable): per-row scales
+// of the FP8 tier copied along.
 cudaError_t launch_gather_flagged(const int* list, const int* count, long long cap,
-                                  const void* Xb, const void* Xl, long long ldb, const float* thr,
-                                  void* XbC, void* XlC, float* thrC, int* over, int* over_count,
-                                  const int* stop, cudaStream_t s);
+                                  const void* Xb, const void* Xl, long long row_bytes,
+                                  const float* thr, void* XbC, void* XlC, float* thrC, int* over,
+                                  int* over_count, const int* stop, cudaStream_t s,
+                                  const float* xs = nullptr, float* xsC = nullptr);
 cudaError_t launch_resolve_candidates(const int* list, const int* count, long long max_list,
                                       const int* cand, const int* cand_cnt, const float* X,
                                       long long ldx, const float* C, long long ldc, const float* cn,
@@ -150,6 +161,14 @@ cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, flo
 // Per-point norms, computed once per data set: qn = ||x||^2 (FP64), xn = upper bound ||x||.
 cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,
                                float* xn, cudaStream_t s);
+// FP8 E4M3 copies (the FP8 tier): every row of X scaled by its own power of two sx[row], the
+// centers (from the operand copy) by one power of two *cscale derived from *cmax; rows zero
+// padded to ld8 bytes (a multiple of 16).
+cudaError_t launch_to_fp8(const float* X, long long ldx, long long n, int d, void* X8,
+                          long long ld8, float* sx, cudaStream_t s, const int* stop = nullptr);
+cudaError_t launch_centers_fp8(const float* Cop, long long ldc, int k, int d, const float* cmax,
+                               void* C8, long long ld8, float* cscale, cudaStream_t s,
+                               const int* stop = nullptr);
 // BF16 copy of the data set (zero padded to ldb columns).
 // Xl (nullable) receives the residual plane bf16(x - bf16(x)); inexact (nullable, zeroed by the
 // caller) is set to 1 when some value is not a BF16 number.

@@ -7,6 +7,8 @@
 // rowTransformMinimum skips NaN the same way, RowTransformMinimum.cu:31).
 #include <cuda_bf16.h>
 
+#include <cuda_fp8.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -174,7 +176,83 @@ __global__ void gather_vec_kernel(const double* __restrict__ qs, const float* __
   }
 }
 
+// FP8 E4M3 operands with power-of-two scales: x = s * x8 + error, s = 2^(e - 8) where the scaled
+// quantity (a row's largest |x_i|, or for the centers the largest ||c||) is below 2^e, so every
+// scaled value is below 2^8 = 256 < 448 (the largest E4M3 number: no saturation) and the division
+// by s is exact; the conversion rounds to nearest even, each element within 2^-4 relative of its
+// value when normal and within s 2^-10 when it falls among the subnormals.
+__device__ __forceinline__ float pow2_scale_for(float mx) {
+  if (!(mx > 0.0f) || !(mx < INFINITY)) return 1.0f;
+  int e;
+  frexpf(mx, &e);  // mx = f 2^e, f in [0.5, 1)
+  return ldexpf(1.0f, e - 8);
+}
+
+// One warp per row: the row's scale (sx[row]) and its E4M3 copy, zero padded to ld8 bytes.
+__global__ void to_fp8_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
+                              uint8_t* __restrict__ X8, long long ld8, float* __restrict__ sx,
+                              const int* stop) {
+  if (stopped(stop)) return;
+  const int lane = threadIdx.x & 31;
+  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
+       r += ((long long)gridDim.x * blockDim.x) >> 5) {
+    const float* x = X + (size_t)r * ldx;
+    float mx = 0.0f;
+    for (int t = lane; t < d; t += 32) mx = fmaxf(mx, fabsf(x[t]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    const float sc = pow2_scale_for(mx);
+    const float inv = 1.0f / sc;  // a power of two: exact
+    for (long long t = lane; t < ld8; t += 32)
+      X8[(size_t)r * ld8 + t] =
+          t < d ? (uint8_t)__nv_cvt_float_to_fp8(x[t] * inv, __NV_SATFINITE, __NV_E4M3) : 0;
+    if (lane == 0) sx[r] = sc;
+  }
+}
+
+// The centers' E4M3 copy with one scale for all of them, from the operand copy (unusable centers
+// are zero rows) and the bound of the largest center norm: cscale = 2^(e - 8), cmax < 2^e.
+__global__ void centers_fp8_kernel(const float* __restrict__ Cop, long long ldc, int k, int d,
+                                   const float* __restrict__ cmax, uint8_t* __restrict__ C8,
+                                   long long ld8, float* __restrict__ cscale, const int* stop) {
+  if (stopped(stop)) return;
+  const float sc = pow2_scale_for(*cmax);
+  const float inv = 1.0f / sc;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *cscale = sc;
+  const long long total = (long long)k * ld8;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long c = i / ld8, t = i % ld8;
+    C8[i] = t < d ? (uint8_t)__nv_cvt_float_to_fp8(Cop[(size_t)c * ldc + t] * inv,
+                                                     __NV_SATFINITE, __NV_E4M3)
+                  : 0;
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_to_fp8(const float* X, long long ldx, long long n, int d, void* X8,
+                          long long ld8, float* sx, cudaStream_t s, const int* stop) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
+  if (n <= 0) return cudaSuccess;
+  if (ld8 % 16 || ld8 < d) return cudaErrorInvalidValue;
+  to_fp8_kernel<<<kmgb::num_sms() * 16, 256, 0, s>>>(X, ldx, n, d, static_cast<uint8_t*>(X8), ld8,
+                                                     sx, stop);
+  kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_centers_fp8(const float* Cop, long long ldc, int k, int d, const float* cmax,
+                               void* C8, long long ld8, float* cscale, cudaStream_t s,
+                               const int* stop) {
+  if (k <= 0) return cudaSuccess;
+  if (ld8 % 16 || ld8 < d) return cudaErrorInvalidValue;
+  centers_fp8_kernel<<<kmgb::num_sms() * 4, 256, 0, s>>>(Cop, ldc, k, d, cmax,
+                                                         static_cast<uint8_t*>(C8), ld8, cscale,
+                                                         stop);
+  kmgb::count_launches(1);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop, void* Cb,
                                 long long ldcb, float* cn, float* cmax, cudaStream_t s,

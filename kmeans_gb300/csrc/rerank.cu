@@ -533,7 +533,8 @@ __global__ void gather_flagged_kernel(const int* __restrict__ list, const int* _
                                       const float* __restrict__ thr, uint4* __restrict__ XbC,
                                       uint4* __restrict__ XlC, float* __restrict__ thrC,
                                       int* __restrict__ over, int* __restrict__ over_count,
-                                      const int* stop) {
+                                      const int* stop, const float* __restrict__ xs,
+                                      float* __restrict__ xsC) {
   if (stopped(stop)) return;
   const long long total = *(volatile const int*)count;
   const long long cnt = min(total, cap);
@@ -548,7 +549,10 @@ __global__ void gather_flagged_kernel(const int* __restrict__ list, const int* _
       XbC[slot * row_vec + v] = Xb[pt * row_vec + v];
       if (Xl) XlC[slot * row_vec + v] = Xl[pt * row_vec + v];
     }
-    if (lane == 0) thrC[slot] = thr[pt];
+    if (lane == 0) {
+      thrC[slot] = thr[pt];
+      if (xs) xsC[slot] = xs[pt];
+    }
   }
 }
 
@@ -805,15 +809,16 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
 }  // namespace
 
 cudaError_t launch_gather_flagged(const int* list, const int* count, long long cap,
-                                  const void* Xb, const void* Xl, long long ldb, const float* thr,
-                                  void* XbC, void* XlC, float* thrC, int* over, int* over_count,
-                                  const int* stop, cudaStream_t s) {
+                                  const void* Xb, const void* Xl, long long row_bytes,
+                                  const float* thr, void* XbC, void* XlC, float* thrC, int* over,
+                                  int* over_count, const int* stop, cudaStream_t s,
+                                  const float* xs, float* xsC) {
   if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
-  if ((ldb * 2) % 16) return cudaErrorInvalidValue;
+  if (row_bytes % 16) return cudaErrorInvalidValue;
   gather_flagged_kernel<<<kmgb::num_sms() * 8, 256, 0, s>>>(
       list, count, cap, reinterpret_cast<const uint4*>(Xb), reinterpret_cast<const uint4*>(Xl),
-      ldb * 2 / 16, thr, reinterpret_cast<uint4*>(XbC), reinterpret_cast<uint4*>(XlC), thrC, over,
-      over_count, stop);
+      row_bytes / 16, thr, reinterpret_cast<uint4*>(XbC), reinterpret_cast<uint4*>(XlC), thrC, over,
+      over_count, stop, xs, xsC);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -131,3 +131,81 @@ def test_ballot_peer_groups_equal_match_any():
                 bit = ((l >> b) & 1) if l >= 0 else 1
                 m &= sets[b] if bit else ~sets[b] & 0xFFFFFFFF
             assert m == ballot([x == l for x in labels])
+
+
+# ------------------------------- FP8 E4M3 tier -------------------------------
+U8 = 2.0 ** -4
+
+
+def e4m3(v) -> np.ndarray:
+    """Round-to-nearest-even to E4M3 (3 mantissa bits, smallest normal 2^-6, subnormal spacing
+    2^-9), in FP64; |v| below 448 (the scaling keeps it below 256)."""
+    v = np.asarray(v, np.float64)
+    a = np.abs(v)
+    e = np.floor(np.log2(np.where(a > 0, a, 1.0)))
+    q = 2.0 ** (np.maximum(e, -6.0) - 3.0)
+    return np.sign(v) * np.round(a / q) * q
+
+
+def pow2_scale(mx):
+    """The FP8 tier's power-of-two scale: 2^(e - 8) with mx = f 2^e, f in [0.5, 1) (1 for 0)."""
+    mx = np.asarray(mx, np.float64)
+    _, e = np.frexp(np.where(mx > 0, mx, 1.0))
+    return np.where(mx > 0, np.ldexp(1.0, e - 8), 1.0)
+
+
+def fp8_operands(X, C, cmax=None):
+    """E4M3 copies as the FP8 tier makes them: per-row scales for X, one scale for C (from the
+    bound of the largest center norm)."""
+    X = np.asarray(X, np.float32)
+    C = np.asarray(C, np.float32)
+    sx = pow2_scale(np.abs(X).max(axis=1))
+    cm = np.sqrt((C.astype(np.float64) ** 2).sum(1)).max() if cmax is None else cmax
+    sc = float(pow2_scale(np.float32(cm * 1.0000001)))
+    return e4m3(X / sx[:, None]), sx, e4m3(C / sc), sc
+
+
+def bound_fp8(xn, cm, d, sx, sc):
+    """Restatement of the kernel's bound_fp8 (FP64 here): |key - (x.c - |c|^2/2)|."""
+    u = 2.0 ** -24
+    ax, ac = sx * 2.0 ** -10, sc * 2.0 ** -10
+    xc = xn * cm * 1.01
+    slack = (1 + U8) * np.sqrt(d) * (ax * cm + ac * xn) + d * ax * ac
+    op = (2 * U8 + U8 * U8) * xc + slack
+    gacc = (d // 16 + 2) * 2.0 ** -21
+    cc = 0.5 * cm * cm
+    e = 0.5 * u * cm * cm + op + (gacc + 2.0 ** -18 + u) * (cc + 1.2 * xc + slack) \
+        + (d + 2) * 1.2e-16 * (xn + cm) ** 2
+    return e * 1.02
+
+
+def test_e4m3_rounding_error():
+    rng = np.random.default_rng(7)
+    v = rng.standard_normal(200_000) * 10.0 ** rng.uniform(-4, 2.3, 200_000)
+    v = v[np.abs(v) < 240]
+    r = e4m3(v)
+    normal = np.abs(v) >= 2.0 ** -6
+    assert np.all(np.abs(r - v)[normal] <= U8 * np.abs(v[normal]))
+    assert np.all(np.abs(r - v)[~normal] <= 2.0 ** -10 + 1e-300)
+    # representable values are fixed points, and the grid has 8 steps per binade
+    assert np.array_equal(e4m3(r), r)
+    assert np.array_equal(e4m3(np.array([1.0625, 1.1875, 3.0e-3])), [1.0, 1.25, 2.0 ** -9 * 2])
+
+
+def test_fp8_operand_bound_holds_exactly():
+    """The operand part of bound_fp8 against exact arithmetic, with rows whose components span
+    many magnitudes (subnormal E4M3 values included)."""
+    rng = np.random.default_rng(8)
+    for seed in range(4):
+        X, C = data(seed, n=300, d=128, k=200)
+        X[:50, :64] *= 1e-4  # components deep below the row's largest: subnormals after scaling
+        X8, sx, C8, sc = fp8_operands(X, C)
+        exact = X.astype(np.float64) @ C.astype(np.float64).T
+        approx = (sx[:, None] * X8) @ (sc * C8).T
+        xn = np.sqrt((X.astype(np.float64) ** 2).sum(1))
+        cm = np.sqrt((C.astype(np.float64) ** 2).sum(1)).max()
+        d = X.shape[1]
+        ax, ac = sx * 2.0 ** -10, sc * 2.0 ** -10
+        op = (2 * U8 + U8 * U8) * xn[:, None] * cm + (1 + U8) * np.sqrt(d) * (
+            ax[:, None] * cm + ac * xn[:, None]) + d * ax[:, None] * ac
+        assert np.all(np.abs(approx - exact) <= op)

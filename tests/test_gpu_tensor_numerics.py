@@ -7,7 +7,7 @@ to be at least 4x below that model."""
 import numpy as np
 import pytest
 
-from test_bounds_cpu import bf16, split
+from test_bounds_cpu import bf16, bound_fp8, fp8_operands, split
 
 pytestmark = pytest.mark.gpu
 
@@ -65,3 +65,29 @@ def test_tc_accumulation_error_model(km, torch_cuda, use_split):
         print(f"{name} split={use_split}: max accumulation error {err:.3e} of scale, "
               f"model {model:.3e} (ratio {err / model:.4f})")
         assert err * 4 <= model, (name, err, model)
+
+
+def test_fp8_keys_within_model_and_certificate_bound(km, torch_cuda):
+    """The FP8 tier's raw keys: against the exact sums of the same E4M3 products (accumulation
+    error >= 4x below the model) and against the exact x.c - |c|^2/2 (within the certificate's
+    bound_fp8, which the label certificate relies on)."""
+    f = lambda a: a.astype(np.float64)
+    for name, X, C in cases():
+        d = X.shape[1]
+        keys = km.tc_accumulators(X, C, 3).astype(np.float64)
+        cn = (f(C) ** 2).sum(1).astype(np.float32)
+        start = -0.5 * f(cn)
+        X8, sx, C8, sc = fp8_operands(X, C)
+        prod = (X8 @ C8.T) * (sx[:, None] * sc)
+        mag = (np.abs(X8) @ np.abs(C8).T) * (sx[:, None] * sc)
+        err = np.max(np.abs(keys - (prod + start[None, :])) / (mag + np.abs(start)[None, :]))
+        model = (d // 16 + 2) * 2.0 ** -21
+        print(f"{name} fp8: max accumulation error {err:.3e} of scale, model {model:.3e}")
+        assert err * 4 <= model, (name, err, model)
+        exact = f(X) @ f(C).T - 0.5 * (f(C) ** 2).sum(1)[None, :]
+        xn = np.sqrt((f(X) ** 2).sum(1))
+        cm = np.sqrt((f(C) ** 2).sum(1)).max()
+        eb = bound_fp8(xn[:, None], cm, d, sx[:, None], sc)
+        worst = np.max(np.abs(keys - exact) / eb)
+        print(f"{name} fp8: key error {worst:.3f} of the certificate bound")
+        assert worst <= 1.0
