@@ -777,6 +777,56 @@ def sharded_arm(args, rank: int, world: int, local: int, dist):
         print(json.dumps(line), flush=True)
 
 
+def c3_resident_workload(args, n=200_000_000, d=96, k=4096, iters=10):
+    """The 200M x 96, K=4096 configuration (sigma 1.5, means U[-15,15]^96, 76.8 GB of FP32) with
+    the data set uploaded once and resident in HBM, 10 Lloyd iterations from the same seeded
+    initial centers in the split BF16 tier and in the FP8 E4M3 tier: GPU time per iteration
+    (CUDA events around the iterations, upload excluded), points the certificate left to the exact
+    settlement, and whether both give the same labels and centers (both are the FP64 arg-min)."""
+    import torch
+    import kmeans_gb300 as km
+    from kmeans_gb300.synthetic import sample_init
+    km.build()
+    if args.n != N:
+        n = args.n
+    t0 = time.perf_counter()
+    Xh = np.empty((n, d), np.float32)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(31)
+    means = torch.empty((k, d), device="cuda").uniform_(-15.0, 15.0, generator=g)
+    for r0 in range(0, n, 1 << 22):
+        r1 = min(n, r0 + (1 << 22))
+        lab = torch.randint(0, k, (r1 - r0,), device="cuda", generator=g)
+        Xh[r0:r1] = (means[lab] + 1.5 * torch.randn((r1 - r0, d), device="cuda", generator=g)
+                     ).cpu().numpy()
+    del means
+    torch.cuda.empty_cache()
+    gen_s = time.perf_counter() - t0
+    init = Xh[sample_init(n, k, seed=17)]
+    flop = 2.0 * n * k * d
+    out = {"metric": f"Lloyd iteration, resident N={n}, D={d}, K={k} (s)", "unit": "s",
+           "higher_is_better": False, "data": "synthetic", "generation_s": gen_s,
+           "config": {"workload": f"lloyd_{n}x{d}_K{k}_resident", "n": n, "d": d, "k": k,
+                      "iterations": iters}}
+    res = {}
+    for name, tier in (("bf16x3", km.ASSIGN_BF16X3), ("fp8", km.ASSIGN_FP8)):
+        km.lloyd(Xh[:1 << 20], k, init=init, max_iters=1, assign_tier=tier)  # warm-up
+        t0 = time.perf_counter()
+        r = km.lloyd(Xh, k, init=init, max_iters=iters, assign_tier=tier)
+        wall = time.perf_counter() - t0
+        out[name] = {"call_s": wall, "gpu_s_per_iteration": r.ms_total / 1000.0 / iters,
+                     "assign_pflop_per_iteration": flop / 1e15,
+                     "reranked_share": r.reranked / (n * iters),
+                     "full_rescan_points": r.reranked_fp64, "sse_last": float(r.sse[-1])}
+        res[name] = (r.labels, r.centers)
+        del r
+    out["value"] = out["fp8"]["gpu_s_per_iteration"]
+    out["fp8_vs_bf16x3"] = out["bf16x3"]["gpu_s_per_iteration"] / out["fp8"]["gpu_s_per_iteration"]
+    out["labels_identical"] = bool(np.array_equal(res["fp8"][0], res["bf16x3"][0]))
+    out["centers_identical"] = bool(np.array_equal(res["fp8"][1], res["bf16x3"][1], equal_nan=True))
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -785,7 +835,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--tier", default="bf16x3",
-                    help="assignment tier: bf16x3 (split BF16 tensor cores, default), bf16, fp32")
+                    help="assignment tier: bf16x3 (split BF16 tensor cores, default), bf16, fp8, "
+                         "fp32")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-large-k", action="store_true",
@@ -800,7 +851,7 @@ def main():
     ap.add_argument("--only-init", action="store_true",
                     help="time only the k-means++ initialisation (profiling captures)")
     ap.add_argument("--workload", default="lloyd",
-                    choices=["lloyd", "batched", "large_k", "streamed", "fp64"],
+                    choices=["lloyd", "batched", "large_k", "streamed", "fp64", "c3_resident"],
                     help="batched: the many-problems workload through kmgb_lloyd_batched_f32; "
                          "large_k: 16M x 256, K=65536 split BF16 vs FP32; streamed: 200M x 96, "
                          "K=4096 host data, streamed tiles vs resident (own JSON lines; not the "
@@ -828,6 +879,8 @@ def main():
     if args.workload == "fp64":
         fp64_workload(args)
         return
+    if args.workload == "c3_resident":
+        return c3_resident_workload(args)
 
     import torch
     import kmeans_gb300 as km
@@ -846,7 +899,8 @@ def main():
     km.build()
     lib = km.lib()
     tier = args.tier
-    tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3}[tier]
+    tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3,
+               "fp8": km.ASSIGN_FP8}[tier]
 
     n, K = args.n, args.k
     X, _, _ = mixture_torch(n, D, K, seed=1234, mean_lo=-20.0, mean_hi=20.0, std=(0.3, 3.0))
