@@ -432,7 +432,8 @@ def batched_workload(args):
     gen_s = time.perf_counter() - t0
     rows = sum(len(p[0]) for p in probs)
     flop = sum(2.0 * len(X) * k * X.shape[1] for X, k in probs)
-    tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3}[args.tier]
+    tier_id = {"fp32": km.ASSIGN_FP32, "bf16": km.ASSIGN_BF16, "bf16x3": km.ASSIGN_BF16X3,
+               "auto": km.ASSIGN_AUTO}[args.tier]
     km.lloyd_batched(probs[:64], max_iters=2, assign_tier=tier_id)  # warm-up: module loading
     t0 = time.perf_counter()
     km.lloyd_batched(probs, max_iters=1, assign_tier=tier_id)
@@ -459,12 +460,16 @@ def batched_workload(args):
                        "gflop_per_iteration": flop / 1e9, "iterations": iters,
                        "tier": args.tier, "certified_labels": True},
             "ms_per_iteration": per_iter * 1000.0,
-            "phase_ms_per_iteration": {nm: st.reserved[1 + i] / 1000.0 / iters for i, nm in
-                                       enumerate(["prep", "assign", "rerank", "update"])},
+            "phase_ms_per_iteration": ({nm: st.reserved[1 + i] / 1000.0 / iters for i, nm in
+                                        enumerate(["prep", "assign", "rerank", "update"])}
+                                       if st.reserved[5] == 0 else
+                                       "not recorded: iterations replayed as CUDA graphs"),
             "setup_s": full - st.ms_total / 1000.0,
             "assign_tflops_per_iteration": flop / per_iter / 1e12,
             "setup_and_one_iteration_s": one, "generation_s": gen_s,
             "reranked_points_total": st.reranked, "gpu_launches": launches,
+            "iteration_graph_launches_per_iteration": st.reserved[5] / iters,
+            "groups": st.reserved[6],
             "single_call_loop": {"problems": len(sample), "loop_s": loop, "batched_s": bsample,
                                  "speedup": loop / bsample}}
     print(json.dumps(line), flush=True)

@@ -212,10 +212,12 @@ enum kmgb_assign_tier {
   KMGB_ASSIGN_FP32 = 0,  /* plain FP32 fused kernel (TMA + FFMA) */
   KMGB_ASSIGN_BF16 = 1,  /* tcgen05 BF16 tensor cores, FP32 accumulate in TMEM (D <= 512) */
   KMGB_ASSIGN_BF16X3 = 2, /* tcgen05 split BF16: x.c = xh.ch + xh.cl + xl.ch (D <= 320) */
-  KMGB_ASSIGN_FP8 = 3     /* tcgen05 FP8 E4M3 (kind::f8f6f4), every point row with its own
+  KMGB_ASSIGN_FP8 = 3,    /* tcgen05 FP8 E4M3 (kind::f8f6f4), every point row with its own
                              power-of-two scale, the centers with one; full batches of resident
                              data, D <= 512; labels certified against the E4M3 bound and settled
                              exactly like the BF16 tiers' */
+  KMGB_ASSIGN_AUTO = 4    /* kmgb_lloyd_batched_f32 only: every problem takes the tier that a
+                             measured table (kmeans_gb300/autotune.py) gives its (d, k) bucket */
 };
 
 enum kmgb_empty_policy {
@@ -349,13 +351,16 @@ typedef struct kmgb_problem {
   long long reserved[4];
 } kmgb_problem;
 
-/* opt: max_iters, criterion, empty_policy and certify are used; the tier must be
- * KMGB_ASSIGN_FP32, mini_batch_fraction 1, stream_tile_rows 0, init_algorithm
- * KMGB_INIT_REFERENCE. stats (nullable): iterations = the largest over the problems, reranked =
- * rows settled by the exact re-rank, ms_total = GPU time of the iterations (CUDA events, summed
- * over the groups of one dimension), reserved[0] = wall time of the whole call in microseconds
- * (uploads, initialisation and result copies included), reserved[1..4] = microseconds of center
- * preparation, assignment, re-rank and update summed over the iterations (CUDA events). */
+/* opt: max_iters, criterion, empty_policy, certify and assign_tier (FP32, BF16, BF16X3 or AUTO:
+ * per problem from the tuned table) are used; mini_batch_fraction 1, stream_tile_rows 0,
+ * init_algorithm KMGB_INIT_REFERENCE. Problems of one dimension and tier form a group whose
+ * iteration is captured once as a CUDA graph and replayed (KMGB_GRAPHS=0: kernel by kernel).
+ * stats (nullable): iterations = the largest over the problems, reranked = rows settled by the
+ * exact re-rank, ms_total = GPU time of the iterations (CUDA events, summed over the groups),
+ * reserved[0] = wall time of the whole call in microseconds (uploads, initialisation and result
+ * copies included), reserved[1..4] = microseconds of center preparation, assignment, re-rank and
+ * update summed over the iterations (CUDA events; kernel-by-kernel runs only), reserved[5] =
+ * iteration-graph launches, reserved[6] = groups. */
 KMGB_EXPORT int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const kmgb_options* opt,
                                        kmgb_stats* stats);
 

@@ -43,6 +43,7 @@ ASSIGN_FP32 = 0
 ASSIGN_BF16 = 1
 ASSIGN_BF16X3 = 2
 ASSIGN_FP8 = 3
+ASSIGN_AUTO = 4  # kmgb_lloyd_batched_f32: per problem from the tuned table
 EMPTY_NAN = 0
 EMPTY_KEEP = 1
 INIT_REFERENCE = 0

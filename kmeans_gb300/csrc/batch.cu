@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -29,10 +30,26 @@
 #include "../../include/kmeans_gb300.h"
 #include "common.cuh"
 #include "kernels.h"
+#include "tuned_batched.h"
 
 using namespace kmgb;
 
 namespace {
+
+// The tier of a problem: the caller's, or with KMGB_ASSIGN_AUTO the tuned table's entry for the
+// smallest tuned dimension >= d and the smallest tuned k bound >= k (the last ones beyond).
+int tier_of(const kmgb_options& o, int d, int k) {
+  if (o.assign_tier != KMGB_ASSIGN_AUTO) return o.assign_tier;
+  int di = 0, ki = 0;
+  const int nd = (int)(sizeof(kTunedDims) / sizeof(kTunedDims[0]));
+  const int nk = (int)(sizeof(kTunedKMax) / sizeof(kTunedKMax[0]));
+  while (di + 1 < nd && kTunedDims[di] < d) ++di;
+  while (ki + 1 < nk && kTunedKMax[ki] < k) ++ki;
+  const int t = kTunedTier[di][ki];
+  if (t != KMGB_ASSIGN_FP32 && !bf16_tc_supported(d, t == KMGB_ASSIGN_BF16X3 ? 2 : 1))
+    return KMGB_ASSIGN_FP32;
+  return t;
+}
 
 constexpr int kTileRows = 128;       // assignment tile (rows of one problem)
 constexpr int kSortTile = 2048;      // counting-sort tile (rows of one problem)
@@ -227,7 +244,7 @@ bool upload_host_rows(const kmgb_problem* pr, const std::vector<int>& ids, int d
 // One group: problems `ids` (all of dimension d).
 int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_options& o,
               cudaStream_t s, unsigned long long* reranked, double* loop_ms, double* phase_ms,
-              Fail& f) {
+              Fail& f, long long* graph_launches) {
   const int P = (int)ids.size();
   const long long ldx = rup(d, 4);
   const long long ldb = rup(d, 8);
@@ -485,25 +502,67 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
     pev.push_back(e);
     return !f.set(cudaEventRecord(e, s), EU, "events");
   };
+  // One iteration of the group. Its launches do not depend on the iteration index (every
+  // problem's SSE slot is its own device-side count), so with graphs on it is captured once and
+  // replayed; phase events (marks) are recorded only in kernel-by-kernel runs.
+  auto issue = [&](bool marks) -> bool {
+    auto mk = [&]() { return !marks || mark(); };
+    return mk() && !f.set(cudaMemsetAsync(cmax, 0, sizeof(float), s), EU, "centers") &&
+           !f.set(launch_prep_centers(C, ldx, (int)K, d, Cop, Cb, ldb, cn, cmax, s, nullptr,
+                                      cinit, Cl),
+                  EU, "center preparation") &&
+           !f.set(cudaMemsetAsync(rr_count, 0, sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS,
+                  "re-rank") &&
+           mk() &&
+           !f.set(tc ? launch_assign_bf16(Xb, Xl, ldb, Cb, Cl, ldb, a, s)
+                     : launch_assign_fp32(X, ldx, Cop, ldx, a, s, &g, tiles),
+                  KMEANS_ERROR_CLOSEST_CENTERS, "assignment") &&
+           mk() &&
+           !(o.certify && f.set(launch_rerank_grouped(ra, g, s), KMEANS_ERROR_CLOSEST_CENTERS,
+                                "re-rank")) &&
+           mk() &&
+           !f.set(launch_update_batched(X, ldx, d, qn, labels, C, ldx, o.empty_policy, w, b, s),
+                  EU, "update") &&
+           mk();
+  };
+  cudaGraphExec_t gexec = nullptr;
+  long long g_launches = 0;
+  struct GraphGuard {
+    cudaGraphExec_t* e;
+    ~GraphGuard() {
+      if (*e) cudaGraphExecDestroy(*e);
+    }
+  } graph_guard{&gexec};
+  const char* gv = std::getenv("KMGB_GRAPHS");
+  if (max_iters > 0 && !(gv && std::strcmp(gv, "0") == 0) &&
+      cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    const long long l0 = launch_count();
+    const bool ok = issue(false);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+    g_launches = launch_count() - l0;
+    count_launches(-g_launches);  // recorded into the graph, not launched
+    if (ok && ec == cudaSuccess && graph &&
+        cudaGraphInstantiate(&gexec, graph, 0) == cudaSuccess) {
+      // captured
+    } else {
+      gexec = nullptr;
+      cudaGetLastError();
+      f.code = 0;  // a capture that failed leaves the kernel-by-kernel launches below
+      f.msg.clear();
+    }
+    if (graph) cudaGraphDestroy(graph);
+  } else {
+    cudaGetLastError();
+  }
   for (int it = 0; it < max_iters; ++it) {
-    if (!mark() || f.set(cudaMemsetAsync(cmax, 0, sizeof(float), s), EU, "centers") ||
-        f.set(launch_prep_centers(C, ldx, (int)K, d, Cop, Cb, ldb, cn, cmax, s, nullptr, cinit,
-                                  Cl),
-              EU, "center preparation") ||
-        f.set(cudaMemsetAsync(rr_count, 0, sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS,
-              "re-rank") ||
-        !mark() ||
-        f.set(tc ? launch_assign_bf16(Xb, Xl, ldb, Cb, Cl, ldb, a, s)
-                 : launch_assign_fp32(X, ldx, Cop, ldx, a, s, &g, tiles),
-              KMEANS_ERROR_CLOSEST_CENTERS, "assignment") ||
-        !mark() ||
-        (o.certify && f.set(launch_rerank_grouped(ra, g, s), KMEANS_ERROR_CLOSEST_CENTERS,
-                            "re-rank")) ||
-        !mark() ||
-        f.set(launch_update_batched(X, ldx, d, qn, labels, C, ldx, o.empty_policy, w, b, it, s),
-              EU, "update") ||
-        !mark())
+    if (gexec) {
+      if (f.set(cudaGraphLaunch(gexec, s), EU, "iteration graph")) return f.code;
+      count_launches(g_launches);
+      ++*graph_launches;
+    } else if (!issue(true)) {
       return f.code;
+    }
     if (o.criterion >= 0.0) {  // stop early once every problem's rule has fired
       std::vector<int> done(P);
       if (f.set(cudaMemcpyAsync(done.data(), d_done, sizeof(int) * P, cudaMemcpyDeviceToHost, s),
@@ -594,20 +653,29 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     if (!q.init && q.k > q.n)
       return reject(KMEANS_ERROR_INITIALIZE,
                     "kmgb_lloyd_batched_f32: the reference initialisation needs k <= n");
-    if (o.assign_tier != KMGB_ASSIGN_FP32 &&
+    if (o.assign_tier == KMGB_ASSIGN_FP8)
+      return reject(KMEANS_ERROR_BUILDDATA,
+                    "kmgb_lloyd_batched_f32: the FP8 tier runs single problems only");
+    if (o.assign_tier != KMGB_ASSIGN_FP32 && o.assign_tier != KMGB_ASSIGN_AUTO &&
         !bf16_tc_supported(q.d, o.assign_tier == KMGB_ASSIGN_BF16X3 ? 2 : 1))
       return reject(KMEANS_ERROR_BUILDDATA,
-                    "kmgb_lloyd_batched_f32: the BF16 tensor-core tiers support D <= 256");
+                    "kmgb_lloyd_batched_f32: the BF16 tensor-core tiers support D <= 512 "
+                    "(320 for the split tier)");
   }
   for (int i = 0; i < count; ++i) {
     problems[i].iterations = 0;
     problems[i].status = KMEANS_NONCONVERGENCE;
   }
-  // groups: problems of one dimension, split so that every group fits the index and scan limits
-  std::vector<int> order(count);
-  for (int i = 0; i < count; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int x, int y) { return problems[x].d < problems[y].d; });
+  // groups: problems of one dimension and tier, split so that every group fits the index and
+  // scan limits
+  std::vector<int> order(count), ptier(count);
+  for (int i = 0; i < count; ++i) {
+    order[i] = i;
+    ptier[i] = tier_of(o, problems[i].d, problems[i].k);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return problems[x].d != problems[y].d ? problems[x].d < problems[y].d : ptier[x] < ptier[y];
+  });
   cudaStream_t s = nullptr;
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
     return reject(KMEANS_ERROR_BUILDDATA, "kmgb_lloyd_batched_f32: stream creation failed");
@@ -615,15 +683,18 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
   unsigned long long reranked = 0;
   double loop_ms = 0.0;
   double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
+  long long graph_launches = 0;
   size_t i = 0;
-  const bool tc = o.assign_tier != KMGB_ASSIGN_FP32;
-  const long long row_pad = tc ? 256 : kTileRows, cen_pad = tc ? 256 : 1;
+  long long groups = 0;
   while (i < order.size() && !f.code) {
     const int d = problems[order[i]].d;
+    const int tier = ptier[order[i]];
+    const bool tc = tier != KMGB_ASSIGN_FP32;
+    const long long row_pad = tc ? 256 : kTileRows, cen_pad = tc ? 256 : 1;
     const long long ldx = rup(d, 4);
     std::vector<int> ids;
     long long rows = 0, hist = 0, K = 0;
-    while (i < order.size() && problems[order[i]].d == d) {
+    while (i < order.size() && problems[order[i]].d == d && ptier[order[i]] == tier) {
       const kmgb_problem& q = problems[order[i]];
       const long long r = rup(q.n, row_pad);
       const long long kspan = rup(q.k, cen_pad);
@@ -643,7 +714,10 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
       ++i;
     }
     if (f.code) break;
-    run_group(problems, ids, d, o, s, &reranked, &loop_ms, phase_ms, f);
+    kmgb_options og = o;
+    og.assign_tier = tier;
+    run_group(problems, ids, d, og, s, &reranked, &loop_ms, phase_ms, f, &graph_launches);
+    ++groups;
   }
   cudaStreamSynchronize(s);
   cudaStreamDestroy(s);
@@ -657,6 +731,8 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     stats->ms_total = loop_ms;
     // reserved[1..4]: microseconds of center preparation, assignment, re-rank and update
     for (int ph = 0; ph < 4; ++ph) stats->reserved[1 + ph] = (long long)(phase_ms[ph] * 1000.0);
+    stats->reserved[5] = graph_launches;
+    stats->reserved[6] = groups;
     stats->reserved[0] = (long long)std::chrono::duration<double, std::micro>(
                              std::chrono::steady_clock::now() - t0)
                              .count();

@@ -255,7 +255,7 @@ struct BatchUpdate {
 };
 cudaError_t launch_update_batched(const float* X, long long ldx, int d, const double* qn,
                                   const int* labels, float* C, long long ldc, int empty_policy,
-                                  const UpdateWork& w, const BatchUpdate& b, int iter,
+                                  const UpdateWork& w, const BatchUpdate& b,
                                   cudaStream_t s);
 
 // Mini-batch gather: rows perm[(start + r) mod m] of Xsrc into Xdst (m_mb rows).

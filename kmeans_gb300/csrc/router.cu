@@ -695,7 +695,7 @@ struct Router {
   long long np = 0;
   float *P = nullptr, *Gr = nullptr, *Am = nullptr, *Av = nullptr;
   float *Xs = nullptr, *Hd = nullptr, *Z = nullptr, *dZ = nullptr, *dH = nullptr,
-        *lrows = nullptr;
+        *lrows = nullptr, *gpart = nullptr;
   int* ys = nullptr;
   int* slab = nullptr;
   float *sdist = nullptr, *sxn = nullptr;
@@ -776,6 +776,7 @@ struct Router {
     c.take(&dZ, (size_t)kBatch * G);
     c.take(&dH, (size_t)kBatch * hidden);
     c.take(&lrows, kBatch);
+    c.take(&gpart, mlp_split_scratch(sh));
     c.take(&slab, Sg);
     c.take(&sdist, Sg);
     c.take(&sxn, Sg);
@@ -995,7 +996,8 @@ cudaError_t router_train(Router* r, const RouterIO& io, cudaStream_t s) {
     count_launches(1);
     for (int b0 = 0; b0 + batch <= r->S; b0 += batch) {
       KMGB_CUDA_TRY(mlp_backward(r->sh, r->P, r->Xs + (size_t)b0 * r->d, r->ys + b0, batch, batch,
-                                 r->Hd, r->Z, r->dZ, r->dH, r->Gr, r->lrows, s));
+                                 r->Hd, r->Z, r->dZ, r->dH, r->Gr, r->lrows, s, r->gpart,
+                                 mlp_split_scratch(r->sh)));
       KMGB_CUDA_TRY(mlp_adam(r->P, r->Gr, r->Am, r->Av, r->np, cfg, ++r->adam_t, s));
     }
   }

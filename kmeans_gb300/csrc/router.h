@@ -28,9 +28,12 @@ cudaError_t mlp_forward(const MlpShape& sh, const float* params, const float* Xs
                         float* Hd, float* Z, cudaStream_t s);
 // Forward, softmax cross-entropy against y and backward over `rows` rows; the loss and its
 // gradient are means over batch_norm_rows. grads: the flat gradient vector; loss_rows[rows].
+// part: scratch of mlp_split_scratch(sh) floats for the weight gradients' split over the batch.
 cudaError_t mlp_backward(const MlpShape& sh, const float* params, const float* Xs, const int* y,
                          int rows, int batch_norm_rows, float* Hd, float* Z, float* dZ,
-                         float* dHd, float* grads, float* loss_rows, cudaStream_t s);
+                         float* dHd, float* grads, float* loss_rows, cudaStream_t s, float* part,
+                         long long part_elems);
+long long mlp_split_scratch(const MlpShape& sh);
 // One Adam step (step = 1, 2, ...) over n parameters.
 cudaError_t mlp_adam(float* params, const float* grads, float* m, float* v, long long n,
                      const AdamCfg& c, long long step, cudaStream_t s);

@@ -12,13 +12,15 @@
 //   forward   Hd = relu(Xs W1^T + b1)              sgemm<NT> with bias + ReLU epilogue
 //             Z  = Hd W2^T + b2                      sgemm<NT> with bias epilogue
 //   loss      mean over the batch of logsumexp(Z_i) - Z_i[y_i]; dZ = (softmax(Z) - onehot(y)) / B
-//   backward  dW2 = dZ^T Hd, db2 = colsum(dZ)        sgemm<TN>, colsum
+//   backward  dW2 = dZ^T Hd, db2 = colsum(dZ)        sgemm<TN> (split over the batch into
+//                                                    slices added in order), colsum
 //             dHd = (dZ W2) * [Hd > 0]               sgemm<NN> with mask epilogue
 //             dW1 = dHd^T Xs, db1 = colsum(dHd)      sgemm<TN>, colsum
 //   update    Adam (Kingma & Ba, 2015) with bias correction, over the flat parameter vector
 //             [W1 | b1 | W2 | b2].
 // Inference on all points runs on the tensor cores (the pair kernel of assign_bf16.cu: store mode
 // for the hidden layer, arg-max mode for the group), see router.cu.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <vector>
@@ -48,12 +50,17 @@ sgemm_kernel(int M, int N, int K, const float* __restrict__ A, long long lda,
   const int tid = threadIdx.x;
   const int tx = tid & 15, ty = tid >> 4;
   const long long m0 = (long long)blockIdx.y * T, n0 = (long long)blockIdx.x * T;
+  // split over k (gridDim.z > 1): slice z sums k in [kb, ke) into its own output C + z M ldc
+  const int kc = (int)(((K + GK - 1) / GK + gridDim.z - 1) / gridDim.z) * GK;
+  const int kb = (int)blockIdx.z * kc;
+  const int ke = min(K, kb + kc);
+  C += (size_t)blockIdx.z * (size_t)M * (size_t)ldc;
   float acc[TM][TM];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
     for (int j = 0; j < TM; ++j) acc[i][j] = 0.0f;
-  for (int k0 = 0; k0 < K; k0 += GK) {
+  for (int k0 = kb; k0 < ke; k0 += GK) {
 #pragma unroll
     for (int r = 0; r < PER; ++r) {
       const int e = tid + r * 256;
@@ -68,7 +75,7 @@ sgemm_kernel(int M, int N, int K, const float* __restrict__ A, long long lda,
       const long long gm = m0 + mm;
       const int gk = k0 + kk;
       float v = 0.0f;
-      if (gm < M && gk < K) v = TA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
+      if (gm < M && gk < ke) v = TA ? A[(size_t)gk * lda + gm] : A[(size_t)gm * lda + gk];
       As[kk][mm] = v;
     }
 #pragma unroll
@@ -85,7 +92,7 @@ sgemm_kernel(int M, int N, int K, const float* __restrict__ A, long long lda,
       const long long gn = n0 + nn;
       const int gk = k0 + kk;
       float v = 0.0f;
-      if (gn < N && gk < K) v = TB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
+      if (gn < N && gk < ke) v = TB ? B[(size_t)gn * ldb + gk] : B[(size_t)gk * ldb + gn];
       Bs[kk][nn] = v;
     }
     __syncthreads();
@@ -182,11 +189,37 @@ __global__ void adam_kernel(float* __restrict__ p, const float* __restrict__ g,
   }
 }
 
+// C[i] = part[0][i] + part[1][i] + ... in slice order (deterministic split-k).
+__global__ void sum_slices_kernel(const float* __restrict__ part, int slices, long long count,
+                                  float* __restrict__ C) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (long long)gridDim.x * blockDim.x) {
+    float v = part[i];
+    for (int z = 1; z < slices; ++z) v += part[(size_t)z * count + i];
+    C[i] = v;
+  }
+}
+
+// part (nullable, part_elems floats): scratch for splitting a long k over slices when the output
+// has too few tiles to fill the GPU (the weight gradients: k = the batch); without epilogue only.
 template <bool TA, bool TB, int EPI>
 cudaError_t sgemm(int M, int N, int K, const float* A, long long lda, const float* B,
                   long long ldb, float* C, long long ldc, const float* bias, const float* mask,
-                  long long ldm, cudaStream_t s) {
+                  long long ldm, cudaStream_t s, float* part = nullptr, long long part_elems = 0) {
   if (M <= 0 || N <= 0) return cudaSuccess;
+  const long long tiles64 = ((long long)(M + 63) / 64) * ((N + 63) / 64);
+  if (part && EPI == kEpiNone && ldc == N && tiles64 < num_sms()) {
+    long long z = std::min<long long>(8, std::max<long long>(1, 2LL * num_sms() / tiles64));
+    z = std::min<long long>(z, (K + GK - 1) / GK);
+    if (z > 1 && z * M * N <= part_elems) {
+      dim3 grid((unsigned)((N + 63) / 64), (unsigned)((M + 63) / 64), (unsigned)z);
+      sgemm_kernel<TA, TB, EPI, 4><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, part, N, bias,
+                                                       mask, ldm);
+      sum_slices_kernel<<<num_sms() * 4, 256, 0, s>>>(part, (int)z, (long long)M * N, C);
+      count_launches(2);
+      return cudaGetLastError();
+    }
+  }
   // 128 x 128 tiles when they still give every SM a tile, else 64 x 64
   const long long big = ((long long)(M + 127) / 128) * ((N + 127) / 128);
   if (big >= num_sms()) {
@@ -218,7 +251,8 @@ cudaError_t mlp_forward(const MlpShape& sh, const float* params, const float* Xs
 
 cudaError_t mlp_backward(const MlpShape& sh, const float* params, const float* Xs, const int* y,
                          int rows, int batch_norm_rows, float* Hd, float* Z, float* dZ,
-                         float* dHd, float* grads, float* loss_rows, cudaStream_t s) {
+                         float* dHd, float* grads, float* loss_rows, cudaStream_t s, float* part,
+                         long long part_elems) {
   KMGB_CUDA_TRY(mlp_forward(sh, params, Xs, rows, Hd, Z, s));
   const float* W2 = params + (size_t)sh.hidden * sh.d + sh.hidden;
   float* gW1 = grads;
@@ -232,7 +266,8 @@ cudaError_t mlp_backward(const MlpShape& sh, const float* params, const float* X
   KMGB_CUDA_TRY(cudaGetLastError());
   // dW2[g][h] = sum_b dZ[b][g] Hd[b][h]
   KMGB_CUDA_TRY((sgemm<true, false, kEpiNone>(sh.groups, sh.hidden, rows, dZ, sh.groups, Hd,
-                                               sh.hidden, gW2, sh.hidden, nullptr, nullptr, 0, s)));
+                                               sh.hidden, gW2, sh.hidden, nullptr, nullptr, 0, s,
+                                               part, part_elems)));
   colsum_kernel<<<(sh.groups + 31) / 32, 256, 0, s>>>(dZ, rows, sh.groups, gb2);
   count_launches(1);
   // dHd[b][h] = (sum_g dZ[b][g] W2[g][h]) [Hd[b][h] > 0]
@@ -241,7 +276,7 @@ cudaError_t mlp_backward(const MlpShape& sh, const float* params, const float* X
                                                 s)));
   // dW1[h][j] = sum_b dHd[b][h] Xs[b][j]
   KMGB_CUDA_TRY((sgemm<true, false, kEpiNone>(sh.hidden, sh.d, rows, dHd, sh.hidden, Xs, sh.d, gW1,
-                                               sh.d, nullptr, nullptr, 0, s)));
+                                               sh.d, nullptr, nullptr, 0, s, part, part_elems)));
   colsum_kernel<<<(sh.hidden + 31) / 32, 256, 0, s>>>(dHd, rows, sh.hidden, gb1);
   count_launches(1);
   return cudaGetLastError();
@@ -255,6 +290,10 @@ cudaError_t mlp_adam(float* params, const float* grads, float* m, float* v, long
                                             (float)c1, (float)c2);
   count_launches(1);
   return cudaGetLastError();
+}
+
+long long mlp_split_scratch(const MlpShape& sh) {
+  return 8LL * std::max((long long)sh.groups * sh.hidden, (long long)sh.hidden * sh.d);
 }
 
 long long mlp_param_count(const MlpShape& sh) {
@@ -306,10 +345,12 @@ int kmgb_router_mlp_train(const float* X, int rows, int d, const int* y, int hid
   const long long np = mlp_param_count(sh);
   const int b = batch < rows ? batch : rows;
   DevBufs db;
-  float *dX, *dP, *dG, *dm, *dv, *Hd, *Z, *dZ, *dH, *lr_rows;
+  float *dX, *dP, *dG, *dm, *dv, *Hd, *Z, *dZ, *dH, *lr_rows, *part;
   int* dy;
+  const long long part_elems = mlp_split_scratch(sh);
   cudaError_t e = cudaSuccess;
-  if ((e = db.get(&dX, (size_t)rows * d)) || (e = db.get(&dy, rows)) || (e = db.get(&dP, np)) ||
+  if ((e = db.get(&part, part_elems)) ||
+      (e = db.get(&dX, (size_t)rows * d)) || (e = db.get(&dy, rows)) || (e = db.get(&dP, np)) ||
       (e = db.get(&dG, np)) || (e = db.get(&dm, np)) || (e = db.get(&dv, np)) ||
       (e = db.get(&Hd, (size_t)b * hidden)) || (e = db.get(&Z, (size_t)b * groups)) ||
       (e = db.get(&dZ, (size_t)b * groups)) || (e = db.get(&dH, (size_t)b * hidden)) ||
@@ -330,7 +371,8 @@ int kmgb_router_mlp_train(const float* X, int rows, int d, const int* y, int hid
   long long r0 = 0;
   for (int t = 0; t < todo && e == cudaSuccess; ++t) {
     if (r0 + b > rows) r0 = 0;
-    e = mlp_backward(sh, dP, dX + (size_t)r0 * d, dy + r0, b, b, Hd, Z, dZ, dH, dG, lr_rows, s);
+    e = mlp_backward(sh, dP, dX + (size_t)r0 * d, dy + r0, b, b, Hd, Z, dZ, dH, dG, lr_rows, s,
+                     part, part_elems);
     if (e == cudaSuccess && steps > 0) e = mlp_adam(dP, dG, dm, dv, np, cfg, t + 1, s);
     r0 += b;
   }

@@ -1046,8 +1046,9 @@ __global__ void scatter_batched_kernel(const int* __restrict__ labels, BatchUpda
 // One warp per problem: SSE = sum of its centers' terms; the reference's stop rule per problem
 // (kmeans.cpp:1194-1237). A problem that has stopped keeps its history; its centers are
 // recomputed from unchanged labels, which reproduces them bit for bit.
-__global__ void sse_batched_kernel(const double* __restrict__ sse_k, int groups, BatchUpdate b,
-                                   int iter) {
+// The problem's SSE history slot is its own count of recorded iterations (a stopped problem
+// records nothing more), so every iteration issues the same launch: a CUDA graph replays it.
+__global__ void sse_batched_kernel(const double* __restrict__ sse_k, int groups, BatchUpdate b) {
   const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (wid >= b.P) return;
@@ -1062,7 +1063,8 @@ __global__ void sse_batched_kernel(const double* __restrict__ sse_k, int groups,
     const double rel = fabs(s - b.sse_prev[prob]) / fabs(s);
     b.sse_prev[prob] = s;
     b.rel[prob] = rel;
-    b.sse_hist[(size_t)prob * b.max_iters + iter] = s;
+    const int iter = b.iters[prob];
+    if (iter < b.max_iters) b.sse_hist[(size_t)prob * b.max_iters + iter] = s;
     b.iters[prob] = iter + 1;
     if (!(rel > b.criterion)) b.done[prob] = 1;
   }
@@ -1072,8 +1074,7 @@ __global__ void sse_batched_kernel(const double* __restrict__ sse_k, int groups,
 
 cudaError_t launch_update_batched(const float* X, long long ldx, int d, const double* qn,
                                   const int* labels, float* C, long long ldc, int empty_policy,
-                                  const UpdateWork& w, const BatchUpdate& b, int iter,
-                                  cudaStream_t s) {
+                                  const UpdateWork& w, const BatchUpdate& b, cudaStream_t s) {
   if (b.P <= 0 || b.K <= 0 || b.n_valid <= 0) return cudaSuccess;
   KMGB_CUDA_TRY(cudaMemsetAsync(w.hist, 0, sizeof(int) * b.hist_elems, s));
   hist_batched_kernel<<<(unsigned)b.stiles, 256, 0, s>>>(labels, b, w.hist, w.err);
@@ -1105,8 +1106,7 @@ cudaError_t launch_update_batched(const float* X, long long ldx, int d, const do
       nullptr);
   count_launches(1);
   KMGB_CUDA_TRY(cudaGetLastError());
-  sse_batched_kernel<<<(unsigned)((b.P * 32LL + 255) / 256), 256, 0, s>>>(w.sse_k, groups, b,
-                                                                         iter);
+  sse_batched_kernel<<<(unsigned)((b.P * 32LL + 255) / 256), 256, 0, s>>>(w.sse_k, groups, b);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -111,11 +111,50 @@ def test_rejections(km, torch_cuda):
     X, _, _ = mixture_numpy(500, 8, 4, seed=3)
     with pytest.raises(km.KmeansError):
         km.lloyd_batched([(X, 501)])  # reference init needs k <= n
-    Xw, _, _ = mixture_numpy(300, 300, 4, seed=4)
-    with pytest.raises(km.KmeansError):  # the tensor-core tiers cover D <= 256
+    Xw, _, _ = mixture_numpy(300, 330, 4, seed=4)
+    with pytest.raises(km.KmeansError):  # the split tier keeps two planes up to D = 320
         km.lloyd_batched([(Xw, 4)], assign_tier=km.ASSIGN_BF16X3)
+    Xw, _, _ = mixture_numpy(300, 600, 4, seed=4)
+    with pytest.raises(km.KmeansError):  # the plain BF16 tier one plane up to D = 512
+        km.lloyd_batched([(Xw, 4)], assign_tier=km.ASSIGN_BF16)
+    with pytest.raises(km.KmeansError):  # the FP8 tier runs single problems
+        km.lloyd_batched([(X, 4)], assign_tier=km.ASSIGN_FP8)
     arr = (km.kmgb_problem * 1)()
     arr[0].X, arr[0].n, arr[0].d, arr[0].k = X.ctypes.data, 500, 8, 4
     for kw in ({"mini_batch_fraction": 0.5}, {"init_algorithm": km.INIT_KMEANSPP}):
         opt = km.default_options(**kw)
         assert km.lib().kmgb_lloyd_batched_f32(arr, 1, km.C.byref(opt), None) == 1
+
+
+def test_auto_tier_and_graph_replay_equal_oracle(km, orc, torch_cuda):
+    """KMGB_ASSIGN_AUTO (each problem's tier from the tuned table, problems of one dimension and
+    tier grouped) and the per-iteration CUDA graph give every problem the oracle's result; the
+    graph path equals the kernel-by-kernel path."""
+    import os
+    rng = np.random.default_rng(71)
+    probs = []
+    for i in range(24):
+        d = int(rng.choice([16, 32, 64, 128]))
+        k = int(rng.choice([5, 20, 60, 150, 300]))
+        n = int(max(k, rng.integers(300, 6000)))
+        X, _, _ = mixture_numpy(n, d, k, seed=500 + i)
+        probs.append((X, k, X[sample_init(n, k, seed=600 + i)].copy()))
+    res, st = km.lloyd_batched(probs, max_iters=4, assign_tier=km.ASSIGN_AUTO)
+    assert st.reserved[5] > 0 and st.reserved[6] >= 4  # graph launches, groups
+    for (X, k, init), r in zip(probs, res):
+        stt, c, lab, sse, it = orc.lloyd(X, init, 4)
+        assert np.array_equal(r.labels, lab) and np.array_equal(r.centers, c, equal_nan=True)
+        np.testing.assert_allclose(r.sse, sse, rtol=1e-10)
+    old = os.environ.get("KMGB_GRAPHS")
+    os.environ["KMGB_GRAPHS"] = "0"
+    try:
+        res2, st2 = km.lloyd_batched(probs, max_iters=4, assign_tier=km.ASSIGN_AUTO)
+    finally:
+        if old is None:
+            os.environ.pop("KMGB_GRAPHS")
+        else:
+            os.environ["KMGB_GRAPHS"] = old
+    assert st2.reserved[5] == 0
+    for a, b in zip(res, res2):
+        assert np.array_equal(a.labels, b.labels)
+        assert np.array_equal(a.centers, b.centers, equal_nan=True)
