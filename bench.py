@@ -1047,6 +1047,9 @@ def main():
                 "phase_ms_per_iter": {n: p / max(piters, 1) for n, p in
                                       zip(["prep", "assign", "rerank", "update"], phase)},
                 "reranked_points_total": st.reranked, "reranked_fp64_total": st.reranked_fp64,
+                "label_audit": {"rows": int(st.reserved[6]), "violations": int(st.reserved[7]),
+                                "what": "rows sampled every iteration (timed ones included) and "
+                                        "checked against the FP64 arg-min over all centers"},
                 "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
                 "init_kmeanspp": init_pp,
                 "accuracy": checks["accuracy"] if checks else None,

@@ -216,8 +216,9 @@ enum kmgb_assign_tier {
                              power-of-two scale, the centers with one; full batches of resident
                              data, D <= 512; labels certified against the E4M3 bound and settled
                              exactly like the BF16 tiers' */
-  KMGB_ASSIGN_AUTO = 4    /* kmgb_lloyd_batched_f32 only: every problem takes the tier that a
-                             measured table (kmeans_gb300/autotune.py) gives its (d, k) bucket */
+  KMGB_ASSIGN_AUTO = 4    /* kmgb_lloyd_batched_f32 only: every dimension's problems take the
+                             tier (FP32 or BF16X3) with the smaller time predicted from a measured
+                             cost table (kmeans_gb300/autotune.py) by (d, k) bucket and rows */
 };
 
 enum kmgb_empty_policy {
@@ -269,7 +270,13 @@ typedef struct kmgb_stats {
   long long reserved[8];           /* with the router: [0] points routed to a group scan, [1]
                                       of those certified, [2] points that took the full scan,
                                       [3] trainings, [4] training wall time (us), [5] routed
-                                      points whose in-group margin took the candidate pass */
+                                      points whose in-group margin took the candidate pass;
+                                      certified resident runs: [6] rows audited, [7] audit
+                                      violations -- every iteration a sample of rows (64 by
+                                      default, KMGB_AUDIT_ROWS, fewer when k x d is large) is
+                                      checked against the FP64 arg-min over all centers, so a
+                                      failure of a rounding model behind the certificate shows
+                                      as a violation count instead of a silently wrong label */
 } kmgb_stats;
 
 /* The learned router's record (kmgb_get_router_stats); counters sum over the iterations run. */
@@ -352,7 +359,7 @@ typedef struct kmgb_problem {
 } kmgb_problem;
 
 /* opt: max_iters, criterion, empty_policy, certify and assign_tier (FP32, BF16, BF16X3 or AUTO:
- * per problem from the tuned table) are used; mini_batch_fraction 1, stream_tile_rows 0,
+ * per dimension from the tuned cost table) are used; mini_batch_fraction 1, stream_tile_rows 0,
  * init_algorithm KMGB_INIT_REFERENCE. Problems of one dimension and tier form a group whose
  * iteration is captured once as a CUDA graph and replayed (KMGB_GRAPHS=0: kernel by kernel).
  * stats (nullable): iterations = the largest over the problems, reranked = rows settled by the
@@ -453,6 +460,13 @@ KMGB_EXPORT void kmgb_debug_fail_nth(int kind, long long nth);
 KMGB_EXPORT void kmgb_debug_withhold_stage(long long stage, unsigned long long wait_cycles);
 /* Bytes of the current device's library pool handed out and not yet given back (-1 on error). */
 KMGB_EXPORT long long kmgb_debug_pool_used_bytes(void);
+/* Test hook: one audit of `rows` (1..256) sampled rows of device data X (n x d, row stride ldx
+ * floats) against the FP64 arg-min over the device centers C (k x d, row stride ldc): a label is
+ * a violation when its FP64 distance exceeds the smallest one. out[0] = rows audited, out[1] =
+ * violations, out[2] = 1 + the last violating row (0: none). 0 on success. */
+KMGB_EXPORT int kmgb_debug_audit(const float* X, long long n, int d, long long ldx, const float* C,
+                                 int k, long long ldc, const int* labels, int rows,
+                                 unsigned long long* out);
 
 /* Last error message of the calling thread (empty string if none). */
 KMGB_EXPORT const char* kmgb_last_error(void);

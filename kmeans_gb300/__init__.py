@@ -43,7 +43,7 @@ ASSIGN_FP32 = 0
 ASSIGN_BF16 = 1
 ASSIGN_BF16X3 = 2
 ASSIGN_FP8 = 3
-ASSIGN_AUTO = 4  # kmgb_lloyd_batched_f32: per problem from the tuned table
+ASSIGN_AUTO = 4  # kmgb_lloyd_batched_f32: per dimension from the tuned cost table
 EMPTY_NAN = 0
 EMPTY_KEEP = 1
 INIT_REFERENCE = 0
@@ -187,6 +187,7 @@ def lib():
             "kmgb_debug_fail_nth": (None, [i32, i64]),
             "kmgb_debug_withhold_stage": (None, [i64, C.c_ulonglong]),
             "kmgb_debug_pool_used_bytes": (i64, []),
+            "kmgb_debug_audit": (i32, [P, i64, i32, i64, P, i32, i64, P, i32, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -238,6 +239,20 @@ def router_mlp_train(X: np.ndarray, y: np.ndarray, params: np.ndarray, hidden: i
     if rc:
         raise KmeansError(rc, last_error())
     return loss.value, grads
+
+
+def debug_audit(X, C, labels, rows: int = 64):
+    """Test hook: one audit of `rows` sampled rows (device tensors X n x d, C k x d float32,
+    labels int32) against the FP64 arg-min. Returns (rows audited, violations, 1 + the last
+    violating row or 0)."""
+    n, d = X.shape
+    k = C.shape[0]
+    out = np.zeros(3, dtype=np.uint64)
+    rc = lib().kmgb_debug_audit(X.data_ptr(), n, d, X.stride(0), C.data_ptr(), k, C.stride(0),
+                                labels.data_ptr(), rows, _ptr(out))
+    if rc:
+        raise KmeansError(rc, last_error())
+    return int(out[0]), int(out[1]), int(out[2])
 
 
 def debug_pool_used_bytes() -> int:
@@ -437,6 +452,8 @@ class LloydResult:
     reranked_fp64: int
     empty_clusters: int
     ms_total: float
+    audited: int = 0           # rows checked against the FP64 arg-min (sampled per iteration)
+    audit_violations: int = 0  # of those, labels farther than the nearest center
 
 
 def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
@@ -469,7 +486,8 @@ def lloyd(X, k: int, init=None, max_iters: int = 20, criterion: float = -1.0,
     if rc not in (KMEANS_SUCCESS, KMEANS_NONCONVERGENCE):
         raise KmeansError(rc, last_error())
     return LloydResult(rc, cen, lab, sse[:st.iterations], st.iterations, st.reranked,
-                       st.reranked_fp64, st.empty_clusters, st.ms_total)
+                       st.reranked_fp64, st.empty_clusters, st.ms_total, int(st.reserved[6]),
+                       int(st.reserved[7]))
 
 
 def lloyd_batched(problems, max_iters: int = 20, criterion: float = -1.0,

@@ -8,9 +8,14 @@ center count (padding waste against tensor throughput). For every (d, k) bucket 
 builds a batch of synthetic problems of that shape (k centers, n = max(256, 2 k^2) rows as in the
 many-problems configuration, K_i = sqrt(N_i / 2)), runs a few Lloyd iterations with each family
 on the GPU (one untimed call first), takes the GPU time per iteration from the call's CUDA events
-and writes the faster family into the table that KMGB_ASSIGN_AUTO reads.
+and writes both families' cost per row and iteration into the table that KMGB_ASSIGN_AUTO reads:
+the library predicts each dimension's cost under each family from its problems' rows and buckets
+and runs the whole dimension with the cheaper one (one group per dimension: splitting a dimension
+between the families costs a second group's set-up and saved nothing measurable on the
+10,000-problem workload).
 
-    python -m kmeans_gb300.autotune [--out PATH] [--iters 5]
+    python -m kmeans_gb300.autotune [--out PATH] [--iters 5] [--json PATH]
+    python -m kmeans_gb300.autotune --from-json PATH [--out PATH]   (header from saved timings)
 
 then rebuild the library. The committed table was produced by this script on a GB300.
 """
@@ -57,42 +62,55 @@ def tune(out: str = DEFAULT_OUT, iters: int = 5):
     import torch
     import kmeans_gb300 as km
     km.build()
-    table, record = [], {}
+    record = {"gpu": torch.cuda.get_device_name(0), "iters": iters,
+              "date": datetime.datetime.now(datetime.timezone.utc).strftime("%Y-%m-%d"),
+              "buckets": {}}
     for d in DIMS:
-        row = []
         for k in KMAX:
             probs = bucket_problems(d, k)
             t32 = time_family(km, probs, km.ASSIGN_FP32, iters)
             t16 = time_family(km, probs, km.ASSIGN_BF16X3, iters)
-            tier = km.ASSIGN_FP32 if t32 <= t16 else km.ASSIGN_BF16X3
-            row.append(tier)
-            record[f"d{d}_k{k}"] = {"problems": len(probs), "rows_each": int(probs[0][0].shape[0]),
-                                   "fp32_ms_per_iter": t32, "bf16x3_ms_per_iter": t16,
-                                   "chosen": "fp32" if tier == km.ASSIGN_FP32 else "bf16x3"}
+            record["buckets"][f"d{d}_k{k}"] = {
+                "problems": len(probs), "rows_each": int(probs[0][0].shape[0]),
+                "fp32_ms_per_iter": t32, "bf16x3_ms_per_iter": t16}
             print(f"d={d:4d} k<={k:4d}: fp32 {t32:8.3f} ms, split bf16 {t16:8.3f} ms per "
-                  f"iteration -> {record[f'd{d}_k{k}']['chosen']}", flush=True)
+                  f"iteration", flush=True)
             del probs
             torch.cuda.empty_cache()
-        table.append(row)
-    gpu = torch.cuda.get_device_name(0)
-    when = datetime.datetime.now(datetime.timezone.utc).strftime("%Y-%m-%d")
-    lines = ["// Tier of a batched problem by its (d, k) bucket, for kmgb_lloyd_batched_f32 with",
-             f"// KMGB_ASSIGN_AUTO. Written by kmeans_gb300/autotune.py on {gpu}, {when}: per bucket",
-             f"// the faster of the two grouped families over {iters} Lloyd iterations of synthetic",
-             "// problems with k centers and max(256, 2 k^2) rows (ms per iteration, FP32 / split BF16):"]
-    for key, v in record.items():
+    write_header(record, out)
+    return record
+
+
+def write_header(record: dict, out: str = DEFAULT_OUT):
+    """tuned_batched.h from a record of bucket timings (as tune() returns it)."""
+    b = record["buckets"]
+
+    def ns_per_row(key, fam):
+        v = b[key]
+        return v[f"{fam}_ms_per_iter"] * 1e6 / (v["problems"] * v["rows_each"])
+
+    lines = ["// Cost of a batched problem's row per Lloyd iteration (ns) by (d, k) bucket and assignment",
+             "// family, for kmgb_lloyd_batched_f32 with KMGB_ASSIGN_AUTO. Written by",
+             f"// kmeans_gb300/autotune.py on {record['gpu']}, {record['date']}: per bucket the GPU time of",
+             f"// {record['iters']} Lloyd iterations of synthetic problems with k centers and max(256, 2 k^2)",
+             "// rows (ms per iteration, FP32 / split BF16, problems x rows):"]
+    for key, v in b.items():
         lines.append(f"//   {key:10s} {v['fp32_ms_per_iter']:9.3f} / {v['bf16x3_ms_per_iter']:9.3f}"
-                     f"  -> {v['chosen']}")
+                     f"   {v['problems']} x {v['rows_each']}")
     lines += ["#pragma once", "", "namespace kmgb {",
               f"constexpr int kTunedDims[] = {{{', '.join(map(str, DIMS))}}};",
               f"constexpr int kTunedKMax[] = {{{', '.join(map(str, KMAX))}}};",
-              "// KMGB_ASSIGN_FP32 = 0, KMGB_ASSIGN_BF16X3 = 2",
-              f"constexpr int kTunedTier[{len(DIMS)}][{len(KMAX)}] = {{"]
-    lines += ["    {" + ", ".join(map(str, r)) + "}," for r in table]
+              "// [family: 0 FP32, 1 split BF16][dimension bucket][center bucket]",
+              f"constexpr float kTunedNsPerRow[2][{len(DIMS)}][{len(KMAX)}] = {{"]
+    for fam in ("fp32", "bf16x3"):
+        lines.append("    {")
+        for d in DIMS:
+            vals = ", ".join(f"{ns_per_row(f'd{d}_k{k}', fam):.5g}f" for k in KMAX)
+            lines.append(f"        {{{vals}}},")
+        lines.append("    },")
     lines += ["};", "}  // namespace kmgb", ""]
     with open(out, "w") as fh:
         fh.write("\n".join(lines))
-    return record
 
 
 if __name__ == "__main__":
@@ -100,8 +118,14 @@ if __name__ == "__main__":
     ap.add_argument("--out", default=DEFAULT_OUT)
     ap.add_argument("--iters", type=int, default=5)
     ap.add_argument("--json", default=None, help="also write the measurements as JSON")
+    ap.add_argument("--from-json", default=None,
+                    help="write the header from measurements saved with --json (no GPU)")
     a = ap.parse_args()
-    rec = tune(a.out, a.iters)
-    if a.json:
-        with open(a.json, "w") as fh:
-            json.dump(rec, fh, indent=1)
+    if a.from_json:
+        with open(a.from_json) as fh:
+            write_header(json.load(fh), a.out)
+    else:
+        rec = tune(a.out, a.iters)
+        if a.json:
+            with open(a.json, "w") as fh:
+                json.dump(rec, fh, indent=1)

@@ -266,7 +266,10 @@ struct MergeSlot {
   int bblk[EPQ - 1][4][32], ncand[EPQ - 1][4][32];
 };
 
-template <int EPQ>
+// EPQ: epilogue warps per lane quadrant; F8: the FP8 tier's instantiation (mode 4 only). One CTA
+// per SM: each SM sub-partition's 16K registers hold ceil(warps / 4) warps, so a thread may use
+// 168 registers with EPQ 2 (10 warps) and 96 with EPQ 4 (18 warps).
+template <int EPQ, bool F8>
 __global__ void __launch_bounds__(threads_for(EPQ), 1)
 assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmXl,
                    const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmCl,
@@ -292,7 +295,12 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   }
   const bool stop_now = stopped(p.stop);  // uniform: every CTA of the grid sees the same flag
   if (stop_now) return;
-  const int bk = mode == 4 ? BK8 : BK;  // elements per k-block (128 bytes per row either way)
+  // The two-plane variant (EPQ 2) runs the split modes 2 and 3 only; the plain BF16 tier, the FP8
+  // tier and the store mode run with EPQ 4, so their code is compiled out of the split variant
+  // (it kept the split epilogue from spilling).
+  constexpr bool kOnePlane = EPQ > 2;
+  constexpr bool fp8 = F8;
+  const int bk = fp8 ? BK8 : BK;  // elements per k-block (128 bytes per row either way)
   const int nkb = (p.d + bk - 1) / bk;
   const int nchunks = (p.k + BN - 1) / BN;
   const long long pair = blockIdx.x >> 1, npairs = gridDim.x >> 1;
@@ -305,7 +313,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const long long n_units = (n_rows + UNIT - 1) / UNIT;
   const bool cand_mode = p.thr_in != nullptr;
   const bool grouped = p.u_prob != nullptr;
-  const bool store_mode = p.store_out != nullptr;
+  const bool store_mode = kOnePlane && p.store_out != nullptr;
   // A unit's chunks: how many, the first center, the rows that exist, and a rotation -- each pair
   // visits the chunks in its own rotated order so that at any moment the pairs stream different
   // chunks of C from L2. Every role of both CTAs derives the same sequence (false: skipped unit).
@@ -471,9 +479,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               const uint32_t acc = (kb | k16) ? 1u : 0u;  // the chunk's first product starts at 0
               const uint64_t ahi = sdesc_sw128(xhi + k16 * 32);
               const uint64_t bhi = sdesc_sw128(chi + k16 * 32);
-              if (mode == 1) {
+              if (kOnePlane && !F8 && mode == 1) {
                 umma_pair(dcol, ahi, bhi, acc);
-              } else if (mode == 4) {
+              } else if (fp8) {
                 umma_pair8(dcol, ahi, bhi, acc);
               } else {
                 // x_hi.c_hi, x_hi.c_lo (x_hi read once into the A collector), then x_lo.c_hi
@@ -525,9 +533,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       const float xn_pt = (p.certify && !cand_mode && h == 0 && prow < n_rows)
                               ? __ldg(p.xnorm + p.out0 + prow) : 0.0f;
       // FP8 tier: the row's scale and the accumulator multiplier sx * sc (a power of two)
-      const float sx_pt = (mode == 4 && prow < n_rows)
+      const float sx_pt = (fp8 && prow < n_rows)
                               ? __ldg(p.xscale + (cand_mode ? p.row0 : p.out0) + prow) : 0.0f;
-      const float sc_all = mode == 4 ? __ldg(p.cscale) : 0.0f;
+      const float sc_all = fp8 ? __ldg(p.cscale) : 0.0f;
       const float mrow = sx_pt * sc_all;
       for (int c = 0; c < ui.nch; ++c, ++g) {
         const int b = (int)(g & 1);
@@ -556,7 +564,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           // padding and unusable centers carry a huge negative start value
           {
             const float4* hs = reinterpret_cast<const float4*>(p.cinit + (size_t)col0 + cb * 32);
-            if (mode == 4) {
+            if (fp8) {
 #pragma unroll
               for (int j4 = 0; j4 < 8; ++j4) {
                 const float4 hv = __ldg(hs + j4);
@@ -699,7 +707,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             (bblk < 0 || none) ? ui.cbase : bblk * 32 + (int)(__float_as_uint(b1) & 0x1Fu);
         p.labels[pt] = label;
         if (p.certify) {
-          const float eb = (mode == 4 ? bound_fp8(xn_pt, cm, p.d, sx_pt, sc_all)
+          const float eb = (fp8 ? bound_fp8(xn_pt, cm, p.d, sx_pt, sc_all)
                                       : bound_acc(xn_pt, cm, p.d, mode)) +
                            1.02f * p.pert * (xn_pt * cm * 1.01f + 0.5f * cm * cm);
           if (none || !(b1 - b2 > 2.0f * eb)) {
@@ -732,10 +740,10 @@ struct VariantInfo {
   size_t smem_budget = 0;  // 1 KB aligned
   size_t static_bytes = 0;
 };
-VariantInfo g_variant[5];
+VariantInfo g_variant[5];  // [0] FP8, [2] split BF16, [4] plain BF16
 int g_num_sms = 0;
 
-template <int EPQ>
+template <int EPQ, bool F8>
 cudaError_t prepare_variant(VariantInfo& vi) {
   if (vi.ready) return cudaSuccess;
   int dev = 0, optin = 0;
@@ -743,12 +751,12 @@ cudaError_t prepare_variant(VariantInfo& vi) {
   KMGB_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
   KMGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   cudaFuncAttributes fa;
-  KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel<EPQ>));
+  KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel<EPQ, F8>));
   // the dynamic area starts on the next 1 KB boundary after the static variables
   vi.static_bytes = (fa.sharedSizeBytes + 1023) / 1024 * 1024;
   size_t budget = (size_t)optin > vi.static_bytes ? (size_t)optin - vi.static_bytes : 0;
   if (budget > SMEM_CAP) budget = SMEM_CAP;
-  KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel<EPQ>,
+  KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel<EPQ, F8>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
   vi.smem_budget = budget;
   cudaLaunchConfig_t qc = {};
@@ -762,7 +770,7 @@ cudaError_t prepare_variant(VariantInfo& vi) {
   qa[0].val.clusterDim.z = 1;
   qc.attrs = qa;
   qc.numAttrs = 1;
-  KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&vi.max_pairs, assign_bf16_kernel<EPQ>, &qc));
+  KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&vi.max_pairs, assign_bf16_kernel<EPQ, F8>, &qc));
   if (vi.max_pairs <= 0) return cudaErrorInvalidConfiguration;
   vi.ready = true;
   return cudaSuccess;
@@ -805,8 +813,8 @@ static cudaError_t launch_assign_fp8(const void* X8, long long ld8x, const void*
       (reinterpret_cast<uintptr_t>(X8) & 15) || (reinterpret_cast<uintptr_t>(C8) & 15) ||
       a.store_out || a.u_prob)
     return cudaErrorInvalidValue;
-  VariantInfo& vi = g_variant[4];
-  KMGB_CUDA_TRY(prepare_variant<4>(vi));
+  VariantInfo& vi = g_variant[0];
+  KMGB_CUDA_TRY((prepare_variant<4, true>(vi)));
   const size_t xbytes = (size_t)((a.d + BK8 - 1) / BK8) * XKB_BYTES;
   const size_t stage_bytes = CKB_BYTES;
   const size_t lim = vi.smem_budget;
@@ -835,7 +843,7 @@ static cudaError_t launch_assign_fp8(const void* X8, long long ld8x, const void*
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4>, tmX, tmX, tmC, tmC, a, stages,
+  KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, true>, tmX, tmX, tmC, tmC, a, stages,
                                    xbufs, 4));
   count_launches(1);
   return cudaSuccess;
@@ -857,8 +865,8 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
     return cudaErrorInvalidValue;
   const int epq = epq_for(mode > 1 ? 2 : 1);
   VariantInfo& vi = g_variant[epq];
-  if (epq == 2) KMGB_CUDA_TRY(prepare_variant<2>(vi));
-  else KMGB_CUDA_TRY(prepare_variant<4>(vi));
+  if (epq == 2) KMGB_CUDA_TRY((prepare_variant<2, false>(vi)));
+  else KMGB_CUDA_TRY((prepare_variant<4, false>(vi)));
   const size_t xbytes = xbuf_bytes_for(a.d, mode == 2 ? 2 : 1);
   const size_t stage_bytes = (size_t)(mode > 1 ? 2 : 1) * CKB_BYTES;
   const size_t lim = vi.smem_budget;
@@ -898,10 +906,10 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   cfg.attrs = at;
   cfg.numAttrs = 1;
   if (epq == 2)
-    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2>, tmX, tmXl, tmC, tmCl, a, stages,
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2, false>, tmX, tmXl, tmC, tmCl, a, stages,
                                      xbufs, mode));
   else
-    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4>, tmX, tmXl, tmC, tmCl, a, stages,
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, false>, tmX, tmXl, tmC, tmCl, a, stages,
                                      xbufs, mode));
   count_launches(1);
   return cudaSuccess;

@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -36,18 +37,35 @@ using namespace kmgb;
 
 namespace {
 
-// The tier of a problem: the caller's, or with KMGB_ASSIGN_AUTO the tuned table's entry for the
-// smallest tuned dimension >= d and the smallest tuned k bound >= k (the last ones beyond).
-int tier_of(const kmgb_options& o, int d, int k) {
-  if (o.assign_tier != KMGB_ASSIGN_AUTO) return o.assign_tier;
+// Predicted GPU time per Lloyd iteration of a problem's rows with one assignment family (0 FP32,
+// 1 split BF16): rows x the tuned cost per row of the smallest tuned dimension >= d and the
+// smallest tuned k bound >= k (the last ones beyond).
+double tuned_cost(int family, int d, int k, long long n) {
   int di = 0, ki = 0;
   const int nd = (int)(sizeof(kTunedDims) / sizeof(kTunedDims[0]));
   const int nk = (int)(sizeof(kTunedKMax) / sizeof(kTunedKMax[0]));
   while (di + 1 < nd && kTunedDims[di] < d) ++di;
   while (ki + 1 < nk && kTunedKMax[ki] < k) ++ki;
-  const int t = kTunedTier[di][ki];
-  if (t != KMGB_ASSIGN_FP32 && !bf16_tc_supported(d, t == KMGB_ASSIGN_BF16X3 ? 2 : 1))
-    return KMGB_ASSIGN_FP32;
+  return (double)n * kTunedNsPerRow[family][di][ki];
+}
+
+// Tier of every problem: the caller's, or with KMGB_ASSIGN_AUTO one tier per dimension -- the
+// family with the smaller predicted time summed over the dimension's problems (the split tier
+// only where the tensor-core kernel supports the dimension).
+std::vector<int> tiers_of(const kmgb_options& o, const kmgb_problem* problems, int count) {
+  std::vector<int> t(count, o.assign_tier);
+  if (o.assign_tier != KMGB_ASSIGN_AUTO) return t;
+  std::map<int, std::pair<double, double>> cost;  // dimension -> (FP32, split BF16)
+  for (int i = 0; i < count; ++i) {
+    auto& c = cost[problems[i].d];
+    c.first += tuned_cost(0, problems[i].d, problems[i].k, problems[i].n);
+    c.second += tuned_cost(1, problems[i].d, problems[i].k, problems[i].n);
+  }
+  for (int i = 0; i < count; ++i) {
+    const auto& c = cost[problems[i].d];
+    t[i] = bf16_tc_supported(problems[i].d, 2) && c.second < c.first ? KMGB_ASSIGN_BF16X3
+                                                                       : KMGB_ASSIGN_FP32;
+  }
   return t;
 }
 
@@ -668,11 +686,8 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
   }
   // groups: problems of one dimension and tier, split so that every group fits the index and
   // scan limits
-  std::vector<int> order(count), ptier(count);
-  for (int i = 0; i < count; ++i) {
-    order[i] = i;
-    ptier[i] = tier_of(o, problems[i].d, problems[i].k);
-  }
+  std::vector<int> order(count), ptier = tiers_of(o, problems, count);
+  for (int i = 0; i < count; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
     return problems[x].d != problems[y].d ? problems[x].d < problems[y].d : ptier[x] < ptier[y];
   });

@@ -210,6 +210,10 @@ struct kmgb_handle {
   int* cand_cnt = nullptr;
   long long cand_cap = 0;  // rows of the compact buffers for the candidate pass
   unsigned long long* rr_stats = nullptr;
+  // audit of certified labels: sampled rows per iteration against the FP64 arg-min
+  // (launch_audit_labels; 0 rows: off)
+  unsigned long long* audit = nullptr;
+  int audit_rows = 0;
   int* err = nullptr;
   void* arena = nullptr;  // one device allocation holding every fixed buffer of the handle
   int* xinexact = nullptr;  // set by the BF16 conversion when some x is not a BF16 number
@@ -298,6 +302,18 @@ struct kmgb_handle {
 };
 
 namespace {
+
+// Rows audited per iteration: KMGB_AUDIT_ROWS (default 64, at most kAuditMaxRows, 0 = off),
+// fewer when one row's scan (k x d, FP32 with FP64 only near the label) is large, so that an
+// audit stays near 2^30 FP32 FMAs (~30 us on GB300). Certified resident runs only.
+int audit_rows_for(const kmgb_options& o, bool streaming, int k, int d) {
+  if (!o.certify || streaming || d > 8192) return 0;
+  long long rows = 64;
+  if (const char* e = std::getenv("KMGB_AUDIT_ROWS")) rows = std::atoll(e);
+  rows = std::max(0LL, std::min<long long>(rows, kAuditMaxRows));
+  const long long cap = std::max(1LL, (1LL << 30) / ((long long)k * d));
+  return (int)std::min(rows, cap);
+}
 
 int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_options* opt) {
   *out = nullptr;
@@ -391,6 +407,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     // a third of the points can miss the certificate after the first update.)
     h->cand_cap = std::min(na, std::min<long long>(8LL << 20, std::max<long long>(1024, na / 2)));
   }
+  h->audit_rows = audit_rows_for(h->opt, h->streaming, k, d);
   UpdateWork& w = h->uw;
   w.n = na;
   w.k = k;
@@ -452,6 +469,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
       a.take(&h->cand_cnt, cc);
     }
     a.take(&h->rr_stats, 2);
+    if (h->audit_rows > 0) a.take(&h->audit, 4 + 2 * (size_t)kAuditMaxRows);
     a.take(&h->err, 1);
     a.take(&h->stop, 1);
     a.take(&h->loopf, 2);
@@ -485,6 +503,9 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
   }
   KM_TRY(cudaMemset(h->labels, 0, sizeof(int) * nl), (delete h, code));
   KM_TRY(cudaMemset(h->rr_stats, 0, sizeof(unsigned long long) * 2), (delete h, code));
+  if (h->audit)
+    KM_TRY(cudaMemset(h->audit, 0, sizeof(unsigned long long) * (4 + 2 * kAuditMaxRows)),
+           (delete h, code));
   KM_TRY(cudaMemset(h->err, 0, sizeof(int)), (delete h, code));
   w.err = h->err;
   w.stop = h->stop;
@@ -967,6 +988,12 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr, bool assign_on
       if (rc) return rc;
     }
   }
+  // the audit reads the centers as they are (an empty cluster's NaN center has a NaN distance and
+  // never counts as nearer), not the operand copy whose unusable rows are zero
+  if (h->audit_rows > 0)
+    KM_TRY(launch_audit_labels(Xa, h->ldx, na, h->d, h->C, h->ldx, h->k, h->labels, h->audit,
+                               h->audit_rows, h->stop, s),
+           KMEANS_ERROR_CLOSEST_CENTERS);
   KM_TRY(h->pmark(3), KMEANS_ERROR_CLOSEST_CENTERS);
   if (assign_only) return 0;
   // cluster centers + compactness (kmeans.cpp:1018-1104)
@@ -1605,6 +1632,31 @@ int kmgb_get_sse(kmgb_handle* h, double* sse, int max_count) {
   return cnt;
 }
 
+int kmgb_debug_audit(const float* X, long long n, int d, long long ldx, const float* C, int k,
+                     long long ldc, const int* labels, int rows, unsigned long long* out) {
+  if (!X || !C || !labels || !out || n <= 0 || d <= 0 || k <= 0 || rows < 1 ||
+      rows > kAuditMaxRows || ldx < d || ldc < d) {
+    set_err("kmgb_debug_audit: invalid arguments");
+    return KMEANS_ERROR_COMPUTE;
+  }
+  const size_t words = 4 + 2 * (size_t)kAuditMaxRows;
+  unsigned long long* ws = nullptr;
+  KM_TRY(dalloc(&ws, words), KMEANS_ERROR_COMPUTE);
+  cudaError_t r = cudaMemset(ws, 0, sizeof(unsigned long long) * words);
+  if (r == cudaSuccess) r = launch_audit_labels(X, ldx, n, d, C, ldc, k, labels, ws, rows, nullptr, 0);
+  unsigned long long host[4] = {0, 0, 0, 0};
+  if (r == cudaSuccess) r = cudaMemcpy(host, ws, sizeof(host), cudaMemcpyDeviceToHost);
+  cudaFree(ws);
+  if (r != cudaSuccess) {
+    set_err("kmgb_debug_audit", r);
+    return KMEANS_ERROR_COMPUTE;
+  }
+  out[0] = host[0];
+  out[1] = host[1];
+  out[2] = host[3];
+  return 0;
+}
+
 int kmgb_get_stats(kmgb_handle* h, kmgb_stats* st) {
   if (!h || !st) return KMEANS_ERROR_COMPUTE;
   std::memset(st, 0, sizeof(*st));
@@ -1630,6 +1682,12 @@ int kmgb_get_stats(kmgb_handle* h, kmgb_stats* st) {
     st->reserved[3] = rs.trainings;
     st->reserved[4] = (long long)(rs.train_ms * 1000.0);
     st->reserved[5] = (long long)rs.flagged;
+  }
+  if (h->audit) {  // reserved[6], [7]: rows audited, violations found
+    unsigned long long au[2] = {0, 0};
+    KM_TRY(cudaMemcpy(au, h->audit, sizeof(au), cudaMemcpyDeviceToHost), KMEANS_ERROR_COMPUTE);
+    st->reserved[6] = (long long)au[0];
+    st->reserved[7] = (long long)au[1];
   }
   return 0;
 }

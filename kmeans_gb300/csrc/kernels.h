@@ -145,6 +145,13 @@ cudaError_t launch_resolve_candidates(const int* list, const int* count, long lo
                                       const int* row_map = nullptr);
 // stats[0] += counts[0] (points flagged by the assignment), stats[1] += counts[full_idx]
 // (points that needed a full rescan of the centers).
+// Audit of certified labels (rerank.cu): `rows` sampled rows (at most kAuditMaxRows) against
+// the FP64 arg-min over all k centers; ws holds 4 + 2 * kAuditMaxRows words, zero before the
+// first audit ([0] rows audited, [1] violations, [3] 1 + the last violating row).
+constexpr int kAuditMaxRows = 256;
+cudaError_t launch_audit_labels(const float* X, long long ldx, long long n, int d, const float* C,
+                                long long ldc, int k, const int* labels, unsigned long long* ws,
+                                int rows, const int* stop, cudaStream_t s);
 cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long long* stats,
                                const int* stop, cudaStream_t s);
 

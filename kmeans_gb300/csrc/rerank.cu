@@ -806,6 +806,121 @@ __global__ void resolve_candidates_kernel(const int* __restrict__ list, const in
     }
   }
 }
+
+// ------------------------------- audit of certified labels -------------------------------
+// A rotating sample of rows is checked against the FP64 arg-min over every center, so that a
+// failure of a rounding model the certificate relies on (the tensor tiers' accumulation bound,
+// the router's separation bound) shows as a counted violation instead of a silently wrong label.
+// A violation is a center strictly nearer than the label in FP64 (exact_value, the oracle's
+// expression and order); ties are not judged. Distances are first evaluated in FP32, one warp
+// per center with the lanes over the dimensions (coalesced rows), each with an interval: any
+// summation order of the d non-negative rounded squares stays within (d + 2) 2^-24 relative to
+// first order, 2.02x that plus an absolute d 2^-125 for underflow is used. A center whose
+// interval lies below the label's is a violation; only overlapping intervals (near ties) are
+// decided in FP64, which keeps the narrow FP64 pipe of GB300 out of the scan.
+// ws: [0] rows audited, [1] violations, [2] sampling sequence, [3] 1 + the last violating row,
+// then per sampled row a violation flag [rows] and the row [rows].
+__device__ __forceinline__ unsigned long long audit_hash(unsigned long long z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// FP32 squared distance of the shared row to center c, lanes over the dimensions (every lane
+// returns the warp's sum).
+__device__ __forceinline__ float audit_dist32(const float* ax, const float* __restrict__ c, int d,
+                                              int lane) {
+  float a = 0.0f;
+  for (int t = lane; t < d; t += 32) {
+    const float u = ax[t] - __ldg(c + t);
+    a = fmaf(u, u, a);
+  }
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  return a;
+}
+
+__global__ void __launch_bounds__(256)
+audit_scan_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
+                  const float* __restrict__ C, long long ldc, int k,
+                  const int* __restrict__ labels, unsigned long long* ws, int rows, int parts,
+                  const int* stop) {
+  if (stopped(stop)) return;
+  extern __shared__ float ax[];
+  __shared__ int viol_sh;
+  const int r = blockIdx.x / parts, part = blockIdx.x % parts;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const unsigned long long seq = *reinterpret_cast<volatile unsigned long long*>(ws + 2);
+  const long long row = (long long)(audit_hash(seq + (unsigned long long)r) % (unsigned long long)n);
+  for (int t = threadIdx.x; t < d; t += blockDim.x) ax[t] = X[(size_t)row * ldx + t];
+  if (threadIdx.x == 0) viol_sh = 0;
+  __syncthreads();
+  const float rel = 2.02f * (float)(d + 2) * 5.9604645e-8f;
+  const float slack = (float)d * 2.3509887e-38f;  // d 2^-125
+  const int lab = labels[row];
+  const bool valid = lab >= 0 && lab < k;
+  // the label's interval (every warp evaluates it; an invalid label or one on an unusable
+  // center is [inf, inf]: every usable center is nearer)
+  float lab_lo = INFINITY, lab_hi = INFINITY;
+  if (valid) {
+    const float a = audit_dist32(ax, C + (size_t)lab * ldc, d, lane);
+    if (a == a) {
+      lab_lo = a * (1.0f - rel) - slack;
+      lab_hi = a * (1.0f + rel) + slack;
+    }
+  }
+  double dl = -1.0;  // the label's FP64 distance, evaluated when first needed
+  const int per = (k + parts - 1) / parts;
+  const int j0 = part * per, j1 = min(k, j0 + per);
+  bool viol = false;
+  for (int j = j0 + warp; j < j1; j += nw) {
+    if (j == lab) continue;
+    const float* c = C + (size_t)j * ldc;
+    const float a = audit_dist32(ax, c, d, lane);
+    if (!(a == a)) continue;  // an unusable (NaN) center
+    const float lo = a * (1.0f - rel) - slack, hi = a * (1.0f + rel) + slack;
+    if (hi < lab_lo) {
+      viol = true;
+    } else if (lo <= lab_hi && lane == 0) {  // overlapping intervals: decide in FP64
+      if (dl < 0.0) {
+        dl = valid ? exact_value(0, ax, C + (size_t)lab * ldc, d, 0.0f) : INFINITY;
+        if (!(dl == dl)) dl = INFINITY;
+      }
+      if (exact_value(0, ax, c, d, 0.0f) < dl) viol = true;
+    }
+  }
+  if (viol) viol_sh = 1;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (viol_sh) atomicOr(ws + 4 + r, 1ull);
+    if (part == 0) ws[4 + rows + r] = (unsigned long long)row;
+  }
+}
+
+__global__ void audit_finish_kernel(unsigned long long* ws, int rows, const int* stop) {
+  if (stopped(stop)) return;
+  __shared__ int nviol;
+  __shared__ unsigned long long last;
+  if (threadIdx.x == 0) {
+    nviol = 0;
+    last = 0;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    if (ws[4 + r]) {
+      atomicAdd(&nviol, 1);
+      atomicMax(&last, ws[4 + rows + r] + 1);
+    }
+    ws[4 + r] = 0;  // ready for the next audit
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ws[0] += (unsigned long long)rows;
+    ws[1] += (unsigned long long)nviol;
+    ws[2] += (unsigned long long)rows;
+    if (last) ws[3] = last;
+  }
+}
 }  // namespace
 
 cudaError_t launch_gather_flagged(const int* list, const int* count, long long cap,
@@ -902,6 +1017,25 @@ cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s) {
   }
   // Persistent grid: the flagged count lives on the device, so no host round trip is needed.
   rerank_kernel<<<kmgb::num_sms() * 4, threads, smem, s>>>(a); kmgb::count_launches(1);
+  return cudaGetLastError();
+}
+
+int audit_parts(int rows) {
+  const int p = 2 * kmgb::num_sms() / (rows > 0 ? rows : 1);
+  return p < 1 ? 1 : (p > 32 ? 32 : p);
+}
+
+cudaError_t launch_audit_labels(const float* X, long long ldx, long long n, int d, const float* C,
+                                long long ldc, int k, const int* labels, unsigned long long* ws,
+                                int rows, const int* stop, cudaStream_t s) {
+  if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
+  if (n <= 0 || k <= 0 || rows <= 0) return cudaSuccess;
+  if (rows > kAuditMaxRows || (size_t)d * sizeof(float) > 48 * 1024) return cudaErrorInvalidValue;
+  const int parts = audit_parts(rows);
+  audit_scan_kernel<<<rows * parts, 256, sizeof(float) * (size_t)d, s>>>(X, ldx, n, d, C, ldc, k,
+                                                                        labels, ws, rows, parts, stop);
+  audit_finish_kernel<<<1, 256, 0, s>>>(ws, rows, stop);
+  count_launches(2);
   return cudaGetLastError();
 }
 

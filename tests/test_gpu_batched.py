@@ -127,9 +127,9 @@ def test_rejections(km, torch_cuda):
 
 
 def test_auto_tier_and_graph_replay_equal_oracle(km, orc, torch_cuda):
-    """KMGB_ASSIGN_AUTO (each problem's tier from the tuned table, problems of one dimension and
-    tier grouped) and the per-iteration CUDA graph give every problem the oracle's result; the
-    graph path equals the kernel-by-kernel path."""
+    """KMGB_ASSIGN_AUTO (one tier per dimension from the tuned cost table) and the per-iteration
+    CUDA graph give every problem the oracle's result; the graph path equals the kernel-by-kernel
+    path."""
     import os
     rng = np.random.default_rng(71)
     probs = []
@@ -140,7 +140,7 @@ def test_auto_tier_and_graph_replay_equal_oracle(km, orc, torch_cuda):
         X, _, _ = mixture_numpy(n, d, k, seed=500 + i)
         probs.append((X, k, X[sample_init(n, k, seed=600 + i)].copy()))
     res, st = km.lloyd_batched(probs, max_iters=4, assign_tier=km.ASSIGN_AUTO)
-    assert st.reserved[5] > 0 and st.reserved[6] >= 4  # graph launches, groups
+    assert st.reserved[5] > 0 and st.reserved[6] >= 4  # graph launches, groups (4 dimensions)
     for (X, k, init), r in zip(probs, res):
         stt, c, lab, sse, it = orc.lloyd(X, init, 4)
         assert np.array_equal(r.labels, lab) and np.array_equal(r.centers, c, equal_nan=True)

@@ -113,6 +113,8 @@ def test_routed_run_equals_oracle(km, orc, torch_cuda):
     assert np.array_equal(res.labels, lab)
     assert np.array_equal(res.centers, c, equal_nan=True)
     assert np.allclose(res.sse, sse, rtol=1e-10)
+    # the label audit also samples the routed iterations
+    assert res.audited == 64 * iters and res.audit_violations == 0
 
 
 def test_router_ablation(km, torch_cuda, capsys):
