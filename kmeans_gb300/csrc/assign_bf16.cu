@@ -19,17 +19,19 @@
 //     chunk g+1) and multicasts its commits (stage free, accumulator ready, points free) to both
 //     CTAs. Warp 1 of both CTAs allocates the 512 TMEM columns collectively.
 //   * warps 2.. (both CTAs) epilogue: EPQ warps per TMEM lane quadrant (2 in the split tier, 4 in
-//     the plain tier), each owning 32 points and 256/EPQ of the chunk's 256 columns. A thread reads 32 columns at a time (tcgen05.ld), adds
-//     -||c_j||^2/2 (FP32, FMA pipe) so that arg-min distance = arg-max key, packs the column
-//     within the 32-column block into the 5 low mantissa bits and keeps the two largest keys with
-//     3.5 ALU ops per element. Accumulator buffers are handed back to the leader by remote
-//     mbarrier arrivals. At the end of a unit the column slices of a point are merged through
-//     shared memory (bounded mbarrier handshake).
+//     the plain tier), each owning 32 points and 256/EPQ of the chunk's 256 columns. A thread
+//     reads 32 columns at a time (tcgen05.ld), adds -||c_j||^2/2 (FP32, FMA pipe) so that arg-min
+//     distance = arg-max key, packs the column within the 32-column block into the 5 low
+//     mantissa bits (one lop3) and keeps the two largest keys with 2.5 more ALU ops per element
+//     (measured with ncu counters: 4.3 ALU instructions per element in all). Accumulator
+//     buffers are handed back to the leader by remote mbarrier arrivals. At the end of a unit the
+//     column slices of a point are merged through shared memory (bounded mbarrier handshake).
 // A point is certified when best - second > 2E, E the rigorous bound of the BF16 evaluation
 // (operand rounding, FP32 accumulation, norm rounding, key packing, FP64 reference error);
 // other points go to the exact re-rank list, so labels equal the FP64 arg-min.
 // Every mbarrier wait is bounded (error word + CTA abort flag); TMEM is freed on every path.
 #include <cfloat>
+#include <utility>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -104,6 +106,34 @@ __device__ __forceinline__ float fmax3(float a, float b, float c) {
   float r;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
   return r;
+}
+
+// Packed key of column J of a 32-column block: the key's bits with the 5 low mantissa bits
+// replaced by J, (x & msk) | J with msk = ~31 held in a register, so that one lop3 with J as its
+// immediate does it (written as C, the two constants took two ALU instructions per element).
+template <int J>
+__device__ __forceinline__ float packed_key(uint32_t x, uint32_t msk) {
+  uint32_t r;
+  asm("lop3.b32 %0, %1, %2, %3, 0xEC;" : "=r"(r) : "r"(x), "n"(J), "r"(msk));
+  return __uint_as_float(r);
+}
+
+// Running top-2 of the packed keys over one pair of columns (J, J + 1).
+template <int J>
+__device__ __forceinline__ void top2_pair(const uint32_t (&cur)[32], uint32_t msk, float& b1,
+                                          float& b2) {
+  const float k0 = packed_key<J>(cur[J], msk);
+  const float k1 = packed_key<J + 1>(cur[J + 1], msk);
+  const float hi = fmaxf(k0, k1);
+  const float lo = fminf(k0, k1);
+  b2 = fmax3(b2, lo, fminf(b1, hi));
+  b1 = fmaxf(b1, hi);
+}
+
+template <int... P>
+__device__ __forceinline__ void top2_block(const uint32_t (&cur)[32], uint32_t msk, float& b1,
+                                           float& b2, std::integer_sequence<int, P...>) {
+  (top2_pair<2 * P>(cur, msk, b1, b2), ...);
 }
 
 // Rigorous bound (in accumulator units) of |key - (x.c - ||c||^2/2)| for any usable center.
@@ -632,15 +662,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             }
           } else {
             const float blk_before = b1;
-#pragma unroll
-            for (int j = 0; j < 32; j += 2) {
-              const float k0 = __uint_as_float((cur[j] & ~0x1Fu) | (uint32_t)j);
-              const float k1 = __uint_as_float((cur[j + 1] & ~0x1Fu) | (uint32_t)(j + 1));
-              const float hi = fmaxf(k0, k1);
-              const float lo = fminf(k0, k1);
-              b2 = fmax3(b2, lo, fminf(b1, hi));
-              b1 = fmaxf(b1, hi);
-            }
+            uint32_t msk;  // ~31 in a register (see packed_key)
+            asm volatile("mov.b32 %0, 0xFFFFFFE0;" : "=r"(msk));
+            top2_block(cur, msk, b1, b2, std::make_integer_sequence<int, 16>{});
             if (b1 != blk_before) bblk = (col0 >> 5) + cb;  // 32-column block of the best
           }
         }
