@@ -68,6 +68,11 @@ constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >
 // the shared-memory layout and the per-MMA byte advance are those of the BF16 path.
 constexpr uint32_t IDESC8 = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(UNIT >> 4) << 24);
 constexpr int BK8 = 128;  // E4M3 elements per k-block (one 128-byte swizzle row)
+// Start-value MMA (AssignArgs::cbias): per chunk and CTA a 128-center x 16-column BF16 box of
+// the bias matrix (32-byte rows, 32-byte swizzle) next to the center planes of the chunk's first
+// stage, and one 128-row x 16-column tile of ones (A) written once per CTA.
+constexpr uint32_t BIAS_BYTES = BNH * kBiasCols * 2;  // 4 KB
+constexpr uint32_t ONES_BYTES = BM * kBiasCols * 2;   // 4 KB
 
 __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
@@ -75,6 +80,16 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   d |= (uint64_t)(1024 >> 4) << 32;  // stride byte offset: 8 rows x 128 B
   d |= (uint64_t)1 << 46;            // descriptor version
   d |= (uint64_t)2 << 61;            // 128-byte swizzle
+  return d;
+}
+
+// The same for a K-major tile of 32-byte rows with the 32-byte swizzle (one K=16 BF16 step).
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;            // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(256 >> 4) << 32;   // stride byte offset: 8 rows x 32 B
+  d |= (uint64_t)1 << 46;            // descriptor version
+  d |= (uint64_t)6 << 61;            // 32-byte swizzle
   return d;
 }
 
@@ -139,7 +154,7 @@ __device__ __forceinline__ void top2_block(const uint32_t (&cur)[32], uint32_t m
 // Rigorous bound (in accumulator units) of |key - (x.c - ||c||^2/2)| for any usable center.
 // mode: 1 plain BF16 (x_hi.c_hi), 2 split (x_hi.c_hi + x_hi.c_lo + x_lo.c_hi), 3 split with every x
 // a BF16 number (x.c_hi + x.c_lo).
-__device__ __forceinline__ float bound_acc(float xn, float cm, int d, int mode) {
+__device__ __forceinline__ float bound_acc(float xn, float cm, int d, int mode, bool bias) {
   const float u = 5.9604645e-8f;            // 2^-24, FP32 rounding
   const float ub = 1.953125e-3f;            // 2^-9, BF16 rounding
   // operand error: plain (2ub + ub^2) |x||c|; split x = xh + xl + ex, c = ch + cl + ec with
@@ -150,7 +165,8 @@ __device__ __forceinline__ float bound_acc(float xn, float cm, int d, int mode) 
   // modelled with margin as (terms/16 + 2) 2^-21 relative to |start| + sum |products|. The
   // measured worst case on GB300 is >= 6x below this (tests/test_gpu_tensor_numerics.py
   // enforces >= 4x on the keys, start value included).
-  const int terms = (mode == 1 ? 1 : (mode == 2 ? 3 : 2)) * d;  // products per element
+  // products per element; the start-value MMA adds one 16-product step
+  const int terms = (mode == 1 ? 1 : (mode == 2 ? 3 : 2)) * d + (bias ? 16 : 0);
   const float gacc = (float)(terms / 16 + 2) * 4.76837158e-7f;
   const float pack = 3.81469727e-6f;        // 2^-18: 5 column bits in the mantissa
   const float cc = 0.5f * cm * cm;
@@ -296,13 +312,15 @@ struct MergeSlot {
   int bblk[EPQ - 1][4][32], ncand[EPQ - 1][4][32];
 };
 
-// EPQ: epilogue warps per lane quadrant; F8: the FP8 tier's instantiation (mode 4 only). One CTA
-// per SM: each SM sub-partition's 16K registers hold ceil(warps / 4) warps, so a thread may use
-// 168 registers with EPQ 2 (10 warps) and 96 with EPQ 4 (18 warps).
-template <int EPQ, bool F8>
+// EPQ: epilogue warps per lane quadrant; F8: the FP8 tier's instantiation (mode 4 only); BIAS:
+// the start values enter by MMA (AssignArgs::cbias) and the epilogue adds nothing. One CTA per
+// SM: each SM sub-partition's 16K registers hold ceil(warps / 4) warps, so a thread may use 168
+// registers with EPQ 2 (10 warps) and 96 with EPQ 4 (18 warps).
+template <int EPQ, bool F8, bool BIAS>
 __global__ void __launch_bounds__(threads_for(EPQ), 1)
 assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmXl,
                    const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmCl,
+                   const __grid_constant__ CUtensorMap tmB,
                    AssignArgs p, int stages, int xbufs, int mode) {
   constexpr int NUM_EPI_WARPS = 4 * EPQ;
   constexpr int EPI_PER_QUAD = EPQ;
@@ -379,8 +397,18 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   const int xplanes = mode == 2 ? 2 : 1;                // BF16 planes of the points
   const int cplanes = (mode == 2 || mode == 3) ? 2 : 1;  // and of the centers
   const size_t xbuf_bytes = (size_t)xplanes * nkb * XKB_BYTES;
-  const uint32_t stage_bytes = (uint32_t)cplanes * CKB_BYTES;
+  // start values by MMA (the launcher picks this variant only where the extra 4 + 4 KB fit)
+  constexpr bool bias = BIAS && !F8;
+  const uint32_t stage_bytes = (uint32_t)cplanes * CKB_BYTES + (bias ? BIAS_BYTES : 0u);
   uint8_t* cs = smem + (size_t)xbufs * xbuf_bytes;
+  uint8_t* ones = cs + (size_t)stages * stage_bytes;  // bias: the A tile of ones
+  if (bias) {
+    // all ones, so that the swizzle of the tile does not matter; made visible to the tensor
+    // core (async proxy) before the barrier below
+    for (int i = tid; i < (int)(ONES_BYTES / 4); i += blockDim.x)
+      reinterpret_cast<uint32_t*>(ones)[i] = 0x3F803F80u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
 
   if (tid == 0) {
     abort_flag = 0;
@@ -404,6 +432,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     prefetch_tmap(&tmC);
     if (xplanes > 1) prefetch_tmap(&tmXl);
     if (cplanes > 1) prefetch_tmap(&tmCl);
+    if (bias) prefetch_tmap(&tmB);
   }
   if (warp == 1) {  // both CTAs: one collective allocation of the pair's TMEM
     asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -460,11 +489,17 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               break;
             }
             const uint32_t cb_local = smem_u32(&bars.c_full[stage]);
-            if (rank == 0) mbar_arrive_expect_tx(cb_local, 2 * stage_bytes);
+            const bool with_bias = bias && kb == 0;  // the chunk's start values ride along
+            if (rank == 0)
+              mbar_arrive_expect_tx(cb_local,
+                                    2 * ((uint32_t)cplanes * CKB_BYTES + (with_bias ? BIAS_BYTES : 0u)));
             const uint32_t cb = map_to_rank(cb_local, 0);
             for (int pl = 0; pl < cplanes; ++pl)
               tma_load_2d_pair(smem_u32(cs + (size_t)stage * stage_bytes + pl * CKB_BYTES),
                                pl ? &tmCl : &tmC, cb, kb * bk, crow);
+            if (with_bias)
+              tma_load_2d_pair(smem_u32(cs + (size_t)stage * stage_bytes + cplanes * CKB_BYTES),
+                               &tmB, cb, 0, crow);
           }
         }
       }
@@ -504,9 +539,14 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             tc_fence_after();
             const uint32_t chi = smem_u32(cs + (size_t)stage * stage_bytes);
             const uint32_t xhi = smem_u32(xs + (size_t)kb * XKB_BYTES);
+            // the start values -||c||^2/2 first: ones x (hi, mid, lo) pieces set the accumulator
+            if (bias && kb == 0)
+              umma_pair(dcol, sdesc_sw32(smem_u32(ones)),
+                        sdesc_sw32(chi + (uint32_t)cplanes * CKB_BYTES), 0u);
 #pragma unroll
             for (int k16 = 0; k16 < BK / 16; ++k16) {
-              const uint32_t acc = (kb | k16) ? 1u : 0u;  // the chunk's first product starts at 0
+              // the chunk's first product starts at 0 unless the start values are in
+              const uint32_t acc = (bias || kb | k16) ? 1u : 0u;
               const uint64_t ahi = sdesc_sw128(xhi + k16 * 32);
               const uint64_t bhi = sdesc_sw128(chi + k16 * 32);
               if (kOnePlane && !F8 && mode == 1) {
@@ -603,7 +643,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
                 cur[4 * j4 + 2] = __float_as_uint(__fmaf_rn(__uint_as_float(cur[4 * j4 + 2]), mrow, hv.z));
                 cur[4 * j4 + 3] = __float_as_uint(__fmaf_rn(__uint_as_float(cur[4 * j4 + 3]), mrow, hv.w));
               }
-            } else {
+            } else if (!bias) {
 #pragma unroll
               for (int j4 = 0; j4 < 8; ++j4) {
                 const float4 hv = __ldg(hs + j4);
@@ -732,7 +772,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         p.labels[pt] = label;
         if (p.certify) {
           const float eb = (fp8 ? bound_fp8(xn_pt, cm, p.d, sx_pt, sc_all)
-                                      : bound_acc(xn_pt, cm, p.d, mode)) +
+                                      : bound_acc(xn_pt, cm, p.d, mode, bias)) +
                            1.02f * p.pert * (xn_pt * cm * 1.01f + 0.5f * cm * cm);
           if (none || !(b1 - b2 > 2.0f * eb)) {
             const int slot = atomicAdd(p.rerank_count, 1);
@@ -764,10 +804,10 @@ struct VariantInfo {
   size_t smem_budget = 0;  // 1 KB aligned
   size_t static_bytes = 0;
 };
-VariantInfo g_variant[5];  // [0] FP8, [2] split BF16, [4] plain BF16
+VariantInfo g_variant[6];  // [0] FP8, [2] split BF16, [4] plain BF16, [3] / [5]: with start-value MMA
 int g_num_sms = 0;
 
-template <int EPQ, bool F8>
+template <int EPQ, bool F8, bool BIAS>
 cudaError_t prepare_variant(VariantInfo& vi) {
   if (vi.ready) return cudaSuccess;
   int dev = 0, optin = 0;
@@ -775,12 +815,12 @@ cudaError_t prepare_variant(VariantInfo& vi) {
   KMGB_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
   KMGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   cudaFuncAttributes fa;
-  KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel<EPQ, F8>));
+  KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel<EPQ, F8, BIAS>));
   // the dynamic area starts on the next 1 KB boundary after the static variables
   vi.static_bytes = (fa.sharedSizeBytes + 1023) / 1024 * 1024;
   size_t budget = (size_t)optin > vi.static_bytes ? (size_t)optin - vi.static_bytes : 0;
   if (budget > SMEM_CAP) budget = SMEM_CAP;
-  KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel<EPQ, F8>,
+  KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel<EPQ, F8, BIAS>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
   vi.smem_budget = budget;
   cudaLaunchConfig_t qc = {};
@@ -794,7 +834,7 @@ cudaError_t prepare_variant(VariantInfo& vi) {
   qa[0].val.clusterDim.z = 1;
   qc.attrs = qa;
   qc.numAttrs = 1;
-  KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&vi.max_pairs, assign_bf16_kernel<EPQ, F8>, &qc));
+  KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&vi.max_pairs, assign_bf16_kernel<EPQ, F8, BIAS>, &qc));
   if (vi.max_pairs <= 0) return cudaErrorInvalidConfiguration;
   vi.ready = true;
   return cudaSuccess;
@@ -838,7 +878,7 @@ static cudaError_t launch_assign_fp8(const void* X8, long long ld8x, const void*
       a.store_out || a.u_prob)
     return cudaErrorInvalidValue;
   VariantInfo& vi = g_variant[0];
-  KMGB_CUDA_TRY((prepare_variant<4, true>(vi)));
+  KMGB_CUDA_TRY((prepare_variant<4, true, false>(vi)));
   const size_t xbytes = (size_t)((a.d + BK8 - 1) / BK8) * XKB_BYTES;
   const size_t stage_bytes = CKB_BYTES;
   const size_t lim = vi.smem_budget;
@@ -867,8 +907,8 @@ static cudaError_t launch_assign_fp8(const void* X8, long long ld8x, const void*
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, true>, tmX, tmX, tmC, tmC, a, stages,
-                                   xbufs, 4));
+  KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, true, false>, tmX, tmX, tmC, tmC, tmC, a,
+                                   stages, xbufs, 4));
   count_launches(1);
   return cudaSuccess;
 }
@@ -888,19 +928,30 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
       (reinterpret_cast<uintptr_t>(Xl) & 15) || (reinterpret_cast<uintptr_t>(Cl) & 15))
     return cudaErrorInvalidValue;
   const int epq = epq_for(mode > 1 ? 2 : 1);
+  // the budget of the variant without bias tiles decides; the variants' static shared memory
+  // is the same
   VariantInfo& vi = g_variant[epq];
-  if (epq == 2) KMGB_CUDA_TRY((prepare_variant<2, false>(vi)));
-  else KMGB_CUDA_TRY((prepare_variant<4, false>(vi)));
+  if (epq == 2) KMGB_CUDA_TRY((prepare_variant<2, false, false>(vi)));
+  else KMGB_CUDA_TRY((prepare_variant<4, false, false>(vi)));
   const size_t xbytes = xbuf_bytes_for(a.d, mode == 2 ? 2 : 1);
-  const size_t stage_bytes = (size_t)(mode > 1 ? 2 : 1) * CKB_BYTES;
   const size_t lim = vi.smem_budget;
-  // double-buffer the unit's points when that still leaves a 3-stage ring (a single buffer
-  // measured no slower on GB300: the next unit's points are prefetched into L2)
-  const int xbufs = (2 * xbytes + 3 * stage_bytes <= lim) ? 2 : 1;
-  if (lim < xbufs * xbytes + 2 * stage_bytes) return cudaErrorInvalidValue;
-  int stages = (int)((lim - xbufs * xbytes) / stage_bytes);
+  // The start values by MMA (a.cbias) need 4 KB more per stage and the 4 KB tile of ones; they
+  // are used where two point buffers and a 2-stage ring still fit (on GB300 the 4M x 128, K=1024
+  // split tier ran as fast with 2 stages as with 3), otherwise the epilogue adds cinit.
+  AssignArgs ab = a;
+  if (ab.store_out) ab.cbias = nullptr;
+  const size_t planes_bytes = (size_t)(mode > 1 ? 2 : 1) * CKB_BYTES;
+  if (ab.cbias && 2 * xbytes + 2 * (planes_bytes + BIAS_BYTES) + ONES_BYTES > lim) ab.cbias = nullptr;
+  const bool bias = ab.cbias != nullptr;
+  const size_t stage_bytes = planes_bytes + (bias ? BIAS_BYTES : 0);
+  const size_t extra = bias ? ONES_BYTES : 0;
+  // double-buffer the unit's points when that still leaves a 3-stage ring (2 with the bias
+  // tiles; a single point buffer measured ~7% slower on GB300)
+  const int xbufs = (2 * xbytes + (bias ? 2 : 3) * stage_bytes + extra <= lim) ? 2 : 1;
+  if (lim < xbufs * xbytes + 2 * stage_bytes + extra) return cudaErrorInvalidValue;
+  int stages = (int)((lim - xbufs * xbytes - extra) / stage_bytes);
   if (stages > MAX_STAGES) stages = MAX_STAGES;
-  const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes;
+  const size_t smem = xbufs * xbytes + (size_t)stages * stage_bytes + extra;
   CUtensorMap tmX, tmC, tmXl, tmCl;
   KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmX, Xb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (uint64_t)a.d,
                                   (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
@@ -908,6 +959,15 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
                                   (uint64_t)a.k, (uint64_t)ldcb * 2, BK, BNH));
   tmXl = tmX;
   tmCl = tmC;
+  CUtensorMap tmB = tmC;
+  if (bias) {
+    // rows: the bias matrix covers round_up(k, kCenterPad) centers, like cinit
+    const uint64_t brows = (uint64_t)((a.k + kCenterPad - 1) / kCenterPad) * kCenterPad;
+    if (reinterpret_cast<uintptr_t>(ab.cbias) & 15) return cudaErrorInvalidValue;
+    KMGB_CUDA_TRY(kmgb_make_tmap_2d_swz(&tmB, ab.cbias, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                        kBiasCols, brows, kBiasCols * 2, kBiasCols, BNH,
+                                        CU_TENSOR_MAP_SWIZZLE_32B));
+  }
   if (mode == 2)
     KMGB_CUDA_TRY(kmgb_make_tmap_2d(&tmXl, Xl, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                                     (uint64_t)a.d, (uint64_t)a.n, (uint64_t)ldxb * 2, BK, BM));
@@ -929,12 +989,24 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  if (epq == 2)
-    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2, false>, tmX, tmXl, tmC, tmCl, a, stages,
-                                     xbufs, mode));
+  if (bias) {  // the bias variants' launch limits (occupancy, shared memory) are set up too
+    VariantInfo& vb = g_variant[epq + 1];
+    if (epq == 2) KMGB_CUDA_TRY((prepare_variant<2, false, true>(vb)));
+    else KMGB_CUDA_TRY((prepare_variant<4, false, true>(vb)));
+    if (vb.smem_budget < smem || vb.max_pairs < pairs) return cudaErrorInvalidConfiguration;
+  }
+  if (epq == 2 && bias)
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2, false, true>, tmX, tmXl, tmC, tmCl,
+                                     tmB, ab, stages, xbufs, mode));
+  else if (epq == 2)
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2, false, false>, tmX, tmXl, tmC,
+                                     tmCl, tmB, ab, stages, xbufs, mode));
+  else if (bias)
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, false, true>, tmX, tmXl, tmC, tmCl,
+                                     tmB, ab, stages, xbufs, mode));
   else
-    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, false>, tmX, tmXl, tmC, tmCl, a, stages,
-                                     xbufs, mode));
+    KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, false, false>, tmX, tmXl, tmC,
+                                     tmCl, tmB, ab, stages, xbufs, mode));
   count_launches(1);
   return cudaSuccess;
 }

@@ -146,6 +146,11 @@ __device__ __forceinline__ unsigned warp_peers(int l, int nbits) {
 cudaError_t kmgb_make_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype,
                               int elem_bytes, uint64_t cols, uint64_t rows, uint64_t row_stride_bytes,
                               uint32_t box_cols, uint32_t box_rows);
+// The same with a given swizzle (the box's inner extent at most the swizzle width).
+cudaError_t kmgb_make_tmap_2d_swz(CUtensorMap* map, const void* base, CUtensorMapDataType dtype,
+                                  int elem_bytes, uint64_t cols, uint64_t rows,
+                                  uint64_t row_stride_bytes, uint32_t box_cols, uint32_t box_rows,
+                                  CUtensorMapSwizzle swizzle);
 
 // Number of kernels this library has launched (process-wide), for launch accounting.
 namespace kmgb {

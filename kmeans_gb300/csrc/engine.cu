@@ -191,6 +191,7 @@ struct kmgb_handle {
   float* cn = nullptr;
   float* cmax = nullptr;
   float* cinit = nullptr;  // BF16 tier accumulator start values, padded to kCenterPad
+  void* cbias = nullptr;   // the same as BF16 pieces for the pair kernel's start-value MMA
   bool have_centers = false;
   // assignment
   int* labels = nullptr;
@@ -451,6 +452,7 @@ int create_handle(kmgb_handle** out, long long n, int d, int k, const kmgb_optio
     a.take(&h->cn, k);
     a.take(&h->cmax, 1);
     if (tcore) a.take(&h->cinit, (size_t)round_up(k, kCenterPad));
+    if (bf16) a.take_bytes(&h->cbias, (size_t)round_up(k, kCenterPad) * kBiasCols * 2);
     a.take(&h->labels, nl);
     a.take(&h->rr_list, na);
     a.take(&h->rr_count, 3);
@@ -821,7 +823,7 @@ int router_maybe_train(kmgb_handle* h, int slot) {
   // the centers' operand copies, norms and planes for the updated centers
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
-                             nullptr, h->cinit, h->Cl),
+                             nullptr, h->cinit, h->Cl, h->cbias),
          KMEANS_ERROR_RESET);
   const RouterIO io = router_io(h);
   if (!h->router) {
@@ -908,7 +910,7 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr, bool assign_on
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
   KM_TRY(cudaMemsetAsync(h->rr_count, 0, 3 * sizeof(int), s), KMEANS_ERROR_RESET);
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
-                             h->stop, h->cinit, h->Cl),
+                             h->stop, h->cinit, h->Cl, h->cbias),
          KMEANS_ERROR_RESET);
   if (h->C8)
     KM_TRY(launch_centers_fp8(h->Cop, h->ldx, h->k, h->d, h->cmax, h->C8, h->ld8, h->cscale, s,
@@ -930,6 +932,7 @@ int step(kmgb_handle* h, int slot, const float* upload = nullptr, bool assign_on
   a.certify = h->opt.certify;
   a.stop = h->stop;
   a.cinit = h->cinit;
+  a.cbias = h->cbias;  // BF16 tiers: start values by MMA where the launcher can
   test_wait_hook(&a.test_withhold, &a.test_wait_cycles);  // zero unless a test asks
   const bool tc = h->opt.assign_tier != KMGB_ASSIGN_FP32;
   const bool routed = h->router && router_trained(h->router) && !upload && !h->mini;
@@ -1015,7 +1018,7 @@ int step_stream(kmgb_handle* h, int slot) {
   KM_TRY(h->pmark(0), KMEANS_ERROR_RESET);
   KM_TRY(cudaMemsetAsync(h->cmax, 0, sizeof(float), s), KMEANS_ERROR_RESET);
   KM_TRY(launch_prep_centers(h->C, h->ldx, h->k, h->d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
-                             h->stop, h->cinit, h->Cl),
+                             h->stop, h->cinit, h->Cl, h->cbias),
          KMEANS_ERROR_RESET);
   KM_TRY(cudaMemsetAsync(h->accS, 0, sizeof(double) * (size_t)h->k * h->d, s), KMEANS_ERROR_RESET);
   KM_TRY(cudaMemsetAsync(h->accQ, 0, sizeof(double) * h->k, s), KMEANS_ERROR_RESET);
@@ -1061,6 +1064,7 @@ int step_stream(kmgb_handle* h, int slot) {
     a.certify = h->opt.certify;
     a.stop = h->stop;
     a.cinit = h->cinit;
+    a.cbias = h->cbias;
     if (tc) {
       a.gamma = assign_bf16_gamma(h->d);
       a.thr_out = h->opt.certify ? h->thr_full : nullptr;
@@ -1871,11 +1875,12 @@ int kmgb_tc_accumulators(const float* X, long long n, int d, const float* C, int
     a.d = d;
     a.certify = 0;
     a.cinit = h->cinit;
+    a.cbias = split == 3 ? nullptr : h->cbias;
     a.dump = dump;
     cudaError_t e = cudaMemsetAsync(h->cmax, 0, sizeof(float), s);
     if (e == cudaSuccess)
       e = launch_prep_centers(h->C, h->ldx, k, d, h->Cop, h->Cb, h->ldb, h->cn, h->cmax, s,
-                              nullptr, h->cinit, h->Cl);
+                              nullptr, h->cinit, h->Cl, h->cbias);
     if (e == cudaSuccess && split == 3) {
       e = launch_centers_fp8(h->Cop, h->ldx, k, d, h->cmax, h->C8, h->ld8, h->cscale, s);
       a.fp8 = 1;

@@ -17,6 +17,9 @@ struct AssignArgs {
   const float* xnorm;     // [n] upper bound of ||x_i||
   const float* cmax;      // device scalar: upper bound of max ||c_j|| over usable centers
   const float* cinit;     // [round_up(k,128)] accumulator start -||c_j||^2/2 (BF16 tier)
+  const void* cbias;      // nullable: the same start values as BF16 pieces (launch_prep_centers'
+                          // cbias); when given, the pair kernel's first MMA of every chunk loads
+                          // them into the accumulator and the epilogue adds nothing
   float* dump;            // diagnostic (nullable): raw accumulators [n][round_up(k,128)]
   // BF16 tiers only:
   const int* n_dev;       // nullable: rows actually present = min(*n_dev, n) (device count)
@@ -159,11 +162,14 @@ cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long lo
 // rows -> 0), optional BF16 copy Cb[k][ldcb], cn (+inf for NaN rows) and atomically raise
 // *cmax (must be zeroed before).
 // cinit (nullable, round_up(k,128) floats) receives -cn/2 per usable center and -3e38 for
-// unusable centers and padding.
+// unusable centers and padding; cbias (nullable, round_up(k,128) rows of kBiasCols BF16) the same
+// start values split exactly into three BF16 numbers (columns 0..2, the rest zero), the B
+// operand of the pair kernel's start-value MMA.
+constexpr int kBiasCols = 16;
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop,
                                 void* Cb, long long ldcb, float* cn, float* cmax, cudaStream_t s,
                                 const int* stop = nullptr, float* cinit = nullptr,
-                                void* Cl = nullptr);
+                                void* Cl = nullptr, void* cbias = nullptr);
 
 // Per-point norms, computed once per data set: qn = ||x||^2 (FP64), xn = upper bound ||x||.
 cudaError_t launch_point_norms(const float* X, long long ldx, long long n, int d, double* qn,

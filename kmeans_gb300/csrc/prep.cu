@@ -15,17 +15,31 @@
 namespace kmgb {
 namespace {
 
+// Row of the bias matrix (kBiasCols BF16 per center): the start value v split exactly into
+// three BF16 numbers, v = hi + mid + lo (v - hi and v - hi - mid are exact in FP32, and what
+// is left after two 8-bit pieces of a 24-bit significand fits the third), then zeros.
+__device__ __forceinline__ void write_bias_row(__nv_bfloat16* row, float v, int lane) {
+  const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+  const float r1 = v - __bfloat162float(hi);
+  const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+  const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+  if (lane < kBiasCols)
+    row[lane] = lane == 0 ? hi : (lane == 1 ? mid : (lane == 2 ? lo : __float2bfloat16_rn(0.0f)));
+}
+
 // One warp per center.
 __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, int k, int d,
                                     float* __restrict__ Cop, __nv_bfloat16* __restrict__ Cb,
                                     long long ldcb, float* __restrict__ cn, float* cmax,
                                     const int* stop, float* __restrict__ cinit, int kpad,
-                                    __nv_bfloat16* __restrict__ Cl) {
+                                    __nv_bfloat16* __restrict__ Cl,
+                                    __nv_bfloat16* __restrict__ cbias) {
   if (stopped(stop)) return;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= k) {
     if (cinit && warp < kpad && lane == 0) cinit[warp] = -3.0e38f;
+    if (cbias && warp < kpad) write_bias_row(cbias + (size_t)warp * kBiasCols, -3.0e38f, lane);
     return;
   }
   const float* c = C + (size_t)warp * ldc;
@@ -50,6 +64,9 @@ __global__ void prep_centers_kernel(const float* __restrict__ C, long long ldc, 
       if (ol) ol[t] = __float2bfloat16_rn(v - __bfloat162float(hi));
     }
   }
+  if (cbias)
+    write_bias_row(cbias + (size_t)warp * kBiasCols,
+                   bad ? -3.0e38f : -0.5f * __double2float_rn(s), lane);
   if (lane == 0) {
     if (bad) {
       cn[warp] = INFINITY;
@@ -256,16 +273,18 @@ cudaError_t launch_centers_fp8(const float* Cop, long long ldc, int k, int d, co
 
 cudaError_t launch_prep_centers(const float* C, long long ldc, int k, int d, float* Cop, void* Cb,
                                 long long ldcb, float* cn, float* cmax, cudaStream_t s,
-                                const int* stop, float* cinit, void* Cl) {
+                                const int* stop, float* cinit, void* Cl, void* cbias) {
   if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (k <= 0) return cudaSuccess;
   const int threads = 256;
   const int kpad = (k + kCenterPad - 1) / kCenterPad * kCenterPad;
-  const int blocks = (int)(((long long)(cinit ? kpad : k) * 32 + threads - 1) / threads);
+  const int blocks = (int)(((long long)(cinit || cbias ? kpad : k) * 32 + threads - 1) / threads);
   prep_centers_kernel<<<blocks, threads, 0, s>>>(C, ldc, k, d, Cop,
                                                  reinterpret_cast<__nv_bfloat16*>(Cb), ldcb, cn,
                                                  cmax, stop, cinit, kpad,
-                                                 reinterpret_cast<__nv_bfloat16*>(Cl)); kmgb::count_launches(1);
+                                                 reinterpret_cast<__nv_bfloat16*>(Cl),
+                                                 reinterpret_cast<__nv_bfloat16*>(cbias));
+  kmgb::count_launches(1);
   return cudaGetLastError();
 }
 

@@ -24,9 +24,19 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 cudaError_t kmgb_make_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDataType dtype,
                               int elem_bytes, uint64_t cols, uint64_t rows,
                               uint64_t row_stride_bytes, uint32_t box_cols, uint32_t box_rows) {
+  return kmgb_make_tmap_2d_swz(map, base, dtype, elem_bytes, cols, rows, row_stride_bytes,
+                               box_cols, box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
+}
+
+cudaError_t kmgb_make_tmap_2d_swz(CUtensorMap* map, const void* base, CUtensorMapDataType dtype,
+                                  int elem_bytes, uint64_t cols, uint64_t rows,
+                                  uint64_t row_stride_bytes, uint32_t box_cols, uint32_t box_rows,
+                                  CUtensorMapSwizzle swizzle) {
   auto fn = encode_fn();
   if (!fn) return cudaErrorNotSupported;
-  if (box_cols * (uint32_t)elem_bytes > 128 || box_rows > 256 || (row_stride_bytes % 16) ||
+  const uint32_t width = swizzle == CU_TENSOR_MAP_SWIZZLE_32B ? 32
+                       : swizzle == CU_TENSOR_MAP_SWIZZLE_64B ? 64 : 128;
+  if (box_cols * (uint32_t)elem_bytes > width || box_rows > 256 || (row_stride_bytes % 16) ||
       (reinterpret_cast<uintptr_t>(base) & 15))
     return cudaErrorInvalidValue;
   cuuint64_t dims[2] = {cols, rows};
@@ -34,7 +44,7 @@ cudaError_t kmgb_make_tmap_2d(CUtensorMap* map, const void* base, CUtensorMapDat
   cuuint32_t box[2] = {box_cols, box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, dtype, 2, const_cast<void*>(base), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
 }
