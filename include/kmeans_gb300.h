@@ -64,7 +64,7 @@ KMGB_EXPORT const char* kmeansGetErrorString(kmeansErrorStatus err);
  * reference). initAlgorithm 1 (an extension) draws k-means++ centers with seeds 0 ..
  * numRetries-1 and keeps the run with the lowest final SSE; result then receives that run's
  * initial centers before its final ones. doFullSGEMM (0/1/2) and matrixFormat (0/1) are accepted and
- * all map to the same fused assignment: the split BF16 tensor-core tier when n <= 256, the FP32
+ * all map to the same fused assignment: the split BF16 tensor-core tier when n <= 320, the FP32
  * tier above (the labels are the certified FP64 arg-min in both; the environment variable
  * KMGB_ASSIGN=fp32|bf16|bf16x3 picks a tier). miniBatchFraction < 1 selects the reference's
  * sliding mini-batch windows. Returns KMEANS_NONCONVERGENCE (13) when the relative SSE change
@@ -82,7 +82,7 @@ KMGB_EXPORT kmeansErrorStatus computeKmeansF(const float* data, const int m, con
 /* Replaces computeKmeansD (main/cpp/kmeans.hpp:127-132, main/cpp/kmeans.cpp:1364-1409), with
  * computeKmeansF's arguments and layouts on FP64 data. Labels are the FP64 arg-min of the
  * direct distance (lowest index on ties); centers are canonical FP64 sums over the counts. Full
- * batches with n <= 256 assign on the tensor cores (the split BF16 tier on FP32 roundings of the
+ * batches with n <= 320 assign on the tensor cores (the split BF16 tier on FP32 roundings of the
  * data and centers, its bound widened by that rounding, the uncertified points rescanned in
  * FP64); mini-batch windows, wider data and KMGB_ASSIGN=fp32 use the FP64 scan for every point. */
 KMGB_EXPORT kmeansErrorStatus computeKmeansD(const double* data, const int m, const int n, const int k,

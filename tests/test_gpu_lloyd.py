@@ -361,9 +361,9 @@ def test_reference_test_configurations(km, orc, torch_cuda, kind, m, n, k, iters
     assert km.computeKmeansF(X, m, n, k, rtol, iters, 1, 0, 1, 0, result_cublas, 1.0) == rc
     assert np.array_equal(result_cublas, result, equal_nan=True)
 
-    # computeKmeansF runs the split BF16 tier where D <= 256, FP32 above; the labels (and so the
+    # computeKmeansF runs the split BF16 tier where D <= 320, FP32 above; the labels (and so the
     # centers) are the certified FP64 arg-min's in either
-    tier = km.ASSIGN_BF16X3 if n <= 256 else km.ASSIGN_FP32
+    tier = km.ASSIGN_BF16X3 if n <= 320 else km.ASSIGN_FP32
     full = km.lloyd(X, k, max_iters=iters, criterion=rtol, assign_tier=tier)
     t = full.iterations
     assert full.status == rc
