@@ -367,6 +367,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
   // chunks of C from L2. Every role of both CTAs derives the same sequence (false: skipped unit).
   struct UnitInfo {
     int nch, rot, cbase;
+    int cend;  // end of the unit's problem's centers (its chunks are padded to 256 past it)
     long long rend;
   };
   auto unit_info = [&](long long u, UnitInfo& ui) -> bool {
@@ -374,12 +375,14 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       ui.nch = nchunks;
       ui.cbase = 0;
       ui.rend = n_rows;
+      ui.cend = p.k;
     } else {
       const int pr = p.u_prob[u];
       if (p.g_done && p.g_done[pr]) return false;
       ui.nch = (p.g_k[pr] + BN - 1) / BN;
       ui.cbase = p.g_coff[pr];
       ui.rend = p.g_rend[pr];
+      ui.cend = ui.cbase + p.g_k[pr];
     }
     ui.rot = (int)(pair % ui.nch);
     return true;
@@ -629,6 +632,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         if (lane == 0) mbar_arrive_remote(b ? acc_empty_leader1 : acc_empty_leader0);
 #pragma unroll
         for (int cb = 0; cb < COLS_PER_WARP / 32; ++cb) {
+          // a 32-column block wholly past the problem's centers holds padding only (unusable
+          // start values): nothing to fold (the MMAs ran over it all the same)
+          if (BIAS && col0 + cb * 32 >= ui.cend) continue;
           uint32_t (&cur)[32] = v[cb];
           // key = x.c - ||c||^2/2: the accumulator plus the column's start value (FMA pipe);
           // padding and unusable centers carry a huge negative start value

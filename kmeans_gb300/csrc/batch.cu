@@ -333,7 +333,7 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       f.set(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)K * ldx, s), E, "centers"))
     return f.code;
   // tensor-core tiers: BF16 planes of the points and centers, the centers' start values
-  void *Xb = nullptr, *Xl = nullptr, *Cb = nullptr, *Cl = nullptr;
+  void *Xb = nullptr, *Xl = nullptr, *Cb = nullptr, *Cl = nullptr, *cbias = nullptr;
   float* cinit = nullptr;
   int* d_unit_prob = nullptr;
   if (tc &&
@@ -344,6 +344,8 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
        (split && f.set(m.alloc(reinterpret_cast<uint16_t**>(&Cl), (size_t)K * ldb), E,
                        "BF16 centers")) ||
        f.set(m.alloc(&cinit, (size_t)rup(K, kCenterPad)), E, "BF16 centers") ||
+       f.set(m.alloc(reinterpret_cast<uint16_t**>(&cbias), (size_t)rup(K, kCenterPad) * kBiasCols),
+             E, "BF16 centers") ||
        f.set(m.upload(&d_unit_prob, unit_prob, s), E, "tables")))
     return f.code;
   // data: host problems are packed by host threads into two pinned staging buffers in the
@@ -471,6 +473,7 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
   a.gamma = tc ? assign_bf16_gamma(d) : assign_fp32_gamma(d);
   if (tc) {
     a.cinit = cinit;
+    a.cbias = cbias;  // start values by MMA; padding blocks of a problem's last chunk are skipped
     a.u_prob = d_unit_prob;
     a.g_coff = d_coff;
     a.g_k = d_k;
@@ -527,7 +530,7 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
     auto mk = [&]() { return !marks || mark(); };
     return mk() && !f.set(cudaMemsetAsync(cmax, 0, sizeof(float), s), EU, "centers") &&
            !f.set(launch_prep_centers(C, ldx, (int)K, d, Cop, Cb, ldb, cn, cmax, s, nullptr,
-                                      cinit, Cl),
+                                      cinit, Cl, cbias),
                   EU, "center preparation") &&
            !f.set(cudaMemsetAsync(rr_count, 0, sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS,
                   "re-rank") &&

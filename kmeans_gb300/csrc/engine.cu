@@ -787,6 +787,7 @@ RouterIO router_io(kmgb_handle* h) {
   io.Cl = h->Cl;
   io.cn = h->cn;
   io.cinit = h->cinit;
+  io.cbias = h->cbias;
   io.cmax = h->cmax;
   io.labels = h->labels;
   io.err = h->err;

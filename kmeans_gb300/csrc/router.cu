@@ -37,6 +37,8 @@
 #include <random>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "../../include/kmeans_gb300.h"
 #include "common.cuh"
 #include "kernels.h"
@@ -249,9 +251,20 @@ __global__ void permute_centers_kernel(const int* __restrict__ cperm, long long 
                                        const float* __restrict__ cn, uint4* __restrict__ CbP,
                                        uint4* __restrict__ ClP, float4* __restrict__ CopP,
                                        float* __restrict__ cinitP, float* __restrict__ cnP,
+                                       const uint4* __restrict__ cbias, uint4* __restrict__ cbiasP,
                                        const int* stop) {
   if (stopped(stop)) return;
   const int lane = threadIdx.x & 31;
+  // the start-value row of a padding slot: -3e38 as three BF16 pieces, then zeros
+  uint4 pad_bias = make_uint4(0, 0, 0, 0);
+  if (cbias) {
+    const __nv_bfloat16 hi = __float2bfloat16_rn(-3.0e38f);
+    const float r1 = -3.0e38f - __bfloat162float(hi);
+    const __nv_bfloat16 mid = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
+    pad_bias.x = (uint32_t)__bfloat16_as_ushort(hi) | ((uint32_t)__bfloat16_as_ushort(mid) << 16);
+    pad_bias.y = (uint32_t)__bfloat16_as_ushort(lo);
+  }
   for (long long j = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; j < KP;
        j += ((long long)gridDim.x * blockDim.x) >> 5) {
     const int c = cperm[j];
@@ -265,6 +278,8 @@ __global__ void permute_centers_kernel(const int* __restrict__ cperm, long long 
       cinitP[j] = c >= 0 ? cinit[c] : -3.0e38f;
       cnP[j] = c >= 0 ? cn[c] : INFINITY;
     }
+    if (cbias && lane < kBiasCols * 2 / 16)  // 32-byte rows: two uint4 per slot
+      cbiasP[j * 2 + lane] = c >= 0 ? cbias[(size_t)c * 2 + lane] : (lane ? make_uint4(0, 0, 0, 0) : pad_bias);
   }
 }
 
@@ -674,7 +689,7 @@ struct Router {
   int* m2 = nullptr;
   double* m0 = nullptr;
   // permuted centers
-  void *CbP = nullptr, *ClP = nullptr;
+  void *CbP = nullptr, *ClP = nullptr, *cbiasP = nullptr;
   float *CopP = nullptr, *cinitP = nullptr, *cnP = nullptr;
   // routing
   int *route = nullptr, *rowmap = nullptr, *labR = nullptr, *flagR = nullptr;
@@ -734,6 +749,7 @@ struct Router {
     if (split) c.take_bytes(&ClP, (size_t)KPmax * ldb * 2);
     c.take(&CopP, (size_t)KPmax * ldx);
     c.take(&cinitP, KPmax);
+    c.take_bytes(&cbiasP, (size_t)KPmax * kBiasCols * 2);
     c.take(&cnP, KPmax);
     c.take(&route, n);
     c.take(&rowmap, rows_cap);
@@ -1047,7 +1063,7 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
       r->cperm, r->KP, static_cast<const uint4*>(io.Cb), static_cast<const uint4*>(io.Cl), vb,
       reinterpret_cast<const float4*>(io.Cop), vx, io.cinit, io.cn, static_cast<uint4*>(r->CbP),
       io.Cl ? static_cast<uint4*>(r->ClP) : nullptr, reinterpret_cast<float4*>(r->CopP), r->cinitP,
-      r->cnP, io.stop);
+      r->cnP, static_cast<const uint4*>(io.cbias), static_cast<uint4*>(r->cbiasP), io.stop);
   count_launches(1);
   KMGB_CUDA_TRY(r->mark(s));
   // inference: hidden layer (store mode), then the group (arg-max mode), in row chunks
@@ -1105,6 +1121,7 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
   a.xnorm = r->xnR;
   a.cmax = io.cmax;
   a.cinit = r->cinitP;
+  a.cbias = io.cbias ? r->cbiasP : nullptr;  // start values by MMA, padding blocks skipped
   a.labels = r->labR;
   a.rerank_list = r->flagR;
   a.rerank_count = r->rcount;

@@ -53,6 +53,8 @@ struct RouterIO {
   const void* Cl;       // k x ldb BF16 residual of the centers, or null (plain tier)
   const float* cn;      // [k] fl(||c||^2), +inf for unusable centers
   const float* cinit;   // [round_up(k, 256)] -||c||^2/2, unusable: -3e38
+  const void* cbias;    // nullable: the same as BF16 pieces (kBiasCols per center), see
+                        // launch_prep_centers
   const float* cmax;    // device scalar: max ||c|| over usable centers
   int* labels;          // [n] out: labels of the certified points
   int* err;             // device error word
