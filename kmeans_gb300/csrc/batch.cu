@@ -320,6 +320,11 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
   double* qn = nullptr;
   int *labels = nullptr, *rr_list = nullptr, *rr_count = nullptr, *err = nullptr;
   unsigned long long* rr_stats = nullptr;
+  // flagged rows' FP32 bands as candidates for the candidate resolve (FP32, then float-float,
+  // FP64 only on near ties); rows past the capacity or with too many candidates take the exact
+  // grouped pass (FP32 band, then FP64)
+  const long long cand_cap = std::min<long long>(nvalid, 1LL << 20);
+  int *cand = nullptr, *cand_cnt = nullptr, *rr_over = nullptr, *over_count = nullptr;
   if (f.set(m.alloc(&X, (size_t)rows * ldx), E, "data") ||
       f.set(cudaMemsetAsync(X, 0, sizeof(float) * (size_t)rows * ldx, s), E, "data") ||
       f.set(m.alloc(&xn, rows), E, "norms") || f.set(m.alloc(&qn, rows), E, "norms") ||
@@ -328,6 +333,10 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       f.set(m.alloc(&cmax, 1), E, "centers") || f.set(m.alloc(&labels, rows), E, "labels") ||
       f.set(m.alloc(&rr_list, nvalid), E, "re-rank") || f.set(m.alloc(&rr_count, 1), E, "re-rank") ||
       f.set(m.alloc(&rr_stats, 2), E, "re-rank") || f.set(m.alloc(&err, 1), E, "error word") ||
+      f.set(m.alloc(&cand, (size_t)cand_cap * kMaxCand), E, "re-rank") ||
+      f.set(m.alloc(&cand_cnt, cand_cap), E, "re-rank") ||
+      f.set(m.alloc(&rr_over, cand_cap), E, "re-rank") ||
+      f.set(m.alloc(&over_count, 1), E, "re-rank") ||
       f.set(cudaMemsetAsync(rr_stats, 0, 2 * sizeof(unsigned long long), s), E, "re-rank") ||
       f.set(cudaMemsetAsync(err, 0, sizeof(int), s), E, "error word") ||
       f.set(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)K * ldx, s), E, "centers"))
@@ -495,6 +504,11 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
   ra.d = d;
   ra.mode = 0;
   ra.max_list = nvalid;
+  RerankArgs rx = ra;  // the exact pass over what the candidate resolve left
+  rx.list = rr_over;
+  rx.count = over_count;
+  rx.max_list = cand_cap;
+  rx.stats = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   if (f.set(cudaEventCreate(&ev[0]), EU, "events") || f.set(cudaEventCreate(&ev[1]), EU, "events") ||
       f.set(cudaEventRecord(ev[0], s), EU, "events")) {
@@ -539,8 +553,16 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
                      : launch_assign_fp32(X, ldx, Cop, ldx, a, s, &g, tiles),
                   KMEANS_ERROR_CLOSEST_CENTERS, "assignment") &&
            mk() &&
-           !(o.certify && f.set(launch_rerank_grouped(ra, g, s), KMEANS_ERROR_CLOSEST_CENTERS,
-                                "re-rank")) &&
+           !(o.certify &&
+             (f.set(cudaMemsetAsync(over_count, 0, sizeof(int), s), KMEANS_ERROR_CLOSEST_CENTERS,
+                    "re-rank") ||
+              f.set(launch_rerank_grouped(ra, g, s, cand, cand_cnt, cand_cap),
+                    KMEANS_ERROR_CLOSEST_CENTERS, "re-rank") ||
+              f.set(launch_resolve_candidates(rr_list, rr_count, cand_cap, cand, cand_cnt, X, ldx,
+                                              Cop, ldx, cn, d, labels, rr_over, over_count,
+                                              nullptr, s),
+                    KMEANS_ERROR_CLOSEST_CENTERS, "re-rank") ||
+              f.set(launch_rerank_grouped(rx, g, s), KMEANS_ERROR_CLOSEST_CENTERS, "re-rank"))) &&
            mk() &&
            !f.set(launch_update_batched(X, ldx, d, qn, labels, C, ldx, o.empty_policy, w, b, s),
                   EU, "update") &&

@@ -126,7 +126,12 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, fl
                                 cudaStream_t s);
 // Grouped problems (batched Lloyd): one CTA per flagged row over its own problem's centers
 // (FP32 band, then FP64); a.C / a.cn cover all problems' centers, a.stats (nullable) counts.
-cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaStream_t s);
+// With cand (capacity cand_cap list slots of kMaxCand): flagged rows in slots below cand_cap only
+// record their FP32 band as candidates (cand_cnt -1 past kMaxCand) for launch_resolve_candidates;
+// the others, and every row without cand, are settled here (FP32 band, then FP64).
+cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaStream_t s,
+                                  int* cand = nullptr, int* cand_cnt = nullptr,
+                                  long long cand_cap = 0);
 // FP64 stage over list2 (one CTA per point), candidates bounded by hi2.
 cudaError_t launch_rerank_exact(const RerankArgs& a, const float* hi2, cudaStream_t s);
 // Candidate re-rank of the BF16 tiers: compact copy of up to `cap` flagged rows (the rest go to

@@ -435,7 +435,8 @@ constexpr int RG_VCAP = 512;
 constexpr int RG_WARPS = 8;
 
 __global__ void __launch_bounds__(RG_WARPS * 32)
-rerank_grouped_kernel(RerankArgs a, GroupArgs g) {
+rerank_grouped_kernel(RerankArgs a, GroupArgs g, int* __restrict__ cand, int* __restrict__ cand_cnt,
+                      long long cand_cap) {
   if (stopped(a.stop)) return;
   extern __shared__ float rg_smem[];  // [warps][RG_VCAP] values, then [warps][d] rows
   const long long cnt = min((long long)*(volatile const int*)a.count, a.max_list);
@@ -486,6 +487,29 @@ rerank_grouped_kernel(RerankArgs a, GroupArgs g) {
     }
     __syncwarp();
     const float best_hi = lo * (1.0f + gam) + 1e-30f;
+    if (cand && slot < cand_cap) {
+      // record the band (every center whose FP64 distance can be the minimum) for the
+      // candidate resolve's FP32 and float-float tiers; more than kMaxCand: the exact pass
+      int n_in = 0;
+      for (int j0 = 0; j0 < kp; j0 += 32) {
+        const int j = j0 + lane;
+        bool in = false;
+        if (j < kp && a.cn[cbeg + j] < INFINITY) {
+          const float v = keep ? vals[j] : approx_value(0, xs, a.C + (size_t)(cbeg + j) * a.ldc,
+                                                        a.d, 0.0f);
+          in = v * (1.0f - gam) - 1e-30f <= best_hi;
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, in);
+        const int at = n_in + __popc(bal & ((1u << lane) - 1u));
+        if (in && at < kMaxCand) cand[slot * kMaxCand + at] = cbeg + j;
+        n_in += __popc(bal);
+      }
+      if (lane == 0) {
+        cand_cnt[slot] = n_in <= kMaxCand ? n_in : -1;
+        if (a.stats) atomicAdd(a.stats, 1ull);
+      }
+      continue;
+    }
     double best = INFINITY;
     int bidx = -1;
     for (int j = lane; j < kp; j += 32) {
@@ -994,14 +1018,16 @@ cudaError_t launch_rerank_tiled(const RerankArgs& a, int* list2, int* count2, fl
   return cudaGetLastError();
 }
 
-cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaStream_t s) {
+cudaError_t launch_rerank_grouped(const RerankArgs& a, const GroupArgs& g, cudaStream_t s,
+                                  int* cand, int* cand_cnt, long long cand_cap) {
   if (a.n <= 0 || a.k <= 0) return cudaSuccess;
   const size_t smem = sizeof(float) * (size_t)RG_WARPS * (RG_VCAP + (size_t)a.d);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
   if (smem > 48 * 1024)
     KMGB_CUDA_TRY(cudaFuncSetAttribute(rerank_grouped_kernel,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  rerank_grouped_kernel<<<kmgb::num_sms() * 4, RG_WARPS * 32, smem, s>>>(a, g);
+  rerank_grouped_kernel<<<kmgb::num_sms() * 4, RG_WARPS * 32, smem, s>>>(a, g, cand, cand_cnt,
+                                                                          cand_cap);
   count_launches(1);
   return cudaGetLastError();
 }
