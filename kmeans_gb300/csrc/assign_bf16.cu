@@ -619,13 +619,17 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           break;
         }
         tc_fence_after();
-        const int col0 = ui.cbase + chunk_of(ui, c) * BN + h * COLS_PER_WARP;  // first center
-        const uint32_t base = lane_addr + (uint32_t)(b * BN + h * COLS_PER_WARP);
+        // the chunk's 32-column blocks are dealt to the EPQ column slices in turn (block cb of
+        // slice h is block cb * EPQ + h), so that a problem's last, partly padded chunk spreads
+        // its real blocks over all slices
+        const int chunk0 = ui.cbase + chunk_of(ui, c) * BN;  // first center of the chunk
+        const uint32_t base = lane_addr + (uint32_t)(b * BN);
         // all of this warp's columns into registers at once, then the buffer goes straight back
         // to the leader's MMA issuer and the folding below overlaps the next MMAs
         uint32_t v[COLS_PER_WARP / 32][32];
 #pragma unroll
-        for (int cb = 0; cb < COLS_PER_WARP / 32; ++cb) tmem_ld32(base + cb * 32, v[cb]);
+        for (int cb = 0; cb < COLS_PER_WARP / 32; ++cb)
+          tmem_ld32(base + (uint32_t)((cb * EPQ + h) * 32), v[cb]);
         tmem_ld_wait();
         tc_fence_before();
         __syncwarp();
@@ -634,12 +638,13 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         for (int cb = 0; cb < COLS_PER_WARP / 32; ++cb) {
           // a 32-column block wholly past the problem's centers holds padding only (unusable
           // start values): nothing to fold (the MMAs ran over it all the same)
-          if (BIAS && col0 + cb * 32 >= ui.cend) continue;
+          const int bcol = chunk0 + (cb * EPQ + h) * 32;  // first center of the block
+          if (BIAS && bcol >= ui.cend) continue;
           uint32_t (&cur)[32] = v[cb];
           // key = x.c - ||c||^2/2: the accumulator plus the column's start value (FMA pipe);
           // padding and unusable centers carry a huge negative start value
           {
-            const float4* hs = reinterpret_cast<const float4*>(p.cinit + (size_t)col0 + cb * 32);
+            const float4* hs = reinterpret_cast<const float4*>(p.cinit + (size_t)bcol);
             if (fp8) {
 #pragma unroll
               for (int j4 = 0; j4 < 8; ++j4) {
@@ -666,7 +671,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             if (prow < n_rows) {
               uint4* dst = reinterpret_cast<uint4*>(
                   static_cast<__nv_bfloat16*>(p.store_out) +
-                  (size_t)(p.out0 + prow) * (size_t)p.store_ld + col0 + cb * 32);
+                  (size_t)(p.out0 + prow) * (size_t)p.store_ld + bcol);
 #pragma unroll
               for (int q4 = 0; q4 < 4; ++q4) {
                 uint32_t w[4];
@@ -688,7 +693,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
           }
           if (p.dump) {  // diagnostic: keys of this point before the column bits are packed
             if (prow < n_rows) {
-              float* dst = p.dump + (size_t)prow * (size_t)((p.k + kCenterPad - 1) / kCenterPad * kCenterPad) + col0 + cb * 32;
+              float* dst = p.dump + (size_t)prow * (size_t)((p.k + kCenterPad - 1) / kCenterPad * kCenterPad) + bcol;
 #pragma unroll
               for (int j = 0; j < 32; ++j) dst[j] = __uint_as_float(cur[j]);
             }
@@ -702,7 +707,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
               if (key >= floor_key) {
                 if (ncand < CAND_PER_WARP && prow < n_rows)
                   p.cand[(size_t)(p.row0 + prow) * kMaxCand + h * CAND_PER_WARP + ncand] =
-                      col0 + cb * 32 + j;
+                      bcol + j;
                 ++ncand;
               }
             }
@@ -711,7 +716,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
             uint32_t msk;  // ~31 in a register (see packed_key)
             asm volatile("mov.b32 %0, 0xFFFFFFE0;" : "=r"(msk));
             top2_block(cur, msk, b1, b2, std::make_integer_sequence<int, 16>{});
-            if (b1 != blk_before) bblk = (col0 >> 5) + cb;  // 32-column block of the best
+            if (b1 != blk_before) bblk = bcol >> 5;  // 32-column block of the best
           }
         }
       }
