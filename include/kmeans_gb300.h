@@ -300,7 +300,7 @@ typedef struct kmgb_router_stats {
   long long device_bytes;       /* device memory of the router (fallback buffers excluded) */
   double stage_ms[7];           /* with profiling on (kmgb_set_profiling): CUDA-event ms of the
                                    routed assignment's stages summed over the routed iterations:
-                                   center separation, centers in group order, network inference,
+                                   centers in group order, center separation, network inference,
                                    sort by group, group scan, in-group near ties, certificate */
   long long reserved[4];
 } kmgb_router_stats;

@@ -100,7 +100,7 @@ class kmgb_router_stats(C.Structure):
                 ("routed_iterations", C.c_longlong), ("device_bytes", C.c_longlong),
                 ("stage_ms", C.c_double * 7), ("reserved", C.c_longlong * 4)]
 
-    STAGES = ("separation", "permute_centers", "inference", "sort", "group_scan",
+    STAGES = ("permute_centers", "separation", "inference", "sort", "group_scan",
               "near_ties", "certificate")
 
     def as_dict(self):

@@ -316,7 +316,7 @@ struct MergeSlot {
 // the start values enter by MMA (AssignArgs::cbias) and the epilogue adds nothing. One CTA per
 // SM: each SM sub-partition's 16K registers hold ceil(warps / 4) warps, so a thread may use 168
 // registers with EPQ 2 (10 warps) and 96 with EPQ 4 (18 warps).
-template <int EPQ, bool F8, bool BIAS>
+template <int EPQ, bool F8, bool BIAS, bool XMAX = false>
 __global__ void __launch_bounds__(threads_for(EPQ), 1)
 assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmXl,
                    const __grid_constant__ CUtensorMap tmC, const __grid_constant__ CUtensorMap tmCl,
@@ -582,7 +582,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
     const int q = warp & 3;       // TMEM lane quadrant this warp may access
     const int h = e >> 2;         // column slice of the chunk (0 .. EPI_PER_QUAD-1)
     const uint32_t lane_addr = tmem_base + ((uint32_t)(q * 32) << 16);
-    const float cm = p.certify ? __ldg(p.cmax) : 0.0f;
+    const float cm = (p.certify || XMAX) ? __ldg(p.cmax) : 0.0f;
     const uint32_t acc_empty_leader0 = map_to_rank(smem_u32(&bars.acc_empty[0]), 0);
     const uint32_t acc_empty_leader1 = map_to_rank(smem_u32(&bars.acc_empty[1]), 0);
 
@@ -603,8 +603,11 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
       if (cand_mode && prow < n_rows) floor_key = __ldg(p.thr_in + p.row0 + prow);
       // the point's norm bound is needed only after the last chunk: load it now so that its
       // HBM latency hides behind the unit's chunks
-      const float xn_pt = (p.certify && !cand_mode && h == 0 && prow < n_rows)
+      const float xn_pt = ((p.certify || XMAX) && !cand_mode && h == 0 && prow < n_rows)
                               ? __ldg(p.xnorm + p.out0 + prow) : 0.0f;
+      // separation mode: the unit's rows (one group: groups fill whole 256-row units) skip the
+      // chunks of their own group
+      const int unit_group = XMAX ? __ldg(p.slot_group + u * UNIT) : 0;
       // FP8 tier: the row's scale and the accumulator multiplier sx * sc (a power of two)
       const float sx_pt = (fp8 && prow < n_rows)
                               ? __ldg(p.xscale + (cand_mode ? p.row0 : p.out0) + prow) : 0.0f;
@@ -634,6 +637,7 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive_remote(b ? acc_empty_leader1 : acc_empty_leader0);
+        if (XMAX && __ldg(p.slot_group + chunk0) == unit_group) continue;
 #pragma unroll
         for (int cb = 0; cb < COLS_PER_WARP / 32; ++cb) {
           // a 32-column block wholly past the problem's centers holds padding only (unusable
@@ -711,6 +715,9 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
                 ++ncand;
               }
             }
+          } else if (XMAX) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) b1 = fmaxf(b1, __uint_as_float(cur[j]));
           } else {
             const float blk_before = b1;
             uint32_t msk;  // ~31 in a register (see packed_key)
@@ -775,6 +782,12 @@ assign_bf16_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constan
         b2 = nb2;
       }
       const long long pt = p.out0 + prow;  // row of the data set
+      if (XMAX) {  // an upper bound of the largest exact key over the other groups' centers
+        if (prow < n_rows)
+          p.xmax_out[pt] = b1 > -1.0e38f ? __fadd_ru(b1, bound_acc(xn_pt, cm, p.d, mode, bias))
+                                          : -INFINITY;
+        continue;
+      }
       if (prow < n_rows) {
         const bool none = !(b1 > -1.0e38f);  // no usable center at all
         // no usable center at all: the first center of the point's problem
@@ -815,10 +828,11 @@ struct VariantInfo {
   size_t smem_budget = 0;  // 1 KB aligned
   size_t static_bytes = 0;
 };
-VariantInfo g_variant[6];  // [0] FP8, [2] split BF16, [4] plain BF16, [3] / [5]: with start-value MMA
+VariantInfo g_variant[8];  // [0] FP8, [2] split BF16, [4] plain BF16, [3] / [5]: with start-value MMA,
+                           // [6] / [7]: separation mode (split / plain)
 int g_num_sms = 0;
 
-template <int EPQ, bool F8, bool BIAS>
+template <int EPQ, bool F8, bool BIAS, bool XMAX = false>
 cudaError_t prepare_variant(VariantInfo& vi) {
   if (vi.ready) return cudaSuccess;
   int dev = 0, optin = 0;
@@ -826,12 +840,12 @@ cudaError_t prepare_variant(VariantInfo& vi) {
   KMGB_CUDA_TRY(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
   KMGB_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   cudaFuncAttributes fa;
-  KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel<EPQ, F8, BIAS>));
+  KMGB_CUDA_TRY(cudaFuncGetAttributes(&fa, assign_bf16_kernel<EPQ, F8, BIAS, XMAX>));
   // the dynamic area starts on the next 1 KB boundary after the static variables
   vi.static_bytes = (fa.sharedSizeBytes + 1023) / 1024 * 1024;
   size_t budget = (size_t)optin > vi.static_bytes ? (size_t)optin - vi.static_bytes : 0;
   if (budget > SMEM_CAP) budget = SMEM_CAP;
-  KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel<EPQ, F8, BIAS>,
+  KMGB_CUDA_TRY(cudaFuncSetAttribute(assign_bf16_kernel<EPQ, F8, BIAS, XMAX>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)budget));
   vi.smem_budget = budget;
   cudaLaunchConfig_t qc = {};
@@ -845,7 +859,7 @@ cudaError_t prepare_variant(VariantInfo& vi) {
   qa[0].val.clusterDim.z = 1;
   qc.attrs = qa;
   qc.numAttrs = 1;
-  KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&vi.max_pairs, assign_bf16_kernel<EPQ, F8, BIAS>, &qc));
+  KMGB_CUDA_TRY(cudaOccupancyMaxActiveClusters(&vi.max_pairs, assign_bf16_kernel<EPQ, F8, BIAS, XMAX>, &qc));
   if (vi.max_pairs <= 0) return cudaErrorInvalidConfiguration;
   vi.ready = true;
   return cudaSuccess;
@@ -952,7 +966,9 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   AssignArgs ab = a;
   if (ab.store_out) ab.cbias = nullptr;
   const size_t planes_bytes = (size_t)(mode > 1 ? 2 : 1) * CKB_BYTES;
-  if (ab.cbias && 2 * xbytes + 2 * (planes_bytes + BIAS_BYTES) + ONES_BYTES > lim) ab.cbias = nullptr;
+  // (the separation mode needs them: one point buffer is enough there)
+  if (ab.cbias && (ab.xmax_out ? 1 : 2) * xbytes + 2 * (planes_bytes + BIAS_BYTES) + ONES_BYTES > lim)
+    ab.cbias = nullptr;
   const bool bias = ab.cbias != nullptr;
   const size_t stage_bytes = planes_bytes + (bias ? BIAS_BYTES : 0);
   const size_t extra = bias ? ONES_BYTES : 0;
@@ -1000,6 +1016,22 @@ cudaError_t launch_assign_bf16(const void* Xb, const void* Xl, long long ldxb, c
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
+  if (ab.xmax_out) {  // separation mode: start values by MMA, rows and chunks of whole groups
+    if (!bias || !ab.slot_group || ab.u_prob || ab.thr_in || ab.certify)
+      return cudaErrorInvalidValue;
+    VariantInfo& vx = g_variant[epq == 2 ? 6 : 7];
+    if (epq == 2) KMGB_CUDA_TRY((prepare_variant<2, false, true, true>(vx)));
+    else KMGB_CUDA_TRY((prepare_variant<4, false, true, true>(vx)));
+    if (vx.smem_budget < smem || vx.max_pairs < pairs) return cudaErrorInvalidConfiguration;
+    if (epq == 2)
+      KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<2, false, true, true>, tmX, tmXl,
+                                       tmC, tmCl, tmB, ab, stages, xbufs, mode));
+    else
+      KMGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, assign_bf16_kernel<4, false, true, true>, tmX, tmXl,
+                                       tmC, tmCl, tmB, ab, stages, xbufs, mode));
+    count_launches(1);
+    return cudaSuccess;
+  }
   if (bias) {  // the bias variants' launch limits (occupancy, shared memory) are set up too
     VariantInfo& vb = g_variant[epq + 1];
     if (epq == 2) KMGB_CUDA_TRY((prepare_variant<2, false, true>(vb)));

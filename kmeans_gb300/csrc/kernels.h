@@ -57,6 +57,13 @@ struct AssignArgs {
   void* store_out;
   long long store_ld;
   int store_relu;
+  // BF16 tiers, separation mode (the router; null otherwise): X and C are the same centers in
+  // group order, every 256-row unit and 256-center chunk inside one group (slot_group[slot]);
+  // for every row xmax_out receives an upper bound of the largest exact key x.c - |c|^2/2 over
+  // the centers of the other groups (-inf if none), the epilogue skipping the row's own group's
+  // chunks; needs cbias, no certificate, no labels
+  float* xmax_out;
+  const int* slot_group;
   // FP8 tier (fp8 = 1): X and C are E4M3 copies, rows of ld bytes (launch_assign_bf16's ldxb /
   // ldcb count bytes); key = acc * (xscale[row] * *cscale) + cinit[j]; xscale is indexed like
   // thr_in in the candidate pass (row0 + row) and like xnorm otherwise (out0 + row)

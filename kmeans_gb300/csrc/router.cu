@@ -23,8 +23,11 @@
 //      as the arg-min over ALL centers when 2 d(x, c*) < m(c*), m(c*) a lower bound of the
 //      distance from c* to every usable center outside its group: for such a center c,
 //      d(x, c) >= d(c*, c) - d(x, c*) > 2 d(x, c*) - d(x, c*) = d(x, c*). m is computed for the
-//      current centers every routed iteration (centers_pair_kernel, min mode, with a rigorous
-//      bound of its FP32 rounding). (A bound carried over from the last training and lowered by
+//      current centers every routed iteration: on the tensor cores by the pair kernel's
+//      separation mode over the centers in group order (each row's largest key over the other
+//      groups, plus the tier's rounding bound), or by centers_pair_kernel's min mode (FP32 SIMT,
+//      with a rigorous bound of its FP32 rounding) where that mode cannot launch. (A bound
+//      carried over from the last training and lowered by
 //      the centers' movement since was tried first: one far-moving center in an early iteration
 //      lowered every center's bound and left 16% of the points certified instead of most.)
 //      Points that fail any step go to the full scan, so labels equal the FP64 arg-min.
@@ -243,6 +246,28 @@ __global__ void m0_kernel(const int* m2bits, int k, double* m0) {
   }
 }
 
+// Separation from the tensor-core pass: for slot j (center c = cperm[j]) every center c' of
+// another group has d^2(c, c') = ||c||^2 - 2 key(c, c') >= cn (1 - 2^-23) - 2 xmax[j] (xmax an
+// upper bound of the exact keys, cn ||c||^2 rounded to nearest), evaluated with downward
+// rounding; min-reduced like the SIMT kernel's output (non-negative float bits).
+__global__ void m2_from_xmax_kernel(const int* __restrict__ cperm, long long KP,
+                                    const float* __restrict__ cnP, const float* __restrict__ xmax,
+                                    int* __restrict__ m2bits, const int* stop) {
+  if (stopped(stop)) return;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < KP;
+       j += (long long)gridDim.x * blockDim.x) {
+    const int c = cperm[j];
+    if (c < 0 || !(cnP[j] < INFINITY)) continue;
+    const float xm = xmax[j];
+    float v = INFINITY;  // no usable center in another group
+    if (xm > -INFINITY) {
+      const double lb = __dsub_rd(__dmul_rd((double)cnP[j], 1.0 - 0x1p-23), 2.0 * (double)xm);
+      v = lb > 0.0 ? __double2float_rd(lb) : 0.0f;
+    }
+    m2bits[c] = __float_as_int(v);
+  }
+}
+
 // Centers in group order: slot j holds center cperm[j] (or padding: zero rows, unusable).
 __global__ void permute_centers_kernel(const int* __restrict__ cperm, long long KP,
                                        const uint4* __restrict__ Cb, const uint4* __restrict__ Cl,
@@ -252,7 +277,7 @@ __global__ void permute_centers_kernel(const int* __restrict__ cperm, long long 
                                        uint4* __restrict__ ClP, float4* __restrict__ CopP,
                                        float* __restrict__ cinitP, float* __restrict__ cnP,
                                        const uint4* __restrict__ cbias, uint4* __restrict__ cbiasP,
-                                       const int* stop) {
+                                       float* __restrict__ xnP, const int* stop) {
   if (stopped(stop)) return;
   const int lane = threadIdx.x & 31;
   // the start-value row of a padding slot: -3e38 as three BF16 pieces, then zeros
@@ -277,6 +302,8 @@ __global__ void permute_centers_kernel(const int* __restrict__ cperm, long long 
     if (lane == 0) {
       cinitP[j] = c >= 0 ? cinit[c] : -3.0e38f;
       cnP[j] = c >= 0 ? cn[c] : INFINITY;
+      // ||c|| <= sqrt(cn (1 + 2^-24)): cn is ||c||^2 rounded to nearest
+      if (xnP) xnP[j] = (c >= 0 && cn[c] < INFINITY) ? __fsqrt_ru(cn[c]) * 1.000001f : 0.0f;
     }
     if (cbias && lane < kBiasCols * 2 / 16)  // 32-byte rows: two uint4 per slot
       cbiasP[j * 2 + lane] = c >= 0 ? cbias[(size_t)c * 2 + lane] : (lane ? make_uint4(0, 0, 0, 0) : pad_bias);
@@ -683,6 +710,7 @@ struct Router {
   size_t arena_bytes = 0;
   bool grouped = false, trained = false;
   std::vector<int> group_h;
+  std::vector<int> slot_group_h;  // host copy kept alive for the asynchronous upload
   // groups and certificate
   int *group = nullptr, *cperm = nullptr, *gcoff = nullptr, *gk = nullptr, *par = nullptr;
   float* thr = nullptr;
@@ -691,6 +719,10 @@ struct Router {
   // permuted centers
   void *CbP = nullptr, *ClP = nullptr, *cbiasP = nullptr;
   float *CopP = nullptr, *cinitP = nullptr, *cnP = nullptr;
+  // separation on the tensor cores: the group of every slot, ||c|| bounds of the slots, and
+  // the bound of every slot's largest key over the other groups
+  int* slot_group = nullptr;
+  float *xnP = nullptr, *xmaxP = nullptr;
   // routing
   int *route = nullptr, *rowmap = nullptr, *labR = nullptr, *flagR = nullptr;
   int *candR = nullptr, *ccntR = nullptr, *uprob = nullptr, *gcnt = nullptr, *fill = nullptr;
@@ -750,6 +782,9 @@ struct Router {
     c.take(&CopP, (size_t)KPmax * ldx);
     c.take(&cinitP, KPmax);
     c.take_bytes(&cbiasP, (size_t)KPmax * kBiasCols * 2);
+    c.take(&slot_group, KPmax);
+    c.take(&xnP, KPmax);
+    c.take(&xmaxP, KPmax);
     c.take(&cnP, KPmax);
     c.take(&route, n);
     c.take(&rowmap, rows_cap);
@@ -947,6 +982,11 @@ static cudaError_t form_groups(Router* r, const RouterIO& io, cudaStream_t s) {
   KMGB_CUDA_TRY(cudaMemcpyAsync(r->cperm, cperm.data(), sizeof(int) * r->KPmax, cudaMemcpyHostToDevice, s));
   KMGB_CUDA_TRY(cudaMemcpyAsync(r->gcoff, gcoff.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice, s));
   KMGB_CUDA_TRY(cudaMemcpyAsync(r->gk, gkh.data(), sizeof(int) * (G + 1), cudaMemcpyHostToDevice, s));
+  r->slot_group_h.assign(r->KPmax, -1);
+  for (int g = 0; g < G; ++g)
+    for (int j = gcoff[g]; j < gcoff[g + 1]; ++j) r->slot_group_h[j] = g;
+  KMGB_CUDA_TRY(cudaMemcpyAsync(r->slot_group, r->slot_group_h.data(), sizeof(int) * r->KPmax,
+                                cudaMemcpyHostToDevice, s));
   // input scale of the network: unit mean square per dimension over the sample
   std::vector<float> xn(r->Sg);
   KMGB_CUDA_TRY(cudaMemcpyAsync(xn.data(), r->sxn, sizeof(float) * r->Sg, cudaMemcpyDeviceToHost, s));
@@ -964,6 +1004,36 @@ static cudaError_t form_groups(Router* r, const RouterIO& io, cudaStream_t s) {
 static cudaError_t refresh_separation(Router* r, const RouterIO& io, cudaStream_t s) {
   const int k = r->k;
   fill_int_kernel<<<num_sms() * 4, 256, 0, s>>>(r->m2, k, 0x7f800000);  // +inf
+  count_launches(1);
+  if (io.cbias) {
+    // on the tensor cores: the permuted centers against themselves in separation mode, every
+    // 256-row unit skipping its own group's chunks (K^2 D work at tensor rate instead of FP32)
+    AssignArgs a{};
+    a.n = r->KP;
+    a.k = (int)r->KP;
+    a.d = r->d;
+    a.cn = r->cnP;
+    a.xnorm = r->xnP;
+    a.cmax = io.cmax;
+    a.cinit = r->cinitP;
+    a.cbias = r->cbiasP;
+    a.err = io.err;
+    a.stop = io.stop;
+    a.xmax_out = r->xmaxP;
+    a.slot_group = r->slot_group;
+    const void* ClP = io.Cl ? r->ClP : nullptr;
+    const cudaError_t e =
+        launch_assign_bf16(r->CbP, ClP, r->ldb, r->CbP, ClP, r->ldb, a, s);
+    if (e == cudaSuccess) {
+      m2_from_xmax_kernel<<<num_sms() * 4, 256, 0, s>>>(r->cperm, r->KP, r->cnP, r->xmaxP, r->m2,
+                                                       io.stop);
+      m0_kernel<<<num_sms() * 4, 256, 0, s>>>(r->m2, k, r->m0);
+      count_launches(2);
+      return cudaGetLastError();
+    }
+    if (e != cudaErrorInvalidValue && e != cudaErrorInvalidConfiguration) return e;
+    cudaGetLastError();  // not launched: the SIMT kernel below
+  }
   const int nt = (k + kPairTile - 1) / kPairTile;
   const long long tiles = (long long)nt * (nt + 1) / 2;
   // |fl(c.c') - c.c'| <= gamma_d |c||c'| <= gamma_d (cn + cn')/2, doubled; the FP32 norms, the
@@ -975,7 +1045,7 @@ static cudaError_t refresh_separation(Router* r, const RouterIO& io, cudaStream_
                                                                nullptr, 0.0f, r->group, nullptr,
                                                                r->m2, err_rel, nt);
   m0_kernel<<<num_sms() * 4, 256, 0, s>>>(r->m2, k, r->m0);
-  count_launches(3);
+  count_launches(2);
   return cudaGetLastError();
 }
 
@@ -1055,16 +1125,17 @@ cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_c
     KMGB_CUDA_TRY(router_stats(r, &tmp, s));
   }
   KMGB_CUDA_TRY(r->mark(s));
-  // the separation bound for the current centers
-  KMGB_CUDA_TRY(refresh_separation(r, io, s));
-  KMGB_CUDA_TRY(r->mark(s));
   // centers in group order
   permute_centers_kernel<<<num_sms() * 8, 256, 0, s>>>(
       r->cperm, r->KP, static_cast<const uint4*>(io.Cb), static_cast<const uint4*>(io.Cl), vb,
       reinterpret_cast<const float4*>(io.Cop), vx, io.cinit, io.cn, static_cast<uint4*>(r->CbP),
       io.Cl ? static_cast<uint4*>(r->ClP) : nullptr, reinterpret_cast<float4*>(r->CopP), r->cinitP,
-      r->cnP, static_cast<const uint4*>(io.cbias), static_cast<uint4*>(r->cbiasP), io.stop);
+      r->cnP, static_cast<const uint4*>(io.cbias), static_cast<uint4*>(r->cbiasP), r->xnP,
+      io.stop);
   count_launches(1);
+  KMGB_CUDA_TRY(r->mark(s));
+  // the separation bound for the current centers (from the permuted ones)
+  KMGB_CUDA_TRY(refresh_separation(r, io, s));
   KMGB_CUDA_TRY(r->mark(s));
   // inference: hidden layer (store mode), then the group (arg-max mode), in row chunks
   for (long long r0 = 0; r0 < r->n; r0 += kChunkRows) {
