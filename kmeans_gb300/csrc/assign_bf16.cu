@@ -55,7 +55,6 @@ constexpr int MAX_STAGES = 8;
 constexpr int MAX_D = 512;  // one plane; the shared-memory check limits two planes to 320
 constexpr uint32_t TMEM_COLS = 512;           // two 256-column accumulator buffers
 constexpr size_t SMEM_CAP = 227 * 1024;       // upper bound; the device's opt-in limit is queried
-constexpr float kUnusable = -3.0e38f;         // start value of padding / unusable centers
 
 static_assert(2 * BN <= (int)TMEM_COLS, "two accumulator buffers");
 static_assert(kCenterPad % BN == 0, "start values are padded to whole chunks");

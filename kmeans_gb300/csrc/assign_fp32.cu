@@ -258,7 +258,7 @@ assign_fp32_grouped_kernel(const __grid_constant__ CUtensorMap tmX,
     }
   };
   // producer cursor (thread 0 only)
-  TileCursor pc;
+  TileCursor pc{};
   auto issue_next = [&](int stage) -> bool {
     if (pc.tile >= ntiles) return false;
     const uint32_t dst = smem_u32(smem + stage * STAGE_BYTES);

@@ -192,7 +192,6 @@ kpp_update_bulk_kernel(const T* __restrict__ X, long long ldx, long long n, int 
   const long long row_elems = ldx;
   const uint32_t row_bytes = (uint32_t)(ldx * (long long)sizeof(T));
   const uint32_t xstage_bytes = row_bytes * (uint32_t)rows_per_stage;
-  const uint32_t dstage_bytes = (uint32_t)(rows_per_stage * sizeof(T));
   T* cs = reinterpret_cast<T*>(kpp_smem);                              // the new center
   unsigned char* ring = kpp_smem + ((d * sizeof(T) + 127) / 128) * 128;  // X stages, then D^2
   T* dring = reinterpret_cast<T*>(ring + (size_t)stages * xstage_bytes);

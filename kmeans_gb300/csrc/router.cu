@@ -1118,7 +1118,7 @@ cudaError_t router_train(Router* r, const RouterIO& io, cudaStream_t s) {
 
 cudaError_t router_assign(Router* r, const RouterIO& io, int* fb_list, int* fb_count,
                           cudaStream_t s) {
-  const int G = r->G, k = r->k;
+  const int G = r->G;
   const long long vb = r->ldb * 2 / 16, vx = r->ldx / 4;
   if (r->prof && r->ev_used - r->ev_read > 4096) {  // read out what has accumulated
     RouterStats tmp;
