@@ -470,6 +470,8 @@ def batched_workload(args):
             "reranked_points_total": st.reranked, "gpu_launches": launches,
             "iteration_graph_launches_per_iteration": st.reserved[5] / iters,
             "groups": st.reserved[6],
+            "label_audit": {"rows": int(st.reserved[7]) >> 24,
+                            "violations": int(st.reserved[7]) & 0xFFFFFF},
             "single_call_loop": {"problems": len(sample), "loop_s": loop, "batched_s": bsample,
                                  "speedup": loop / bsample}}
     print(json.dumps(line), flush=True)

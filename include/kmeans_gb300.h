@@ -367,7 +367,10 @@ typedef struct kmgb_problem {
  * reserved[0] = wall time of the whole call in microseconds (uploads, initialisation and result
  * copies included), reserved[1..4] = microseconds of center preparation, assignment, re-rank and
  * update summed over the iterations (CUDA events; kernel-by-kernel runs only), reserved[5] =
- * iteration-graph launches, reserved[6] = groups. */
+ * iteration-graph launches, reserved[6] = groups, reserved[7] = the label audit of certified
+ * runs: rows audited (bits 24 and up) and violations found (bits 0-23, saturating) -- every
+ * iteration of every group KMGB_AUDIT_ROWS sampled rows (default 64) are checked against the
+ * FP64 arg-min over their own problem's centers (padding rows and stopped problems skipped). */
 KMGB_EXPORT int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const kmgb_options* opt,
                                        kmgb_stats* stats);
 

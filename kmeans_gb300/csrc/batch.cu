@@ -262,7 +262,7 @@ bool upload_host_rows(const kmgb_problem* pr, const std::vector<int>& ids, int d
 // One group: problems `ids` (all of dimension d).
 int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_options& o,
               cudaStream_t s, unsigned long long* reranked, double* loop_ms, double* phase_ms,
-              Fail& f, long long* graph_launches) {
+              Fail& f, long long* graph_launches, unsigned long long* audit) {
   const int P = (int)ids.size();
   const long long ldx = rup(d, 4);
   const long long ldb = rup(d, 8);
@@ -325,6 +325,15 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
   // grouped pass (FP32 band, then FP64)
   const long long cand_cap = std::min<long long>(nvalid, 1LL << 20);
   int *cand = nullptr, *cand_cnt = nullptr, *rr_over = nullptr, *over_count = nullptr;
+  // label audit (certified runs): KMGB_AUDIT_ROWS sampled rows (default 64) per iteration, each
+  // against its own problem's centers
+  int audit_rows = 0;
+  if (o.certify) {
+    long long ar = 64;
+    if (const char* e = std::getenv("KMGB_AUDIT_ROWS")) ar = std::atoll(e);
+    audit_rows = (int)std::max(0LL, std::min<long long>(ar, kAuditMaxRows));
+  }
+  unsigned long long* audit_ws = nullptr;
   if (f.set(m.alloc(&X, (size_t)rows * ldx), E, "data") ||
       f.set(cudaMemsetAsync(X, 0, sizeof(float) * (size_t)rows * ldx, s), E, "data") ||
       f.set(m.alloc(&xn, rows), E, "norms") || f.set(m.alloc(&qn, rows), E, "norms") ||
@@ -337,6 +346,9 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       f.set(m.alloc(&cand_cnt, cand_cap), E, "re-rank") ||
       f.set(m.alloc(&rr_over, cand_cap), E, "re-rank") ||
       f.set(m.alloc(&over_count, 1), E, "re-rank") ||
+      f.set(m.alloc(&audit_ws, 4 + 2 * (size_t)kAuditMaxRows), E, "audit") ||
+      f.set(cudaMemsetAsync(audit_ws, 0, sizeof(unsigned long long) * (4 + 2 * kAuditMaxRows), s),
+            E, "audit") ||
       f.set(cudaMemsetAsync(rr_stats, 0, 2 * sizeof(unsigned long long), s), E, "re-rank") ||
       f.set(cudaMemsetAsync(err, 0, sizeof(int), s), E, "error word") ||
       f.set(cudaMemsetAsync(C, 0, sizeof(float) * (size_t)K * ldx, s), E, "centers"))
@@ -563,6 +575,10 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
                                               nullptr, s),
                     KMEANS_ERROR_CLOSEST_CENTERS, "re-rank") ||
               f.set(launch_rerank_grouped(rx, g, s), KMEANS_ERROR_CLOSEST_CENTERS, "re-rank"))) &&
+           !(audit_rows > 0 &&
+             f.set(launch_audit_labels(X, ldx, rows, d, C, ldx, (int)K, labels, audit_ws,
+                                       audit_rows, nullptr, s, &g),
+                   KMEANS_ERROR_CLOSEST_CENTERS, "audit")) &&
            mk() &&
            !f.set(launch_update_batched(X, ldx, d, qn, labels, C, ldx, o.empty_policy, w, b, s),
                   EU, "update") &&
@@ -647,10 +663,13 @@ int run_group(kmgb_problem* pr, const std::vector<int>& ids, int d, const kmgb_o
       f.set(cudaMemcpyAsync(&e, err, sizeof(int), cudaMemcpyDeviceToHost, s), EG, "error word") ||
       f.set(cudaStreamSynchronize(s), EG, "results"))
     return f.code;
-  unsigned long long rs[2] = {0, 0};
-  if (f.set(cudaMemcpy(rs, rr_stats, sizeof(rs), cudaMemcpyDeviceToHost), EG, "statistics"))
+  unsigned long long rs[2] = {0, 0}, au[2] = {0, 0};
+  if (f.set(cudaMemcpy(rs, rr_stats, sizeof(rs), cudaMemcpyDeviceToHost), EG, "statistics") ||
+      f.set(cudaMemcpy(au, audit_ws, sizeof(au), cudaMemcpyDeviceToHost), EG, "statistics"))
     return f.code;
   *reranked += rs[0];
+  audit[0] += au[0];
+  audit[1] += au[1];
   if (e) {
     f.code = e == KMGB_DEV_BAD_LABEL ? KMEANS_ERROR_CLUSTER_CENTERS : KMEANS_ERROR_CLOSEST_CENTERS;
     f.msg = "kmgb_lloyd_batched_f32: device error word " + std::to_string(e);
@@ -720,7 +739,7 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
   if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
     return reject(KMEANS_ERROR_BUILDDATA, "kmgb_lloyd_batched_f32: stream creation failed");
   Fail f;
-  unsigned long long reranked = 0;
+  unsigned long long reranked = 0, audit[2] = {0, 0};  // audit: rows audited, violations
   double loop_ms = 0.0;
   double phase_ms[4] = {0.0, 0.0, 0.0, 0.0};
   long long graph_launches = 0;
@@ -756,7 +775,7 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     if (f.code) break;
     kmgb_options og = o;
     og.assign_tier = tier;
-    run_group(problems, ids, d, og, s, &reranked, &loop_ms, phase_ms, f, &graph_launches);
+    run_group(problems, ids, d, og, s, &reranked, &loop_ms, phase_ms, f, &graph_launches, audit);
     ++groups;
   }
   cudaStreamSynchronize(s);
@@ -773,6 +792,9 @@ extern "C" int kmgb_lloyd_batched_f32(kmgb_problem* problems, int count, const k
     for (int ph = 0; ph < 4; ++ph) stats->reserved[1 + ph] = (long long)(phase_ms[ph] * 1000.0);
     stats->reserved[5] = graph_launches;
     stats->reserved[6] = groups;
+    // rows audited against the FP64 arg-min over their problem's centers (high 40 bits) and
+    // violations found (low 24 bits, saturating)
+    stats->reserved[7] = (long long)((audit[0] << 24) | std::min<unsigned long long>(audit[1], 0xFFFFFF));
     stats->reserved[0] = (long long)std::chrono::duration<double, std::micro>(
                              std::chrono::steady_clock::now() - t0)
                              .count();

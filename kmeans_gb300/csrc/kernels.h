@@ -164,9 +164,12 @@ cudaError_t launch_resolve_candidates(const int* list, const int* count, long lo
 // the FP64 arg-min over all k centers; ws holds 4 + 2 * kAuditMaxRows words, zero before the
 // first audit ([0] rows audited, [1] violations, [3] 1 + the last violating row).
 constexpr int kAuditMaxRows = 256;
+// With grp (batched problems): each sampled row against its own problem's centers; padding rows
+// and rows of stopped problems are skipped (not counted in ws[0]).
 cudaError_t launch_audit_labels(const float* X, long long ldx, long long n, int d, const float* C,
                                 long long ldc, int k, const int* labels, unsigned long long* ws,
-                                int rows, const int* stop, cudaStream_t s);
+                                int rows, const int* stop, cudaStream_t s,
+                                const GroupArgs* grp = nullptr);
 cudaError_t launch_count_stats(const int* counts, int full_idx, unsigned long long* stats,
                                const int* stop, cudaStream_t s);
 

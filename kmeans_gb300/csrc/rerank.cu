@@ -868,7 +868,7 @@ __global__ void __launch_bounds__(256)
 audit_scan_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
                   const float* __restrict__ C, long long ldc, int k,
                   const int* __restrict__ labels, unsigned long long* ws, int rows, int parts,
-                  const int* stop) {
+                  GroupArgs g, const int* stop) {
   if (stopped(stop)) return;
   extern __shared__ float ax[];
   __shared__ int viol_sh;
@@ -876,13 +876,25 @@ audit_scan_kernel(const float* __restrict__ X, long long ldx, long long n, int d
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const unsigned long long seq = *reinterpret_cast<volatile unsigned long long*>(ws + 2);
   const long long row = (long long)(audit_hash(seq + (unsigned long long)r) % (unsigned long long)n);
+  // batched problems: the row's problem and its centers; padding rows and rows of stopped
+  // problems (their labels belong to the centers before the last update) are not audited
+  int cbeg = 0, kk = k;
+  if (g.tile_prob) {
+    const int prob = g.tile_prob[row >> 7];
+    if (row >= g.row_end[prob] || (g.done && g.done[prob])) {  // uniform over the block
+      if (threadIdx.x == 0 && part == 0) ws[4 + rows + r] = ~0ull;
+      return;
+    }
+    cbeg = g.c_off[prob];
+    kk = g.k[prob];
+  }
   for (int t = threadIdx.x; t < d; t += blockDim.x) ax[t] = X[(size_t)row * ldx + t];
   if (threadIdx.x == 0) viol_sh = 0;
   __syncthreads();
   const float rel = 2.02f * (float)(d + 2) * 5.9604645e-8f;
   const float slack = (float)d * 2.3509887e-38f;  // d 2^-125
   const int lab = labels[row];
-  const bool valid = lab >= 0 && lab < k;
+  const bool valid = lab >= cbeg && lab < cbeg + kk;
   // the label's interval (every warp evaluates it; an invalid label or one on an unusable
   // center is [inf, inf]: every usable center is nearer)
   float lab_lo = INFINITY, lab_hi = INFINITY;
@@ -894,8 +906,8 @@ audit_scan_kernel(const float* __restrict__ X, long long ldx, long long n, int d
     }
   }
   double dl = -1.0;  // the label's FP64 distance, evaluated when first needed
-  const int per = (k + parts - 1) / parts;
-  const int j0 = part * per, j1 = min(k, j0 + per);
+  const int per = (kk + parts - 1) / parts;
+  const int j0 = cbeg + part * per, j1 = min(cbeg + kk, j0 + per);
   bool viol = false;
   for (int j = j0 + warp; j < j1; j += nw) {
     if (j == lab) continue;
@@ -923,14 +935,16 @@ audit_scan_kernel(const float* __restrict__ X, long long ldx, long long n, int d
 
 __global__ void audit_finish_kernel(unsigned long long* ws, int rows, const int* stop) {
   if (stopped(stop)) return;
-  __shared__ int nviol;
+  __shared__ int nviol, naud;
   __shared__ unsigned long long last;
   if (threadIdx.x == 0) {
     nviol = 0;
+    naud = 0;
     last = 0;
   }
   __syncthreads();
   for (int r = threadIdx.x; r < rows; r += blockDim.x) {
+    if (ws[4 + rows + r] != ~0ull) atomicAdd(&naud, 1);  // not a skipped row
     if (ws[4 + r]) {
       atomicAdd(&nviol, 1);
       atomicMax(&last, ws[4 + rows + r] + 1);
@@ -939,7 +953,7 @@ __global__ void audit_finish_kernel(unsigned long long* ws, int rows, const int*
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    ws[0] += (unsigned long long)rows;
+    ws[0] += (unsigned long long)naud;
     ws[1] += (unsigned long long)nviol;
     ws[2] += (unsigned long long)rows;
     if (last) ws[3] = last;
@@ -1053,13 +1067,15 @@ int audit_parts(int rows) {
 
 cudaError_t launch_audit_labels(const float* X, long long ldx, long long n, int d, const float* C,
                                 long long ldc, int k, const int* labels, unsigned long long* ws,
-                                int rows, const int* stop, cudaStream_t s) {
+                                int rows, const int* stop, cudaStream_t s, const GroupArgs* grp) {
   if (inject_fault(kFaultLaunch)) return cudaErrorLaunchOutOfResources;
   if (n <= 0 || k <= 0 || rows <= 0) return cudaSuccess;
   if (rows > kAuditMaxRows || (size_t)d * sizeof(float) > 48 * 1024) return cudaErrorInvalidValue;
   const int parts = audit_parts(rows);
+  const GroupArgs g = grp ? *grp : GroupArgs{};
   audit_scan_kernel<<<rows * parts, 256, sizeof(float) * (size_t)d, s>>>(X, ldx, n, d, C, ldc, k,
-                                                                        labels, ws, rows, parts, stop);
+                                                                        labels, ws, rows, parts, g,
+                                                                        stop);
   audit_finish_kernel<<<1, 256, 0, s>>>(ws, rows, stop);
   count_launches(2);
   return cudaGetLastError();

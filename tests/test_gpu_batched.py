@@ -46,6 +46,10 @@ def test_mixed_batch_matches_oracle(km, orc, torch_cuda, tier):
         ini = orc.reference_init(X, k) if init is None else init
         check(r, orc.lloyd(X, ini, 6))
     assert st.iterations == 6
+    # the label audit ran in every group iteration (sampled rows that fall in padding or in a
+    # stopped problem are skipped) and found nothing
+    audited, violations = st.reserved[7] >> 24, st.reserved[7] & 0xFFFFFF
+    assert audited > 0 and violations == 0
 
 
 @pytest.mark.parametrize("tier", TIERS)
