@@ -347,93 +347,178 @@ __global__ void piece_sums_kernel(const T* __restrict__ X, long long ldx,
   }
 }
 
-// FP32 rows whose width and stride are multiples of 4 (16-byte aligned): one warp per piece, a
-// lane owns 4 consecutive dimensions (one float4 per row, so a warp instruction reads a whole
-// 128-dimension row), the piece's point ids are read 32 at a time and broadcast by shuffles, and
-// 16 rows are in flight per warp. Every dimension still adds the piece's points in sorted order
-// with the same float-float TwoSum as the generic kernel: the sums are identical. The piece's
-// sum of ||x||^2 (SSE only) is added as a tree over 32 rows at a time.
-__global__ void piece_sums_vec4_kernel(const float* __restrict__ X, long long ldx,
-                                       const double* __restrict__ qn, const int* __restrict__ sorted,
-                                       const int* __restrict__ label_off, const int* __restrict__ pstart,
-                                       int k, int d, double* __restrict__ part,
-                                       double* __restrict__ partq, const int* stop) {
+// FP32 rows with D > 64 whose width and stride are multiples of 4 (16-byte aligned). One warp per
+// piece; lane l owns dimensions d0 + 4l .. d0 + 4l + 3 of each 128-dimension chunk d0 of a row.
+// The rows travel by cp.async (16 bytes per lane and row) into a per-warp ring of kRingStages
+// stages of kRingRows rows in shared memory, so the loads in flight hold no registers: the issuing
+// side runs kRingStages - 1 stages ahead of the summing side along the warp's sequence of
+// (piece, chunk, 8-row stage), across piece boundaries. A lane reads back only the 16 bytes it
+// copied itself, so cp.async.wait_group alone orders its data. Every (piece, dimension) adds the
+// piece's points in sorted order with the same float-float TwoSum as the generic kernel, so the
+// sums are identical; the piece's sum of ||x||^2 (SSE only) is added as a tree over 32 rows at a
+// time.
+constexpr int kRingStages = 3;
+constexpr int kRingRows = 8;
+constexpr int kRingWarps = 4;
+static_assert(32 % kRingRows == 0, "a stage never straddles a 32-row id window");
+static_assert(kRingWarps * kRingStages * kRingRows * 32 * 16 <= 48 * 1024, "static shared memory");
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Issuing side of piece_sums_ring_kernel: the cursor over the warp's (piece, chunk, stage)
+// sequence. Pieces gw, gw + nw, ...; rows b..e-1 of the current piece, chunk d0, next row t; the
+// ids of the 32-row window starting at row wt in `id` (lane l: row wt + l) and, prefetched, of the
+// window after it in the same chunk in `id_nx`.
+struct RingCursor {
+  long long p;
+  int b, e, d0, t, wt, id, id_nx;
+  double qs;
+};
+
+__device__ __forceinline__ int ring_window_id(const int* __restrict__ sorted, int t0, int e,
+                                              int lane) {
+  return t0 + lane < e ? __ldg(sorted + t0 + lane) : 0;
+}
+
+__device__ __forceinline__ void ring_start_piece(RingCursor& q, long long ptot,
+                                                 const int* __restrict__ sorted,
+                                                 const int* __restrict__ label_off,
+                                                 const int* __restrict__ pstart, int k, int lane) {
+  q.d0 = 0;
+  q.qs = 0.0;
+  if (q.p >= ptot) return;
+  const int j = find_label(pstart, k, (int)q.p);
+  q.b = label_off[j] + ((int)q.p - pstart[j]) * kSumPiece;
+  q.e = min(q.b + kSumPiece, label_off[j + 1]);
+  q.t = q.b;
+  q.id_nx = ring_window_id(sorted, q.b, q.e, lane);
+}
+
+// Issues the next stage into ring slot `slot` (one cp.async group, empty once the warp's pieces
+// are done) and describes it in `desc`: bit 0 valid, bit 1 last stage of its (piece, chunk),
+// bits 2-5 rows, bits 8+ chunk; `dp` = its piece.
+__device__ __forceinline__ void ring_issue(RingCursor& q, long long ptot, long long nw,
+                                           const float* __restrict__ X, long long ldx,
+                                           const double* __restrict__ qn,
+                                           const int* __restrict__ sorted,
+                                           const int* __restrict__ label_off,
+                                           const int* __restrict__ pstart, int k, int d,
+                                           double* __restrict__ partq, uint32_t slot_addr, int lane,
+                                           int& dp, int& desc) {
+  if (q.p >= ptot) {
+    cp_async_commit();
+    dp = 0;
+    desc = 0;
+    return;
+  }
+  const bool window = ((q.t - q.b) & 31) == 0;
+  double qv = 0.0;
+  if (window) {  // a new window: its ids were prefetched; prefetch the next one of the chunk
+    q.wt = q.t;
+    q.id = q.id_nx;
+    q.id_nx = ring_window_id(sorted, q.t + 32, q.e, lane);
+    if (qn && q.d0 == 0 && q.t + lane < q.e) qv = __ldg(qn + q.id);
+  }
+  const int nr = min(kRingRows, q.e - q.t);
+  const int c = q.d0 + 4 * lane;
+#pragma unroll
+  for (int r = 0; r < kRingRows; ++r) {
+    const int i = __shfl_sync(0xffffffffu, q.id, (q.t - q.wt + r) & 31);
+    if (r < nr && c < d) cp_async16(slot_addr + r * 512, X + (size_t)i * ldx + c);
+  }
+  cp_async_commit();
+  if (window && qn && q.d0 == 0) {  // ||x||^2 of the window's rows: tree sum (FP64)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) qv += __shfl_xor_sync(0xffffffffu, qv, o);
+    q.qs += qv;
+  }
+  const bool last = q.t + nr >= q.e;
+  dp = (int)q.p;
+  desc = (q.d0 << 8) | (nr << 2) | (last ? 2 : 0) | 1;
+  q.t += nr;
+  if (last) {
+    if (q.d0 == 0 && partq && lane == 0) partq[q.p] = q.qs;
+    q.d0 += 128;
+    if (q.d0 < d) {  // the piece's next chunk: rows from the start again
+      q.t = q.b;
+      q.id_nx = ring_window_id(sorted, q.b, q.e, lane);
+    } else {
+      q.p += nw;
+      ring_start_piece(q, ptot, sorted, label_off, pstart, k, lane);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kRingWarps * 32, 4)
+piece_sums_ring_kernel(const float* __restrict__ X, long long ldx, const double* __restrict__ qn,
+                       const int* __restrict__ sorted, const int* __restrict__ label_off,
+                       const int* __restrict__ pstart, int k, int d, double* __restrict__ part,
+                       double* __restrict__ partq, const int* stop) {
   if (stopped(stop)) return;
-  const int ptot = pstart[k];
-  const int lane = threadIdx.x & 31;
-  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long p = gw; p < ptot; p += nw) {
-    const int j = find_label(pstart, k, (int)p);
-    const int q = (int)p - pstart[j];
-    const int b = label_off[j] + q * kSumPiece;
-    const int e = min(b + kSumPiece, label_off[j + 1]);
-    for (int d0 = 0; d0 < d; d0 += 128) {
-      const int c = d0 + 4 * lane;
-      const bool on = c < d;
-      PieceAcc<float> a0, a1, a2, a3;
-      double qs = 0.0;
-      for (int t0 = b; t0 < e; t0 += 32) {
-        const int nt = min(32, e - t0);
-        const int my_i = lane < nt ? __ldg(sorted + t0 + lane) : 0;
-        if (qn && d0 == 0) {  // ||x||^2 of these 32 rows: one load per lane, tree sum (FP64)
-          double qv = lane < nt ? __ldg(qn + my_i) : 0.0;
-          for (int o = 16; o > 0; o >>= 1) qv += __shfl_xor_sync(0xffffffffu, qv, o);
-          qs += qv;
-        }
-        int tt = 0;
-        for (; tt + 16 <= nt; tt += 16) {  // sixteen rows in flight
-          float4 v[16];
+  __shared__ __align__(16) float4 ring[kRingWarps][kRingStages][kRingRows][32];
+  const long long ptot = pstart[k];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const long long nw = (long long)gridDim.x * kRingWarps;
+  const uint32_t ring0 = (uint32_t)__cvta_generic_to_shared(&ring[w][0][0][lane]);
+  constexpr uint32_t kSlotBytes = kRingRows * 32 * 16;
+  static_assert(kRingStages == 3, "the descriptor queue below holds two stages");
+  RingCursor q;
+  q.p = (long long)blockIdx.x * kRingWarps + w;
+  q.b = q.e = q.t = q.wt = q.id = q.id_nx = 0;
+  ring_start_piece(q, ptot, sorted, label_off, pstart, k, lane);
+  // descriptors of the two stages in flight ahead of the one being issued
+  int p0, f0, p1, f1;
+  ring_issue(q, ptot, nw, X, ldx, qn, sorted, label_off, pstart, k, d, partq, ring0, lane, p0, f0);
+  ring_issue(q, ptot, nw, X, ldx, qn, sorted, label_off, pstart, k, d, partq, ring0 + kSlotBytes,
+             lane, p1, f1);
+  PieceAcc<float> a0, a1, a2, a3;
+  int slot_sum = 0, slot_issue = 2;
+  for (;;) {
+    int p2, f2;
+    ring_issue(q, ptot, nw, X, ldx, qn, sorted, label_off, pstart, k, d, partq,
+               ring0 + slot_issue * kSlotBytes, lane, p2, f2);
+    cp_async_wait<kRingStages - 1>();  // this lane's copies of stage slot_sum have landed
+    if (!(f0 & 1)) break;
+    const int c = (f0 >> 8) + 4 * lane;
+    const int nr = (f0 >> 2) & 15;
+    if (c < d) {
+      const float4* src = &ring[w][slot_sum][0][lane];
 #pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            const int i = __shfl_sync(0xffffffffu, my_i, tt + r);
-            v[r] = on ? __ldg(reinterpret_cast<const float4*>(X + (size_t)i * ldx + c))
-                      : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-#pragma unroll
-          for (int r = 0; r < 16; ++r) {
-            a0.add(v[r].x);
-            a1.add(v[r].y);
-            a2.add(v[r].z);
-            a3.add(v[r].w);
-          }
-        }
-        for (; tt + 8 <= nt; tt += 8) {
-          float4 v[8];
-#pragma unroll
-          for (int r = 0; r < 8; ++r) {
-            const int i = __shfl_sync(0xffffffffu, my_i, tt + r);
-            v[r] = on ? __ldg(reinterpret_cast<const float4*>(X + (size_t)i * ldx + c))
-                      : make_float4(0.f, 0.f, 0.f, 0.f);
-          }
-#pragma unroll
-          for (int r = 0; r < 8; ++r) {
-            a0.add(v[r].x);
-            a1.add(v[r].y);
-            a2.add(v[r].z);
-            a3.add(v[r].w);
-          }
-        }
-        for (; tt < nt; ++tt) {
-          const int i = __shfl_sync(0xffffffffu, my_i, tt);
-          const float4 v = on ? __ldg(reinterpret_cast<const float4*>(X + (size_t)i * ldx + c))
-                              : make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int r = 0; r < kRingRows; ++r) {
+        if (r < nr) {
+          const float4 v = src[r * 32];
           a0.add(v.x);
           a1.add(v.y);
           a2.add(v.z);
           a3.add(v.w);
         }
       }
-      if (on) {
-        double* o = part + (size_t)p * d + c;
+      if (f0 & 2) {
+        double* o = part + (size_t)p0 * d + c;
         o[0] = a0.value();
         o[1] = a1.value();
         o[2] = a2.value();
         o[3] = a3.value();
       }
-      if (d0 == 0 && lane == 0 && partq) partq[p] = qs;
     }
+    if (f0 & 2) a0 = a1 = a2 = a3 = PieceAcc<float>{};
+    p0 = p1;
+    f0 = f1;
+    p1 = p2;
+    f1 = f2;
+    slot_sum = slot_sum == kRingStages - 1 ? 0 : slot_sum + 1;
+    slot_issue = slot_issue == kRingStages - 1 ? 0 : slot_issue + 1;
   }
+  cp_async_wait<0>();
 }
 
 // Small D (a multiple of 4, at most 64): L lanes per piece, each owning 4 consecutive
@@ -514,8 +599,8 @@ __global__ void piece_sums_small_kernel(const float* __restrict__ X, long long l
   }
 }
 
-// Canonical piece sums of FP32 rows: the small-D kernel where D <= 64, the float4 kernel for other
-// 16-byte-aligned rows, the scalar kernel otherwise.
+// Canonical piece sums of FP32 rows: the small-D kernel where D <= 64, the cp.async ring kernel
+// for other 16-byte-aligned rows, the scalar kernel otherwise.
 cudaError_t launch_piece_sums_f32(const float* X, long long ldx, const double* qn,
                                   const int* sorted, const int* label_off, const int* pstart, int k,
                                   int d, double* part, double* partq, const int* stop,
@@ -534,10 +619,13 @@ cudaError_t launch_piece_sums_f32(const float* X, long long ldx, const double* q
   else if (vec && lanes == 16)
     piece_sums_small_kernel<16><<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k,
                                                        d, part, partq, stop);
-  else if (vec)
-    piece_sums_vec4_kernel<<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k, d,
-                                                  part, partq, stop);
-  else
+  else if (vec) {
+    // four 4-warp blocks (48 KB of ring each) per SM
+    const long long cap = kmgb::num_sms() * 4LL * kRingWarps;
+    const long long rw = max_pieces < cap ? max_pieces : cap;
+    piece_sums_ring_kernel<<<(unsigned)((rw + kRingWarps - 1) / kRingWarps), kRingWarps * 32, 0,
+                             s>>>(X, ldx, qn, sorted, label_off, pstart, k, d, part, partq, stop);
+  } else
     piece_sums_kernel<float><<<blocks, 256, 0, s>>>(X, ldx, qn, sorted, label_off, pstart, k, d,
                                                     part, partq, stop);
   kmgb::count_launches(1);
