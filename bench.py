@@ -40,6 +40,7 @@ sys.path.insert(0, ROOT)
 
 N, D, K = 4_000_000, 128, 1024
 NUM_CENTERS = K
+L2_BYTES = 129e6  # GB300's L2
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one assignment launch per row of
 # X, from one ncu capture of the current split-tier kernel on the 1,000,000 x 128, K=1024 case
 # (517.0 MB read + 7.6 MB written). X is read once per launch and C stays in L2, so the traffic
@@ -1043,12 +1044,16 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32" if tier == "fp32" else "bf16", "data": "synthetic",
-                "config": {"workload": ("lloyd_4Mx128_K1024" if n == N else f"lloyd_{n}x128_K1024")
+                "config": {"workload": ("lloyd_4Mx128_K1024" if (n, K) == (N, NUM_CENTERS)
+                                        else f"lloyd_{n}x{D}_K{K}")
                            + ("_bf16" if args.bf16_data else ""),
                            "n": n, "d": D, "k": K,
                            "tier": tier, "certified_labels": True,
                            "storage": "bf16 values" if args.bf16_data else "fp32",
-                           "l2": "inputs larger than L2 (X: 2.05 GB FP32 per pass)",
+                           "l2": (f"inputs larger than L2 (X: {n * D * 4 / 1e9:.2f} GB FP32 per "
+                                  f"pass)" if n * D * 4 > L2_BYTES else
+                                  f"X ({n * D * 4 / 1e6:.0f} MB) fits in L2: profiling size, "
+                                  f"not a bench figure"),
                            "parallelism": "single"},
                 "assign_tflops": achieved,
                 "phase_ms_per_iter": {n: p / max(piters, 1) for n, p in
