@@ -864,6 +864,32 @@ __device__ __forceinline__ float audit_dist32(const float* ax, const float* __re
   return a;
 }
 
+// The same for four consecutive centers j .. j + 3 (clamped to jend - 1), their loads and trees
+// interleaved; every center's sum is formed exactly as audit_dist32 forms it.
+__device__ __forceinline__ void audit_dist32x4(const float* ax, const float* __restrict__ C,
+                                               long long ldc, int j, int jend, int d, int lane,
+                                               float out[4]) {
+  const float* c[4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {
+    c[u] = C + (size_t)min(j + u, jend - 1) * ldc;
+    out[u] = 0.0f;
+  }
+  for (int t = lane; t < d; t += 32) {
+    const float xt = ax[t];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float v = xt - __ldg(c[u] + t);
+      out[u] = fmaf(v, v, out[u]);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) out[u] += __shfl_xor_sync(0xffffffffu, out[u], o);
+  }
+}
+
 __global__ void __launch_bounds__(256)
 audit_scan_kernel(const float* __restrict__ X, long long ldx, long long n, int d,
                   const float* __restrict__ C, long long ldc, int k,
@@ -909,20 +935,25 @@ audit_scan_kernel(const float* __restrict__ X, long long ldx, long long n, int d
   const int per = (kk + parts - 1) / parts;
   const int j0 = cbeg + part * per, j1 = min(cbeg + kk, j0 + per);
   bool viol = false;
-  for (int j = j0 + warp; j < j1; j += nw) {
-    if (j == lab) continue;
-    const float* c = C + (size_t)j * ldc;
-    const float a = audit_dist32(ax, c, d, lane);
-    if (!(a == a)) continue;  // an unusable (NaN) center
-    const float lo = a * (1.0f - rel) - slack, hi = a * (1.0f + rel) + slack;
-    if (hi < lab_lo) {
-      viol = true;
-    } else if (lo <= lab_hi && lane == 0) {  // overlapping intervals: decide in FP64
-      if (dl < 0.0) {
-        dl = valid ? exact_value(0, ax, C + (size_t)lab * ldc, d, 0.0f) : INFINITY;
-        if (!(dl == dl)) dl = INFINITY;
+  for (int jb = j0 + 4 * warp; jb < j1; jb += 4 * nw) {  // four centers per warp step
+    float a4[4];
+    audit_dist32x4(ax, C, ldc, jb, j1, d, lane, a4);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = jb + u;
+      if (j >= j1 || j == lab) continue;
+      const float a = a4[u];
+      if (!(a == a)) continue;  // an unusable (NaN) center
+      const float lo = a * (1.0f - rel) - slack, hi = a * (1.0f + rel) + slack;
+      if (hi < lab_lo) {
+        viol = true;
+      } else if (lo <= lab_hi && lane == 0) {  // overlapping intervals: decide in FP64
+        if (dl < 0.0) {
+          dl = valid ? exact_value(0, ax, C + (size_t)lab * ldc, d, 0.0f) : INFINITY;
+          if (!(dl == dl)) dl = INFINITY;
+        }
+        if (exact_value(0, ax, C + (size_t)j * ldc, d, 0.0f) < dl) viol = true;
       }
-      if (exact_value(0, ax, c, d, 0.0f) < dl) viol = true;
     }
   }
   if (viol) viol_sh = 1;
@@ -1061,7 +1092,7 @@ cudaError_t launch_rerank(const RerankArgs& a, cudaStream_t s) {
 }
 
 int audit_parts(int rows) {
-  const int p = 2 * kmgb::num_sms() / (rows > 0 ? rows : 1);
+  const int p = 8 * kmgb::num_sms() / (rows > 0 ? rows : 1);
   return p < 1 ? 1 : (p > 32 ? 32 : p);
 }
 
