@@ -15,7 +15,8 @@ included, one call running the workload's 30 iterations; `roofline` covers the a
 (2*N*K*D FLOP per launch, per-launch time from CUDA events bracketing it inside the timed
 region; `tensor_*` counts the tensor-core products the tier actually issues, three per element
 in the split tier; `traffic` is the DRAM bytes of one launch from an ncu capture, scaled to N);
-`cpu_baseline` is the CPU restatement (oracle FP32 port, all host threads) on a sample.
+`update_roofline` puts the update phase (sort, piece sums, finalize, SSE; N*D*4 + N*4 + K*D*8
+bytes per iteration) against the measured HBM copy rate; `cpu_baseline` is the CPU restatement (oracle FP32 port, all host threads) on a sample.
 The reference arm (--impl reference) times that CPU path: the reference has no CPU
 implementation of its own and its host code is not built (its sources are only in the x86
 development container; its driver also needs a CMake-generated config.h and cuBLAS). Its line also
@@ -968,6 +969,18 @@ def main():
         roofline["tensor_tflops"] = tf / (assign_ms / 1000.0) / 1e12
         roofline["tensor_frac"] = roofline["tensor_tflops"] / bf16_peak
 
+    # the update phase (counting sort, piece sums, finalize, SSE; event-timed together) against
+    # HBM: its algorithmic bytes per iteration are X once, the labels and the FP64 per-cluster
+    # sums
+    upd_ms = phase[3] / max(piters, 1)
+    upd_bytes = n * D * 4 + n * 4 + K * D * 8
+    upd_gbs = upd_bytes / (upd_ms / 1000.0) / 1e9 if upd_ms > 0 else None
+    update_roofline = {"bound": "hbm", "achieved": upd_gbs, "peak": hbm_peak, "unit": "GB/s",
+                       "frac": upd_gbs / hbm_peak if upd_gbs else None,
+                       "bytes_per_iteration": upd_bytes, "ms_per_iteration": upd_ms,
+                       "kernels": "hist, scans, scatter_multi, piece_sums_ring, finalize, sse",
+                       "peak_source": f"{src} HBM copy (MEASURED_PEAKS.json)"}
+
     checks = None
     if not args.no_checks and rank == 0:
         checks = accuracy_and_plain_fp32(km, torch, h, X, n, K)
@@ -1062,7 +1075,8 @@ def main():
                 "label_audit": {"rows": int(st.reserved[6]), "violations": int(st.reserved[7]),
                                 "what": "rows sampled every iteration (timed ones included) and "
                                         "checked against the FP64 arg-min over all centers"},
-                "roofline": roofline, "cpu_baseline": cb, "e2e": e2e,
+                "roofline": roofline, "update_roofline": update_roofline,
+                "cpu_baseline": cb, "e2e": e2e,
                 "init_kmeanspp": init_pp,
                 "accuracy": checks["accuracy"] if checks else None,
                 "plain_fp32": checks["plain_fp32"] if checks else None,
