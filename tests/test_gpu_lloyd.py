@@ -32,12 +32,14 @@ def test_c1_config(km, orc, torch_cuda, tier):
     assert res.status == 13
 
 
+# D = 196 and 300: rows of 2 and 3 128-dimension chunks, the last one partial, in the piece sums
 @pytest.mark.parametrize("n,d,k", [(1, 1, 1), (130, 3, 7), (1000, 129, 200), (4097, 64, 129),
-                                   (20000, 128, 256), (3001, 17, 1), (2000, 256, 300)])
+                                   (20000, 128, 256), (3001, 17, 1), (2000, 256, 300),
+                                   (5000, 196, 37), (2500, 300, 50)])
 @pytest.mark.parametrize("tier", TIERS)
 def test_odd_shapes(km, orc, torch_cuda, n, d, k, tier):
-    if tier != 0 and d > 256:
-        pytest.skip("the tensor-core tiers cover D <= 256")
+    if (tier == 1 and d > 512) or (tier == 2 and d > 320):
+        pytest.skip("the BF16 tier covers D <= 512, the split tier D <= 320")
     X, _, _ = mixture_numpy(n, d, max(k, 1), seed=n + d + k)
     init = X[sample_init(n, k, seed=3)]
     res = km.lloyd(X, k, init=init, max_iters=6, assign_tier=tier)
