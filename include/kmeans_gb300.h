@@ -181,7 +181,7 @@ KMGB_EXPORT kmeansCudaErrorStatus ClusterCentersF_noalloc(const int m0, const in
                                                           float* centers_large, int* counts_large,
                                                           float* centers, int* counts);
 
-/* Replace CompactnessF/D (KmeansCudaKernels.h:389-414, Compactness.cu:258-327): the squared
+/* Replace CompactnessF/D (KmeansCudaKernels.h:389-414, Compactness.cu:62-139): the squared
  * distance of every row to centers[indices[m0+i]] (K x n row-major) is added to a running FP64
  * total kept inside the caller's buffer (compactness[2..3] viewed as one double for F,
  * compactness[1] for D; the caller zeroes the buffer before the first tile, as the reference's

@@ -4,7 +4,8 @@
 // kmeans.cpp:1161-1163) and rowNormalize (Normalize.cu:3-31, kmeans.cpp:838-840). Norms are
 // accumulated in FP64 and rounded once; an empty-cluster (NaN) center becomes an unusable
 // center: zero operand row, +inf norm, so it can never win an arg-min (the reference's
-// rowTransformMinimum skips NaN the same way, RowTransformMinimum.cu:31).
+// rowTransformMinimum skips NaN the same way: its val < dataReg is false for NaN,
+// RowTransformMinimum.cu:29-31).
 #include <cuda_bf16.h>
 
 #include <cuda_fp8.h>
