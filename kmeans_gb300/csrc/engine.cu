@@ -306,7 +306,8 @@ namespace {
 
 // Rows audited per iteration: KMGB_AUDIT_ROWS (default 64, at most kAuditMaxRows, 0 = off),
 // fewer when one row's scan (k x d, FP32 with FP64 only near the label) is large, so that an
-// audit stays near 2^30 FP32 FMAs (~30 us on GB300). Certified resident runs only.
+// audit stays within about 2^30 FP32 FMAs (at 4M x 128, K=1024 the 64 rows take ~13 us on
+// GB300). Certified resident runs only.
 int audit_rows_for(const kmgb_options& o, bool streaming, int k, int d) {
   if (!o.certify || streaming || d > 8192) return 0;
   long long rows = 64;
