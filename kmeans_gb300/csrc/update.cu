@@ -605,7 +605,9 @@ cudaError_t launch_piece_sums_f32(const float* X, long long ldx, const double* q
                                   const int* sorted, const int* label_off, const int* pstart, int k,
                                   int d, double* part, double* partq, const int* stop,
                                   long long max_pieces, cudaStream_t s) {
-  const bool vec = ldx % 4 == 0 && d % 4 == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  // (the ring kernel's stage descriptor holds the chunk offset in 23 bits)
+  const bool vec = ldx % 4 == 0 && d % 4 == 0 && d < (1 << 23) &&
+                   (reinterpret_cast<uintptr_t>(X) & 15) == 0;
   const int lanes = !vec || d > 64 ? 32 : (d <= 16 ? 4 : (d <= 32 ? 8 : 16));
   long long warps = (max_pieces + 32 / lanes - 1) / (32 / lanes);
   if (warps > kmgb::num_sms() * 64LL) warps = kmgb::num_sms() * 64LL;
